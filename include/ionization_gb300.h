@@ -1,0 +1,265 @@
+/*
+ * ionization_gb300 — C ABI of the GB300 (sm_103a) mesh time-evolution library.
+ *
+ * Conventions for every entry point:
+ *   - all array arguments are DEVICE pointers owned by the caller; the library
+ *     never allocates device memory on these paths (scratch, where needed, is
+ *     passed in and its size is given by the matching *_scratch_bytes query);
+ *   - complex arrays are interleaved (re, im) pairs: c128 = two doubles,
+ *     c64 = two floats;
+ *   - ``stream`` is a cudaStream_t (NULL = legacy default stream); work is
+ *     enqueued asynchronously and the call returns without synchronising;
+ *   - the return value is ION_OK (0) or a negative ION_ERR_* code; a text
+ *     description of the last error on the calling thread is available from
+ *     ion_last_error().  No C++ exception crosses this boundary;
+ *   - calls on distinct streams are independent; a call is thread-safe with
+ *     respect to other calls that touch different buffers.
+ *
+ * Reference interfaces replaced (paths relative to the ionization project):
+ *   ion_tdma_*            ionization/cy.pyx:9 ``tdma(matrix, d)`` as called by
+ *                         TDMAOperator._apply, ionization/mesh/mesh_operators.py:109-111
+ *   ion_line_*_run_*      one LineMesh step, QuantumMesh.evolve
+ *                         (ionization/mesh/meshes.py:251-257) with
+ *                         AlternatingDirectionImplicit / SplitInteractionOperator
+ *                         (ionization/mesh/evolution_methods.py:46-123) over
+ *                         LineLengthGaugeOperators (mesh_operators.py:304-341)
+ *   ion_sh_split_run_*    one SphericalHarmonicMesh step with
+ *                         SplitInteractionOperator (evolution_methods.py:80-123) over
+ *                         SphericalHarmonicLengthGaugeOperators (mesh_operators.py:815-1080)
+ *   ion_cyl_adi_run_*     one CylindricalSliceMesh ADI step
+ *                         (evolution_methods.py:46-77, mesh_operators.py:550-640)
+ *   ion_reduce_*          QuantumMesh.inner_product / norm (meshes.py:195-217) and the
+ *                         SphericalHarmonicMesh inner-product shortcut (meshes.py:1099-1131)
+ */
+#ifndef IONIZATION_GB300_H
+#define IONIZATION_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    ION_OK = 0,
+    ION_ERR_INVALID_ARGUMENT = -1,
+    ION_ERR_CUDA = -2,
+    ION_ERR_UNSUPPORTED = -3,
+    ION_ERR_SCRATCH_TOO_SMALL = -4,
+    ION_ERR_NONFINITE = -5
+};
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *ion_last_error(void);
+/* Library ABI version (major * 10000 + minor * 100 + patch). */
+int ion_version(void);
+
+/* ------------------------------------------------------------------------
+ * Thomas / tridiagonal solves — replaces ionization/cy.pyx:9 tdma(matrix, d)
+ *
+ * The matrix is given exactly as cy.tdma reads a scipy dia_matrix with offsets
+ * (-1, 0, 1) (cy.pyx:18-21):
+ *   sub[k]  = A[k+1, k]   k = 0..n-2   (matrix.data[0][:-1])
+ *   diag[k] = A[k, k]     k = 0..n-1   (matrix.data[1])
+ *   sup[k]  = A[k, k+1]   k = 0..n-2   (matrix.data[2][1:])
+ * and x = A^-1 d.  Like cy.tdma there is no pivoting: a zero pivot gives
+ * inf/nan in x.  ``x`` may not alias the inputs.
+ * ------------------------------------------------------------------------ */
+
+/* Scratch (device bytes) needed by ion_tdma_* for one system of n rows. */
+int64_t ion_tdma_scratch_bytes_c128(int64_t n);
+int64_t ion_tdma_scratch_bytes_c64(int64_t n);
+
+/* One system of n rows (any n >= 1). */
+int ion_tdma_c128(int64_t n, const void *sub, const void *diag, const void *sup, const void *d,
+                  void *x, void *scratch, int64_t scratch_bytes, void *stream);
+int ion_tdma_c64(int64_t n, const void *sub, const void *diag, const void *sup, const void *d,
+                 void *x, void *scratch, int64_t scratch_bytes, void *stream);
+
+/* nsys independent systems of n rows each, flattened back to back as the mesh
+ * operators hand them to cy.tdma (system s = rows [s*n, (s+1)*n) of one long
+ * vector of nsys*n rows; sub/sup hold nsys*n-1 entries).  The entries that
+ * couple consecutive systems (sub[s*n-1], sup[s*n-1]) must be zero, as the
+ * reference operators build them, and are not read.  Requires n >= 2 and
+ * n <= ion_tdma_batched_max_n_*(). */
+int ion_tdma_batched_c128(int64_t nsys, int64_t n, const void *sub, const void *diag,
+                          const void *sup, const void *d, void *x, void *stream);
+int ion_tdma_batched_c64(int64_t nsys, int64_t n, const void *sub, const void *diag,
+                         const void *sup, const void *d, void *x, void *stream);
+int64_t ion_tdma_batched_max_n_c128(void);
+int64_t ion_tdma_batched_max_n_c64(void);
+
+/* ------------------------------------------------------------------------
+ * Spherical-harmonic mesh, length gauge, split-interaction operator.
+ *
+ * One step from time index t to t+1 is, as in SplitInteractionOperator
+ * (evolution_methods.py:89-123) and QuantumMesh.evolve (meshes.py:251-257):
+ *   R_even(t+1), R_odd(t+1), (1 - i tau H0), (1 + i tau H0)^-1,
+ *   R_odd(t+1), R_even(t+1), g *= mask(r)
+ * with tau = (times[t+1] - times[t]) / 2 and the rotations built from
+ * E(times[t+1] + time_step/2) (mesh_operators.py:1011-1013, 1037-1080).  The
+ * pairing of the rotations is over the F-order (r-major, l fastest) index of
+ * the (l, r) mesh, exactly as the reference builds its even/odd matrices.
+ *
+ * psi of every simulation is stored (n_l, n_r) in C order (r contiguous),
+ * the layout of the reference's ``mesh.g``, at its own device pointer.  A batch
+ * is any number of simulations of different sizes, each with its own time
+ * index ``t`` (kept and advanced on the device), its own final index and its
+ * own field table.  Data (norm and test-state inner products, the Norm and
+ * InnerProducts datastores, data.py:189-260) are reduced on the device in
+ * FP64 at the reference's data times (sims.py:84-90) into ``out_norm`` /
+ * ``out_ip`` slots.
+ * ------------------------------------------------------------------------ */
+typedef struct ion_sh_sim {
+    void *g;             /* device psi (n_l, n_r), C order, complex128 or complex64 */
+    int32_t n_r, n_l;
+    int64_t t;           /* current time index; advanced on the device */
+    int64_t t_final;     /* last time index (number of steps of the run) */
+    int64_t store_every; /* data at t = 0, t = t_final and t % store_every == 0 if >= 1 */
+    /* FP64 tables (complex128 path) */
+    const double *hd;     /* [n_l*n_r] diagonal of the internal Hamiltonian (C order) */
+    const double *hoff;   /* [n_r-1]   its off-diagonal (identical for every l) */
+    const double *rq;     /* [n_r]     (-test_charge) * r_j */
+    const double *cl;     /* [n_l]     c_l = (l+1)/sqrt((2l+1)(2l+3)) */
+    const double *mask;   /* [n_r]     mask(r_j), or NULL for no mask */
+    const double *tau;    /* [t_final+1] tau at each time index (entry 0 unused) */
+    const double *efield; /* [t_final+1] E(times[t] + time_step/2) (entry 0 unused) */
+    /* FP32 tables (complex64 path), rounded from FP64 */
+    const float *kinv32;  /* [n_r] -2 p beta(j) + V(r_j)  (diagonal without the l term) */
+    const float *cent32;  /* [n_r] hbar^2 / (2 mu r_j^2) */
+    const float *hoff32;  /* [n_r-1] */
+    const float *rq32;    /* [n_r] */
+    const float *cl32;    /* [n_l] */
+    const float *mask32;  /* [n_r] or NULL */
+    float corr0_32;       /* extra diagonal term at (l=0, j=0) (hydrogen correction) */
+    /* data */
+    int32_t n_states;
+    const int32_t *state_l; /* [n_states] angular momentum of each test state */
+    const double *state_g;  /* [n_states*n_r*2] radial g of each test state (complex128) */
+    double weight;          /* inner-product multiplier (delta r) */
+    double *out_norm;       /* [n_data] */
+    double *out_ip;         /* [n_data*n_states*2] complex128 */
+    double *partials;       /* [n_tiles * (1 + 2*n_states)] device scratch for reductions */
+    int32_t n_tiles;        /* number of row tiles of this simulation */
+    int32_t pad_;
+} ion_sh_sim;
+
+typedef struct ion_sh_plan {
+    ion_sh_sim *sims;         /* device array [n_sims] */
+    int32_t n_sims;
+    int32_t max_n_l;          /* largest n_l of the batch */
+    int32_t max_n_r;          /* largest n_r of the batch */
+    int32_t pad_;
+    const int32_t *cn_items;  /* device [n_cn_items*2]: (sim, l) handled by one CTA */
+    int32_t n_cn_items;
+    int32_t cn_threads;       /* CTA size of the radial solve (multiple of 32) */
+    const int32_t *rot_items; /* device [n_rot_items*2]: (sim, row tile) */
+    int32_t n_rot_items;
+    int32_t rot_rows;         /* rows (r points) per tile */
+} ion_sh_plan;
+
+/* Advance every simulation of the plan by n_steps (fewer for simulations that
+ * reach t_final).  Data reductions happen at data times on the way. */
+int ion_sh_split_run_c128(const ion_sh_plan *plan, int64_t n_steps, void *stream);
+int ion_sh_split_run_c64(const ion_sh_plan *plan, int64_t n_steps, void *stream);
+/* Reduce the data of the current time index (used for t = 0 before the run). */
+int ion_sh_reduce_c128(const ion_sh_plan *plan, void *stream);
+int ion_sh_reduce_c64(const ion_sh_plan *plan, void *stream);
+/* Largest n_r the radial solve supports in one CTA. */
+int64_t ion_sh_max_n_r_c128(void);
+int64_t ion_sh_max_n_r_c64(void);
+
+/* ------------------------------------------------------------------------
+ * Line mesh, length gauge (LineLengthGaugeOperators, mesh_operators.py:304-341).
+ *
+ * method ION_LINE_ADI — AlternatingDirectionImplicit (evolution_methods.py:46-77):
+ *     (1 + i tau H)^-1 (1 - i tau H),  H = H0 + diag(zq * E(times[t+1]))
+ * method ION_LINE_SPLIT — SplitInteractionOperator (evolution_methods.py:80-123):
+ *     S (1 + i tau H0)^-1 (1 - i tau H0) S,  S = diag(exp(-i tau zq E(times[t+1])))
+ * followed by g *= mask (meshes.py:256-257).  One CTA advances one
+ * simulation; data reductions are fused into the same pass.
+ * ------------------------------------------------------------------------ */
+enum { ION_LINE_ADI = 0, ION_LINE_SPLIT = 1 };
+
+typedef struct ion_line_sim {
+    void *g;          /* device psi [n], complex128 or complex64 */
+    int32_t n;
+    int32_t method;   /* ION_LINE_ADI or ION_LINE_SPLIT */
+    int64_t t, t_final, store_every;
+    const double *hd;     /* [n]   diagonal of H0 = kinetic + V */
+    const double *hoff;   /* [n-1] off-diagonal of H0 */
+    const double *zq;     /* [n]   interaction per unit field, (-z) * test_charge */
+    const double *mask;   /* [n] or NULL */
+    const double *tau;    /* [t_final+1] */
+    const double *efield; /* [t_final+1] E(times[t]) */
+    const float *hd32;
+    const float *hoff32;
+    const float *zq32;
+    const float *mask32;
+    int32_t n_states;
+    int32_t pad_;
+    const double *state_g; /* [n_states*n*2] complex128 test states */
+    double weight;         /* delta z */
+    double *out_norm;      /* [n_data] */
+    double *out_ip;        /* [n_data*n_states*2] */
+} ion_line_sim;
+
+typedef struct ion_line_plan {
+    ion_line_sim *sims; /* device array [n_sims] */
+    int32_t n_sims;
+    int32_t max_n;
+    int32_t threads; /* CTA size (multiple of 32) */
+    int32_t pad_;
+} ion_line_plan;
+
+int ion_line_run_c128(const ion_line_plan *plan, int64_t n_steps, void *stream);
+int ion_line_run_c64(const ion_line_plan *plan, int64_t n_steps, void *stream);
+int ion_line_reduce_c128(const ion_line_plan *plan, void *stream);
+int ion_line_reduce_c64(const ion_line_plan *plan, void *stream);
+int64_t ion_line_max_n_c128(void);
+int64_t ion_line_max_n_c64(void);
+
+/* ------------------------------------------------------------------------
+ * Cylindrical slice mesh, length gauge, ADI (CylindricalSliceLengthGaugeOperators,
+ * mesh_operators.py:550-640; AlternatingDirectionImplicit, evolution_methods.py:46-77).
+ * psi is (n_z, n_rho) in C order (rho contiguous), as the reference's g.
+ * One step from t to t+1 with E = E(times[t+1]):
+ *   pass 1:  g_tmp = (1 + i tau H_z)^-1 (1 - i tau H_rho) g
+ *   pass 2:  g     = (1 + i tau H_rho)^-1 (1 - i tau H_z) g_tmp   (then *= mask)
+ * H_d = H0_d + 0.5 zq E on the diagonal (mesh_operators.py:271-298).
+ * ------------------------------------------------------------------------ */
+typedef struct ion_cyl_mesh {
+    int32_t n_z, n_rho;
+    const double *hz_d;   /* [n_z*n_rho] diagonal of the internal H_z */
+    const double *hz_off; /* [n_z-1] */
+    const double *hr_d;   /* [n_z*n_rho] diagonal of the internal H_rho */
+    const double *hr_off; /* [n_rho-1] */
+    const double *zq;     /* [n_z] */
+    const double *mask;   /* [n_z*n_rho] or NULL */
+    const double *tau;    /* indexed by time index */
+    const double *efield; /* E(times[t]) indexed by time index */
+} ion_cyl_mesh;
+
+/* Advance psi from time index t0 by n_steps.  g_tmp is a psi-sized buffer. */
+int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t t0,
+                         int64_t n_steps, void *stream);
+int64_t ion_cyl_max_points_c128(void);
+
+/* ------------------------------------------------------------------------
+ * Norm and inner products on a whole mesh (QuantumMesh.norm / inner_product,
+ * meshes.py:195-217):  norm = weight * sum |g|^2,
+ * ip[s] = weight * sum conj(states[s]) g, in FP64 with a compensated
+ * two-level sum.  ``partials`` is device scratch of
+ * ion_reduce_scratch_bytes(M, n_states) bytes.
+ * ------------------------------------------------------------------------ */
+int64_t ion_reduce_scratch_bytes(int64_t M, int32_t n_states);
+int ion_reduce_c128(int64_t M, const void *g, int32_t n_states, const void *states, double weight,
+                    double *out_norm, double *out_ip, void *partials, void *stream);
+int ion_reduce_c64(int64_t M, const void *g, int32_t n_states, const void *states, double weight,
+                   double *out_norm, double *out_ip, void *partials, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IONIZATION_GB300_H */

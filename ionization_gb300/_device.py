@@ -1,0 +1,399 @@
+"""Device-resident simulation state and the plans handed to the C ABI.
+
+PyTorch provides device memory and the stream; every kernel is ours, called
+through ``_native``.  A *batch* owns the psi buffers, coefficient tables and
+data buffers of any number of simulations and builds the descriptor array
+(``ion_sh_sim`` / ``ion_line_sim``) and work lists that one launch sweeps.
+The plain meshes are batches of one; the batched and served forms put many
+simulations of different sizes in one batch.
+"""
+
+import ctypes
+import dataclasses
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .core import Precision
+
+
+class DeviceUnavailable(RuntimeError):
+    pass
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise DeviceUnavailable("ionization_gb300 needs a CUDA device; none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def to_dev(a, dtype=None) -> torch.Tensor:
+    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+    return torch.from_numpy(a).to(device(), non_blocking=False)
+
+
+def ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def n_data_slots(t_final: int, store_every: int) -> int:
+    """Number of data times of MeshSimulation.__init__ (sims.py:84-90)."""
+    if store_every >= 1:
+        return t_final // store_every + 1 + (1 if t_final % store_every != 0 else 0)
+    return 2 if t_final > 0 else 1
+
+
+def data_slot(t: int, t_final: int, store_every: int) -> int:
+    if store_every >= 1:
+        return t // store_every if t % store_every == 0 else t_final // store_every + 1
+    return 0 if t == 0 else 1
+
+
+def is_data_time(t: int, t_final: int, store_every: int) -> bool:
+    return t == 0 or t == t_final or (store_every >= 1 and t % store_every == 0)
+
+
+def complex_dtype(precision) -> torch.dtype:
+    return torch.complex128 if Precision(precision) == Precision.C128 else torch.complex64
+
+
+def _round32(x: int) -> int:
+    return (x + 31) // 32 * 32
+
+
+# ==========================================================================
+# spherical-harmonic split operator
+# ==========================================================================
+
+
+@dataclasses.dataclass
+class ShTables:
+    """Host FP64 inputs of one spherical-harmonic simulation."""
+
+    n_r: int
+    n_l: int
+    hd: np.ndarray  # [n_l * n_r] internal diagonal, C order
+    hoff: np.ndarray  # [n_r - 1]
+    rq: np.ndarray  # [n_r]
+    cl: np.ndarray  # [n_l]
+    mask: Optional[np.ndarray]  # [n_r]
+    tau: np.ndarray  # [t_final + 1]
+    efield: np.ndarray  # [t_final + 1]
+    kinv: np.ndarray  # [n_r]  -2p beta(j) + V(r_j)
+    cent: np.ndarray  # [n_r]
+    corr0: float
+    state_l: List[int]
+    state_g: np.ndarray  # [n_states, n_r] complex128
+    weight: float
+    g0: np.ndarray  # [n_l, n_r] complex128
+    t0: int
+    t_final: int
+    store_every: int
+
+
+SH_ROT_ROWS = 32
+
+
+def sh_line_threads(n_r: int, precision) -> int:
+    maxm = 8 if Precision(precision) == Precision.C128 else 16
+    T = (n_r + maxm - 1) // maxm
+    T = min(T, n_r // 2)
+    return max(T, 1)
+
+
+class ShDeviceSim:
+    """Device buffers of one spherical-harmonic simulation."""
+
+    def __init__(self, tab: ShTables, precision):
+        self.precision = Precision(precision)
+        self.tab = tab
+        self.n_r, self.n_l = tab.n_r, tab.n_l
+        self.t = int(tab.t0)
+        self.t_final = int(tab.t_final)
+        self.store_every = int(tab.store_every)
+        f64 = np.float64
+        f32 = np.float32
+        self.g = to_dev(tab.g0.astype(np.complex128)).to(complex_dtype(precision))
+        c128 = self.precision == Precision.C128
+        self.d_hd = to_dev(tab.hd, f64) if c128 else None
+        self.d_hoff = to_dev(tab.hoff, f64)
+        self.d_rq = to_dev(tab.rq, f64)
+        self.d_cl = to_dev(tab.cl, f64)
+        self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
+        self.d_tau = to_dev(tab.tau, f64)
+        self.d_ef = to_dev(tab.efield, f64)
+        self.d_kinv32 = to_dev(tab.kinv, f32)
+        self.d_cent32 = to_dev(tab.cent, f32)
+        self.d_hoff32 = to_dev(tab.hoff, f32)
+        self.d_rq32 = to_dev(tab.rq, f32)
+        self.d_cl32 = to_dev(tab.cl, f32)
+        self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
+        self.n_states = len(tab.state_l)
+        self.d_state_l = to_dev(np.asarray(tab.state_l, dtype=np.int32).reshape(-1))
+        sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(self.n_states, self.n_r)
+        self.d_state_g = to_dev(sg.view(np.float64).reshape(-1)) if self.n_states else to_dev(np.zeros(2))
+        self.n_data = n_data_slots(self.t_final, self.store_every)
+        self.d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
+        self.d_ip = torch.full((self.n_data * max(self.n_states, 1) * 2,), float("nan"), dtype=torch.float64,
+                               device=device())
+        self.n_tiles = (self.n_r + SH_ROT_ROWS - 1) // SH_ROT_ROWS
+        self.d_partials = torch.zeros(self.n_tiles * (1 + 2 * self.n_states), dtype=torch.float64, device=device())
+
+    def nbytes(self) -> int:
+        tot = 0
+        for v in vars(self).values():
+            if isinstance(v, torch.Tensor):
+                tot += v.numel() * v.element_size()
+        return tot
+
+    def descriptor(self) -> nat.ShSim:
+        d = nat.ShSim()
+        d.g = ptr(self.g)
+        d.n_r, d.n_l = self.n_r, self.n_l
+        d.t, d.t_final, d.store_every = self.t, self.t_final, self.store_every
+        d.hd, d.hoff, d.rq, d.cl = ptr(self.d_hd), ptr(self.d_hoff), ptr(self.d_rq), ptr(self.d_cl)
+        d.mask, d.tau, d.efield = ptr(self.d_mask), ptr(self.d_tau), ptr(self.d_ef)
+        d.kinv32, d.cent32, d.hoff32 = ptr(self.d_kinv32), ptr(self.d_cent32), ptr(self.d_hoff32)
+        d.rq32, d.cl32, d.mask32 = ptr(self.d_rq32), ptr(self.d_cl32), ptr(self.d_mask32)
+        d.corr0_32 = float(self.tab.corr0)
+        d.n_states = self.n_states
+        d.state_l, d.state_g = ptr(self.d_state_l), ptr(self.d_state_g)
+        d.weight = float(self.tab.weight)
+        d.out_norm, d.out_ip, d.partials = ptr(self.d_norm), ptr(self.d_ip), ptr(self.d_partials)
+        d.n_tiles = self.n_tiles
+        return d
+
+    def data(self):
+        """(norm[n_data], inner_products[n_states, n_data]) on the host."""
+        norm = self.d_norm.cpu().numpy()
+        ip = self.d_ip.cpu().numpy()[: self.n_data * self.n_states * 2].view(np.complex128)
+        return norm, ip.reshape(self.n_data, self.n_states).T.copy()
+
+    def psi_host(self) -> np.ndarray:
+        return self.g.cpu().numpy().astype(np.complex128)
+
+
+class ShBatch:
+    """Many spherical-harmonic simulations advanced together."""
+
+    def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None):
+        self.precision = Precision(precision)
+        self.sims: List[ShDeviceSim] = list(sims or [])
+        self._plan = None
+        self._keep = None
+
+    def add(self, sim: ShDeviceSim):
+        self.sims.append(sim)
+        self._plan = None
+
+    def remove(self, sim: ShDeviceSim):
+        self.sims.remove(sim)
+        self._plan = None
+
+    def _build_plan(self):
+        sims = self.sims
+        descs = (nat.ShSim * max(len(sims), 1))()
+        for i, s in enumerate(sims):
+            descs[i] = s.descriptor()
+        raw = np.frombuffer(bytes(descs), dtype=np.uint8).copy()
+        d_descs = to_dev(raw)
+        # work lists, longest radial lines / widest tiles first
+        cn = sorted(((i, l) for i, s in enumerate(sims) for l in range(s.n_l)),
+                    key=lambda it: -sims[it[0]].n_r)
+        rot = sorted(((i, k) for i, s in enumerate(sims) for k in range(s.n_tiles)),
+                     key=lambda it: -sims[it[0]].n_l)
+        d_cn = to_dev(np.asarray(cn if cn else [(0, 0)], dtype=np.int32).reshape(-1))
+        d_rot = to_dev(np.asarray(rot if rot else [(0, 0)], dtype=np.int32).reshape(-1))
+        plan = nat.ShPlan()
+        plan.sims = ptr(d_descs)
+        plan.n_sims = len(sims)
+        plan.max_n_l = max([s.n_l for s in sims] + [1])
+        plan.max_n_r = max([s.n_r for s in sims] + [2])
+        plan.cn_items = ptr(d_cn)
+        plan.n_cn_items = len(cn)
+        plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision) for s in sims] + [1]))
+        plan.rot_items = ptr(d_rot)
+        plan.n_rot_items = len(rot)
+        plan.rot_rows = SH_ROT_ROWS
+        self._plan = plan
+        self._keep = (d_descs, d_cn, d_rot)
+
+    @property
+    def plan(self):
+        if self._plan is None:
+            self._build_plan()
+        return self._plan
+
+    def _fn(self, base):
+        return base + ("_c128" if self.precision == Precision.C128 else "_c64")
+
+    def run(self, n_steps: int):
+        if n_steps <= 0 or not self.sims:
+            return
+        nat.call(self._fn("ion_sh_split_run"), ctypes.byref(self.plan), int(n_steps), stream_ptr())
+        for s in self.sims:
+            s.t = min(s.t + int(n_steps), s.t_final)
+
+    def reduce(self):
+        if self.sims:
+            nat.call(self._fn("ion_sh_reduce"), ctypes.byref(self.plan), stream_ptr())
+
+    def invalidate(self):
+        """Rebuild descriptors on the next call (after host-side changes)."""
+        self._plan = None
+
+
+# ==========================================================================
+# line mesh
+# ==========================================================================
+
+
+@dataclasses.dataclass
+class LineTables:
+    n: int
+    method: int  # nat.ION_LINE_ADI or nat.ION_LINE_SPLIT
+    hd: np.ndarray
+    hoff: np.ndarray
+    zq: np.ndarray
+    mask: Optional[np.ndarray]
+    tau: np.ndarray
+    efield: np.ndarray
+    state_g: np.ndarray  # [n_states, n] complex128
+    weight: float
+    g0: np.ndarray
+    t0: int
+    t_final: int
+    store_every: int
+
+
+def line_threads(n: int, precision) -> int:
+    maxm = 8 if Precision(precision) == Precision.C128 else 16
+    T = (n + maxm - 1) // maxm
+    return max(min(T, n // 2), 1)
+
+
+class LineDeviceSim:
+    def __init__(self, tab: LineTables, precision):
+        self.precision = Precision(precision)
+        self.tab = tab
+        self.n = tab.n
+        self.t = int(tab.t0)
+        self.t_final = int(tab.t_final)
+        self.store_every = int(tab.store_every)
+        f64, f32 = np.float64, np.float32
+        self.g = to_dev(tab.g0.astype(np.complex128)).to(complex_dtype(precision))
+        self.d_hd, self.d_hoff, self.d_zq = to_dev(tab.hd, f64), to_dev(tab.hoff, f64), to_dev(tab.zq, f64)
+        self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
+        self.d_tau, self.d_ef = to_dev(tab.tau, f64), to_dev(tab.efield, f64)
+        self.d_hd32, self.d_hoff32, self.d_zq32 = to_dev(tab.hd, f32), to_dev(tab.hoff, f32), to_dev(tab.zq, f32)
+        self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
+        sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(-1, self.n)
+        self.n_states = sg.shape[0]
+        self.d_state_g = to_dev(sg.view(np.float64).reshape(-1)) if self.n_states else to_dev(np.zeros(2))
+        self.n_data = n_data_slots(self.t_final, self.store_every)
+        self.d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
+        self.d_ip = torch.full((self.n_data * max(self.n_states, 1) * 2,), float("nan"), dtype=torch.float64,
+                               device=device())
+
+    def nbytes(self) -> int:
+        return sum(v.numel() * v.element_size() for v in vars(self).values() if isinstance(v, torch.Tensor))
+
+    def descriptor(self) -> nat.LineSim:
+        d = nat.LineSim()
+        d.g = ptr(self.g)
+        d.n, d.method = self.n, int(self.tab.method)
+        d.t, d.t_final, d.store_every = self.t, self.t_final, self.store_every
+        d.hd, d.hoff, d.zq, d.mask = ptr(self.d_hd), ptr(self.d_hoff), ptr(self.d_zq), ptr(self.d_mask)
+        d.tau, d.efield = ptr(self.d_tau), ptr(self.d_ef)
+        d.hd32, d.hoff32, d.zq32, d.mask32 = ptr(self.d_hd32), ptr(self.d_hoff32), ptr(self.d_zq32), ptr(self.d_mask32)
+        d.n_states = self.n_states
+        d.state_g = ptr(self.d_state_g)
+        d.weight = float(self.tab.weight)
+        d.out_norm, d.out_ip = ptr(self.d_norm), ptr(self.d_ip)
+        return d
+
+    def data(self):
+        norm = self.d_norm.cpu().numpy()
+        ip = self.d_ip.cpu().numpy()[: self.n_data * self.n_states * 2].view(np.complex128)
+        return norm, ip.reshape(self.n_data, self.n_states).T.copy()
+
+    def psi_host(self) -> np.ndarray:
+        return self.g.cpu().numpy().astype(np.complex128)
+
+
+class LineBatch:
+    def __init__(self, precision, sims: Optional[List[LineDeviceSim]] = None):
+        self.precision = Precision(precision)
+        self.sims: List[LineDeviceSim] = list(sims or [])
+        self._plan = None
+        self._keep = None
+
+    def add(self, sim):
+        self.sims.append(sim)
+        self._plan = None
+
+    def remove(self, sim):
+        self.sims.remove(sim)
+        self._plan = None
+
+    def invalidate(self):
+        self._plan = None
+
+    @property
+    def plan(self):
+        if self._plan is None:
+            descs = (nat.LineSim * max(len(self.sims), 1))()
+            for i, s in enumerate(self.sims):
+                descs[i] = s.descriptor()
+            d = to_dev(np.frombuffer(bytes(descs), dtype=np.uint8).copy())
+            p = nat.LinePlan()
+            p.sims = ptr(d)
+            p.n_sims = len(self.sims)
+            p.max_n = max([s.n for s in self.sims] + [2])
+            p.threads = _round32(max([line_threads(s.n, self.precision) for s in self.sims] + [1]))
+            self._plan = p
+            self._keep = d
+        return self._plan
+
+    def _fn(self, base):
+        return base + ("_c128" if self.precision == Precision.C128 else "_c64")
+
+    def run(self, n_steps: int):
+        if n_steps <= 0 or not self.sims:
+            return
+        nat.call(self._fn("ion_line_run"), ctypes.byref(self.plan), int(n_steps), stream_ptr())
+        for s in self.sims:
+            s.t = min(s.t + int(n_steps), s.t_final)
+
+    def reduce(self):
+        if self.sims:
+            nat.call(self._fn("ion_line_reduce"), ctypes.byref(self.plan), stream_ptr())
+
+
+# ==========================================================================
+# whole-mesh reductions
+# ==========================================================================
+
+
+class Reducer:
+    """norm and inner products of a device psi with fixed device states."""
+
+    def __init__(self, M: int, states_c128: np.ndarray, weight: float):
+        self.M = int(M)
+        st = np.asarray(states_c128, dtype=np.complex128).reshape(-1, self.M)
+        self.n_states = st.shape[0]
+        self.d_states = to_dev(st.view(np.float64).reshape(-1)) if self.n_states else None
+        self.weight = float(weight)
+        nbytes = nat.value("ion_reduce_scratch_bytes", self.M, self.n_states)
+        self.d_part = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=device())
+
+    def __call__(self, g: torch.Tensor, out_norm: torch.Tensor, out_ip: Optional[torch.Tensor]):
+        fn = "ion_reduce_c128" if g.dtype == torch.complex128 else "ion_reduce_c64"
+        nat.call(fn, self.M, ptr(g), self.n_states, ptr(self.d_states), self.weight, ptr(out_norm),
+                 ptr(out_ip), ptr(self.d_part), stream_ptr())

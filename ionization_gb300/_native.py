@@ -1,0 +1,219 @@
+"""ctypes binding of the C ABI declared in ``include/ionization_gb300.h``.
+
+The library is the only compute path of this package: if it is missing or
+fails to load, every entry point raises ``NativeLibraryError`` (there is no
+CPU fallback).  Structures below mirror the header field by field.
+"""
+
+import ctypes
+import os
+import threading
+
+from . import _build
+
+c_i32, c_i64, c_f32, c_f64, c_vp = (
+    ctypes.c_int32,
+    ctypes.c_int64,
+    ctypes.c_float,
+    ctypes.c_double,
+    ctypes.c_void_p,
+)
+
+ION_OK = 0
+ION_LINE_ADI = 0
+ION_LINE_SPLIT = 1
+
+
+class NativeLibraryError(RuntimeError):
+    pass
+
+
+class IonError(RuntimeError):
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+class ShSim(ctypes.Structure):
+    _fields_ = [
+        ("g", c_vp),
+        ("n_r", c_i32),
+        ("n_l", c_i32),
+        ("t", c_i64),
+        ("t_final", c_i64),
+        ("store_every", c_i64),
+        ("hd", c_vp),
+        ("hoff", c_vp),
+        ("rq", c_vp),
+        ("cl", c_vp),
+        ("mask", c_vp),
+        ("tau", c_vp),
+        ("efield", c_vp),
+        ("kinv32", c_vp),
+        ("cent32", c_vp),
+        ("hoff32", c_vp),
+        ("rq32", c_vp),
+        ("cl32", c_vp),
+        ("mask32", c_vp),
+        ("corr0_32", c_f32),
+        ("n_states", c_i32),
+        ("state_l", c_vp),
+        ("state_g", c_vp),
+        ("weight", c_f64),
+        ("out_norm", c_vp),
+        ("out_ip", c_vp),
+        ("partials", c_vp),
+        ("n_tiles", c_i32),
+        ("pad_", c_i32),
+    ]
+
+
+class ShPlan(ctypes.Structure):
+    _fields_ = [
+        ("sims", c_vp),
+        ("n_sims", c_i32),
+        ("max_n_l", c_i32),
+        ("max_n_r", c_i32),
+        ("pad_", c_i32),
+        ("cn_items", c_vp),
+        ("n_cn_items", c_i32),
+        ("cn_threads", c_i32),
+        ("rot_items", c_vp),
+        ("n_rot_items", c_i32),
+        ("rot_rows", c_i32),
+    ]
+
+
+class LineSim(ctypes.Structure):
+    _fields_ = [
+        ("g", c_vp),
+        ("n", c_i32),
+        ("method", c_i32),
+        ("t", c_i64),
+        ("t_final", c_i64),
+        ("store_every", c_i64),
+        ("hd", c_vp),
+        ("hoff", c_vp),
+        ("zq", c_vp),
+        ("mask", c_vp),
+        ("tau", c_vp),
+        ("efield", c_vp),
+        ("hd32", c_vp),
+        ("hoff32", c_vp),
+        ("zq32", c_vp),
+        ("mask32", c_vp),
+        ("n_states", c_i32),
+        ("pad_", c_i32),
+        ("state_g", c_vp),
+        ("weight", c_f64),
+        ("out_norm", c_vp),
+        ("out_ip", c_vp),
+    ]
+
+
+class LinePlan(ctypes.Structure):
+    _fields_ = [
+        ("sims", c_vp),
+        ("n_sims", c_i32),
+        ("max_n", c_i32),
+        ("threads", c_i32),
+        ("pad_", c_i32),
+    ]
+
+
+class CylMesh(ctypes.Structure):
+    _fields_ = [
+        ("n_z", c_i32),
+        ("n_rho", c_i32),
+        ("hz_d", c_vp),
+        ("hz_off", c_vp),
+        ("hr_d", c_vp),
+        ("hr_off", c_vp),
+        ("zq", c_vp),
+        ("mask", c_vp),
+        ("tau", c_vp),
+        ("efield", c_vp),
+    ]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "ion_last_error": (ctypes.c_char_p, []),
+    "ion_version": (ctypes.c_int, []),
+    "ion_tdma_scratch_bytes_c128": (c_i64, [c_i64]),
+    "ion_tdma_scratch_bytes_c64": (c_i64, [c_i64]),
+    "ion_tdma_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "ion_tdma_c64": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "ion_tdma_batched_c128": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ion_tdma_batched_c64": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ion_tdma_batched_max_n_c128": (c_i64, []),
+    "ion_tdma_batched_max_n_c64": (c_i64, []),
+    "ion_sh_split_run_c128": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_i64, c_vp]),
+    "ion_sh_split_run_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_i64, c_vp]),
+    "ion_sh_reduce_c128": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
+    "ion_sh_reduce_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
+    "ion_sh_max_n_r_c128": (c_i64, []),
+    "ion_sh_max_n_r_c64": (c_i64, []),
+    "ion_line_run_c128": (ctypes.c_int, [ctypes.POINTER(LinePlan), c_i64, c_vp]),
+    "ion_line_run_c64": (ctypes.c_int, [ctypes.POINTER(LinePlan), c_i64, c_vp]),
+    "ion_line_reduce_c128": (ctypes.c_int, [ctypes.POINTER(LinePlan), c_vp]),
+    "ion_line_reduce_c64": (ctypes.c_int, [ctypes.POINTER(LinePlan), c_vp]),
+    "ion_line_max_n_c128": (c_i64, []),
+    "ion_line_max_n_c64": (c_i64, []),
+    "ion_cyl_adi_run_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
+    "ion_cyl_max_points_c128": (c_i64, []),
+    "ion_reduce_scratch_bytes": (c_i64, [c_i64, c_i32]),
+    "ion_reduce_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
+    "ion_reduce_c64": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) and return the ctypes library."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing and (not os.path.exists(path) or _build.needs_build()):
+            try:
+                _build.build()
+            except Exception as e:  # noqa: BLE001
+                raise NativeLibraryError(f"cannot build the CUDA library: {e}") from e
+        if not os.path.exists(path):
+            raise NativeLibraryError(f"CUDA library missing: {path}")
+        try:
+            lib = ctypes.CDLL(path)
+        except OSError as e:
+            raise NativeLibraryError(f"cannot load {path}: {e}") from e
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def call(name, *args):
+    """Call an int-returning entry point and raise IonError on failure."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != ION_OK:
+        msg = lib.ion_last_error().decode(errors="replace")
+        raise IonError(name, rc, msg)
+    return rc
+
+
+def value(name, *args):
+    return getattr(load(), name)(*args)
+
+
+def exported_symbols():
+    return list(_SIGS)

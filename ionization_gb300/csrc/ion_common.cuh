@@ -1,0 +1,70 @@
+// Shared device/host helpers for the ionization_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ionization_gb300.h"
+
+namespace ion {
+
+// ---------------------------------------------------------------------------
+// complex numbers over a real type R (double for c128, float for c64)
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Cx {
+    R re, im;
+};
+
+template <typename R> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+template <typename R>
+__device__ __forceinline__ Cx<R> cx(R re, R im) { return Cx<R>{re, im}; }
+
+template <typename R>
+__device__ __forceinline__ Cx<R> operator+(Cx<R> a, Cx<R> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a, Cx<R> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a) { return {-a.re, -a.im}; }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator*(Cx<R> a, Cx<R> b) {
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> scale(Cx<R> a, R s) { return {a.re * s, a.im * s}; }
+// i * h * a for real h: (-h a.im, h a.re)
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_ih(R h, Cx<R> a) { return {-h * a.im, h * a.re}; }
+
+// 1/z as conj(z)/|z|^2.  The scalar division is the compiler's IEEE division.
+template <typename R>
+__device__ __forceinline__ Cx<R> crecip(Cx<R> z) {
+    R inv = R(1) / (z.re * z.re + z.im * z.im);
+    return {z.re * inv, -z.im * inv};
+}
+
+template <typename R>
+__device__ __forceinline__ Cx<R> ld(const Cx<R>* p) {
+    typename Vec2<R>::type v = *reinterpret_cast<const typename Vec2<R>::type*>(p);
+    return {v.x, v.y};
+}
+template <typename R>
+__device__ __forceinline__ void st(Cx<R>* p, Cx<R> a) {
+    typename Vec2<R>::type v;
+    v.x = a.re;
+    v.y = a.im;
+    *reinterpret_cast<typename Vec2<R>::type*>(p) = v;
+}
+
+// ---------------------------------------------------------------------------
+// host-side status plumbing
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+int check_launch(const char* what);
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+}  // namespace ion

@@ -1,0 +1,122 @@
+// Whole-mesh norm and inner products: QuantumMesh.inner_product / norm
+// (ionization/mesh/meshes.py:195-217) feeding the Norm and InnerProducts
+// datastores (ionization/mesh/data.py:189-260).
+//
+// Stage 1: a grid of 2 x 152 CTAs (one wave on GB300) accumulates FP64
+// partial sums of |g|^2 and conj(s) g per CTA (grid-stride, coalesced loads).
+// Stage 2: one CTA adds the per-CTA partials with Neumaier compensation and
+// applies the inner-product multiplier.
+#include "ion_common.cuh"
+
+namespace ion {
+
+constexpr int RED_BLOCKS = 304;
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double block_reduce(double v, double* sh) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(RED_THREADS) reduce_stage1(int64_t M, const Cx<R>* g, int ns,
+                                                             const Cx<double>* states, double* part) {
+    __shared__ double sh[32];
+    const int nq = 1 + 2 * ns;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    double acc = 0.0;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < M; k += stride) {
+        const Cx<R> x = ld(g + k);
+        acc += double(x.re) * double(x.re) + double(x.im) * double(x.im);
+    }
+    double r = block_reduce(acc, sh);
+    if (threadIdx.x == 0) part[int64_t(blockIdx.x) * nq] = r;
+    for (int s = 0; s < ns; ++s) {
+        const Cx<double>* sv = states + int64_t(s) * M;
+        double re = 0.0, im = 0.0;
+        for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < M; k += stride) {
+            const Cx<R> x = ld(g + k);
+            const Cx<double> a = ld(sv + k);
+            re += a.re * double(x.re) + a.im * double(x.im);  // conj(a) * x
+            im += a.re * double(x.im) - a.im * double(x.re);
+        }
+        const double tr = block_reduce(re, sh);
+        const double ti = block_reduce(im, sh);
+        if (threadIdx.x == 0) {
+            part[int64_t(blockIdx.x) * nq + 1 + 2 * s] = tr;
+            part[int64_t(blockIdx.x) * nq + 2 + 2 * s] = ti;
+        }
+    }
+}
+
+__global__ void reduce_stage2(int nblocks, int ns, const double* part, double weight, double* out_norm,
+                              double* out_ip) {
+    const int nq = 1 + 2 * ns;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double sum = 0.0, comp = 0.0;
+        for (int b = 0; b < nblocks; ++b) {
+            const double v = part[int64_t(b) * nq + q];
+            const double t = sum + v;
+            comp += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+            sum = t;
+        }
+        sum = (sum + comp) * weight;
+        if (q == 0) {
+            if (out_norm) *out_norm = sum;
+        } else if (out_ip) {
+            out_ip[q - 1] = sum;
+        }
+    }
+}
+
+template <typename R>
+static int reduce_impl(int64_t M, const void* g, int32_t ns, const void* states, double weight,
+                       double* out_norm, double* out_ip, void* partials, void* stream) {
+    if (M < 1 || !g || ns < 0 || (ns > 0 && (!states || !out_ip)) || !partials) {
+        set_error("ion_reduce: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t s = as_stream(stream);
+    int blocks = int((M + RED_THREADS - 1) / RED_THREADS);
+    if (blocks > RED_BLOCKS) blocks = RED_BLOCKS;
+    reduce_stage1<R><<<blocks, RED_THREADS, 0, s>>>(M, static_cast<const Cx<R>*>(g), ns,
+                                                    static_cast<const Cx<double>*>(states),
+                                                    static_cast<double*>(partials));
+    if (int e = check_launch("reduce_stage1")) return e;
+    reduce_stage2<<<1, 64, 0, s>>>(blocks, ns, static_cast<const double*>(partials), weight, out_norm, out_ip);
+    return check_launch("reduce_stage2");
+}
+
+}  // namespace ion
+
+using namespace ion;
+
+extern "C" {
+int64_t ion_reduce_scratch_bytes(int64_t M, int32_t n_states) {
+    (void)M;
+    return int64_t(RED_BLOCKS) * (1 + 2 * int64_t(n_states < 0 ? 0 : n_states)) * int64_t(sizeof(double));
+}
+int ion_reduce_c128(int64_t M, const void* g, int32_t n_states, const void* states, double weight,
+                    double* out_norm, double* out_ip, void* partials, void* stream) {
+    return reduce_impl<double>(M, g, n_states, states, weight, out_norm, out_ip, partials, stream);
+}
+int ion_reduce_c64(int64_t M, const void* g, int32_t n_states, const void* states, double weight,
+                   double* out_norm, double* out_ip, void* partials, void* stream) {
+    return reduce_impl<float>(M, g, n_states, states, weight, out_norm, out_ip, partials, stream);
+}
+}

@@ -1,0 +1,34 @@
+"""Mesh time-evolution API (same names as ionization.mesh)."""
+
+from .data import (  # noqa: F401
+    DATA_NAME_TO_DATASTORE_TYPE,
+    DEFAULT_DATASTORE_TYPES,
+    Data,
+    Datastore,
+    Fields,
+    InnerProducts,
+    Norm,
+)
+from .evolution_methods import AlternatingDirectionImplicit, EvolutionMethod, SplitInteractionOperator  # noqa: F401
+from .mesh_operators import (  # noqa: F401
+    CylindricalSliceLengthGaugeOperators,
+    DotOperator,
+    KineticEnergyDerivation,
+    LineLengthGaugeOperators,
+    MeshOperator,
+    MeshOperators,
+    SphericalHarmonicLengthGaugeOperators,
+    SumOfOperators,
+    TDMAOperator,
+    add_to_diagonal_sparse_matrix_diagonal,
+    apply_operators_sequentially,
+)
+from .meshes import CylindricalSliceMesh, LineMesh, QuantumMesh, SphericalHarmonicMesh, WrappingDirection  # noqa: F401
+from .sims import (  # noqa: F401
+    CylindricalSliceSpecification,
+    LineSpecification,
+    MeshSimulation,
+    MeshSpecification,
+    SphericalHarmonicSimulation,
+    SphericalHarmonicSpecification,
+)

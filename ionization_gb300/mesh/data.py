@@ -1,0 +1,156 @@
+"""Datastores (ionization/mesh/data.py:14-275): Fields, Norm, InnerProducts.
+
+Norm and InnerProducts are filled from the FP64 device reductions made at the
+data times of the run (fused into the step kernels, or a reduction kernel at
+the data time); ``Fields`` is evaluated on the host from the pulse.  The
+attribute names on ``sim.data`` are the reference's.
+"""
+
+import numpy as np
+
+from .. import exceptions
+
+
+class Data:
+    def __init__(self, sim):
+        self.sim = sim
+        self.times = sim.data_times
+
+    def __getattr__(self, item):
+        if item.startswith("__") and item.endswith("__"):
+            raise AttributeError(item)
+        ds = DATA_NAME_TO_DATASTORE_TYPE.get(item)
+        if ds is None:
+            raise exceptions.UnknownData(f"Couldn't find any data named '{item}' on {self.sim}.")
+        raise exceptions.MissingDatastore(
+            f"Couldn't get data '{item}' for {self.sim} because it does not include a {ds.__name__} datastore."
+        )
+
+
+DATA_NAME_TO_DATASTORE_TYPE = {}
+
+
+class Datastore:
+    def init(self, sim):
+        self.sim = sim
+        self.spec = sim.spec
+        self.attach()
+
+    def store(self):  # host-side datastores fill at data times
+        pass
+
+    def attach(self):
+        raise NotImplementedError
+
+    def pull(self, norm, ips):
+        """Receive the device reductions (norm[n_data], ips[n_states, n_data])."""
+
+    def __repr__(self):
+        return self.__class__.__name__
+
+
+def link_property_to_data(datastore_type, method):
+    def get(data):
+        try:
+            return getattr(data.sim.datastores_by_type[datastore_type], method.__name__)()
+        except KeyError:
+            raise exceptions.MissingDatastore(
+                f"Couldn't get data {method.__name__} for {data.sim} because it does not include a "
+                f"{datastore_type.__name__} datastore."
+            )
+
+    return property(get)
+
+
+class Fields(Datastore):
+    """E(t) and A(t) = -integral of E (simps over times_to_current, as
+    data.py:161-170 and pulses.py:75-77), evaluated at the data times."""
+
+    def init(self, sim):
+        self.electric_field_amplitude = sim.get_blank_data()
+        self.vector_potential_amplitude = sim.get_blank_data()
+        super().init(sim)
+
+    def attach(self):
+        self.sim.data.electric_field_amplitude = self.electric_field_amplitude
+        self.sim.data.vector_potential_amplitude = self.vector_potential_amplitude
+
+    def pull(self, norm, ips):
+        sim = self.sim
+        ep = self.spec.electric_potential
+        for k, t_index in enumerate(sim.data_indices):
+            if t_index > sim.time_index or not np.isnan(self.electric_field_amplitude[k]) and k > 0:
+                continue
+            t = sim.times[t_index]
+            self.electric_field_amplitude[k] = ep.get_electric_field_amplitude(t)
+            self.vector_potential_amplitude[k] = ep.get_vector_potential_amplitude_numeric(
+                times=sim.times[: t_index + 1]
+            )
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"electric_field_amplitude": Fields, "vector_potential_amplitude": Fields})
+
+
+class Norm(Datastore):
+    def init(self, sim):
+        self.norm = sim.get_blank_data()
+        super().init(sim)
+
+    def attach(self):
+        self.sim.data.norm = self.norm
+
+    def pull(self, norm, ips):
+        self.norm[:] = norm
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"norm": Norm})
+
+
+class InnerProducts(Datastore):
+    def init(self, sim):
+        self.inner_products = {state: sim.get_blank_data(dtype=np.complex128) for state in sim.spec.test_states}
+        super().init(sim)
+
+    def attach(self):
+        self.sim.data.inner_products = self.inner_products
+        self.sim.data.initial_state_inner_product = self.inner_products[self.spec.initial_state]
+
+    def pull(self, norm, ips):
+        for k, state in enumerate(self.spec.test_states):
+            self.inner_products[state][:] = ips[k]
+
+    def state_overlaps(self):
+        return {state: np.abs(ip) ** 2 for state, ip in self.inner_products.items()}
+
+    def initial_state_overlap(self):
+        return np.abs(self.inner_products[self.spec.initial_state]) ** 2
+
+    def bound_state_overlap(self):
+        return sum(o for s, o in self.state_overlaps().items() if s.bound)
+
+    def free_state_overlap(self):
+        return sum(o for s, o in self.state_overlaps().items() if s.free)
+
+    def total_state_overlap(self):
+        return sum(self.state_overlaps().values())
+
+
+Data.state_overlaps = link_property_to_data(InnerProducts, InnerProducts.state_overlaps)
+Data.initial_state_overlap = link_property_to_data(InnerProducts, InnerProducts.initial_state_overlap)
+Data.bound_state_overlap = link_property_to_data(InnerProducts, InnerProducts.bound_state_overlap)
+Data.free_state_overlap = link_property_to_data(InnerProducts, InnerProducts.free_state_overlap)
+Data.total_state_overlap = link_property_to_data(InnerProducts, InnerProducts.total_state_overlap)
+
+DATA_NAME_TO_DATASTORE_TYPE.update(
+    {
+        "inner_products": InnerProducts,
+        "initial_state_inner_product": InnerProducts,
+        "state_overlaps": InnerProducts,
+        "initial_state_overlap": InnerProducts,
+        "bound_state_overlap": InnerProducts,
+        "free_state_overlap": InnerProducts,
+        "total_state_overlap": InnerProducts,
+    }
+)
+
+DEFAULT_DATASTORE_TYPES = (Fields, Norm, InnerProducts)

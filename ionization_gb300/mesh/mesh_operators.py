@@ -1,0 +1,305 @@
+"""Discretised Hamiltonians of the mesh path (host FP64 coefficient build).
+
+The classes keep the reference's names and plug-in role
+(ionization/mesh/mesh_operators.py:221-1128): a ``MeshOperators`` instance is
+given to a specification and turns a mesh into operators.  Here their main
+product is the set of FP64 coefficient tables the CUDA kernels consume
+(``device_tables``); the tables are computed with the reference's formulas and
+operation order so that the device sees bit-identical coefficients.  The
+sparse-matrix views (``kinetic_energy``, ``internal_hamiltonian``, ...) are
+kept for inspection and for host-side operator application.
+"""
+
+import numpy as np
+import scipy.sparse as sparse
+
+from .. import core
+from .. import units as u
+
+
+class SimilarityOperatorParity(core.StrEnum):
+    EVEN = "even"
+    ODD = "odd"
+
+
+class KineticEnergyDerivation(core.StrEnum):
+    HAMILTONIAN = "hamiltonian"
+    LAGRANGIAN = "lagrangian"
+
+
+def add_to_diagonal_sparse_matrix_diagonal(dia_matrix, value=1):
+    """mesh_operators.py:30-35."""
+    s = dia_matrix.copy()
+    s.setdiag(s.diagonal() + value)
+    return s
+
+
+class MeshOperator:
+    """A sparse tridiagonal operator with a wrapping direction
+    (mesh_operators.py:45-93).  ``apply`` works on host arrays."""
+
+    def __init__(self, matrix, *, wrapping_direction):
+        self.matrix = matrix
+        self.wrapping_direction = wrapping_direction
+
+    def __repr__(self):
+        return f"{self.__class__.__name__}(wrapping_direction = {self.wrapping_direction})"
+
+    def apply(self, mesh, g, current_wrapping_direction):
+        if current_wrapping_direction != self.wrapping_direction:
+            g = mesh.flatten_mesh(mesh.wrap_vector(g, current_wrapping_direction), self.wrapping_direction)
+        return self._apply(g), self.wrapping_direction
+
+    def _apply(self, g):
+        raise NotImplementedError
+
+
+class DotOperator(MeshOperator):
+    def _apply(self, g):
+        return self.matrix.dot(g)
+
+
+class TDMAOperator(MeshOperator):
+    """Implicit half-step: solved by the GPU Thomas solver (the drop-in for
+    ``cy.tdma``, mesh_operators.py:109-111)."""
+
+    def _apply(self, g):
+        from ..cy import tdma
+
+        return tdma(self.matrix, g)
+
+
+class SumOfOperators:
+    def __init__(self, *operators):
+        self.operators = tuple(operators)
+
+    def apply(self, mesh, g, current_wrapping_direction):
+        if len(self.operators) == 0:
+            return g, current_wrapping_direction
+        result = np.zeros_like(g)
+        for operator in self.operators:
+            r, wrapping = operator.apply(mesh, g, current_wrapping_direction)
+            result += mesh.wrap_vector(r, wrapping)
+        return result, current_wrapping_direction
+
+    def __iter__(self):
+        yield from self.operators
+
+    def __getitem__(self, item):
+        return self.operators[item]
+
+
+def apply_operators_sequentially(mesh, g, operators):
+    """mesh_operators.py:207-218 (host application)."""
+    current = None
+    for operator in operators:
+        g, current = operator.apply(mesh, g, current)
+    return mesh.wrap_vector(g, current)
+
+
+class MeshOperators:
+    gauge = None
+
+    def __repr__(self):
+        return f"{self.__class__.__name__}()"
+
+    def info(self):
+        return self.__class__.__name__
+
+
+def _memo(method):
+    """Per-(operators, mesh) memoisation, like si.utils.memoize on methods."""
+    name = "_memo_" + method.__name__
+
+    def wrapper(self, mesh, *args):
+        cache = mesh.__dict__.setdefault(name, {})
+        key = (id(self),) + args
+        if key not in cache:
+            cache[key] = method(self, mesh, *args)
+        return cache[key]
+
+    wrapper.__name__ = method.__name__
+    wrapper.__doc__ = method.__doc__
+    return wrapper
+
+
+# --------------------------------------------------------------------------
+# line mesh
+# --------------------------------------------------------------------------
+
+
+class LineLengthGaugeOperators(MeshOperators):
+    """mesh_operators.py:304-341."""
+
+    gauge = core.Gauge.LENGTH
+
+    @_memo
+    def device_tables(self, mesh):
+        """(hd, hoff, zq): diagonal of H0 = kinetic + V (mesh_operators.py:309-318,
+        244-269), its off-diagonal, and the interaction per unit field
+        -z * test_charge (pulses.py:37-56)."""
+        spec = mesh.spec
+        prefactor = -(u.hbar ** 2) / (2 * spec.test_mass * (mesh.delta_z ** 2))
+        diag = -2 * prefactor * np.ones(len(mesh.z_mesh), dtype=np.complex128)
+        off = prefactor * np.ones(len(mesh.z_mesh) - 1, dtype=np.complex128)
+        V = spec.internal_potential(r=mesh.r_mesh, z=mesh.z_mesh, test_charge=spec.test_charge)
+        hd = (diag + 1.0 * V).real.copy()
+        zq = -mesh.z_mesh * spec.test_charge
+        return hd, off.real.copy(), np.asarray(zq, dtype=np.float64)
+
+    @_memo
+    def internal_hamiltonian(self, mesh):
+        hd, hoff, _ = self.device_tables(mesh)
+        m = sparse.diags((hoff.astype(np.complex128), hd.astype(np.complex128), hoff.astype(np.complex128)),
+                         offsets=(-1, 0, 1))
+        return SumOfOperators(DotOperator(m, wrapping_direction=None))
+
+    def interaction_hamiltonian(self, mesh):
+        epot = mesh.spec.electric_potential(t=mesh.sim.time, z=mesh.z_mesh, test_charge=mesh.spec.test_charge)
+        return SumOfOperators(DotOperator(sparse.diags((epot,), offsets=(0,)), wrapping_direction=None))
+
+    def total_hamiltonian(self, mesh):
+        internal = self.internal_hamiltonian(mesh).operators[0]
+        interaction = self.interaction_hamiltonian(mesh).operators[0]
+        return SumOfOperators(
+            DotOperator(
+                add_to_diagonal_sparse_matrix_diagonal(internal.matrix, value=1.0 * interaction.matrix.diagonal()),
+                wrapping_direction=None,
+            )
+        )
+
+
+# --------------------------------------------------------------------------
+# spherical-harmonic mesh
+# --------------------------------------------------------------------------
+
+
+class SphericalHarmonicLengthGaugeOperators(MeshOperators):
+    """mesh_operators.py:815-1080.  Only the Lagrangian kinetic energy has a
+    device path (the reference default)."""
+
+    gauge = core.Gauge.LENGTH
+
+    def __init__(
+        self,
+        kinetic_energy_derivation=KineticEnergyDerivation.LAGRANGIAN,
+        hydrogen_zero_angular_momentum_correction: bool = True,
+    ):
+        self.kinetic_energy_derivation = KineticEnergyDerivation(kinetic_energy_derivation)
+        self.hydrogen_zero_angular_momentum_correction = hydrogen_zero_angular_momentum_correction
+
+    @staticmethod
+    def alpha(j):
+        x = (j ** 2) + (2 * j)
+        return (x + 1) / (x + 0.75)
+
+    @staticmethod
+    def beta(j):
+        x = 2 * (j ** 2) + (2 * j)
+        return (x + 1) / (x + 0.5)
+
+    @staticmethod
+    def c_l(l):
+        return (l + 1) / np.sqrt(((2 * l) + 1) * ((2 * l) + 3))
+
+    @_memo
+    def device_tables(self, mesh):
+        """Radial Hamiltonian (kinetic_energy_from_lagrangian + internal
+        potential, mesh_operators.py:889-928 and 244-269) and the l-coupling
+        factors (interaction_hamiltonian_matrices_without_field, :988-1005).
+
+        Returns a dict with hd [L*Nr] (C order), hoff [Nr-1], rq [Nr], cl [L]
+        and the FP64 pieces of the diagonal used by the complex64 path:
+        kinv [Nr] (= beta(j) (-2p) + V(r_j)), cent [Nr] and corr0."""
+        if self.kinetic_energy_derivation != KineticEnergyDerivation.LAGRANGIAN:
+            from ..exceptions import UnsupportedMesh
+
+            raise UnsupportedMesh("only the Lagrangian kinetic energy has a device path")
+        spec = mesh.spec
+        nr, L = spec.r_points, spec.l_bound
+        M = nr * L
+        mu = u.electron_mass_reduced
+        p = -(u.hbar ** 2) / (2 * mu * (mesh.delta_r ** 2))
+        j = np.arange(M) % nr
+        diag = self.beta(j).astype(np.complex128)
+        corr = 0.0
+        if self.hydrogen_zero_angular_momentum_correction:
+            dr = mesh.delta_r / u.bohr_radius
+            corr = dr * (1 + dr) / 8
+            diag[0] += corr
+        kk = np.arange(M - 1)
+        off = np.where((kk + 1) % nr != 0, self.alpha(kk % nr), 0).astype(np.complex128)
+        diag *= -2 * p
+        off *= p
+        l_mesh, r_mesh = mesh.l_mesh, mesh.r_mesh
+        eff = ((u.hbar ** 2) / (2 * mu)) * l_mesh * (l_mesh + 1) / (r_mesh ** 2)
+        diag += eff.flatten("C")
+        V = spec.internal_potential(r=r_mesh, test_charge=spec.test_charge)
+        hd = (diag + 1.0 * np.asarray(V).flatten("C")).real.copy()
+        hoff = off.real[: nr - 1].copy()
+        rq = -spec.test_charge * mesh.r
+        cl = self.c_l(np.arange(L))
+        beta_r = self.beta(np.arange(nr)).astype(np.float64)
+        V_r = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge), dtype=np.float64)
+        kinv = beta_r * (-2 * p) + V_r
+        cent = ((u.hbar ** 2) / (2 * mu)) / (mesh.r ** 2)
+        corr0 = (beta_r[0] + corr) * (-2 * p) - beta_r[0] * (-2 * p)
+        return dict(hd=hd, hoff=hoff, rq=np.asarray(rq, dtype=np.float64), cl=cl, kinv=kinv, cent=cent,
+                    corr0=float(corr0))
+
+    @_memo
+    def internal_hamiltonian(self, mesh):
+        t = self.device_tables(mesh)
+        nr, L = mesh.spec.r_points, mesh.spec.l_bound
+        off = np.zeros(nr * L - 1)
+        for l in range(L):
+            off[l * nr: l * nr + nr - 1] = t["hoff"]
+        m = sparse.diags((off.astype(np.complex128), t["hd"].astype(np.complex128), off.astype(np.complex128)),
+                         offsets=(-1, 0, 1))
+        return SumOfOperators(DotOperator(m, wrapping_direction="r"))
+
+    def interaction_hamiltonian(self, mesh):
+        t = self.device_tables(mesh)
+        L = mesh.spec.l_bound
+        efield = mesh.spec.electric_potential.get_electric_field_amplitude(mesh.sim.time + (mesh.spec.time_step / 2))
+        rF = mesh.r_mesh.flatten("F")[:-1]
+        kk = np.arange(len(rF))
+        off = np.where((kk + 1) % L != 0, self.c_l(kk % L), 0) * (-mesh.spec.test_charge * rF)
+        m = sparse.diags((off * efield, np.zeros(len(rF) + 1), off * efield), offsets=(-1, 0, 1))
+        return SumOfOperators(DotOperator(m, wrapping_direction="l"))
+
+
+# --------------------------------------------------------------------------
+# cylindrical slice mesh
+# --------------------------------------------------------------------------
+
+
+class CylindricalSliceLengthGaugeOperators(MeshOperators):
+    """mesh_operators.py:550-640."""
+
+    gauge = core.Gauge.LENGTH
+
+    @_memo
+    def device_tables(self, mesh):
+        """Diagonals of the internal H_z and H_rho (each with half of V,
+        mesh_operators.py:244-269) in C order of the (z, rho) mesh, their
+        off-diagonals, and zq = -z * test_charge."""
+        spec = mesh.spec
+        nz, nr = spec.z_points, spec.rho_points
+        M = nz * nr
+        m = spec.test_mass
+        pz = -(u.hbar ** 2) / (2 * m * (mesh.delta_z ** 2))
+        prho = -(u.hbar ** 2) / (2 * m * (mesh.delta_rho ** 2))
+        z_diag = pz * (-2) * np.ones(M, dtype=np.complex128)
+        rho_diag = prho * (-2) * np.ones(M, dtype=np.complex128)
+        jj = np.arange(1, nr)
+        cj = jj / np.sqrt((jj ** 2) - 0.25)
+        hr_off = (cj.astype(np.complex128) * prho).real.copy()
+        hz_off = (pz * np.ones(nz - 1, dtype=np.complex128)).real.copy()
+        V = spec.internal_potential(r=mesh.r_mesh, z=mesh.z_mesh, test_charge=spec.test_charge)
+        pre = 1 / 2
+        hz_d_F = (z_diag + pre * np.asarray(V).flatten("F")).real
+        hz_d = np.reshape(hz_d_F, (nz, nr), "F").flatten("C")
+        hr_d = (rho_diag + pre * np.asarray(V).flatten("C")).real.copy()
+        zq = -mesh.z * spec.test_charge
+        return dict(hz_d=hz_d, hz_off=hz_off, hr_d=hr_d, hr_off=hr_off, zq=np.asarray(zq, dtype=np.float64))

@@ -1,0 +1,462 @@
+"""Meshes: grids, the device-resident wavefunction ``g`` and data reductions.
+
+Grids, state projection and inner-product conventions follow
+ionization/mesh/meshes.py (LineMesh :263-341, CylindricalSliceMesh :509-607,
+SphericalHarmonicMesh :985-1136).  The wavefunction lives on the GPU between
+steps; ``mesh.g`` is a host copy made on access (and uploaded on assignment),
+so datastores and user code see the reference's array shapes:
+line (z_points,), spherical harmonic (l_bound, r_points), cylindrical
+(z_points, rho_points).
+"""
+
+from typing import Optional
+
+import numpy as np
+import torch
+
+from .. import _device as dev
+from .. import _native as nat
+from .. import core, exceptions, states
+from .. import units as u
+from . import evolution_methods as em
+from . import mesh_operators as mo
+
+
+class WrappingDirection(core.StrEnum):
+    X = "x"
+    Y = "y"
+    Z = "z"
+    RHO = "rho"
+    CHI = "chi"
+    THETA = "theta"
+    R = "r"
+    L = "l"
+
+
+class QuantumMesh:
+    """Base mesh.  Subclasses set the grid, ``mesh_shape``, ``inner_product_multiplier``,
+    ``g_factor`` and build their device state in ``_init_device``."""
+
+    fused_data = True  # data reductions happen inside the step kernels
+
+    def __init__(self, sim):
+        self.sim = sim
+        self.spec = sim.spec
+        self.operators = self.spec.operators
+        self.precision = core.Precision(getattr(self.spec, "precision", core.Precision.C128))
+        self.inner_product_multiplier = None
+
+    # ---- layout helpers (meshes.py:117-133) ----
+    def wrapping_direction_to_order(self, wrapping_direction) -> Optional[str]:
+        return None
+
+    def flatten_mesh(self, mesh, flatten_along):
+        order = self.wrapping_direction_to_order(flatten_along)
+        return mesh if order is None else mesh.flatten(order)
+
+    def wrap_vector(self, vector, wrap_along):
+        order = self.wrapping_direction_to_order(wrap_along)
+        return vector if order is None else np.reshape(vector, self.mesh_shape, order)
+
+    # ---- wavefunction ----
+    @property
+    def g(self) -> np.ndarray:
+        return self._psi_device().cpu().numpy().astype(np.complex128).reshape(self.mesh_shape)
+
+    @g.setter
+    def g(self, value):
+        d = self._psi_device()
+        d.copy_(torch.from_numpy(np.ascontiguousarray(np.asarray(value, dtype=np.complex128).reshape(d.shape))).to(
+            d.device, d.dtype))
+
+    @property
+    def psi(self):
+        return self.g / self.g_factor
+
+    @property
+    def g2(self):
+        return np.abs(self.g) ** 2
+
+    @property
+    def psi2(self):
+        return np.abs(self.psi) ** 2
+
+    # ---- states and inner products (meshes.py:135-217) ----
+    def state_to_g(self, state_or_mesh):
+        if state_or_mesh is None:
+            return self.g
+        if isinstance(state_or_mesh, states.QuantumState):
+            return self.get_g_for_state(state_or_mesh)
+        return state_or_mesh
+
+    def inner_product(self, a=None, b=None):
+        return np.sum(np.conj(self.state_to_g(a)) * self.state_to_g(b)) * self.inner_product_multiplier
+
+    def state_overlap(self, a=None, b=None):
+        return np.abs(self.inner_product(a, b)) ** 2
+
+    def norm(self, state=None):
+        return self.inner_product(state, state).real
+
+    # ---- stepping ----
+    def _method_supported(self):
+        raise NotImplementedError
+
+    def _device_evolve(self, method, time_step):
+        """One step through the device path; ``time_step`` replaces the
+        tabulated step of the current time index if it differs."""
+        t = self.sim.time_index
+        tau = time_step / (2 * u.hbar)
+        self._set_tau(t, tau)
+        self._evolve_steps(1)
+        return self._psi_device()
+
+    def evolve(self, time_step):
+        """QuantumMesh.evolve (meshes.py:251-257): one step then the mask."""
+        self.spec.evolution_method.evolve(self, None, time_step)
+
+    def _set_tau(self, t_now, tau):
+        if self._tau_host[t_now] != tau:
+            self._tau_host[t_now] = tau
+            self._tau_dev()[t_now] = tau
+
+
+# ==========================================================================
+# line
+# ==========================================================================
+
+
+class LineMesh(QuantumMesh):
+    mesh_storage_method = ("z",)
+
+    def __init__(self, sim):
+        super().__init__(sim)
+        self.z_mesh = np.linspace(-self.spec.z_bound, self.spec.z_bound, self.spec.z_points)
+        self.delta_z = np.abs(self.z_mesh[1] - self.z_mesh[0])
+        self.z_center_index = int(np.argmin(np.abs(self.z_mesh)))
+        self.mesh_points = len(self.z_mesh)
+        self.mesh_shape = (self.mesh_points,)
+        self.inner_product_multiplier = self.delta_z
+        self.g_factor = 1
+        self._state_g_cache = {}
+        self._init_device()
+
+    @property
+    def z(self):
+        return self.z_mesh
+
+    @property
+    def r(self):
+        return self.z
+
+    @property
+    def r_mesh(self):
+        return self.z_mesh
+
+    def get_g_for_state(self, state):
+        """LineMesh.get_g_for_state (meshes.py:327-341)."""
+        if state in self._state_g_cache:
+            return self._state_g_cache[state]
+        g = state(self.z_mesh)
+        g = g / np.sqrt(np.sum(np.conj(g) * g).real * self.inner_product_multiplier)
+        g = g * state.amplitude
+        self._state_g_cache[state] = g
+        return g
+
+    def _init_device(self):
+        spec, sim = self.spec, self.sim
+        method = spec.evolution_method
+        if not isinstance(self.operators, mo.LineLengthGaugeOperators):
+            raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on LineMesh")
+        if isinstance(method, em.AlternatingDirectionImplicit):
+            kind = nat.ION_LINE_ADI
+        elif isinstance(method, em.SplitInteractionOperator):
+            kind = nat.ION_LINE_SPLIT
+        else:
+            raise exceptions.UnsupportedMesh(f"{type(method).__name__} has no device path on LineMesh")
+        hd, hoff, zq = self.operators.device_tables(self)
+        mask = spec.mask(r=self.r_mesh)
+        mask = None if np.isscalar(mask) and mask == 1 else np.broadcast_to(np.asarray(mask, np.float64), (self.mesh_points,))
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
+        test_g = np.array([self.get_g_for_state(s) for s in spec.test_states], dtype=np.complex128).reshape(-1, self.mesh_points)
+        g0 = self.get_g_for_state(spec.initial_state)
+        maxn = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_line_max_n_" + self.precision.value)
+        if self.mesh_points > maxn:
+            raise exceptions.UnsupportedMesh(f"line of {self.mesh_points} points exceeds the device limit {maxn}")
+        self.tables = dev.LineTables(
+            n=self.mesh_points, method=kind, hd=hd, hoff=hoff, zq=zq, mask=mask, tau=self._tau_host.copy(),
+            efield=efield, state_g=test_g, weight=self.inner_product_multiplier, g0=g0, t0=0,
+            t_final=len(times) - 1, store_every=spec.store_data_every,
+        )
+        if getattr(spec, "host_only", False):
+            return
+        self._dsim = dev.LineDeviceSim(self.tables, self.precision)
+        self._batch = dev.LineBatch(self.precision, [self._dsim])
+
+    def _psi_device(self):
+        return self._dsim.g
+
+    def _tau_dev(self):
+        return self._dsim.d_tau
+
+    def _evolve_steps(self, n):
+        self._batch.run(n)
+
+    def _reduce_current(self):
+        self._batch.reduce()
+
+    def _pull_data(self):
+        return self._dsim.data()
+
+
+# ==========================================================================
+# spherical harmonic
+# ==========================================================================
+
+
+class SphericalHarmonicMesh(QuantumMesh):
+    mesh_storage_method = ("l", "r")
+
+    def __init__(self, sim):
+        super().__init__(sim)
+        self.r = np.linspace(0, self.spec.r_bound, self.spec.r_points)
+        self.delta_r = self.r[1] - self.r[0]
+        self.r = self.r + self.delta_r / 2
+        self.r_max = np.max(self.r)
+        self.inner_product_multiplier = self.delta_r
+        self.l = np.array(range(self.spec.l_bound), dtype=int)
+        self.mesh_points = len(self.r) * len(self.l)
+        self.l_mesh, self.r_mesh = np.meshgrid(self.l, self.r, indexing="ij")
+        self.mesh_shape = np.shape(self.r_mesh)
+        self._radial_cache = {}
+        self._init_device()
+
+    @property
+    def g_factor(self):
+        return self.r
+
+    def wrapping_direction_to_order(self, wrapping_direction):
+        if wrapping_direction is None:
+            return None
+        if wrapping_direction == WrappingDirection.L:
+            return "F"
+        if wrapping_direction == WrappingDirection.R:
+            return "C"
+        raise ValueError(f"{wrapping_direction} is not a valid specifier for flatten_mesh (valid specifiers: 'l', 'r')")
+
+    def get_radial_g_for_state(self, state):
+        """meshes.py:1089-1097: R(r) * r normalised on the radial grid."""
+        if state in self._radial_cache:
+            return self._radial_cache[state]
+        g = state.radial_function(self.r) * self.g_factor
+        g = g / np.sqrt(np.sum(np.conj(g) * g).real * self.inner_product_multiplier)
+        g = g * state.amplitude
+        g = np.asarray(g, dtype=np.complex128)
+        self._radial_cache[state] = g
+        return g
+
+    def get_g_for_state(self, state):
+        """meshes.py:1066-1087."""
+        if not all(hasattr(s, "radial_function") for s in state):
+            raise NotImplementedError(
+                "States with non-definite angular momentum components are not currently supported by SphericalHarmonicMesh"
+            )
+        g = np.zeros(self.mesh_shape, dtype=np.complex128)
+        for s in state:
+            g[s.l, :] += self.get_radial_g_for_state(s)
+        return g
+
+    def inner_product(self, a=None, b=None):
+        """The per-l shortcut of meshes.py:1099-1131 when ``a`` is a state and
+        ``b`` the current wavefunction."""
+        if isinstance(a, states.QuantumState) and all(hasattr(s, "radial_function") for s in a) and b is None:
+            g = self.g
+            ip = 0
+            for s in a:
+                ip += np.sum(np.conj(self.get_radial_g_for_state(s)) * g[s.l, :])
+            return ip * self.inner_product_multiplier
+        return super().inner_product(a, b)
+
+    def norm_by_l(self, state=None):
+        g = self.state_to_g(state)
+        return np.abs(np.sum(np.conj(g) * g, axis=1) * self.delta_r)
+
+    def _init_device(self):
+        spec, sim = self.spec, self.sim
+        if not isinstance(self.operators, mo.SphericalHarmonicLengthGaugeOperators):
+            raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on SphericalHarmonicMesh")
+        if not isinstance(spec.evolution_method, em.SplitInteractionOperator):
+            raise exceptions.UnsupportedMesh(
+                f"{type(spec.evolution_method).__name__} has no device path on SphericalHarmonicMesh"
+            )
+        maxr = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_sh_max_n_r_" + self.precision.value)
+        if spec.r_points > maxr:
+            raise exceptions.UnsupportedMesh(f"r_points {spec.r_points} exceeds the device limit {maxr}")
+        tb = self.operators.device_tables(self)
+        mask = spec.mask(r=self.r)
+        mask = None if np.isscalar(mask) and mask == 1 else np.asarray(mask, dtype=np.float64) * np.ones(len(self.r))
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(
+            spec.electric_potential.get_electric_field_amplitude(times[1:] + (spec.time_step / 2)), np.float64
+        ) * np.ones(len(times) - 1)
+        sl, sg = [], []
+        for s in spec.test_states:
+            comps = list(s)
+            if len(comps) != 1:
+                raise exceptions.UnsupportedMesh("device inner products need single-l test states")
+            sl.append(comps[0].l)
+            sg.append(self.get_radial_g_for_state(comps[0]) * 1)
+        g0 = self.get_g_for_state(spec.initial_state)
+        self.tables = dev.ShTables(
+            n_r=spec.r_points, n_l=spec.l_bound, hd=tb["hd"], hoff=tb["hoff"], rq=tb["rq"], cl=tb["cl"], mask=mask,
+            tau=self._tau_host.copy(), efield=efield, kinv=tb["kinv"], cent=tb["cent"], corr0=tb["corr0"],
+            state_l=sl, state_g=np.array(sg, dtype=np.complex128).reshape(len(sl), spec.r_points),
+            weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
+            store_every=spec.store_data_every,
+        )
+        if getattr(spec, "host_only", False):
+            return
+        self._dsim = dev.ShDeviceSim(self.tables, self.precision)
+        self._batch = dev.ShBatch(self.precision, [self._dsim])
+
+    def _psi_device(self):
+        return self._dsim.g
+
+    def _tau_dev(self):
+        return self._dsim.d_tau
+
+    def _evolve_steps(self, n):
+        self._batch.run(n)
+
+    def _reduce_current(self):
+        self._batch.reduce()
+
+    def _pull_data(self):
+        return self._dsim.data()
+
+
+# ==========================================================================
+# cylindrical slice
+# ==========================================================================
+
+
+class CylindricalSliceMesh(QuantumMesh):
+    mesh_storage_method = ("z", "rho")
+    fused_data = False
+
+    def __init__(self, sim):
+        super().__init__(sim)
+        self.z = np.linspace(-self.spec.z_bound, self.spec.z_bound, self.spec.z_points)
+        self.rho = np.delete(np.linspace(0, self.spec.rho_bound, self.spec.rho_points + 1), 0)
+        self.delta_z = self.z[1] - self.z[0]
+        self.delta_rho = self.rho[1] - self.rho[0]
+        self.inner_product_multiplier = self.delta_z * self.delta_rho
+        self.rho = self.rho - self.delta_rho / 2
+        self.z_center_index = int(self.spec.z_points // 2)
+        self.z_mesh, self.rho_mesh = np.meshgrid(self.z, self.rho, indexing="ij")
+        self.r_mesh = np.sqrt((self.z_mesh ** 2) + (self.rho_mesh ** 2))
+        self.mesh_points = len(self.z) * len(self.rho)
+        self.mesh_shape = np.shape(self.r_mesh)
+        self._state_g_cache = {}
+        self._init_device()
+
+    @property
+    def g_factor(self):
+        return np.sqrt(u.twopi * self.rho_mesh)
+
+    @property
+    def theta_mesh(self):
+        return np.arccos(self.z_mesh / self.r_mesh)
+
+    def wrapping_direction_to_order(self, wrapping_direction):
+        if wrapping_direction is None:
+            return None
+        if wrapping_direction == WrappingDirection.Z:
+            return "F"
+        if wrapping_direction == WrappingDirection.RHO:
+            return "C"
+        raise ValueError(f"{wrapping_direction} is not a valid specifier for flatten_mesh (valid specifiers: 'z', 'rho')")
+
+    def get_g_for_state(self, state):
+        """meshes.py:601-607."""
+        if state in self._state_g_cache:
+            return self._state_g_cache[state]
+        g = self.g_factor * state(self.r_mesh, self.theta_mesh, 0)
+        g = g / np.sqrt(np.sum(np.conj(g) * g).real * self.inner_product_multiplier)
+        g = g * state.amplitude
+        g = np.asarray(g, dtype=np.complex128)
+        self._state_g_cache[state] = g
+        return g
+
+    def _init_device(self):
+        spec, sim = self.spec, self.sim
+        if not isinstance(self.operators, mo.CylindricalSliceLengthGaugeOperators):
+            raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on CylindricalSliceMesh")
+        if not isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
+            raise exceptions.UnsupportedMesh(
+                f"{type(spec.evolution_method).__name__} has no device path on CylindricalSliceMesh"
+            )
+        if self.precision != core.Precision.C128:
+            raise exceptions.UnsupportedMesh("the cylindrical device path is complex128")
+        tb = self.operators.device_tables(self)
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
+        mask = spec.mask(r=self.r_mesh)
+        mask = None if np.isscalar(mask) and mask == 1 else np.asarray(mask, np.float64) * np.ones(self.mesh_shape)
+        g0 = self.get_g_for_state(spec.initial_state)
+        test_g = np.array([self.get_g_for_state(s).reshape(-1) for s in spec.test_states], dtype=np.complex128)
+        self.tables = dict(tb, mask=mask, tau=self._tau_host.copy(), efield=efield, g0=g0, state_g=test_g)
+        if getattr(spec, "host_only", False):
+            return
+        f64 = np.float64
+        self._d = dict(
+            hz_d=dev.to_dev(tb["hz_d"], f64), hz_off=dev.to_dev(tb["hz_off"], f64),
+            hr_d=dev.to_dev(tb["hr_d"], f64), hr_off=dev.to_dev(tb["hr_off"], f64),
+            zq=dev.to_dev(tb["zq"], f64), tau=dev.to_dev(self._tau_host, f64), efield=dev.to_dev(efield, f64),
+            mask=dev.to_dev(mask.reshape(-1), f64) if mask is not None else None,
+        )
+        self._g = dev.to_dev(g0.astype(np.complex128))
+        self._gtmp = torch.empty_like(self._g)
+        cm = nat.CylMesh()
+        cm.n_z, cm.n_rho = spec.z_points, spec.rho_points
+        for k in ("hz_d", "hz_off", "hr_d", "hr_off", "zq", "mask", "tau", "efield"):
+            setattr(cm, k, dev.ptr(self._d[k]))
+        self._cm = cm
+        self._reducer = dev.Reducer(self.mesh_points, test_g, self.inner_product_multiplier)
+        self._t = 0
+        self.n_data = dev.n_data_slots(len(times) - 1, spec.store_data_every)
+        self._d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=dev.device())
+        self._d_ip = torch.full((self.n_data, max(len(test_g), 1), 2), float("nan"), dtype=torch.float64,
+                                device=dev.device())
+
+    def _psi_device(self):
+        return self._g
+
+    def _tau_dev(self):
+        return self._d["tau"]
+
+    def _evolve_steps(self, n):
+        nat.call("ion_cyl_adi_run_c128", self._cm, dev.ptr(self._g), dev.ptr(self._gtmp), self._t, int(n),
+                 dev.stream_ptr())
+        self._t += int(n)
+
+    def _reduce_current(self):
+        tf = len(self.sim.times) - 1
+        slot = dev.data_slot(self._t, tf, self.spec.store_data_every)
+        self._reducer(self._g, self._d_norm[slot:slot + 1], self._d_ip[slot])
+
+    def _pull_data(self):
+        norm = self._d_norm.cpu().numpy()
+        ns = len(self.spec.test_states)
+        ip = self._d_ip.cpu().numpy()[:, :ns, :].copy().view(np.complex128)[..., 0]
+        return norm, ip.T.copy()

@@ -1,0 +1,204 @@
+"""Quantum states used as initial and test states (host FP64).
+
+Restates the parts of ionization/states/ the mesh path needs:
+QuantumState (state.py:52-213), Superposition, HydrogenBoundState
+(three_d.py:298-400).  ``GaussianState`` has no reference class; it is the
+user QuantumState subclass the 1D Gaussian workload needs.
+"""
+
+import abc
+from copy import deepcopy
+
+import numpy as np
+import scipy.special as special
+
+from .. import core, exceptions, summables
+from .. import units as u
+
+
+class Eigenvalues(core.StrEnum):
+    DISCRETE = "discrete"
+    CONTINUOUS = "continuous"
+
+
+class Binding(core.StrEnum):
+    BOUND = "bound"
+    FREE = "free"
+
+
+class Derivation(core.StrEnum):
+    ANALYTIC = "analytic"
+    NUMERIC = "numeric"
+    VARIATIONAL = "variational"
+
+
+class QuantumState(summables.Summand, abc.ABC):
+    eigenvalues = None
+    binding = None
+    derivation = None
+
+    def __init__(self, amplitude=1):
+        super().__init__()
+        self.amplitude = amplitude
+        self.summation_class = Superposition
+
+    @property
+    def numeric(self):
+        return self.derivation == Derivation.NUMERIC
+
+    @property
+    def analytic(self):
+        return self.derivation == Derivation.ANALYTIC
+
+    @property
+    def bound(self):
+        return self.binding == Binding.BOUND
+
+    @property
+    def free(self):
+        return self.binding == Binding.FREE
+
+    @property
+    def norm(self):
+        return np.abs(self.amplitude) ** 2
+
+    def __mul__(self, other):
+        new = deepcopy(self)
+        new.amplitude *= other
+        return new
+
+    def __rmul__(self, other):
+        return self * other
+
+    def __truediv__(self, other):
+        return self * (1 / other)
+
+    @property
+    @abc.abstractmethod
+    def tuple(self):
+        raise NotImplementedError
+
+    def __hash__(self):
+        return hash((self.__class__.__name__,) + self.tuple)
+
+    def __eq__(self, other):
+        return isinstance(other, self.__class__) and self.tuple == other.tuple
+
+    def __lt__(self, other):
+        return isinstance(other, self.__class__) and self.tuple < other.tuple
+
+    def __gt__(self, other):
+        return isinstance(other, self.__class__) and self.tuple > other.tuple
+
+    @abc.abstractmethod
+    def __call__(self, *args, **kwargs):
+        raise NotImplementedError
+
+    def __str__(self):
+        return self.ket
+
+    @property
+    def ket(self):
+        return f"|{self.__class__.__name__}>"
+
+
+class Superposition(summables.Sum, QuantumState):
+    container_name = "states"
+
+    def __init__(self, *states):
+        norm = np.sqrt(sum(s.norm for s in states))
+        super().__init__(*(s / norm for s in states), amplitude=1)
+
+    @property
+    def tuple(self):
+        return tuple(sorted(s.tuple for s in self.states))
+
+    def __call__(self, *args, **kwargs):
+        return sum(s(*args, **kwargs) for s in self.states)
+
+
+class SphericalHarmonicState(QuantumState):
+    def __init__(self, l=0, m=0, amplitude=1):
+        super().__init__(amplitude=amplitude)
+        self.l = l
+        self.m = m
+
+    @property
+    def spherical_harmonic(self):
+        return (self.l, self.m)
+
+    @abc.abstractmethod
+    def radial_function(self, r):
+        raise NotImplementedError
+
+    def __call__(self, r, theta, phi):
+        """amplitude * R(r) * Y_l^m(theta, phi)  (three_d.py:198-203)."""
+        return self.amplitude * self.radial_function(r) * special.sph_harm_y(self.l, self.m, theta, phi)
+
+
+class HydrogenBoundState(SphericalHarmonicState):
+    eigenvalues = Eigenvalues.DISCRETE
+    binding = Binding.BOUND
+    derivation = Derivation.ANALYTIC
+
+    def __init__(self, n=1, l=0, m=0, amplitude=1):
+        if int(n) != n or n < 1:
+            raise exceptions.IllegalQuantumState(f"n ({n}) must be an integer greater than zero")
+        if int(l) != l or not 0 <= l < n:
+            raise exceptions.IllegalQuantumState(
+                f"l ({l}) must be an integer greater than or equal to zero and less than n ({n})"
+            )
+        if int(m) != m or not -l <= m <= l:
+            raise exceptions.IllegalQuantumState(f"|m| (|{m}|) must be an integer less than or equal to l ({l})")
+        self.n = int(n)
+        super().__init__(l=int(l), m=int(m), amplitude=amplitude)
+
+    @property
+    def energy(self):
+        return -u.rydberg / (self.n ** 2)
+
+    @property
+    def tuple(self):
+        return self.n, self.l, self.m
+
+    def __repr__(self):
+        return f"HydrogenBoundState(n = {self.n}, l = {self.l}, m = {self.m}, amplitude = {self.amplitude})"
+
+    @property
+    def ket(self):
+        return f"|{self.n},{self.l},{self.m}>"
+
+    def radial_function(self, r):
+        """Griffiths-normalised radial function (three_d.py:375-391)."""
+        n, l = self.n, self.l
+        normalization = np.sqrt(
+            ((2 / (n * u.bohr_radius)) ** 3)
+            * (special.factorial(n - l - 1) / (2 * n * special.factorial(n + l)))
+        )
+        r_dep = np.exp(-r / (n * u.bohr_radius)) * ((2 * r / (n * u.bohr_radius)) ** l)
+        lag_poly = special.eval_genlaguerre(n - l - 1, (2 * l) + 1, 2 * r / (n * u.bohr_radius))
+        return self.amplitude * normalization * r_dep * lag_poly
+
+
+class GaussianState(QuantumState):
+    """exp(-(z - center)^2 / (2 width^2)), normalised on the mesh when
+    projected (a 1D bound wavepacket; user-state extension)."""
+
+    eigenvalues = Eigenvalues.DISCRETE
+    binding = Binding.BOUND
+    derivation = Derivation.ANALYTIC
+
+    def __init__(self, width=1.0, center=0.0, amplitude=1):
+        self.width = width
+        self.center = center
+        super().__init__(amplitude=amplitude)
+
+    @property
+    def tuple(self):
+        return (self.width, self.center)
+
+    def __call__(self, z):
+        return np.exp(-((z - self.center) ** 2) / (2 * self.width ** 2)).astype(np.complex128)
+
+    def __repr__(self):
+        return f"GaussianState(width = {self.width}, center = {self.center})"

@@ -1,0 +1,428 @@
+"""ORACLE — numpy restatement of the reference's mesh time-evolution path.
+
+Every builder below mirrors one reference function (file:line in its
+docstring) and keeps the reference's data layout: operators are the three
+diagonals of a tridiagonal matrix over the mesh flattened in the operator's
+wrapping order ("C" or "F", ionization/mesh/meshes.py:117-133), explicit
+halves are a dia-matrix product (mesh_operators.py:104-106) and implicit
+halves the Thomas solve of ``tdma.c`` on the whole flattened vector
+(mesh_operators.py:109-111), exactly as the reference calls ``cy.tdma``.
+
+Used only by tests/, smoke() and bench.py's CPU-baseline legs.
+"""
+
+import math
+
+import numpy as np
+
+from . import physics as ph
+from ._lib import tdma
+
+
+# --------------------------------------------------------------------------
+# generic pieces
+# --------------------------------------------------------------------------
+
+def get_times(time_initial, time_final, time_step):
+    """MeshSimulation.get_times, ionization/mesh/sims.py:198-205."""
+    total_time = time_final - time_initial
+    return np.linspace(time_initial, time_final, int(total_time / time_step) + 1)
+
+
+def data_mask(n_times, store_data_every):
+    """MeshSimulation.__init__ data mask, sims.py:84-90."""
+    idx = np.arange(n_times)
+    mask = np.equal(idx, 0) + np.equal(idx, n_times - 1)
+    if store_data_every >= 1:
+        mask += np.equal(idx % store_data_every, 0)
+    return mask
+
+
+class Tridiag:
+    """A tridiagonal operator over a flattened mesh.
+
+    ``sub[i]`` = A[i+1, i], ``diag[i]`` = A[i, i], ``sup[i]`` = A[i, i+1];
+    ``order`` is the numpy flatten order of its wrapping direction (None for
+    1D meshes)."""
+
+    def __init__(self, sub, diag, sup, order):
+        self.sub, self.diag, self.sup, self.order = sub, diag, sup, order
+
+    def scaled_plus_identity(self, scale):
+        """add_to_diagonal_sparse_matrix_diagonal(scale * M, value=1),
+        mesh_operators.py:30-35 with evolution_methods.py:57-74."""
+        return Tridiag(scale * self.sub, (scale * self.diag) + 1, scale * self.sup, self.order)
+
+
+def dia_matvec(op: Tridiag, x):
+    """y = A x accumulated diagonal by diagonal in the dia_matrix storage order
+    (offsets -1, 0, +1), as DotOperator._apply (mesh_operators.py:104-106)."""
+    y = np.zeros_like(x)
+    y[1:] += op.sub * x[:-1]
+    y += op.diag * x
+    y[:-1] += op.sup * x[1:]
+    return y
+
+
+def _flat(g2d, order):
+    return g2d if order is None else g2d.flatten(order)
+
+
+def _wrap(vec, shape, order):
+    return vec if order is None else np.reshape(vec, shape, order)
+
+
+def apply_explicit(op, g, shape):
+    return _wrap(dia_matvec(op, _flat(g, op.order)), shape, op.order)
+
+
+def apply_implicit(op, g, shape):
+    return _wrap(tdma(op.sub, op.diag, op.sup, _flat(g, op.order)), shape, op.order)
+
+
+def run(stepper, times, store_data_every, max_steps=None):
+    """The data/evolve skeleton of MeshSimulation.run, sims.py:289-333.
+
+    ``stepper`` exposes ``evolve(dt, t_now)``, ``norm()`` and
+    ``inner_products()``.  Returns data-time norms and inner products."""
+    mask = data_mask(len(times), store_data_every)
+    norms, ips, dtimes = [], [], []
+    time_index = 0
+    steps = 0
+    while True:
+        if mask[time_index]:
+            norms.append(stepper.norm())
+            ips.append(stepper.inner_products())
+            dtimes.append(times[time_index])
+        if time_index == len(times) - 1:
+            break
+        if max_steps is not None and steps >= max_steps:
+            break
+        time_index += 1
+        stepper.evolve(times[time_index] - times[time_index - 1], times[time_index])
+        steps += 1
+    return dict(
+        data_times=np.array(dtimes),
+        norm=np.array(norms),
+        inner_products=np.array(ips).T if ips else np.zeros((0, 0)),
+        steps=steps,
+    )
+
+
+# --------------------------------------------------------------------------
+# line mesh (LineMesh + LineLengthGaugeOperators)
+# --------------------------------------------------------------------------
+
+class LineLength:
+    """LineMesh (meshes.py:263-341) with LineLengthGaugeOperators
+    (mesh_operators.py:304-341); ``method`` is "AlternatingDirectionImplicit"
+    (evolution_methods.py:46-77) or "SplitInteractionOperator"
+    (evolution_methods.py:80-123).  The mask is RadialCosineMask evaluated at
+    |z| (both line ends), and the initial state a Gaussian normalised on the
+    mesh."""
+
+    def __init__(self, z_points, z_bound, test_mass, softening_distance, pulse, mask, method,
+                 gaussian_width=1.0):
+        self.z = np.linspace(-z_bound, z_bound, z_points)
+        self.dz = np.abs(self.z[1] - self.z[0])
+        self.shape = (z_points,)
+        self.test_mass = test_mass
+        self.pulse = pulse
+        self.method = method
+        self.mask = (
+            ph.radial_cosine_mask(np.abs(self.z), **mask) if mask is not None else None
+        )
+        p = -(ph.HBAR ** 2) / (2 * test_mass * (self.dz ** 2))
+        diag = -2 * p * np.ones(z_points, dtype=np.complex128)
+        off = p * np.ones(z_points - 1, dtype=np.complex128)
+        V = ph.soft_coulomb(self.z, softening_distance)
+        self.H0 = Tridiag(off, diag + 1.0 * V, off.copy(), None)  # mesh_operators.py:244-269
+        g = ph.gaussian(self.z, gaussian_width)
+        g = g / np.sqrt(self._norm(g))
+        self.g = g
+        self.test_g = [g.copy()]
+
+    def _norm(self, g):
+        return (np.sum(np.conj(g) * g) * self.dz).real
+
+    def norm(self):
+        return self._norm(self.g)
+
+    def inner_products(self):
+        return [np.sum(np.conj(s) * self.g) * self.dz for s in self.test_g]
+
+    def v_int(self, t):
+        """UniformLinearlyPolarizedElectricPotential.__call__, pulses.py:37-56."""
+        return -self.z * ph.ELECTRON_CHARGE * self.pulse.field(t)
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        vint = self.v_int(t_now)  # mesh.sim.time is already t_{n+1}
+        g = self.g
+        if self.method == "AlternatingDirectionImplicit":
+            H = Tridiag(self.H0.sub, self.H0.diag + 1.0 * vint, self.H0.sup, None)
+            g = apply_explicit(H.scaled_plus_identity(-1j * tau), g, self.shape)
+            g = apply_implicit(H.scaled_plus_identity(1j * tau), g, self.shape)
+        else:
+            s = np.exp(-1j * vint * tau)  # mesh_operators.py:329-341
+            g = s * g
+            g = apply_explicit(self.H0.scaled_plus_identity(-1j * tau), g, self.shape)
+            g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
+            g = s * g
+        if self.mask is not None:
+            g = g * self.mask  # meshes.py:256-257
+        self.g = g
+
+
+# --------------------------------------------------------------------------
+# spherical-harmonic mesh, length gauge, split-interaction operator
+# --------------------------------------------------------------------------
+
+def _alpha(j):
+    x = (j ** 2) + (2 * j)
+    return (x + 1) / (x + 0.75)
+
+
+def _beta(j):
+    x = 2 * (j ** 2) + (2 * j)
+    return (x + 1) / (x + 0.5)
+
+
+def _c_l(l):
+    return (l + 1) / np.sqrt(((2 * l) + 1) * ((2 * l) + 3))
+
+
+class SphericalHarmonicSplit:
+    """SphericalHarmonicMesh (meshes.py:985-1136) with
+    SphericalHarmonicLengthGaugeOperators (mesh_operators.py:815-1080,
+    Lagrangian kinetic energy with the hydrogen l=0 correction) and
+    SplitInteractionOperator (evolution_methods.py:80-123)."""
+
+    def __init__(self, r_points, r_bound, l_bound, pulse, mask, test_states, time_step,
+                 initial_state=(1, 0)):
+        r = np.linspace(0, r_bound, r_points)
+        self.dr = r[1] - r[0]
+        self.r = r + self.dr / 2
+        self.Nr, self.L = r_points, l_bound
+        self.shape = (l_bound, r_points)
+        self.M = r_points * l_bound
+        self.pulse = pulse
+        self.time_step = time_step
+        l_mesh, r_mesh = np.meshgrid(np.arange(l_bound), self.r, indexing="ij")
+        self.r_mesh = r_mesh
+        self.mask = ph.radial_cosine_mask(r_mesh, **mask) if mask is not None else None
+
+        # kinetic_energy_from_lagrangian, mesh_operators.py:889-928
+        mu = ph.ELECTRON_MASS_REDUCED
+        p = -(ph.HBAR ** 2) / (2 * mu * (self.dr ** 2))
+        k = np.arange(self.M)
+        j = k % r_points
+        diag = _beta(j).astype(np.complex128)
+        dr_au = self.dr / ph.BOHR_RADIUS
+        diag[0] += dr_au * (1 + dr_au) / 8
+        kk = np.arange(self.M - 1)
+        off = np.where((kk + 1) % r_points != 0, _alpha(kk % r_points), 0).astype(np.complex128)
+        diag *= -2 * p
+        off *= p
+        eff = ((ph.HBAR ** 2) / (2 * mu)) * l_mesh * (l_mesh + 1) / (r_mesh ** 2)
+        diag += eff.flatten("C")
+        V = ph.coulomb(r_mesh)
+        self.H0 = Tridiag(off, diag + 1.0 * V.flatten("C"), off.copy(), "C")
+
+        # interaction_hamiltonian_matrices_without_field, mesh_operators.py:988-1005
+        l_prefactor = -ph.ELECTRON_CHARGE * r_mesh.flatten("F")[:-1]
+        l_off = np.where(
+            (kk + 1) % l_bound != 0, _c_l(kk % l_bound), 0
+        ).astype(np.complex128)
+        l_off *= l_prefactor
+        self.l_off = l_off
+
+        self.test_states = list(test_states)
+        self.radial_g = {}
+        for (n, l) in self.test_states + [tuple(initial_state)]:
+            gs = ph.hydrogen_radial(n, l, self.r) * self.r
+            gs = gs / np.sqrt((np.sum(np.conj(gs) * gs) * self.dr).real)
+            self.radial_g[(n, l)] = gs
+        g = np.zeros(self.shape, dtype=np.complex128)
+        n0, l0 = initial_state
+        g[l0, :] += self.radial_g[(n0, l0)]
+        self.g = g
+        self._cn_cache = {}
+
+    def norm(self):
+        return (np.sum(np.conj(self.g) * self.g) * self.dr).real
+
+    def inner_products(self):
+        """SphericalHarmonicMesh.inner_product shortcut, meshes.py:1118-1129."""
+        return [
+            (0 + np.sum(np.conj(self.radial_g[(n, l)]) * self.g[l, :])) * self.dr
+            for (n, l) in self.test_states
+        ]
+
+    def split_operators(self, tau, efield):
+        """split_interaction_operators, mesh_operators.py:1037-1080."""
+        a = tau * (self.l_off * efield)
+        a_even, a_odd = a[::2], a[1::2]
+        len_a = len(a)
+        even_diag = np.zeros(len_a + 1, dtype=np.complex128)
+        even_off = np.zeros(len_a, dtype=np.complex128)
+        odd_diag = np.zeros(len_a + 1, dtype=np.complex128)
+        odd_off = np.zeros(len_a, dtype=np.complex128)
+        if self.Nr % 2 != 0 and self.L % 2 != 0:
+            even_diag[:-1] = np.cos(a_even).repeat(2)
+            even_diag[-1] = 1
+            even_off[::2] = -1j * np.sin(a_even)
+            odd_diag[0] = 1
+            odd_diag[1:] = np.cos(a_odd).repeat(2)
+            odd_off[1::2] = -1j * np.sin(a_odd)
+        else:
+            even_diag = np.cos(a_even).repeat(2)
+            even_off[::2] = -1j * np.sin(a_even)
+            odd_diag[0] = odd_diag[-1] = 1
+            odd_diag[1:-1] = np.cos(a_odd).repeat(2)
+            odd_off[1::2] = -1j * np.sin(a_odd)
+        even = Tridiag(even_off, even_diag, even_off, "F")
+        odd = Tridiag(odd_off, odd_diag, odd_off, "F")
+        return even, odd
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        efield = self.pulse.field(t_now + (self.time_step / 2))  # mesh_operators.py:1011-1013
+        even, odd = self.split_operators(tau, efield)
+        g = self.g
+        g = apply_explicit(even, g, self.shape)
+        g = apply_explicit(odd, g, self.shape)
+        g = apply_explicit(self.H0.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
+        g = apply_explicit(odd, g, self.shape)
+        g = apply_explicit(even, g, self.shape)
+        if self.mask is not None:
+            g = g * self.mask
+        self.g = g
+
+
+# --------------------------------------------------------------------------
+# cylindrical slice mesh, length gauge, ADI
+# --------------------------------------------------------------------------
+
+class CylindricalSliceADI:
+    """CylindricalSliceMesh (meshes.py:509-607) with
+    CylindricalSliceLengthGaugeOperators (mesh_operators.py:550-640) and
+    AlternatingDirectionImplicit (evolution_methods.py:46-77)."""
+
+    def __init__(self, z_points, z_bound, rho_points, rho_bound, pulse, test_states,
+                 test_mass=ph.ELECTRON_MASS_REDUCED, initial_state=(1, 0)):
+        self.z = np.linspace(-z_bound, z_bound, z_points)
+        rho = np.delete(np.linspace(0, rho_bound, rho_points + 1), 0)
+        self.dz = self.z[1] - self.z[0]
+        self.drho = rho[1] - rho[0]
+        self.rho = rho - self.drho / 2
+        self.shape = (z_points, rho_points)
+        self.Nz, self.Nrho = z_points, rho_points
+        self.M = z_points * rho_points
+        self.pulse = pulse
+        self.z_mesh, self.rho_mesh = np.meshgrid(self.z, self.rho, indexing="ij")
+        self.r_mesh = np.sqrt((self.z_mesh ** 2) + (self.rho_mesh ** 2))
+        self.theta_mesh = np.arccos(self.z_mesh / self.r_mesh)
+        self.g_factor = np.sqrt(ph.TWOPI * self.rho_mesh)
+        self.mult = self.dz * self.drho
+
+        M = self.M
+        kk = np.arange(M - 1)
+        pz = -(ph.HBAR ** 2) / (2 * test_mass * (self.dz ** 2))
+        z_diag = pz * (-2) * np.ones(M, dtype=np.complex128)
+        z_off = pz * np.where((kk + 1) % z_points != 0, 1, 0).astype(np.complex128)
+        prho = -(ph.HBAR ** 2) / (2 * test_mass * (self.drho ** 2))
+        rho_diag = prho * (-2) * np.ones(M, dtype=np.complex128)
+        jj = (kk % rho_points) + 1
+        cj = jj / np.sqrt((jj ** 2) - 0.25)
+        rho_off = np.where((kk + 1) % rho_points != 0, cj, 0).astype(np.complex128)
+        rho_off *= prho
+        V = ph.coulomb(self.r_mesh)
+        pre = 1 / 2
+        # internal_hamiltonian, mesh_operators.py:244-269 (order: rho, z)
+        self.H_rho0 = Tridiag(rho_off, rho_diag + pre * V.flatten("C"), rho_off.copy(), "C")
+        self.H_z0 = Tridiag(z_off, z_diag + pre * V.flatten("F"), z_off.copy(), "F")
+
+        self.test_states = list(test_states)
+        self.test_g = {}
+        for (n, l) in self.test_states + [tuple(initial_state)]:
+            self.test_g[(n, l)] = self._state_g(n, l)
+        self.g = self.test_g[tuple(initial_state)].copy()
+
+    def _state_g(self, n, l):
+        """CylindricalSliceMesh.get_g_for_state, meshes.py:601-607."""
+        psi = 1 * ph.hydrogen_radial(n, l, self.r_mesh) * ph.spherical_harmonic(
+            l, 0, self.theta_mesh, 0
+        )
+        g = self.g_factor * psi
+        g = g / np.sqrt((np.sum(np.conj(g) * g) * self.mult).real)
+        return g
+
+    def norm(self):
+        return (np.sum(np.conj(self.g) * self.g) * self.mult).real
+
+    def inner_products(self):
+        return [np.sum(np.conj(self.test_g[s]) * self.g) * self.mult for s in self.test_states]
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        epot = -self.z_mesh * ph.ELECTRON_CHARGE * self.pulse.field(t_now)
+        pre = 1 / 2
+        # total_hamiltonian, mesh_operators.py:271-298
+        H_rho = Tridiag(self.H_rho0.sub, self.H_rho0.diag + pre * epot.flatten("C"), self.H_rho0.sup, "C")
+        H_z = Tridiag(self.H_z0.sub, self.H_z0.diag + pre * epot.flatten("F"), self.H_z0.sup, "F")
+        g = self.g
+        g = apply_explicit(H_rho.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(H_z.scaled_plus_identity(1j * tau), g, self.shape)
+        g = apply_explicit(H_z.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(H_rho.scaled_plus_identity(1j * tau), g, self.shape)
+        self.g = g
+
+
+# --------------------------------------------------------------------------
+# builders from fixture parameter dicts
+# --------------------------------------------------------------------------
+
+def pulse_from_params(p):
+    return ph.CosSquaredPulse(
+        amplitude=p["amplitude"],
+        omega_carrier=p["omega_carrier"],
+        number_of_cycles=p["number_of_cycles"],
+        phase=p["phase"],
+        pulse_center=p["pulse_center"],
+    )
+
+
+def build_from_params(kind, params):
+    pulse = pulse_from_params(params["pulse"])
+    if kind == "line":
+        method = params["method"]
+        return LineLength(
+            params["z_points"], params["z_bound"], params["test_mass"],
+            params["softening_distance"], pulse, params.get("mask"), method,
+            params.get("gaussian_width", 1.0),
+        )
+    if kind == "sh":
+        return SphericalHarmonicSplit(
+            params["r_points"], params["r_bound"], params["l_bound"], pulse, params.get("mask"),
+            [tuple(s) for s in params["test_states"]], params["time_step"],
+        )
+    if kind == "cyl":
+        return CylindricalSliceADI(
+            params["z_points"], params["z_bound"], params["rho_points"], params["rho_bound"],
+            pulse, [tuple(s) for s in params["test_states"]],
+        )
+    raise ValueError(kind)
+
+
+def run_from_params(kind, params, max_steps=None):
+    stepper = build_from_params(kind, params)
+    times = get_times(params["time_initial"], params["time_final"], params["time_step"])
+    g0 = stepper.g.copy()
+    out = run(stepper, times, params["store_data_every"], max_steps=max_steps)
+    out["times"] = times
+    out["g_initial"] = g0
+    out["g_final"] = stepper.g
+    out["stepper"] = stepper
+    return out

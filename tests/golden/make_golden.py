@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Generate golden fixtures by running the REFERENCE ionization library.
+
+This script needs a checkout of the reference (default ``/root/reference``,
+override with ``--ref``); it imports it read-only through ``refstub/loader.py``
+(atomic-unit ``simulacra`` stub) and writes ``tests/golden/*.npz``.  The
+fixtures are committed; tests only read them.
+
+Cases (reference call sites in parentheses):
+  tdma.npz         random complex tridiagonal systems solved by ``cy.tdma``
+                   (ionization/cy.pyx:9-50; distribution as tests/conftest.py:4-5)
+  line_adi_small   LineMesh + LineLengthGaugeOperators + AlternatingDirectionImplicit
+  line_split_small LineMesh + LineLengthGaugeOperators + SplitInteractionOperator
+  sh_split_*       SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators
+                   + SplitInteractionOperator (even L; odd L; odd Nr and odd L)
+  cyl_adi_small    CylindricalSliceMesh + CylindricalSliceLengthGaugeOperators + ADI
+  line_cfg1_full   the full 1D workload: 4096 points, 4000 steps (optional --full)
+  sh_cfg2_full     the full spherical-harmonic workload: Nr=2000, L=41, 20000 steps
+                   (optional --full-sh, ~10 min single core)
+  cyl_cfg3_full    the full cylindrical workload: 2000 x 1000, 5000 steps
+                   (optional --full-cyl, ~1 h single core; psi stored subsampled)
+
+Each npz holds the spec parameters (``params`` JSON string), the time grid,
+the initial and final ``g``, and the Norm / InnerProducts datastore arrays.
+"""
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "refstub"))
+
+
+def _pulse_kwargs(E0, omega, cycles, cep):
+    """sin^2-envelope pulse E0 sin^2(pi t/T) cos(w t + cep) as CosSquaredPulse args.
+
+    CosSquaredPulse (potentials/pulses.py:1696-1814) centres the carrier at
+    ``pulse_center``; with pulse_center = T/2 the carrier phase must be
+    cep + pi * cycles so that E(t) = E0 sin^2(pi t/T) cos(w t + cep).
+    """
+    T = cycles * 2 * np.pi / omega
+    return dict(
+        amplitude=E0,
+        omega_carrier=omega,
+        number_of_cycles=cycles,
+        phase=float(np.mod(cep + np.pi * cycles, 2 * np.pi)),
+        pulse_center=T / 2,
+    )
+
+
+def build_helpers(ion):
+    from ionization import states, potentials
+
+    class GaussianState(states.QuantumState):
+        """Normalised-on-mesh Gaussian exp(-(z - z0)^2 / (2 w^2)) (1D)."""
+
+        eigenvalues = states.Eigenvalues.DISCRETE
+        binding = states.Binding.BOUND
+        derivation = states.Derivation.ANALYTIC
+
+        def __init__(self, width=1.0, center=0.0, amplitude=1):
+            self.width = width
+            self.center = center
+            super().__init__(amplitude=amplitude)
+
+        @property
+        def tuple(self):
+            return (self.width, self.center)
+
+        def __call__(self, z):
+            return np.exp(-((z - self.center) ** 2) / (2 * self.width ** 2)).astype(
+                np.complex128
+            )
+
+        @property
+        def ket(self):
+            return "|gauss>"
+
+        @property
+        def tex_ket(self):
+            return "gauss"
+
+    class AbsRadialCosineMask(potentials.RadialCosineMask):
+        """RadialCosineMask evaluated at |r| (absorbs at both ends of a line)."""
+
+        def __call__(self, *, r, **kwargs):
+            return super().__call__(r=np.abs(r))
+
+    return GaussianState, AbsRadialCosineMask
+
+
+def run_and_collect(spec, extra=None, subsample=None):
+    sim = spec.to_sim()
+    g0 = np.array(sim.mesh.g, copy=True)
+    t0 = time.time()
+    sim.run()
+    elapsed = time.time() - t0
+    out = dict(
+        times=np.asarray(sim.times),
+        data_times=np.asarray(sim.data_times),
+        norm=np.asarray(sim.data.norm),
+        g_initial=g0,
+        g_final=np.asarray(sim.mesh.g),
+        elapsed_s=np.float64(elapsed),
+    )
+    ips = sim.data.inner_products
+    keys = list(ips.keys())
+    out["inner_products"] = np.array([ips[k] for k in keys])
+    out["state_keys"] = np.array([str(k.tuple) for k in keys])
+    out["initial_state_overlap"] = np.asarray(sim.data.initial_state_overlap)
+    if extra:
+        out.update(extra)
+    if subsample is not None:
+        out["g_initial"] = out["g_initial"][subsample]
+        out["g_final"] = out["g_final"][subsample]
+    return sim, out
+
+
+def save(name, params, arrays):
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, params=json.dumps(params), **arrays)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.1f} KiB)", flush=True)
+
+
+def gen_tdma(ion):
+    from ionization.cy import tdma
+    from scipy import sparse
+
+    rng = np.random.default_rng(20261203)
+    cases = {}
+    sizes = [2, 3, 4, 5, 17, 64, 100, 257, 1000]
+    for i, n in enumerate(sizes):
+        cs = lambda k: rng.random(k) + 1j * rng.random(k)  # noqa: E731
+        a, b, c, d = cs(n - 1), cs(n), cs(n - 1), cs(n)
+        dia = sparse.diags([a, b, c], offsets=[-1, 0, 1])
+        x = tdma(dia, d)
+        # the dia_matrix rows exactly as cy.tdma reads them
+        cases[f"n{i}_data"] = np.asarray(dia.data)
+        cases[f"n{i}_d"] = d
+        cases[f"n{i}_x"] = x
+    # a batch of independent lines flattened into one call, the way the mesh
+    # operators hand cy.tdma a whole mesh (zero off-diagonals at line ends)
+    nl, n = 7, 33
+    b = 2.5 + rng.random(nl * n) + 1j * rng.random(nl * n)
+    off = rng.random(nl * n - 1) + 1j * rng.random(nl * n - 1)
+    off[n - 1 :: n] = 0
+    dia = sparse.diags([off, b, off.copy()], offsets=[-1, 0, 1])
+    d = rng.random(nl * n) + 1j * rng.random(nl * n)
+    cases["batch_data"] = np.asarray(dia.data)
+    cases["batch_d"] = d
+    cases["batch_x"] = tdma(dia, d)
+    cases["batch_shape"] = np.array([nl, n])
+    save("tdma", {"sizes": sizes, "seed": 20261203}, cases)
+
+
+def line_spec(ion, name, z_points, z_bound, steps, dt, pulse, method, mask, store_every):
+    GaussianState, AbsRadialCosineMask = build_helpers(ion)
+    import simulacra.units as u
+
+    params = dict(
+        z_points=z_points,
+        z_bound=z_bound,
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        softening_distance=float(np.sqrt(2)),
+        test_mass=1.0,
+        pulse=pulse,
+        mask=mask,
+        method=method,
+        store_data_every=store_every,
+        gaussian_width=1.0,
+    )
+    spec = ion.mesh.LineSpecification(
+        name,
+        z_bound=z_bound,
+        z_points=z_points,
+        test_mass=u.electron_mass,
+        internal_potential=ion.potentials.SoftCoulombPotential(
+            softening_distance=np.sqrt(2)
+        ),
+        initial_state=GaussianState(width=1.0),
+        electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+        mask=AbsRadialCosineMask(**mask),
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        operators=ion.mesh.LineLengthGaugeOperators(),
+        evolution_method=getattr(ion.mesh, method)(),
+        store_data_every=store_every,
+    )
+    return spec, params
+
+
+def gen_line(ion, full=False):
+    pulse = _pulse_kwargs(0.05, 0.057, 4, 0.0)
+    mask = dict(inner_radius=80.0, outer_radius=100.0, smoothness=8)
+    if not full:
+        fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.3)
+        for method, name in (
+            ("AlternatingDirectionImplicit", "line_adi_small"),
+            ("SplitInteractionOperator", "line_split_small"),
+        ):
+            spec, params = line_spec(
+                ion, name, 512, 40.0, 600, 0.05, fast_pulse, method,
+                dict(inner_radius=30.0, outer_radius=40.0, smoothness=8), 50,
+            )
+            _, out = run_and_collect(spec)
+            save(name, params, out)
+    else:
+        spec, params = line_spec(
+            ion, "line_cfg1_full", 4096, 100.0, 4000, 0.05, pulse,
+            "AlternatingDirectionImplicit", mask, 500,
+        )
+        _, out = run_and_collect(spec)
+        save("line_cfg1_full", params, out)
+
+
+def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3):
+    from ionization import states
+
+    r_bound = 0.125 * (r_points - 1)
+    r_max = r_bound + 0.125 / 2
+    test_states = [states.HydrogenBoundState(n, l) for n in range(1, n_max + 1) for l in range(n)]
+    mask = dict(inner_radius=r_max - mask_width, outer_radius=r_max, smoothness=8)
+    params = dict(
+        r_points=r_points,
+        r_bound=r_bound,
+        l_bound=l_bound,
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        pulse=pulse,
+        mask=mask,
+        store_data_every=store_every,
+        test_states=[[s.n, s.l] for s in test_states],
+    )
+    spec = ion.mesh.SphericalHarmonicSpecification(
+        name,
+        r_points=r_points,
+        r_bound=r_bound,
+        l_bound=l_bound,
+        use_numeric_eigenstates=False,
+        initial_state=states.HydrogenBoundState(1, 0),
+        test_states=test_states,
+        electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+        mask=ion.potentials.RadialCosineMask(**mask),
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        operators=ion.mesh.SphericalHarmonicLengthGaugeOperators(),
+        evolution_method=ion.mesh.SplitInteractionOperator(),
+        store_data_every=store_every,
+    )
+    return spec, params
+
+
+def gen_sh(ion, full=False):
+    if not full:
+        fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+        for name, nr, L in (
+            ("sh_split_small_evenL", 160, 8),
+            ("sh_split_small_oddL", 160, 11),
+            ("sh_split_small_oddNr_oddL", 151, 7),
+        ):
+            spec, params = sh_spec(ion, name, nr, L, 1250, 0.02, fast_pulse, 5.0, 125)
+            _, out = run_and_collect(spec)
+            save(name, params, out)
+    else:
+        pulse = _pulse_kwargs(0.05, 0.057, 6, 0.0)
+        spec, params = sh_spec(ion, "sh_cfg2_full", 2000, 41, 20000, 0.02, pulse, 25.0, 1000, n_max=5)
+        _, out = run_and_collect(spec)
+        save("sh_cfg2_full", params, out)
+
+
+def cyl_spec(ion, name, z_points, z_bound, rho_points, rho_bound, steps, dt, pulse, store_every):
+    from ionization import states
+
+    test_states = [states.HydrogenBoundState(1, 0), states.HydrogenBoundState(2, 0), states.HydrogenBoundState(2, 1)]
+    params = dict(
+        z_points=z_points,
+        z_bound=z_bound,
+        rho_points=rho_points,
+        rho_bound=rho_bound,
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        pulse=pulse,
+        store_data_every=store_every,
+        test_states=[[s.n, s.l] for s in test_states],
+    )
+    spec = ion.mesh.CylindricalSliceSpecification(
+        name,
+        z_points=z_points,
+        z_bound=z_bound,
+        rho_points=rho_points,
+        rho_bound=rho_bound,
+        initial_state=states.HydrogenBoundState(1, 0),
+        test_states=test_states,
+        electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        operators=ion.mesh.CylindricalSliceLengthGaugeOperators(),
+        evolution_method=ion.mesh.AlternatingDirectionImplicit(),
+        store_data_every=store_every,
+    )
+    return spec, params
+
+
+def gen_cyl(ion, full=False):
+    if not full:
+        fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+        spec, params = cyl_spec(ion, "cyl_adi_small", 120, 15.0, 60, 15.0, 500, 0.05, fast_pulse, 50)
+        _, out = run_and_collect(spec)
+        save("cyl_adi_small", params, out)
+    else:
+        pulse = _pulse_kwargs(0.02, 0.1, 4, 0.0)
+        spec, params = cyl_spec(ion, "cyl_cfg3_full", 2000, 100.0, 1000, 100.0, 5000, 0.02, pulse, 500)
+        sub = (slice(None, None, 10), slice(None, None, 10))
+        params["g_subsample"] = [10, 10]
+        _, out = run_and_collect(spec, subsample=sub)
+        save("cyl_cfg3_full", params, out)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl")
+    ap.add_argument("--full", action="store_true", help="also the full 1D workload")
+    ap.add_argument("--full-sh", action="store_true")
+    ap.add_argument("--full-cyl", action="store_true")
+    args = ap.parse_args()
+
+    from loader import import_reference
+
+    ion = import_reference(args.ref)
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl"}
+    if "tdma" in only:
+        gen_tdma(ion)
+    if "line" in only:
+        gen_line(ion)
+    if "sh" in only:
+        gen_sh(ion)
+    if "cyl" in only:
+        gen_cyl(ion)
+    if args.full:
+        gen_line(ion, full=True)
+    if args.full_sh:
+        gen_sh(ion, full=True)
+    if args.full_cyl:
+        gen_cyl(ion, full=True)
+
+
+if __name__ == "__main__":
+    main()

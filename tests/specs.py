@@ -1,0 +1,70 @@
+"""Build product specifications from golden-fixture parameter dicts."""
+
+import numpy as np
+
+import ionization_gb300 as ig
+from ionization_gb300 import mesh, potentials, states
+from ionization_gb300 import units as u
+
+
+def pulse(p):
+    return potentials.CosSquaredPulse.from_omega_carrier(
+        amplitude=p["amplitude"],
+        omega_carrier=p["omega_carrier"],
+        number_of_cycles=p["number_of_cycles"],
+        phase=p["phase"],
+        pulse_center=p["pulse_center"],
+    )
+
+
+def product_spec(kind, params, **kw):
+    common = dict(
+        time_initial=params["time_initial"],
+        time_final=params["time_final"],
+        time_step=params["time_step"],
+        electric_potential=pulse(params["pulse"]),
+        store_data_every=params["store_data_every"],
+    )
+    common.update(kw)
+    if kind == "line":
+        return mesh.LineSpecification(
+            "line",
+            z_bound=params["z_bound"],
+            z_points=params["z_points"],
+            test_mass=params["test_mass"],
+            internal_potential=potentials.SoftCoulombPotential(softening_distance=params["softening_distance"]),
+            initial_state=states.GaussianState(width=params.get("gaussian_width", 1.0)),
+            mask=potentials.AbsoluteRadialCosineMask(**params["mask"]),
+            operators=mesh.LineLengthGaugeOperators(),
+            evolution_method=getattr(mesh, params["method"])(),
+            **common,
+        )
+    if kind == "sh":
+        return mesh.SphericalHarmonicSpecification(
+            "sh",
+            r_points=params["r_points"],
+            r_bound=params["r_bound"],
+            l_bound=params["l_bound"],
+            use_numeric_eigenstates=False,
+            initial_state=states.HydrogenBoundState(1, 0),
+            test_states=[states.HydrogenBoundState(n, l) for n, l in params["test_states"]],
+            mask=potentials.RadialCosineMask(**params["mask"]),
+            **common,
+        )
+    if kind == "cyl":
+        return mesh.CylindricalSliceSpecification(
+            "cyl",
+            z_points=params["z_points"],
+            z_bound=params["z_bound"],
+            rho_points=params["rho_points"],
+            rho_bound=params["rho_bound"],
+            initial_state=states.HydrogenBoundState(1, 0),
+            test_states=[states.HydrogenBoundState(n, l) for n, l in params["test_states"]],
+            **common,
+        )
+    raise ValueError(kind)
+
+
+def test_state_order(spec):
+    """Product test states are sorted like the reference's (sims.py:530-538)."""
+    return [s.tuple for s in spec.test_states]

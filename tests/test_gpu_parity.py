@@ -1,0 +1,177 @@
+"""GPU parity: the CUDA path against the reference's own outputs.
+
+Plain complex128 must match the reference to relative L2 <= 1e-10 on psi and
+1e-10 absolute on norms / inner products (the benchmark spec's tolerance).  The
+Thomas drop-in is checked like the reference's tests/test_tdma.py
+(np.allclose against the reference solve) and tightly on well-conditioned
+systems.  Everything here goes through the C ABI of libiongb300.so."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from oracle import mesh as om
+
+from .conftest import load_golden, rel_l2
+from .specs import product_spec
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+# ---------------------------------------------------------------- tdma
+
+
+def test_tdma_c128_matches_cy_tdma(cuda):
+    from ionization_gb300 import cy
+    from scipy import sparse
+
+    _, z = load_golden("tdma")
+    for i in range(9):
+        data = z[f"n{i}_data"]
+        n = data.shape[1]
+        m = sparse.dia_matrix((data, [-1, 0, 1]), shape=(n, n))
+        x = cy.tdma(m, z[f"n{i}_d"])
+        ref = z[f"n{i}_x"]
+        assert np.allclose(x, ref), i  # the reference test's criterion
+        assert np.allclose(m.dot(x), z[f"n{i}_d"]), i
+
+
+def test_tdma_batched_matches_cy_tdma(cuda):
+    from ionization_gb300 import cy
+
+    _, z = load_golden("tdma")
+    nl, n = (int(v) for v in z["batch_shape"])
+    data = z["batch_data"]
+    x = cy.tdma_batched_device(nl, n, _dev(data[0][:-1].copy()), _dev(data[1]), _dev(data[2][1:].copy()),
+                               _dev(z["batch_d"])).cpu().numpy()
+    assert rel_l2(x, z["batch_x"]) < 1e-14
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 64, 4096, 4097, 100_000, 2_000_000])
+def test_tdma_long_system_c128(cuda, n):
+    """Diagonally dominant CN-like systems of any length: single CTA up to 4096
+    rows, multi-level partition beyond."""
+    from ionization_gb300 import cy
+
+    rng = np.random.default_rng(n)
+    off = 1j * rng.uniform(-5, 5, max(n - 1, 0))
+    diag = 1 + 1j * rng.uniform(-12, 12, n)
+    d = rng.normal(size=n) + 1j * rng.normal(size=n)
+    want = oracle.tdma(off, diag, off, d)
+    got = cy.tdma_device(_dev(off), _dev(diag), _dev(off.copy()), _dev(d)).cpu().numpy()
+    assert rel_l2(got, want) < 1e-13
+
+
+def test_tdma_c64_close_to_c128(cuda):
+    from ionization_gb300 import cy
+
+    n = 50_000
+    rng = np.random.default_rng(7)
+    off = 1j * rng.uniform(-5, 5, n - 1)
+    diag = 1 + 1j * rng.uniform(-12, 12, n)
+    d = rng.normal(size=n) + 1j * rng.normal(size=n)
+    want = oracle.tdma(off, diag, off, d)
+    c64 = lambda a: _dev(a.astype(np.complex64))  # noqa: E731
+    got = cy.tdma_device(c64(off), c64(diag), c64(off), c64(d)).cpu().numpy()
+    assert rel_l2(got, want) < 1e-5
+
+
+# ---------------------------------------------------------------- meshes
+
+CASES = [
+    ("line", "line_adi_small"),
+    ("line", "line_split_small"),
+    ("sh", "sh_split_small_evenL"),
+    ("sh", "sh_split_small_oddL"),
+    ("sh", "sh_split_small_oddNr_oddL"),
+    ("cyl", "cyl_adi_small"),
+]
+
+
+def _check_against_golden(sim, z, tol=TOL):
+    assert rel_l2(sim.mesh.g, z["g_final"]) < tol
+    np.testing.assert_allclose(sim.data.norm, z["norm"], rtol=0, atol=tol)
+    ips = np.array([sim.data.inner_products[s] for s in sim.spec.test_states])
+    np.testing.assert_allclose(ips, z["inner_products"], rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("kind,name", CASES)
+def test_mesh_c128_matches_reference(cuda, kind, name):
+    params, z = load_golden(name)
+    sim = product_spec(kind, params).to_sim()
+    assert rel_l2(sim.mesh.g, z["g_initial"]) == 0.0
+    sim.run()
+    np.testing.assert_array_equal(sim.data.times, z["data_times"])
+    _check_against_golden(sim, z)
+
+
+@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] != "cyl"])
+def test_mesh_c64_population_error(cuda, kind, name):
+    """complex64 state with FP64 field, coefficients and reductions."""
+    params, z = load_golden(name)
+    sim = product_spec(kind, params, precision="c64").to_sim()
+    sim.run()
+    p64 = sim.data.initial_state_overlap[-1]
+    p128 = z["initial_state_overlap"][-1]
+    assert abs(p64 - p128) < 2e-6
+    assert rel_l2(sim.mesh.g, z["g_final"]) < 1e-4
+
+
+def test_run_with_callback_and_resume(cuda):
+    """Per-step callbacks and max_steps/resume give the same result."""
+    params, z = load_golden("sh_split_small_oddL")
+    sim = product_spec("sh", params).to_sim()
+    seen = []
+    sim.run(callback=lambda s: seen.append(s.time_index), max_steps=300)
+    assert seen[-1] == 300 and len(seen) == 301
+    sim.run()
+    _check_against_golden(sim, z)
+
+
+def test_save_and_load_roundtrip(cuda, tmp_path):
+    params, z = load_golden("line_adi_small")
+    sim = product_spec("line", params).to_sim()
+    sim.run(max_steps=250)
+    g_mid = sim.mesh.g
+    path = sim.save(target_dir=str(tmp_path), save_mesh=True)
+    from ionization_gb300.mesh import MeshSimulation
+
+    sim2 = MeshSimulation.load(path)
+    np.testing.assert_array_equal(sim2.mesh.g, g_mid)
+    assert sim2.time_index == 250
+    sim2.run()
+    _check_against_golden(sim2, z)
+
+
+@pytest.mark.slow
+def test_full_line_workload_matches_reference(cuda):
+    params, z = load_golden("line_cfg1_full")
+    sim = product_spec("line", params).to_sim()
+    sim.run()
+    _check_against_golden(sim, z)
+
+
+@pytest.mark.slow
+def test_full_spherical_harmonic_workload_matches_reference(cuda):
+    params, z = load_golden("sh_cfg2_full")
+    sim = product_spec("sh", params).to_sim()
+    sim.run()
+    _check_against_golden(sim, z)
+
+
+@pytest.mark.slow
+def test_full_cylindrical_workload_matches_reference(cuda):
+    params, z = load_golden("cyl_cfg3_full")
+    sim = product_spec("cyl", params).to_sim()
+    sim.run()
+    sz, sr = params["g_subsample"]
+    g = sim.mesh.g[::sz, ::sr]
+    assert rel_l2(g, z["g_final"]) < TOL
+    np.testing.assert_allclose(sim.data.norm, z["norm"], rtol=0, atol=TOL)

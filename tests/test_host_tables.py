@@ -1,0 +1,89 @@
+"""Host-side coefficient build of the product against the oracle (CPU only).
+
+The device kernels consume FP64 tables built on the host; these must be
+identical to the reference's operator diagonals (the oracle restates them and
+is itself pinned to the reference by test_oracle_golden)."""
+
+import numpy as np
+import pytest
+
+from oracle import mesh as om
+
+from .conftest import load_golden
+from .specs import product_spec
+
+
+@pytest.mark.parametrize("name", ["line_adi_small", "line_split_small"])
+def test_line_tables(name):
+    params, z = load_golden(name)
+    sim = product_spec("line", params, host_only=True).to_sim()
+    tb = sim.mesh.tables
+    ref = om.build_from_params("line", params)
+    np.testing.assert_array_equal(tb.hd, ref.H0.diag.real)
+    np.testing.assert_array_equal(tb.hoff, ref.H0.sub.real)
+    np.testing.assert_array_equal(tb.mask, ref.mask)
+    np.testing.assert_array_equal(tb.g0, z["g_initial"])
+    times = om.get_times(params["time_initial"], params["time_final"], params["time_step"])
+    np.testing.assert_array_equal(sim.times, times)
+    np.testing.assert_array_equal(tb.efield[1:], ref.pulse.field(times[1:]))
+    np.testing.assert_array_equal(tb.zq * 0.3, (-ref.z * -1.0) * 0.3)
+
+
+@pytest.mark.parametrize("name", ["sh_split_small_evenL", "sh_split_small_oddL", "sh_split_small_oddNr_oddL"])
+def test_sh_tables(name):
+    params, z = load_golden(name)
+    sim = product_spec("sh", params, host_only=True).to_sim()
+    tb = sim.mesh.tables
+    ref = om.build_from_params("sh", params)
+    np.testing.assert_array_equal(tb.hd, ref.H0.diag.real)
+    nr, L = params["r_points"], params["l_bound"]
+    np.testing.assert_array_equal(tb.hoff, ref.H0.sub.real[: nr - 1])
+    # the rotation coupling c_l * r evaluated on the fly equals the reference's table
+    k = np.arange(nr * L - 1)
+    coupling = np.where((k + 1) % L != 0, tb.cl[k % L] * tb.rq[k // L], 0)
+    np.testing.assert_array_equal(coupling, ref.l_off.real)
+    np.testing.assert_array_equal(tb.mask, ref.mask[0])
+    np.testing.assert_array_equal(tb.g0, z["g_initial"])
+    times = sim.times
+    np.testing.assert_array_equal(tb.efield[1:], ref.pulse.field(times[1:] + params["time_step"] / 2))
+    # test states: sorted like the reference, radial g identical
+    for (n, l), sl, sg in zip(params["test_states"], tb.state_l, tb.state_g):
+        assert sl == l
+        np.testing.assert_array_equal(sg, ref.radial_g[(n, l)])
+    # complex64 pieces reproduce the FP64 diagonal to rounding
+    for l in (0, 1, L - 1):
+        h = tb.kinv + l * (l + 1) * tb.cent
+        if l == 0:
+            h = h.copy()
+            h[0] += tb.corr0
+        np.testing.assert_allclose(h, tb.hd[l * nr:(l + 1) * nr], rtol=1e-13, atol=1e-10)
+
+
+def test_cyl_tables():
+    params, z = load_golden("cyl_adi_small")
+    sim = product_spec("cyl", params, host_only=True).to_sim()
+    tb = sim.mesh.tables
+    ref = om.build_from_params("cyl", params)
+    nz, nr = params["z_points"], params["rho_points"]
+    np.testing.assert_array_equal(tb["hr_d"], ref.H_rho0.diag.real)
+    np.testing.assert_array_equal(tb["hz_d"], np.reshape(ref.H_z0.diag.real, (nz, nr), "F").ravel())
+    np.testing.assert_array_equal(tb["hr_off"], ref.H_rho0.sub.real[: nr - 1])
+    np.testing.assert_array_equal(tb["hz_off"], ref.H_z0.sub.real[: nz - 1])
+    np.testing.assert_array_equal(tb["g0"], z["g_initial"])
+    for s, gs in zip(params["test_states"], tb["state_g"]):
+        np.testing.assert_array_equal(gs.reshape(nz, nr), ref.test_g[tuple(s)])
+
+
+def test_data_slots_match_reference_mask():
+    from ionization_gb300 import _device as dev
+
+    for tf in (0, 1, 7, 100, 101):
+        for every in (-1, 1, 3, 10, 200):
+            idx = np.arange(tf + 1)
+            mask = om.data_mask(tf + 1, every)
+            assert dev.n_data_slots(tf, every) == mask.sum()
+            slots = np.cumsum(mask) - 1
+            for t in idx:
+                assert dev.is_data_time(t, tf, every) == bool(mask[t])
+                if mask[t]:
+                    assert dev.data_slot(t, tf, every) == slots[t]
