@@ -1,0 +1,523 @@
+#!/usr/bin/env python
+"""Benchmark: batched uneven spherical-harmonic sweep on one GB300.
+
+Workload ``uneven_sh_sweep``: 512 spherical-harmonic split-operator
+simulations (Nr 800-3200 at dr 0.125, l_max 20-80, seeded pulses), complex64
+psi with FP64 fields, coefficients and reductions, 52.3 M mesh points,
+419 MB of psi (larger than L2).  A step advances all 512 simulations by one
+time step: three kernel launches (radial solve, rotation/mask/reduction pass,
+time-index advance).
+
+Prints one JSON line:
+  value      mesh-point-steps/s over the timed steps, psi resident in HBM
+  e2e        the same metric through the public API from host buffers
+             (H2D of psi and tables, the steps, D2H of data and psi)
+  roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
+             against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (CPU restatement of the reference, complex128)
+             on a bounded sample of the same workload on the host cores
+  plain_c128 the single-simulation complex128 drop-in path (Nr 2000, l < 41)
+  accuracy   |P_ground(c64) - P_ground(c128)| and the same for the
+             ionization probability over the full 10000 steps, on a seeded
+             subset of the sweep
+
+``--impl reference`` times the CPU oracle (the reference's algorithm,
+complex128) on the same workload with all host cores instead.
+Multi-GPU (torchrun): replicas, each rank its own seeded sweep, no collective
+on the data path (weak scaling).
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "mesh-pt-steps/s on 1 GB300: batched c64 vs plain c128 @≤1e-6 pop err; p50/p99 lat"
+UNIT = "mesh-pt-steps/s"
+SEED = 20261203
+N_SIMS = 512
+SIM_STEPS = 10000
+FALLBACK_HBM_GBS = 6800.0
+
+
+# --------------------------------------------------------------------------
+# CPU oracle workers (spawned processes; import numpy/scipy only)
+# --------------------------------------------------------------------------
+
+_W = {}
+
+
+def _oracle_sim(p, dt=0.02):
+    from oracle import mesh as om
+    from oracle import physics as ph
+
+    T = p["cycles"] * 2 * np.pi / p["omega"]
+    pulse = ph.CosSquaredPulse(p["E0"], p["omega"], p["cycles"], float(np.mod(p["cep"] + np.pi * p["cycles"], 2 * np.pi)),
+                               T / 2)
+    nr = p["r_points"]
+    r_bound = 0.125 * (nr - 1)
+    r_max = r_bound + 0.0625
+    mask = dict(inner_radius=r_max - 25.0, outer_radius=r_max, smoothness=8)
+    ts = [(n, l) for n in range(1, 6) for l in range(n)]
+    return om.SphericalHarmonicSplit(nr, r_bound, p["l_bound"], pulse, mask, ts, dt)
+
+
+def _worker_init(params):
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import oracle
+
+    oracle.build()
+    _W["sims"] = [_oracle_sim(p) for p in params]
+    _W["t"] = 0.0
+
+
+def _worker_step(_):
+    t0 = time.perf_counter()
+    _W["t"] += 0.02
+    for s in _W["sims"]:
+        s.evolve(0.02, _W["t"])
+    return time.perf_counter() - t0, sum(s.M for s in _W["sims"])
+
+
+def _worker_run(args):
+    params, steps = args
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import oracle
+
+    oracle.build()
+    sims = [_oracle_sim(p) for p in params]
+    t0 = time.perf_counter()
+    t = 0.0
+    for _ in range(steps):
+        t += 0.02
+        for s in sims:
+            s.evolve(0.02, t)
+    return time.perf_counter() - t0, sum(s.M for s in sims) * steps
+
+
+def cpu_cores():
+    return max(1, min(os.cpu_count() or 1, 64))
+
+
+def cpu_baseline_sample(params, cores, steps=10):
+    """Oracle throughput on ``cores`` processes, one slice of sims each."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    chunks = [params[i::cores] for i in range(cores)]
+    chunks = [c for c in chunks if c]
+    t0 = time.perf_counter()
+    with ctx.Pool(len(chunks)) as pool:
+        res = pool.map(_worker_run, [(c, steps) for c in chunks])
+    wall = time.perf_counter() - t0
+    pts = sum(r[1] for r in res)
+    busy = max(r[0] for r in res)
+    return pts / busy, wall, pts
+
+
+# --------------------------------------------------------------------------
+# helpers
+# --------------------------------------------------------------------------
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per mesh point of each kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import ionization_gb300 as ig
+    from ionization_gb300 import _device as dev
+    from ionization_gb300 import _native as nat
+    from ionization_gb300 import batch as bm
+    from ionization_gb300 import workloads as wl
+
+    torch.cuda.set_device(local_rank)
+    ig.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- the workload: this rank's seeded sweep ----
+    t_setup = time.perf_counter()
+    specs = wl.uneven_sh_sweep(N_SIMS, seed=SEED + rank, steps=SIM_STEPS, precision="c64")
+    tables = [bm._host_tables(s)[0] for s in specs]
+    setup_host_s = time.perf_counter() - t_setup
+    points = int(sum(t.n_r * t.n_l for t in tables))
+
+    (best_rows, best_gs), tune = bm.autotune(specs, "c64", graph_steps=(32,), steps=16, tables=tables)
+    b = bm.BatchedSphericalHarmonicSimulation(specs, precision="c64", graph_steps=best_gs, cn_rows=best_rows,
+                                              tables=tables)
+    b.step(max(args.warmup, 3))
+    torch.cuda.synchronize()
+
+    # ---- timed region: K steps, per-kernel events on the launching stream ----
+    K = args.steps
+    plan = b.batch.plan
+    fn = "ion_sh_split_phase_c64"
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    e_cn = [(ev(), ev()) for _ in range(K)]
+    e_rot = [(ev(), ev()) for _ in range(K)]
+    e0, e1 = ev(), ev()
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local_rank) as clk:
+        e0.record(stream)
+        nat.call(fn, nat.ctypes.byref(plan), 1, sp)  # rotations before the first solve
+        for k in range(K):
+            e_cn[k][0].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 2, sp)
+            e_cn[k][1].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 4 if k + 1 < K else 3, sp)
+            e_rot[k][1].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 5, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    for s in b.sims:
+        s.t = min(s.t + K, s.t_final)
+    elapsed_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(tt.item())
+    cn_ms = float(np.mean([a.elapsed_time(c) for a, c in e_cn]))
+    rot_ms = float(np.mean([e_cn[k][1].elapsed_time(e_rot[k][1]) for k in range(K)]))
+    gpu_launches = 1 + 3 * K
+
+    value = world * points * K / (elapsed_ms / 1e3)
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return None
+
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 16 * points  # complex64: psi read once and written once per kernel
+    dominant, dom_ms = ("sh_cn_kernel", cn_ms) if cn_ms >= rot_ms else ("sh_rot_kernel", rot_ms)
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
+    traffic = profile_traffic().get(dominant + "_c64_bytes_per_point")
+    roofline = {
+        "bound": "hbm",
+        "kernel": dominant,
+        "achieved": round(achieved, 1),
+        "peak": peak,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": round(achieved / peak, 4),
+        "traffic": None if traffic is None else int(traffic * points),
+        "algorithmic_bytes": alg_bytes,
+        "kernel_ms": {"sh_cn_kernel": round(cn_ms, 4), "sh_rot_kernel": round(rot_ms, 4)},
+        "frac_by_kernel": {"sh_cn_kernel": round(alg_bytes / (cn_ms / 1e3) / 1e9 / peak, 4),
+                           "sh_rot_kernel": round(alg_bytes / (rot_ms / 1e3) / 1e9 / peak, 4)},
+    }
+
+    # ---- e2e through the public API from host buffers ----
+    e2e = run_e2e(args, specs, tables, best_rows, best_gs, points)
+
+    # ---- plain complex128 drop-in path, single simulation ----
+    plain = run_plain_c128(args)
+
+    # ---- accuracy on a seeded subset: c64 vs c128 over the full run ----
+    acc = None if args.quick else run_accuracy()
+
+    # ---- CPU oracle on a bounded sample ----
+    cpu = None
+    if not args.no_cpu:
+        cores = cpu_cores()
+        params = wl.uneven_sh_parameters(N_SIMS, SEED)
+        sample = params[: 2 * cores]
+        rate, wall, pts = cpu_baseline_sample(sample, cores, steps=args.cpu_steps)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"first {len(sample)} simulations of the sweep x {args.cpu_steps} steps on {cores} "
+                         f"processes (complex128 oracle), {wall:.1f} s wall"}
+
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": K,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": elapsed_ms / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c64",
+        "data": "synthetic",
+        "config": {
+            "workload": "uneven_sh_sweep: 512 spherical-harmonic sims, Nr 800-3200, l_max 20-80, split operator",
+            "n_sims": N_SIMS,
+            "mesh_points": points,
+            "psi_bytes": points * 8,
+            "l2": "inputs larger than L2 (psi 419 MB)",
+            "parallelism": f"replicas x{world}",
+            "autotune": {"chosen": {"cn_rows_per_thread": best_rows, "graph_steps": best_gs},
+                         "ms_per_step": {f"rows{r}_graph{g}": round(v, 4) for (r, g), v in tune.items()}},
+            "host_setup_s": round(setup_host_s, 2),
+        },
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clocks,
+        "plain_c128": plain,
+        "accuracy": acc,
+    }
+    if plain and plain.get("value"):
+        out["vs_plain_c128"] = round(value / world / plain["value"], 2)
+    if dist is not None:
+        dist.destroy_process_group()
+    return out
+
+
+def run_e2e(args, specs, tables, rows, gs, points):
+    """Public API from host buffers: build the batch (H2D of psi, tables and
+    field tables), K steps, then read back every simulation's data and psi."""
+    import torch
+
+    from ionization_gb300 import batch as bm
+
+    K = args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b = bm.BatchedSphericalHarmonicSimulation(specs, precision="c64", graph_steps=gs, cn_rows=rows, tables=tables)
+    b.step(K)
+    res = b.results()
+    psis = [s.g.cpu() for s in b.sims]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    h2d = sum(s.nbytes() for s in b.sims) - sum(int(s.d_partials.numel()) * 8 for s in b.sims)
+    d2h = sum(int(p.numel()) * 8 for p in psis) + sum(r["norm"].nbytes + 16 * len(r["inner_products"]) * len(r["norm"])
+                                                       for r in res)
+    del b, psis
+    return {"value": points * K / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / K),
+            "d2h_bytes_per_step": int(d2h / K), "steps": K, "wall_s": round(wall, 3)}
+
+
+def run_plain_c128(args):
+    import torch
+
+    from ionization_gb300 import workloads as wl
+
+    steps = 400 if args.quick else 2000
+    spec = wl.sh_hydrogen_2000x41(steps=steps + 10, precision="c128")
+    sim = spec.to_sim()
+    sim.run(max_steps=5)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim.run(max_steps=steps)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    M = sim.mesh.mesh_points
+    return {"workload": "sh_hydrogen_2000x41 (Nr 2000, l < 41, split operator)", "dtype": "c128",
+            "value": M * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps, "steps": steps}
+
+
+def run_accuracy(subset=(0, 37, 101, 163, 255, 300, 411, 500)):
+    """Final ground-state population and ionization probability: complex64
+    batch against the complex128 batch (itself matched to the reference to
+    <= 1e-10 on the single-simulation workloads) over all 10000 steps."""
+    import torch
+
+    from ionization_gb300 import batch as bm
+    from ionization_gb300 import workloads as wl
+
+    out = {}
+    for prec in ("c128", "c64"):
+        specs = wl.uneven_sh_sweep(N_SIMS, seed=SEED, steps=SIM_STEPS, precision=prec, subset=list(subset))
+        b = bm.BatchedSphericalHarmonicSimulation(specs, precision=prec)
+        b.run()
+        out[prec] = b.results()
+        del b
+        torch.cuda.synchronize()
+    dg = [abs(a["initial_state_overlap"][-1] - c["initial_state_overlap"][-1]) for a, c in zip(out["c64"], out["c128"])]
+    di = [abs((1 - a["bound_state_overlap"][-1]) - (1 - c["bound_state_overlap"][-1]))
+          for a, c in zip(out["c64"], out["c128"])]
+    return {"subset": list(subset), "steps": SIM_STEPS, "max_abs_err_ground_population": float(max(dg)),
+            "max_abs_err_ionization_probability": float(max(di)),
+            "ground_population_c128": [float(c["initial_state_overlap"][-1]) for c in out["c128"]]}
+
+
+# --------------------------------------------------------------------------
+# reference arm: the CPU oracle on all host cores
+# --------------------------------------------------------------------------
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+
+    from ionization_gb300 import workloads as wl
+
+    cores = cpu_cores()
+    params = wl.uneven_sh_parameters(N_SIMS, SEED)
+    # size the per-step sample so that warm-up + timed steps fit the budget
+    budget_s = float(os.environ.get("ION_REF_BUDGET_S", "150"))
+    probe_rate = 2.5e6 * cores  # pt-steps/s, refined after the first step
+    per_step = budget_s / (args.steps + max(args.warmup, 3))
+    n_sample = 0
+    pts = 0
+    for p in params:
+        if pts + p["r_points"] * p["l_bound"] > probe_rate * per_step:
+            break
+        pts += p["r_points"] * p["l_bound"]
+        n_sample += 1
+    n_sample = max(n_sample, min(cores, len(params)))
+    sample = params[:n_sample]
+    ctx = mp.get_context("spawn")
+    chunks = [c for c in (sample[i::cores] for i in range(cores)) if c]
+    times = []
+    pools = [ctx.Pool(1, initializer=_worker_init, initargs=(c,)) for c in chunks]
+    try:
+        for k in range(max(args.warmup, 3) + args.steps):
+            t0 = time.perf_counter()
+            rs = [pl.apply_async(_worker_step, (0,)) for pl in pools]
+            res = [r.get() for r in rs]
+            dt = time.perf_counter() - t0
+            if k >= max(args.warmup, 3):
+                times.append(dt)
+        M = sum(r[1] for r in res)
+    finally:
+        for pl in pools:
+            pl.terminate()
+    total = float(np.sum(times))
+    value = M * len(times) / total
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "c128",
+        "data": "synthetic",
+        "config": {"workload": "uneven_sh_sweep: 512 spherical-harmonic sims, split operator", "n_sims": N_SIMS,
+                   "sample_sims_per_step": n_sample, "sample_mesh_points": M},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(chunks), "kind": "port",
+                         "sample": f"{n_sample} of {N_SIMS} simulations advanced one step per timed step, "
+                                   f"{len(chunks)} processes (complex128 oracle restating the reference)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the 10000-step accuracy run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
+    ap.add_argument("--cpu-steps", type=int, default=5)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if "WORLD_SIZE" not in os.environ:
+        world = 1
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local_rank)
+    if out is not None and rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

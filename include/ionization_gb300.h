@@ -155,13 +155,27 @@ typedef struct ion_sh_plan {
     int32_t cn_threads;       /* CTA size of the radial solve (multiple of 32) */
     const int32_t *rot_items; /* device [n_rot_items*2]: (sim, row tile) */
     int32_t n_rot_items;
-    int32_t rot_rows;         /* rows (r points) per tile */
+    int32_t rot_rows;         /* rows (r points) per tile, <= 64 */
+    int32_t cn_rows;          /* rows per thread of the radial solve: 0 = default,
+                                 complex128 4 or 8, complex64 8 or 16 */
+    int32_t pad2_;
 } ion_sh_plan;
 
 /* Advance every simulation of the plan by n_steps (fewer for simulations that
  * reach t_final).  Data reductions happen at data times on the way. */
 int ion_sh_split_run_c128(const ion_sh_plan *plan, int64_t n_steps, void *stream);
 int ion_sh_split_run_c64(const ion_sh_plan *plan, int64_t n_steps, void *stream);
+/* One kernel of the step sequence (for per-kernel timing or custom drivers):
+ * a run of n steps is PRE, then n times (CN, ROT_PRE or ROT on the last, ADVANCE). */
+enum {
+    ION_SH_PHASE_PRE = 1,     /* rotations before the first radial solve */
+    ION_SH_PHASE_CN = 2,      /* radial Crank-Nicolson solve of every (simulation, l) line */
+    ION_SH_PHASE_ROT = 3,     /* rotations after the solve, mask, data reductions */
+    ION_SH_PHASE_ROT_PRE = 4, /* as ROT, then the rotations before the next solve */
+    ION_SH_PHASE_ADVANCE = 5  /* finish reductions, advance every time index */
+};
+int ion_sh_split_phase_c128(const ion_sh_plan *plan, int phase, void *stream);
+int ion_sh_split_phase_c64(const ion_sh_plan *plan, int phase, void *stream);
 /* Reduce the data of the current time index (used for t = 0 before the run). */
 int ion_sh_reduce_c128(const ion_sh_plan *plan, void *stream);
 int ion_sh_reduce_c64(const ion_sh_plan *plan, void *stream);

@@ -34,7 +34,7 @@ def stream_ptr() -> int:
 
 
 def to_dev(a, dtype=None) -> torch.Tensor:
-    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+    a = np.array(a, dtype=dtype, copy=True, order="C")
     return torch.from_numpy(a).to(device(), non_blocking=False)
 
 
@@ -100,11 +100,12 @@ class ShTables:
 SH_ROT_ROWS = 32
 
 
-def sh_line_threads(n_r: int, precision) -> int:
-    maxm = 8 if Precision(precision) == Precision.C128 else 16
-    T = (n_r + maxm - 1) // maxm
-    T = min(T, n_r // 2)
-    return max(T, 1)
+SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8)}  # default first
+
+
+def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
+    maxm = rows or SH_ROWS_CHOICES[Precision(precision)][0]
+    return (n_r + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
 class ShDeviceSim:
@@ -182,9 +183,14 @@ class ShDeviceSim:
 class ShBatch:
     """Many spherical-harmonic simulations advanced together."""
 
-    def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None):
+    def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None, cn_rows: int = 0,
+                 rot_rows: int = SH_ROT_ROWS):
         self.precision = Precision(precision)
         self.sims: List[ShDeviceSim] = list(sims or [])
+        self.cn_rows = int(cn_rows)
+        self.rot_rows = int(rot_rows)
+        if self.rot_rows != SH_ROT_ROWS:
+            raise ValueError("row tiles of the rotation pass are fixed by the partial-sum layout")
         self._plan = None
         self._keep = None
 
@@ -217,10 +223,11 @@ class ShBatch:
         plan.max_n_r = max([s.n_r for s in sims] + [2])
         plan.cn_items = ptr(d_cn)
         plan.n_cn_items = len(cn)
-        plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision) for s in sims] + [1]))
+        plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, self.cn_rows) for s in sims] + [1]))
         plan.rot_items = ptr(d_rot)
         plan.n_rot_items = len(rot)
-        plan.rot_rows = SH_ROT_ROWS
+        plan.rot_rows = self.rot_rows
+        plan.cn_rows = self.cn_rows
         self._plan = plan
         self._keep = (d_descs, d_cn, d_rot)
 
@@ -274,8 +281,7 @@ class LineTables:
 
 def line_threads(n: int, precision) -> int:
     maxm = 8 if Precision(precision) == Precision.C128 else 16
-    T = (n + maxm - 1) // maxm
-    return max(min(T, n // 2), 1)
+    return (n + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
 class LineDeviceSim:

@@ -81,6 +81,8 @@ class ShPlan(ctypes.Structure):
         ("rot_items", c_vp),
         ("n_rot_items", c_i32),
         ("rot_rows", c_i32),
+        ("cn_rows", c_i32),
+        ("pad2_", c_i32),
     ]
 
 
@@ -150,6 +152,8 @@ _SIGS = {
     "ion_tdma_batched_max_n_c64": (c_i64, []),
     "ion_sh_split_run_c128": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_i64, c_vp]),
     "ion_sh_split_run_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_i64, c_vp]),
+    "ion_sh_split_phase_c128": (ctypes.c_int, [ctypes.POINTER(ShPlan), ctypes.c_int, c_vp]),
+    "ion_sh_split_phase_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), ctypes.c_int, c_vp]),
     "ion_sh_reduce_c128": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
     "ion_sh_reduce_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
     "ion_sh_max_n_r_c128": (c_i64, []),

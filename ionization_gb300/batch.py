@@ -1,0 +1,159 @@
+"""Batched form: many independent spherical-harmonic simulations per step.
+
+The reference runs parameter scans as one simulation per HTCondor job
+(ionization_scans/scan_utils.py:638-663).  Here every simulation of a scan
+lives in one device batch: each step is one launch of each fused kernel over
+all simulations (radial solve of every (simulation, l) line; rotation / mask /
+reduction pass over every (simulation, row tile); time-index advance), whatever
+their sizes, pulses and step counts.  Runs are captured into CUDA graphs of
+``graph_steps`` steps so the host issues one graph launch per chunk.
+
+The launch shape (rows per thread of the radial solve, graph chunk) comes
+from ``autotune``, a project-written autotuner that times candidates on the
+actual batch.
+"""
+
+import time
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _device as dev
+from . import _native as nat
+from .core import Precision
+
+
+def _host_tables(spec):
+    spec.host_only = True
+    try:
+        sim = spec.to_sim()
+        return sim.mesh.tables, sim
+    finally:
+        spec.host_only = False
+
+
+class BatchedSphericalHarmonicSimulation:
+    """Advance ``specs`` (SphericalHarmonicSpecification, split operator,
+    length gauge) together on one GPU.
+
+    ``precision`` overrides the specifications' precision ("c64" stores psi
+    in complex64 with FP64 fields, coefficient tables and reductions)."""
+
+    def __init__(self, specs, precision: Optional[str] = None, graph_steps: int = 64, use_graphs: bool = True,
+                 cn_rows: int = 0, tables=None):
+        self.specs = list(specs)
+        self.precision = Precision(precision or self.specs[0].precision)
+        if tables is None:
+            tables = [_host_tables(spec)[0] for spec in self.specs]
+        self.tables = tables
+        dsims = [dev.ShDeviceSim(tab, self.precision) for tab in tables]
+        self.sims = dsims
+        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows)
+        self.graph_steps = int(graph_steps)
+        self.use_graphs = use_graphs
+        self._graphs = {}
+        self._started = False
+        self.mesh_points = np.array([s.n_r * s.n_l for s in dsims], dtype=np.int64)
+
+    @property
+    def total_mesh_points(self) -> int:
+        return int(self.mesh_points.sum())
+
+    @property
+    def steps_remaining(self) -> int:
+        return max(s.t_final - s.t for s in self.sims)
+
+    def start(self):
+        if not self._started:
+            self.batch.reduce()
+            self._started = True
+
+    def _graph_for(self, n):
+        g = self._graphs.get(n)
+        if g is None:
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    nat.call(self.batch._fn("ion_sh_split_run"), nat.ctypes.byref(self.batch.plan), int(n),
+                             dev.stream_ptr())
+            torch.cuda.current_stream().wait_stream(s)
+            self._graphs[n] = g
+        return g
+
+    def step(self, n_steps: int = 1):
+        """Advance every unfinished simulation by up to ``n_steps``."""
+        self.start()
+        n_steps = int(min(n_steps, self.steps_remaining))
+        if n_steps <= 0:
+            return
+        if not self.use_graphs:
+            self.batch.run(n_steps)
+            return
+        # first use: run one plain step so every kernel attribute is set
+        if not self._graphs and n_steps > 0:
+            self.batch.run(1)
+            n_steps -= 1
+        k = self.graph_steps
+        while n_steps >= k:
+            self._graph_for(k).replay()
+            for s in self.sims:
+                s.t = min(s.t + k, s.t_final)
+            n_steps -= k
+        if n_steps:
+            self.batch.run(n_steps)
+
+    def run(self):
+        self.step(self.steps_remaining)
+
+    def results(self) -> List[dict]:
+        torch.cuda.synchronize()
+        out = []
+        for spec, s in zip(self.specs, self.sims):
+            norm, ips = s.data()
+            ip = {st: ips[k] for k, st in enumerate(spec.test_states)}
+            ov = {st: np.abs(v) ** 2 for st, v in ip.items()}
+            out.append(dict(
+                name=spec.name,
+                t=s.t,
+                norm=norm,
+                inner_products=ip,
+                initial_state_overlap=ov[spec.initial_state],
+                bound_state_overlap=sum(v for st, v in ov.items() if st.bound),
+            ))
+        return out
+
+    def psi(self, i) -> np.ndarray:
+        return self.sims[i].psi_host()
+
+
+def autotune(specs, precision="c64", graph_steps=(32,), steps=32, tables=None):
+    """Choose the launch shape of a batch by timing every candidate on it.
+
+    Candidates are (rows per thread of the radial solve -> threads per
+    radial system, graph chunk length).  Each is timed with CUDA events on
+    the launching stream after a warm-up; returns (best, {candidate: ms per
+    step})."""
+    precision = Precision(precision)
+    if tables is None:
+        tables = [_host_tables(spec)[0] for spec in specs]
+    timings = {}
+    for rows in dev.SH_ROWS_CHOICES[precision]:
+        for gs in graph_steps:
+            b = BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows,
+                                                   tables=tables)
+            b.step(1 + gs)  # warm-up and capture
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n = max(steps, gs)
+            e0.record()
+            b.step(n)
+            e1.record()
+            torch.cuda.synchronize()
+            timings[(rows, gs)] = e0.elapsed_time(e1) / n
+            del b
+    best = min(timings, key=timings.get)
+    return best, timings

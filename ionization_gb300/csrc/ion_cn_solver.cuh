@@ -1,0 +1,278 @@
+// Crank-Nicolson line solver used by every mesh kernel.
+//
+// Every implicit half-step of the mesh path solves A x = y with
+// A = 1 + i B, B = tau * H real and tridiagonal (H a discretised Hamiltonian
+// restricted to one line).  The solve is done in increment form: with psi the
+// line before the step,
+//     A (x - psi) = -i (w (B psi) + X)          x = psi + Delta
+// where w = 2 when the explicit half-step acts along the same line
+// (Crank-Nicolson: x = A^-1 (2 - A) psi) and w = 1 with X = (tau H' psi) the
+// explicit half-step along the other direction of an ADI pass.  Solving for
+// the increment keeps the rounding of the solve relative to |Delta| instead of
+// |psi|, which matters for the complex64 state.
+//
+// Parallel scheme (as in ion_solver.cuh): T threads, thread t owns the M rows
+// [t M, t M + M) (M compile-time, the line padded to T M rows with decoupled
+// rows B = 0, psi = 0), partition-method elimination of each chunk in
+// registers, PCR on the 2T reduced unknowns in shared memory, expansion.
+// psi sits in shared memory interleaved by chunk: row i at slot
+// (i % M) T + i / M, so the chunk reads of consecutive threads fall on
+// consecutive slots.
+//
+// Functors:  coef(i, bo, bd): bo = B[i][i+1] (0 on the last row and on
+// padding), bd = B[i][i] (0 on padding);  extra(i): X_i;  out(i, delta).
+#pragma once
+
+#include "ion_solver.cuh"
+
+namespace ion {
+
+template <int M>
+__host__ __device__ __forceinline__ int islot(int i, int T) {
+    return (i % M) * T + i / M;
+}
+
+__device__ __forceinline__ float rcp_ieee(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_ieee(double x) { return __drcp_rn(x); }
+
+template <typename R>
+__device__ __forceinline__ Cx<R> crecip_fast(Cx<R> z) {
+    const R inv = rcp_ieee(z.re * z.re + z.im * z.im);
+    return {z.re * inv, -z.im * inv};
+}
+
+// a0 x0 + a1 x1 + a2 x2.  FP64: plain.  FP32: compensated (error-free
+// products by FMA, TwoSum accumulation; Ogita, Rump & Oishi, "Accurate sum and
+// dot product", SIAM J. Sci. Comput. 26, 2005), so the result is the
+// correctly rounded value up to O(eps^2) even when the terms cancel.  The
+// intrinsics keep the compiler from contracting the error-free steps.
+__device__ __forceinline__ double dot3(double a0, double x0, double a1, double x1, double a2, double x2) {
+    return a0 * x0 + a1 * x1 + a2 * x2;
+}
+__device__ __forceinline__ float dot3(float a0, float x0, float a1, float x1, float a2, float x2) {
+    const float p0 = __fmul_rn(a0, x0), p1 = __fmul_rn(a1, x1), p2 = __fmul_rn(a2, x2);
+    const float e0 = __fmaf_rn(a0, x0, -p0), e1 = __fmaf_rn(a1, x1, -p1), e2 = __fmaf_rn(a2, x2, -p2);
+    float s = __fadd_rn(p0, p1);
+    float bb = __fsub_rn(s, p0);
+    const float t0 = __fadd_rn(__fsub_rn(p0, __fsub_rn(s, bb)), __fsub_rn(p1, bb));
+    const float s2 = __fadd_rn(s, p2);
+    bb = __fsub_rn(s2, s);
+    const float t1 = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bb)), __fsub_rn(p2, bb));
+    return __fadd_rn(s2, ((t0 + t1) + (e0 + e1)) + e2);
+}
+
+struct NoExtra {
+    template <typename R>
+    __device__ __forceinline__ Cx<R> get(int) const {
+        return Cx<R>{R(0), R(0)};
+    }
+};
+
+template <typename R, int M, class Coef, class Extra>
+__device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R>* psi, const Coef& coef,
+                                                   const Extra& extra, Cx<R> (&al)[M], Cx<R> (&be)[M],
+                                                   Cx<R> (&ga)[M], RedRow<R>& rowS, RedRow<R>& rowE) {
+    static_assert(M >= 3, "chunks need an interior");
+    const Cx<R> zero = {R(0), R(0)};
+    const int s = t * M;
+    R bo[M], bd[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) coef(s + k, bo[k], bd[k]);
+    R bom1 = R(0);
+    if (t > 0) {
+        R d_;
+        coef(s - 1, bom1, d_);
+    }
+    // psi of the chunk with one neighbour on each side
+    const Cx<R> pm1 = (t > 0) ? psi[(M - 1) * T + t - 1] : zero;
+    const Cx<R> pM = (t + 1 < T) ? psi[t + 1] : zero;
+    auto P = [&](int k) -> Cx<R> { return k < 0 ? pm1 : (k >= M ? pM : psi[k * T + t]); };
+    auto ao = [&](int k) -> R { return k == 0 ? bom1 : bo[k - 1]; };
+    // y_k = -i (w (B psi)_k + X_k)
+    auto Y = [&](int k) -> Cx<R> {
+        const Cx<R> p0 = P(k - 1), p1 = P(k), p2 = P(k + 1);
+        const R a0 = ao(k);
+        Cx<R> v = {dot3(a0, p0.re, bd[k], p1.re, bo[k], p2.re), dot3(a0, p0.im, bd[k], p1.im, bo[k], p2.im)};
+        const Cx<R> X = extra.template get<R>(s + k);
+        v = Cx<R>{w * v.re + X.re, w * v.im + X.im};
+        return Cx<R>{v.im, -v.re};  // -i v
+    };
+
+    Cx<R> cprev = zero, daprev = zero, dbprev = zero, glast = zero;
+#pragma unroll
+    for (int k = 1; k < M - 1; ++k) {
+        const Cx<R> b = {R(1), bd[k]};
+        const R a = ao(k);  // A[k][k-1] = i a
+        const Cx<R> denom = (k == 1) ? b : b - mul_ih(a, cprev);
+        const Cx<R> inv = crecip_fast(denom);
+        const Cx<R> cp = mul_ih(bo[k], inv);
+        const Cx<R> yk = Y(k);
+        const Cx<R> da = (k == 1) ? yk * inv : (yk - mul_ih(a, daprev)) * inv;
+        const Cx<R> db = (k == 1) ? -mul_ih(a, inv) : -(mul_ih(a, dbprev) * inv);
+        glast = -cp;
+        al[k] = da;
+        be[k] = db;
+        ga[k] = (k == M - 2) ? glast : cp;
+        cprev = cp;
+        daprev = da;
+        dbprev = db;
+    }
+#pragma unroll
+    for (int k = M - 3; k >= 1; --k) {
+        const Cx<R> cp = ga[k];
+        al[k] = al[k] - cp * al[k + 1];
+        be[k] = be[k] - cp * be[k + 1];
+        ga[k] = -(cp * ga[k + 1]);
+    }
+    // reduced rows: first row (coupled to the previous chunk's last unknown)
+    const Cx<R> b0 = {R(1), bd[0]};
+    const Cx<R> BS = b0 + mul_ih(bo[0], be[1]);
+    const Cx<R> CS = mul_ih(bo[0], ga[1]);
+    const Cx<R> DS = Y(0) - mul_ih(bo[0], al[1]);
+    // last row (coupled to the next chunk's first unknown)
+    const R aE = bo[M - 2];
+    const Cx<R> bE = {R(1), bd[M - 1]};
+    const Cx<R> AE = mul_ih(aE, dbprev);
+    const Cx<R> BE = bE + mul_ih(aE, glast);
+    const Cx<R> DE = Y(M - 1) - mul_ih(aE, daprev);
+    const Cx<R> iS = crecip_fast(BS), iE = crecip_fast(BE);
+    rowS.a = mul_ih(bom1, iS);
+    rowS.c = CS * iS;
+    rowS.d = DS * iS;
+    rowE.a = AE * iE;
+    rowE.c = mul_ih(bo[M - 1], iE);
+    rowE.d = DE * iE;
+}
+
+// PCR over 2T normalised rows; row k = 2u + q is stored at slot q T + u of
+// double-buffered A, C, D arrays (pcr_smem_bytes<R>(T) bytes).
+template <typename R>
+__device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2]) {
+    const Cx<R> zero = {R(0), R(0)};
+    const int N = 2 * T;
+    Cx<R>* Ab = red;
+    Cx<R>* Cb = red + 2 * N;
+    Cx<R>* Db = red + 4 * N;
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            Ab[q * T + t] = r[q].a;
+            Cb[q * T + t] = r[q].c;
+            Db[q * T + t] = r[q].d;
+        }
+    }
+    __syncthreads();
+    const int levels = pcr_levels(N);
+    int p = 0;
+    for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
+        if (active) {
+            const int base = p * N;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int k = 2 * t + q;
+                Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
+                const int km = k - sig, kp = k + sig;
+                if (km >= 0) {
+                    const int sl = base + (km & 1) * T + (km >> 1);
+                    am = Ab[sl];
+                    cm = Cb[sl];
+                    dm = Db[sl];
+                }
+                if (kp < N) {
+                    const int sl = base + (kp & 1) * T + (kp >> 1);
+                    ap = Ab[sl];
+                    cpp = Cb[sl];
+                    dp = Db[sl];
+                }
+                const Cx<R> a = r[q].a, c = r[q].c, d = r[q].d;
+                const Cx<R> nb = Cx<R>{R(1), R(0)} - cm * a - ap * c;
+                const Cx<R> inv = crecip_fast(nb);
+                r[q].a = -(am * a) * inv;
+                r[q].c = -(cpp * c) * inv;
+                r[q].d = (d - dm * a - dp * c) * inv;
+            }
+            const int wb = (p ^ 1) * N;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                Ab[wb + q * T + t] = r[q].a;
+                Cb[wb + q * T + t] = r[q].c;
+                Db[wb + q * T + t] = r[q].d;
+            }
+        }
+        p ^= 1;
+        __syncthreads();
+    }
+}
+
+// All threads of the CTA call this (threads t >= T only meet the barriers).
+// ``out(i, delta)`` is called for the T*M rows of the padded line.
+template <typename R, int M, class Coef, class Extra, class Out>
+__device__ __forceinline__ void block_cn_solve(int T, int t, R w, const Cx<R>* psi, Cx<R>* red, const Coef& coef,
+                                               const Extra& extra, const Out& out) {
+    const bool active = t < T;
+    Cx<R> al[M], be[M], ga[M];
+    RedRow<R> r[2];
+    if (active) cn_chunk_eliminate<R, M>(T, t, w, psi, coef, extra, al, be, ga, r[0], r[1]);
+    pcr_solve_cn<R>(T, t, active, red, r);
+    if (active) {
+        const int s = t * M;
+        const Cx<R> xs = r[0].d, xe = r[1].d;
+        out(s, xs);
+#pragma unroll
+        for (int k = 1; k < M - 1; ++k) out(s + k, al[k] + be[k] * xs + ga[k] * xe);
+        out(s + M - 1, xe);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rotation coefficients cos(a) - 1 and sin(a).
+// |a| <= 0.5: Maclaurin series of sin and cos evaluated with Horner's rule in
+// a^2 (truncated where the next term is below 1e-10 of the last kept one in
+// FP32 and below 1e-22 in FP64); otherwise sincos() with
+// cos(a) - 1 = -2 sin^2(a/2).  Returning cos - 1 lets the rotation be
+// applied in increment form.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rot_coeffs(float a, float& cm1, float& s) {
+    if (fabsf(a) <= 0.5f) {
+        const float a2 = a * a;
+        s = a * (1.f - a2 * (1.f / 6.f) * (1.f - a2 * (1.f / 20.f) * (1.f - a2 * (1.f / 42.f) * (1.f - a2 * (1.f / 72.f)))));
+        cm1 = -0.5f * a2 *
+              (1.f - a2 * (1.f / 12.f) * (1.f - a2 * (1.f / 30.f) * (1.f - a2 * (1.f / 56.f) * (1.f - a2 * (1.f / 90.f)))));
+    } else {
+        float c;
+        sincosf(a, &s, &c);
+        const float h = sinf(0.5f * a);
+        cm1 = -2.f * h * h;
+    }
+}
+
+__device__ __forceinline__ void rot_coeffs(double a, double& cm1, double& s) {
+    if (fabs(a) <= 0.5) {
+        const double a2 = a * a;
+        double ps = 1.0 - a2 * (1.0 / 272.0);
+        ps = 1.0 - a2 * (1.0 / 210.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 156.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 110.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 72.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 42.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 20.0) * ps;
+        ps = 1.0 - a2 * (1.0 / 6.0) * ps;
+        s = a * ps;
+        double pc = 1.0 - a2 * (1.0 / 306.0);
+        pc = 1.0 - a2 * (1.0 / 240.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 182.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 132.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 90.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 56.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 30.0) * pc;
+        pc = 1.0 - a2 * (1.0 / 12.0) * pc;
+        cm1 = -0.5 * a2 * pc;
+    } else {
+        double c;
+        sincos(a, &s, &c);
+        const double h = sin(0.5 * a);
+        cm1 = -2.0 * h * h;
+    }
+}
+
+}  // namespace ion

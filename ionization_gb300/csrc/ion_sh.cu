@@ -21,12 +21,16 @@
 #include <cstdio>
 
 #include "ion_common.cuh"
-#include "ion_solver.cuh"
+#include <type_traits>
+
+#include "ion_cn_solver.cuh"
 
 namespace ion {
 
 enum : int { ROT_PRE_ONLY = 1, ROT_STEP = 2, ROT_STEP_PRE = 3, ROT_REDUCE_ONLY = 4 };
 enum : int { ADV_STEP = 1, ADV_FINALIZE = 2 };
+
+constexpr int ROT_LANES = 8;  // threads sharing one row of a rotation tile
 
 template <typename R> struct ShCfg;
 template <> struct ShCfg<double> {
@@ -38,12 +42,9 @@ template <> struct ShCfg<float> {
     static constexpr int MAX_T = 512;
 };
 
-__host__ __device__ inline int sh_line_threads(int nr, int maxm) {
-    int T = (nr + maxm - 1) / maxm;
-    if (T > nr / 2) T = nr / 2;
-    if (T < 1) T = 1;
-    return T;
-}
+// threads of the radial solve of a line of nr points: nr rounded up to
+// whole chunks of maxm rows
+__host__ __device__ inline int sh_line_threads(int nr, int maxm) { return (nr + maxm - 1) / maxm; }
 
 __host__ __device__ inline bool is_data_time(int64_t t, int64_t t_final, int64_t every) {
     return t == 0 || t == t_final || (every >= 1 && t % every == 0);
@@ -83,51 +84,40 @@ template <> struct ShH<float> {  // FP32 tables rounded from FP64
     }
 };
 
+// A = 1 + i tau H0 on line l: coefficients for the CN solver (tau-scaled)
 template <typename R>
-struct ShCoef {
+struct ShCnCoef {
     ShH<R> h;
     R tau;
     int n;
-    __device__ void operator()(int64_t i, Cx<R>& a, Cx<R>& b, Cx<R>& c) const {
-        const Cx<R> zero = {R(0), R(0)};
-        a = (i > 0) ? Cx<R>{R(0), tau * h.off(int(i) - 1)} : zero;
-        b = Cx<R>{R(1), tau * h.diag(int(i))};
-        c = (i < n - 1) ? Cx<R>{R(0), tau * h.off(int(i))} : zero;
+    __device__ __forceinline__ void operator()(int i, R& bo, R& bd) const {
+        if (i >= n) {
+            bo = R(0);
+            bd = R(0);
+            return;
+        }
+        bd = tau * h.diag(i);
+        bo = (i < n - 1) ? tau * h.off(i) : R(0);
     }
 };
 
-// y_i = ((1 - i tau H) psi)_i with psi staged in shared memory; terms are
-// accumulated sub, diag, super as in the dia-matrix product
-template <typename R>
-struct ShExplicit {
-    ShH<R> h;
-    R tau;
-    int n;
-    const Cx<R>* psi;
-    __device__ Cx<R> operator()(int64_t i_) const {
-        const int i = int(i_);
-        Cx<R> y = {R(0), R(0)};
-        if (i > 0) y = mul_ih(-tau * h.off(i - 1), psi[i - 1]);
-        const Cx<R> p = psi[i];
-        const R hd = -tau * h.diag(i);
-        y = y + Cx<R>{p.re - hd * p.im, p.im + hd * p.re};
-        if (i < n - 1) y = y + mul_ih(-tau * h.off(i), psi[i + 1]);
-        return y;
-    }
-};
-
-template <typename R>
-struct SmemOut {
+// psi + delta into the interleaved line
+template <typename R, int M>
+struct AddOut {
     Cx<R>* line;
-    __device__ void operator()(int64_t i, Cx<R> x) const { line[i] = x; }
+    int T;
+    __device__ __forceinline__ void operator()(int i, Cx<R> d) const {
+        Cx<R>* p = line + islot<M>(i, T);
+        *p = *p + d;
+    }
 };
 
 template <typename R>
-__host__ __device__ inline size_t sh_cn_smem(int max_nr, int threads) {
-    return (size_t(max_nr) + 1) / 2 * 2 * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
+__host__ __device__ inline size_t sh_cn_smem(int threads, int M) {
+    return size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
 }
 
-template <typename R, int MAXM>
+template <typename R, int M>
 __global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int item = blockIdx.x;
@@ -137,19 +127,19 @@ __global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan) {
     const int64_t t = S.t;
     if (t >= S.t_final) return;  // whole CTA leaves together
     const int nr = S.n_r;
-    const int T = sh_line_threads(nr, MAXM);
+    const int T = (nr + M - 1) / M;
+    const int npad = T * M;
     Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* red = line + (plan.max_n_r + 1) / 2 * 2;
+    Cx<R>* red = line + plan.cn_threads * M;
     Cx<R>* g = static_cast<Cx<R>*>(S.g) + int64_t(l) * nr;
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) line[i] = ld(g + i);
+    const Cx<R> zero = {R(0), R(0)};
+    for (int i = threadIdx.x; i < npad; i += blockDim.x) line[islot<M>(i, T)] = (i < nr) ? ld(g + i) : zero;
     __syncthreads();
     const R tau = R(S.tau[t + 1]);
-    const ShH<R> h = ShH<R>::make(S, l);
-    ShCoef<R> coef{h, tau, nr};
-    ShExplicit<R> rhs{h, tau, nr, line};
-    block_line_solve<R, MAXM>(nr, T, threadIdx.x, int(threadIdx.x) < T, red, coef, rhs, SmemOut<R>{line});
+    const ShCnCoef<R> coef{ShH<R>::make(S, l), tau, nr};
+    block_cn_solve<R, M>(T, threadIdx.x, R(2), line, red, coef, NoExtra{}, AddOut<R, M>{line, T});
     __syncthreads();
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) st(g + i, line[i]);
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) st(g + i, line[islot<M>(i, T)]);
 }
 
 // ---------------------------------------------------------------------------
@@ -170,33 +160,74 @@ template <> struct RotTab<float> {
     __device__ static RotTab make(const ion_sh_sim& S) { return RotTab{S.cl32, S.rq32, S.mask32}; }
 };
 
-__device__ __forceinline__ void sincos_r(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ void sincos_r(float x, float* s, float* c) { sincosf(x, s, c); }
+// error-free sum (Knuth's TwoSum): a + b = s + e exactly
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+    const float s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+    return s;
+}
 
-constexpr int ROT_LANES = 8;  // threads sharing one row
+// The tile holds psi as hi (+ lo for complex64: a compensation word that
+// collects the rounding of every update inside the pass, folded in once
+// when psi is stored).
+template <typename R> struct Tile;
+template <> struct Tile<double> {
+    Cx<double>* hi;
+    static constexpr bool comp = false;
+    __device__ Cx<double> value(int k) const { return hi[k]; }
+    __device__ void rotate(int k0, int k1, double cm1, double s) const {
+        const Cx<double> x0 = hi[k0], x1 = hi[k1];
+        hi[k0] = Cx<double>{x0.re + (cm1 * x0.re + s * x1.im), x0.im + (cm1 * x0.im - s * x1.re)};
+        hi[k1] = Cx<double>{x1.re + (cm1 * x1.re + s * x0.im), x1.im + (cm1 * x1.im - s * x0.re)};
+    }
+    __device__ void scale(int k, double m) const { hi[k] = Cx<double>{hi[k].re * m, hi[k].im * m}; }
+    __device__ Cx<double> out(int k) const { return hi[k]; }
+};
+template <> struct Tile<float> {
+    Cx<float>* hi;
+    Cx<float>* lo;
+    static constexpr bool comp = true;
+    __device__ Cx<double> value(int k) const {
+        return Cx<double>{double(hi[k].re) + double(lo[k].re), double(hi[k].im) + double(lo[k].im)};
+    }
+    __device__ void rotate(int k0, int k1, float cm1, float s) const {
+        const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo[k0], l1 = lo[k1];
+        float e0r, e0i, e1r, e1i;
+        const float h0r = two_sum(x0.re, cm1 * x0.re + s * x1.im, e0r);
+        const float h0i = two_sum(x0.im, cm1 * x0.im - s * x1.re, e0i);
+        const float h1r = two_sum(x1.re, cm1 * x1.re + s * x0.im, e1r);
+        const float h1i = two_sum(x1.im, cm1 * x1.im - s * x0.re, e1i);
+        hi[k0] = Cx<float>{h0r, h0i};
+        hi[k1] = Cx<float>{h1r, h1i};
+        lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.im) + e0r, l0.im + (cm1 * l0.im - s * l1.re) + e0i};
+        lo[k1] = Cx<float>{l1.re + (cm1 * l1.re + s * l0.im) + e1r, l1.im + (cm1 * l1.im - s * l0.re) + e1i};
+    }
+    __device__ void scale(int k, float m) const {
+        hi[k] = Cx<float>{hi[k].re * m, hi[k].im * m};
+        lo[k] = Cx<float>{lo[k].re * m, lo[k].im * m};
+    }
+    __device__ Cx<float> out(int k) const { return Cx<float>{hi[k].re + lo[k].re, hi[k].im + lo[k].im}; }
+};
 
-// Apply one rotation operator (parity 0: pairs at even F index, 1: odd) of
-// time index n to the rows of the tile.  Pairs crossing a row boundary have a
+// One rotation operator (parity 0: pairs at even F index, 1: odd) of time
+// index n on every row of the tile.  Pairs crossing a row boundary have a
 // zero angle in the reference (mesh_operators.py:996-999) and are skipped.
+// Thread (jj, lane): jj = row of the tile, lane strides over the pairs.
 template <typename R>
-__device__ __forceinline__ void rotate_rows(Cx<R>* tile, int rows, int nl, int j0, int jj, int lane,
+__device__ __forceinline__ void rotate_rows(const Tile<R>& tl, int rows, int nl, int j0, int jj, int lane, int lanes,
                                             int parity, const RotTab<R>& tb, R tau, R efield) {
     if (jj < rows) {
         const int j = j0 + jj;
         const int l0 = int((int64_t(j) * nl + parity) & 1);
         const R rqj = tb.rq[j];
-        for (int l = l0 + 2 * lane; l + 1 < nl; l += 2 * ROT_LANES) {
-            const R theta = tau * ((tb.cl[l] * rqj) * efield);
-            R s, c;
-            sincos_r(theta, &s, &c);
-            Cx<R>* p0 = tile + l * rows + jj;
-            Cx<R>* p1 = p0 + rows;
-            const Cx<R> x0 = *p0, x1 = *p1;
-            *p0 = Cx<R>{c * x0.re + s * x1.im, c * x0.im - s * x1.re};
-            *p1 = Cx<R>{s * x0.im + c * x1.re, c * x1.im - s * x0.re};
+        for (int l = l0 + 2 * lane; l + 1 < nl; l += 2 * lanes) {
+            R cm1, s;
+            rot_coeffs(tau * ((tb.cl[l] * rqj) * efield), cm1, s);
+            tl.rotate(l * rows + jj, (l + 1) * rows + jj, cm1, s);
         }
     }
-    __syncwarp();
+    __syncthreads();
 }
 
 // block-wide FP64 sum (result valid in thread 0)
@@ -217,29 +248,26 @@ __device__ __forceinline__ double block_sum(double v, double* scratch) {
 
 // per-tile partial sums of |g|^2 and conj(s) g for every test state
 template <typename R>
-__device__ void reduce_tile(const ion_sh_sim& S, const Cx<R>* tile, int rows, int nl, int j0,
-                            int tile_idx, double* scratch) {
+__device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, int nl, int j0, int tile_idx,
+                            double* scratch) {
     const int nq = 1 + 2 * S.n_states;
-    const int jj = threadIdx.x / ROT_LANES, lane = threadIdx.x % ROT_LANES;
-    // norm
     double acc = 0.0;
-    if (jj < rows)
-        for (int l = lane; l < nl; l += ROT_LANES) {
-            const Cx<R> x = tile[l * rows + jj];
-            acc += double(x.re) * double(x.re) + double(x.im) * double(x.im);
-        }
-    double tot = block_sum(acc, scratch);
+    for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
+        const Cx<double> x = tl.value(f);
+        acc += x.re * x.re + x.im * x.im;
+    }
+    const double tot = block_sum(acc, scratch);
     if (threadIdx.x == 0) S.partials[int64_t(tile_idx) * nq] = tot;
-    // inner products with the test states: only row l_s of each state
     for (int s = 0; s < S.n_states; ++s) {
         const int ls = S.state_l[s];
         double re = 0.0, im = 0.0;
-        if (lane == 0 && jj < rows && ls < nl) {
-            const Cx<R> x = tile[ls * rows + jj];
+        const int jj = threadIdx.x;
+        if (jj < rows && ls < nl) {
+            const Cx<double> x = tl.value(ls * rows + jj);
             const double* sg = S.state_g + (int64_t(s) * S.n_r + j0 + jj) * 2;
             const double ar = sg[0], ai = -sg[1];  // conj(state)
-            re = ar * double(x.re) - ai * double(x.im);
-            im = ar * double(x.im) + ai * double(x.re);
+            re = ar * x.re - ai * x.im;
+            im = ar * x.im + ai * x.re;
         }
         const double tr = block_sum(re, scratch);
         const double ti = block_sum(im, scratch);
@@ -248,6 +276,11 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Cx<R>* tile, int rows, in
             S.partials[int64_t(tile_idx) * nq + 2 + 2 * s] = ti;
         }
     }
+}
+
+template <typename R>
+__host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
+    return size_t(max_nl) * rows * sizeof(Cx<R>) * (std::is_same<R, float>::value ? 2 : 1) + 32 * sizeof(double);
 }
 
 template <typename R>
@@ -260,7 +293,7 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode)
     const int64_t tf = S.t_final;
 
     bool post = false, do_mask = false, reduce = false, pre = false;
-    int64_t n_post = 0, n_pre = 0, t_reduce = 0;
+    int64_t n_post = 0, n_pre = 0;
     if (mode == ROT_PRE_ONLY) {
         if (t >= tf) return;
         pre = true;
@@ -271,62 +304,64 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode)
         n_post = t + 1;
         do_mask = S.mask != nullptr;
         reduce = is_data_time(t + 1, tf, S.store_every);
-        t_reduce = t + 1;
         if (mode == ROT_STEP_PRE && t + 1 < tf) {
             pre = true;
             n_pre = t + 2;
         }
     } else if (mode == ROT_REDUCE_ONLY) {
         reduce = is_data_time(t, tf, S.store_every);
-        t_reduce = t;
         if (!reduce) return;
     }
-    (void)t_reduce;
 
     const int nr = S.n_r, nl = S.n_l;
     const int rows_max = plan.rot_rows;
     const int j0 = tile_idx * rows_max;
     const int rows = min(rows_max, nr - j0);
     if (rows <= 0) return;
-    Cx<R>* tile = reinterpret_cast<Cx<R>*>(smem_raw);
-    double* scratch = reinterpret_cast<double*>(tile + size_t(plan.max_n_l) * rows_max);
+    const size_t tile_elems = size_t(plan.max_n_l) * rows_max;
+    Cx<R>* hi = reinterpret_cast<Cx<R>*>(smem_raw);
+    Tile<R> tl;
+    tl.hi = hi;
+    double* scratch;
+    if constexpr (Tile<R>::comp) {
+        tl.lo = hi + tile_elems;
+        scratch = reinterpret_cast<double*>(hi + 2 * tile_elems);
+    } else {
+        scratch = reinterpret_cast<double*>(hi + tile_elems);
+    }
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
-
     for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
         const int l = f / rows, jj = f - l * rows;
-        tile[l * rows + jj] = ld(g + int64_t(l) * nr + j0 + jj);
+        hi[f] = ld(g + int64_t(l) * nr + j0 + jj);
+        if constexpr (Tile<R>::comp) tl.lo[f] = Cx<R>{R(0), R(0)};
     }
     __syncthreads();
 
     const RotTab<R> tb = RotTab<R>::make(S);
-    const int jj = threadIdx.x / ROT_LANES, lane = threadIdx.x % ROT_LANES;
+    const int jj = threadIdx.x % rows_max, lane = threadIdx.x / rows_max;
+    const int lanes = blockDim.x / rows_max;
     if (post) {
         const R tau = R(S.tau[n_post]), ef = R(S.efield[n_post]);
-        rotate_rows<R>(tile, rows, nl, j0, jj, lane, 1, tb, tau, ef);  // odd
-        rotate_rows<R>(tile, rows, nl, j0, jj, lane, 0, tb, tau, ef);  // even
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
     }
-    if (do_mask && jj < rows) {
-        const R mk = tb.mask[j0 + jj];
-        for (int l = lane; l < nl; l += ROT_LANES) {
-            Cx<R>* p = tile + l * rows + jj;
-            *p = Cx<R>{p->re * mk, p->im * mk};
-        }
+    if (do_mask) {
+        for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) tl.scale(f, tb.mask[j0 + f % rows]);
+        __syncthreads();
     }
-    __syncthreads();
     if (reduce) {
-        reduce_tile<R>(S, tile, rows, nl, j0, tile_idx, scratch);
+        reduce_tile<R>(S, tl, rows, nl, j0, tile_idx, scratch);
         __syncthreads();
     }
     if (pre) {
         const R tau = R(S.tau[n_pre]), ef = R(S.efield[n_pre]);
-        rotate_rows<R>(tile, rows, nl, j0, jj, lane, 0, tb, tau, ef);  // even
-        rotate_rows<R>(tile, rows, nl, j0, jj, lane, 1, tb, tau, ef);  // odd
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
     }
-    __syncthreads();
     if (post || pre || do_mask) {
         for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
-            const int l = f / rows, jj2 = f - l * rows;
-            st(g + int64_t(l) * nr + j0 + jj2, tile[l * rows + jj2]);
+            const int l = f / rows, j2 = f - l * rows;
+            st(g + int64_t(l) * nr + j0 + j2, tl.out(f));
         }
     }
 }
@@ -370,17 +405,34 @@ __global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// rows per thread of the radial solve: the compile-time register capacity
+// of sh_cn_kernel; plan.cn_rows = 0 selects the default
+template <typename R> struct ShRows;
+template <> struct ShRows<double> {
+    static bool ok(int r) { return r == 4 || r == 8; }
+};
+template <> struct ShRows<float> {
+    static bool ok(int r) { return r == 8 || r == 16; }
+};
+
+template <typename R>
+static int sh_rows(const ion_sh_plan* p) {
+    return p->cn_rows == 0 ? ShCfg<R>::MAXM : p->cn_rows;
+}
+
 template <typename R>
 static int sh_validate(const ion_sh_plan* p) {
     if (!p || !p->sims || p->n_sims < 0 || p->n_cn_items < 0 || p->n_rot_items < 0 ||
-        p->rot_rows <= 0 || p->rot_rows > 64 || p->max_n_l <= 0 || p->max_n_r < 2 ||
+        p->rot_rows <= 0 || p->rot_rows > 32 || p->max_n_l <= 0 || p->max_n_r < 2 ||
         p->cn_threads <= 0 || p->cn_threads > ShCfg<R>::MAX_T || (p->cn_threads & 31) ||
-        int64_t(p->max_n_r) > int64_t(ShCfg<R>::MAXM) * ShCfg<R>::MAX_T) {
+        (p->cn_rows != 0 && !ShRows<R>::ok(p->cn_rows))) {
         set_error("ion_sh: invalid plan");
         return ION_ERR_INVALID_ARGUMENT;
     }
-    if (sh_line_threads(p->max_n_r, ShCfg<R>::MAXM) > p->cn_threads) {
-        set_error("ion_sh: cn_threads %d too small for n_r %d", p->cn_threads, p->max_n_r);
+    const int rows = sh_rows<R>(p);
+    if (int64_t(p->max_n_r) > int64_t(rows) * ShCfg<R>::MAX_T ||
+        sh_line_threads(p->max_n_r, rows) > p->cn_threads) {
+        set_error("ion_sh: cn_threads %d / rows %d too small for n_r %d", p->cn_threads, rows, p->max_n_r);
         return ION_ERR_INVALID_ARGUMENT;
     }
     return ION_OK;
@@ -388,7 +440,7 @@ static int sh_validate(const ion_sh_plan* p) {
 
 template <typename R>
 static size_t rot_smem(const ion_sh_plan* p) {
-    return size_t(p->max_n_l) * p->rot_rows * sizeof(Cx<R>) + 32 * sizeof(double);
+    return rot_smem_bytes<R>(p->max_n_l, p->rot_rows);
 }
 
 template <typename R>
@@ -404,11 +456,9 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     return check_launch("sh_rot_kernel");
 }
 
-template <typename R>
-static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s) {
-    if (p->n_cn_items == 0) return ION_OK;
-    constexpr int MAXM = ShCfg<R>::MAXM;
-    const size_t smem = sh_cn_smem<R>(p->max_n_r, p->cn_threads);
+template <typename R, int MAXM>
+static int sh_launch_cn_m(const ion_sh_plan* p, cudaStream_t s) {
+    const size_t smem = sh_cn_smem<R>(p->cn_threads, MAXM);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(sh_cn_kernel<R, MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -420,6 +470,21 @@ static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s) {
     }
     sh_cn_kernel<R, MAXM><<<p->n_cn_items, p->cn_threads, smem, s>>>(*p);
     return check_launch("sh_cn_kernel");
+}
+
+template <typename R>
+static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s);
+
+template <>
+int sh_launch_cn<double>(const ion_sh_plan* p, cudaStream_t s) {
+    if (p->n_cn_items == 0) return ION_OK;
+    return sh_rows<double>(p) == 4 ? sh_launch_cn_m<double, 4>(p, s) : sh_launch_cn_m<double, 8>(p, s);
+}
+
+template <>
+int sh_launch_cn<float>(const ion_sh_plan* p, cudaStream_t s) {
+    if (p->n_cn_items == 0) return ION_OK;
+    return sh_rows<float>(p) == 8 ? sh_launch_cn_m<float, 8>(p, s) : sh_launch_cn_m<float, 16>(p, s);
 }
 
 template <typename R>
@@ -439,6 +504,26 @@ static int sh_run(const ion_sh_plan* p, int64_t n_steps, void* stream) {
         if (int e = check_launch("sh_advance_kernel")) return e;
     }
     return ION_OK;
+}
+
+// one kernel of the step sequence, for per-kernel timing and custom drivers
+template <typename R>
+static int sh_phase(const ion_sh_plan* p, int phase, void* stream) {
+    if (int e = sh_validate<R>(p)) return e;
+    if (p->n_sims == 0) return ION_OK;
+    cudaStream_t s = as_stream(stream);
+    switch (phase) {
+        case ION_SH_PHASE_PRE: return sh_launch_rot<R>(p, ROT_PRE_ONLY, s);
+        case ION_SH_PHASE_CN: return sh_launch_cn<R>(p, s);
+        case ION_SH_PHASE_ROT: return sh_launch_rot<R>(p, ROT_STEP, s);
+        case ION_SH_PHASE_ROT_PRE: return sh_launch_rot<R>(p, ROT_STEP_PRE, s);
+        case ION_SH_PHASE_ADVANCE:
+            sh_advance_kernel<<<p->n_sims, 32, 0, s>>>(*p, ADV_STEP);
+            return check_launch("sh_advance_kernel");
+        default:
+            set_error("ion_sh: unknown phase %d", phase);
+            return ION_ERR_INVALID_ARGUMENT;
+    }
 }
 
 template <typename R>
@@ -462,6 +547,12 @@ int ion_sh_split_run_c128(const ion_sh_plan* plan, int64_t n_steps, void* stream
 }
 int ion_sh_split_run_c64(const ion_sh_plan* plan, int64_t n_steps, void* stream) {
     return sh_run<float>(plan, n_steps, stream);
+}
+int ion_sh_split_phase_c128(const ion_sh_plan* plan, int phase, void* stream) {
+    return sh_phase<double>(plan, phase, stream);
+}
+int ion_sh_split_phase_c64(const ion_sh_plan* plan, int phase, void* stream) {
+    return sh_phase<float>(plan, phase, stream);
 }
 int ion_sh_reduce_c128(const ion_sh_plan* plan, void* stream) { return sh_reduce<double>(plan, stream); }
 int ion_sh_reduce_c64(const ion_sh_plan* plan, void* stream) { return sh_reduce<float>(plan, stream); }

@@ -100,7 +100,9 @@ class Norm(Datastore):
         self.sim.data.norm = self.norm
 
     def pull(self, norm, ips):
-        self.norm[:] = norm
+        # slots the device has not written (NaN) keep their host value, which
+        # matters after a reload from a checkpoint
+        self.norm[:] = np.where(np.isnan(norm), self.norm, norm)
 
 
 DATA_NAME_TO_DATASTORE_TYPE.update({"norm": Norm})
@@ -117,7 +119,8 @@ class InnerProducts(Datastore):
 
     def pull(self, norm, ips):
         for k, state in enumerate(self.spec.test_states):
-            self.inner_products[state][:] = ips[k]
+            cur = self.inner_products[state]
+            cur[:] = np.where(np.isnan(ips[k]), cur, ips[k])
 
     def state_overlaps(self):
         return {state: np.abs(ip) ** 2 for state, ip in self.inner_products.items()}

@@ -22,7 +22,7 @@ def test_line_tables(name):
     np.testing.assert_array_equal(tb.hd, ref.H0.diag.real)
     np.testing.assert_array_equal(tb.hoff, ref.H0.sub.real)
     np.testing.assert_array_equal(tb.mask, ref.mask)
-    np.testing.assert_array_equal(tb.g0, z["g_initial"])
+    np.testing.assert_allclose(tb.g0, z["g_initial"], rtol=1e-14, atol=1e-300)
     times = om.get_times(params["time_initial"], params["time_final"], params["time_step"])
     np.testing.assert_array_equal(sim.times, times)
     np.testing.assert_array_equal(tb.efield[1:], ref.pulse.field(times[1:]))
@@ -43,7 +43,7 @@ def test_sh_tables(name):
     coupling = np.where((k + 1) % L != 0, tb.cl[k % L] * tb.rq[k // L], 0)
     np.testing.assert_array_equal(coupling, ref.l_off.real)
     np.testing.assert_array_equal(tb.mask, ref.mask[0])
-    np.testing.assert_array_equal(tb.g0, z["g_initial"])
+    np.testing.assert_allclose(tb.g0, z["g_initial"], rtol=1e-14, atol=1e-300)
     times = sim.times
     np.testing.assert_array_equal(tb.efield[1:], ref.pulse.field(times[1:] + params["time_step"] / 2))
     # test states: sorted like the reference, radial g identical
@@ -69,7 +69,7 @@ def test_cyl_tables():
     np.testing.assert_array_equal(tb["hz_d"], np.reshape(ref.H_z0.diag.real, (nz, nr), "F").ravel())
     np.testing.assert_array_equal(tb["hr_off"], ref.H_rho0.sub.real[: nr - 1])
     np.testing.assert_array_equal(tb["hz_off"], ref.H_z0.sub.real[: nz - 1])
-    np.testing.assert_array_equal(tb["g0"], z["g_initial"])
+    np.testing.assert_allclose(tb["g0"], z["g_initial"], rtol=1e-14, atol=1e-300)
     for s, gs in zip(params["test_states"], tb["state_g"]):
         np.testing.assert_array_equal(gs.reshape(nz, nr), ref.test_g[tuple(s)])
 

@@ -50,7 +50,7 @@ def test_oracle_run_matches_reference(kind, name):
     params, z = load_golden(name)
     out = om.run_from_params(kind, params)
     np.testing.assert_array_equal(out["times"], z["times"])
-    assert rel_l2(out["g_initial"], z["g_initial"]) == 0.0
+    assert rel_l2(out["g_initial"], z["g_initial"]) < 1e-14  # fixtures come from x86 libm
     assert rel_l2(out["g_final"], z["g_final"]) < 1e-13
     np.testing.assert_allclose(out["norm"], z["norm"], rtol=0, atol=1e-13)
     np.testing.assert_allclose(out["inner_products"], z["inner_products"], rtol=0, atol=1e-13)
