@@ -158,7 +158,12 @@ typedef struct ion_sh_plan {
     int32_t rot_rows;         /* rows (r points) per tile, <= 64 */
     int32_t cn_rows;          /* rows per thread of the radial solve: 0 = default,
                                  complex128 4 or 8, complex64 8 or 16 */
-    int32_t pad2_;
+    int32_t n_cn_buckets;     /* 0: one launch of cn_threads for all items; else the
+                                 items are sorted so that bucket b is the range
+                                 [cn_bucket_end[b-1], cn_bucket_end[b]) launched with
+                                 cn_bucket_threads[b] threads per CTA */
+    int32_t cn_bucket_end[8];
+    int32_t cn_bucket_threads[8];
 } ion_sh_plan;
 
 /* Advance every simulation of the plan by n_steps (fewer for simulations that

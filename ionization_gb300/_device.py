@@ -209,9 +209,16 @@ class ShBatch:
             descs[i] = s.descriptor()
         raw = np.frombuffer(bytes(descs), dtype=np.uint8).copy()
         d_descs = to_dev(raw)
-        # work lists, longest radial lines / widest tiles first
+        # radial items grouped in buckets of equal CTA size (largest first);
+        # each bucket is one launch whose blocks have exactly the threads its
+        # lines need
+        need = [_round32(sh_line_threads(s.n_r, self.precision, self.cn_rows)) for s in sims]
+        gran = 32
+        while len({(n + gran - 1) // gran * gran for n in need}) > 8:
+            gran *= 2
+        bsize = [(n + gran - 1) // gran * gran for n in need]
         cn = sorted(((i, l) for i, s in enumerate(sims) for l in range(s.n_l)),
-                    key=lambda it: -sims[it[0]].n_r)
+                    key=lambda it: (-bsize[it[0]], -sims[it[0]].n_r))
         rot = sorted(((i, k) for i, s in enumerate(sims) for k in range(s.n_tiles)),
                      key=lambda it: -sims[it[0]].n_l)
         d_cn = to_dev(np.asarray(cn if cn else [(0, 0)], dtype=np.int32).reshape(-1))
@@ -228,6 +235,18 @@ class ShBatch:
         plan.n_rot_items = len(rot)
         plan.rot_rows = self.rot_rows
         plan.cn_rows = self.cn_rows
+        ends, threads = [], []
+        for k, (i, _) in enumerate(cn):
+            if threads and threads[-1] == bsize[i]:
+                ends[-1] = k + 1
+            else:
+                threads.append(bsize[i])
+                ends.append(k + 1)
+        plan.cn_threads = max(threads + [32])
+        plan.n_cn_buckets = len(threads)
+        for b, (e, th) in enumerate(zip(ends, threads)):
+            plan.cn_bucket_end[b] = e
+            plan.cn_bucket_threads[b] = th
         self._plan = plan
         self._keep = (d_descs, d_cn, d_rot)
 

@@ -82,7 +82,9 @@ class ShPlan(ctypes.Structure):
         ("n_rot_items", c_i32),
         ("rot_rows", c_i32),
         ("cn_rows", c_i32),
-        ("pad2_", c_i32),
+        ("n_cn_buckets", c_i32),
+        ("cn_bucket_end", c_i32 * 8),
+        ("cn_bucket_threads", c_i32 * 8),
     ]
 
 

@@ -32,7 +32,9 @@ __host__ __device__ __forceinline__ int islot(int i, int T) {
     return (i % M) * T + i / M;
 }
 
-__device__ __forceinline__ float rcp_ieee(float x) { return __frcp_rn(x); }
+// complex64 pivots: the hardware reciprocal (MUFU, ~1 ulp) is ample for FP32
+// sweeps; complex128 keeps the correctly rounded reciprocal
+__device__ __forceinline__ float rcp_ieee(float x) { return __fdividef(1.0f, x); }
 __device__ __forceinline__ double rcp_ieee(double x) { return __drcp_rn(x); }
 
 template <typename R>
@@ -41,24 +43,24 @@ __device__ __forceinline__ Cx<R> crecip_fast(Cx<R> z) {
     return {z.re * inv, -z.im * inv};
 }
 
-// a0 x0 + a1 x1 + a2 x2.  FP64: plain.  FP32: compensated (error-free
-// products by FMA, TwoSum accumulation; Ogita, Rump & Oishi, "Accurate sum and
-// dot product", SIAM J. Sci. Comput. 26, 2005), so the result is the
-// correctly rounded value up to O(eps^2) even when the terms cancel.  The
-// intrinsics keep the compiler from contracting the error-free steps.
-__device__ __forceinline__ double dot3(double a0, double x0, double a1, double x1, double a2, double x2) {
-    return a0 * x0 + a1 * x1 + a2 * x2;
+// cp.async (LDGSTS) helpers: global -> shared copies that bypass registers,
+// completed with commit/wait groups
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ float dot3(float a0, float x0, float a1, float x1, float a2, float x2) {
-    const float p0 = __fmul_rn(a0, x0), p1 = __fmul_rn(a1, x1), p2 = __fmul_rn(a2, x2);
-    const float e0 = __fmaf_rn(a0, x0, -p0), e1 = __fmaf_rn(a1, x1, -p1), e2 = __fmaf_rn(a2, x2, -p2);
-    float s = __fadd_rn(p0, p1);
-    float bb = __fsub_rn(s, p0);
-    const float t0 = __fadd_rn(__fsub_rn(p0, __fsub_rn(s, bb)), __fsub_rn(p1, bb));
-    const float s2 = __fadd_rn(s, p2);
-    bb = __fsub_rn(s2, s);
-    const float t1 = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bb)), __fsub_rn(p2, bb));
-    return __fadd_rn(s2, ((t0 + t1) + (e0 + e1)) + e2);
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 struct NoExtra {
@@ -92,7 +94,7 @@ __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R
     auto Y = [&](int k) -> Cx<R> {
         const Cx<R> p0 = P(k - 1), p1 = P(k), p2 = P(k + 1);
         const R a0 = ao(k);
-        Cx<R> v = {dot3(a0, p0.re, bd[k], p1.re, bo[k], p2.re), dot3(a0, p0.im, bd[k], p1.im, bo[k], p2.im)};
+        Cx<R> v = {a0 * p0.re + bd[k] * p1.re + bo[k] * p2.re, a0 * p0.im + bd[k] * p1.im + bo[k] * p2.im};
         const Cx<R> X = extra.template get<R>(s + k);
         v = Cx<R>{w * v.re + X.re, w * v.im + X.im};
         return Cx<R>{v.im, -v.re};  // -i v

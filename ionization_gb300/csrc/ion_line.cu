@@ -160,7 +160,10 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     const R ef = R(S.efield[t + 1]);
     const bool split = S.method == ION_LINE_SPLIT;
 
-    for (int i = threadIdx.x; i < npad; i += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) {  // npad <= blockDim * M: loads issue together
+        const int i = threadIdx.x + k * blockDim.x;
+        if (i >= npad) continue;
         Cx<R> x = zero;
         if (i < n) {
             x = ld(g + i);

@@ -31,6 +31,7 @@ enum : int { ROT_PRE_ONLY = 1, ROT_STEP = 2, ROT_STEP_PRE = 3, ROT_REDUCE_ONLY =
 enum : int { ADV_STEP = 1, ADV_FINALIZE = 2 };
 
 constexpr int ROT_LANES = 8;  // threads sharing one row of a rotation tile
+constexpr int ROT_ROWS = 32;  // r rows per rotation tile (the shared-memory stride)
 
 template <typename R> struct ShCfg;
 template <> struct ShCfg<double> {
@@ -112,15 +113,63 @@ struct AddOut {
     }
 };
 
+template <typename R, int M>
+struct SmemCoef {  // (bo, bd) of every row staged in shared memory, interleaved
+    const Cx<R>* cf;
+    int T;
+    __device__ __forceinline__ void operator()(int i, R& bo, R& bd) const {
+        const Cx<R> v = cf[islot<M>(i, T)];
+        bo = v.re;
+        bd = v.im;
+    }
+};
+
 template <typename R>
 __host__ __device__ inline size_t sh_cn_smem(int threads, int M) {
-    return size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
+    return 2 * size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
 }
 
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+
+// L2 prefetch of the psi line of radial item ``item`` (128-byte lines)
+template <typename R>
+__device__ __forceinline__ void prefetch_cn_item(const ion_sh_plan& plan, int item) {
+    const int si = plan.cn_items[2 * item];
+    const int l = plan.cn_items[2 * item + 1];
+    const ion_sh_sim& S = plan.sims[si];
+    const char* p = reinterpret_cast<const char*>(static_cast<const Cx<R>*>(S.g) + int64_t(l) * S.n_r);
+    const int bytes = S.n_r * int(sizeof(Cx<R>));
+    for (int o = threadIdx.x * 128; o < bytes; o += blockDim.x * 128) prefetch_l2(p + o);
+}
+
+// L2 prefetch of the rows of rotation tile ``item`` (n_l segments of
+// ROT_ROWS points)
+template <typename R>
+__device__ __forceinline__ void prefetch_rot_item(const ion_sh_plan& plan, int item) {
+    const int si = plan.rot_items[2 * item];
+    const int tile = plan.rot_items[2 * item + 1];
+    const ion_sh_sim& S = plan.sims[si];
+    const Cx<R>* g = static_cast<const Cx<R>*>(S.g);
+    constexpr int per_seg = (32 * int(sizeof(Cx<R>)) + 127) / 128;  // cache lines per l segment
+    for (int f = threadIdx.x; f < S.n_l * per_seg; f += blockDim.x) {
+        const int l = f / per_seg, c = f - l * per_seg;
+        const char* p = reinterpret_cast<const char*>(g + int64_t(l) * S.n_r + tile * 32) + c * 128;
+        prefetch_l2(p);
+    }
+}
+
+// One CTA per (simulation, l) item of plan.cn_items[item0 + blockIdx.x].
+// The line and its tau-scaled coefficients are staged in shared memory in
+// one pass (all global loads issued together), then solved.  Each CTA first
+// asks L2 for the line of the item ``pf_dist`` ahead (about one resident
+// wave later), so later CTAs start from L2 instead of HBM.
 template <typename R, int M>
-__global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan) {
+__global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan, int item0, int item_end, int pf_dist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int item = blockIdx.x;
+    const int item = item0 + blockIdx.x;
+    if (pf_dist > 0 && item + pf_dist < item_end) prefetch_cn_item<R>(plan, item + pf_dist);
     const int si = plan.cn_items[2 * item];
     const int l = plan.cn_items[2 * item + 1];
     const ion_sh_sim& S = plan.sims[si];
@@ -129,17 +178,30 @@ __global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan) {
     const int nr = S.n_r;
     const int T = (nr + M - 1) / M;
     const int npad = T * M;
+    const int cap = blockDim.x * M;
     Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* red = line + plan.cn_threads * M;
+    Cx<R>* cf = line + cap;
+    Cx<R>* red = cf + cap;
     Cx<R>* g = static_cast<Cx<R>*>(S.g) + int64_t(l) * nr;
-    const Cx<R> zero = {R(0), R(0)};
-    for (int i = threadIdx.x; i < npad; i += blockDim.x) line[islot<M>(i, T)] = (i < nr) ? ld(g + i) : zero;
-    __syncthreads();
     const R tau = R(S.tau[t + 1]);
     const ShCnCoef<R> coef{ShH<R>::make(S, l), tau, nr};
-    block_cn_solve<R, M>(T, threadIdx.x, R(2), line, red, coef, NoExtra{}, AddOut<R, M>{line, T});
+    const Cx<R> zero = {R(0), R(0)};
+#pragma unroll 4
+    for (int i = threadIdx.x; i < npad; i += blockDim.x) {
+        const int sl = islot<M>(i, T);
+        line[sl] = (i < nr) ? ld(g + i) : zero;
+        R bo, bd;
+        coef(i, bo, bd);
+        cf[sl] = Cx<R>{bo, bd};
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < nr; i += blockDim.x) st(g + i, line[islot<M>(i, T)]);
+    block_cn_solve<R, M>(T, threadIdx.x, R(2), line, red, SmemCoef<R, M>{cf, T}, NoExtra{}, AddOut<R, M>{line, T});
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        if (i < nr) st(g + i, line[islot<M>(i, T)]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -160,11 +222,11 @@ template <> struct RotTab<float> {
     __device__ static RotTab make(const ion_sh_sim& S) { return RotTab{S.cl32, S.rq32, S.mask32}; }
 };
 
-// error-free sum (Knuth's TwoSum): a + b = s + e exactly
+// Dekker's Fast2Sum: a + b = s + e exactly when |a| >= |b|, which holds for
+// the small rotation increments added to psi here
 __device__ __forceinline__ float two_sum(float a, float b, float& e) {
     const float s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    e = b - (s - a);
     return s;
 }
 
@@ -224,7 +286,7 @@ __device__ __forceinline__ void rotate_rows(const Tile<R>& tl, int rows, int nl,
         for (int l = l0 + 2 * lane; l + 1 < nl; l += 2 * lanes) {
             R cm1, s;
             rot_coeffs(tau * ((tb.cl[l] * rqj) * efield), cm1, s);
-            tl.rotate(l * rows + jj, (l + 1) * rows + jj, cm1, s);
+            tl.rotate(l * ROT_ROWS + jj, (l + 1) * ROT_ROWS + jj, cm1, s);
         }
     }
     __syncthreads();
@@ -252,7 +314,8 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, in
                             double* scratch) {
     const int nq = 1 + 2 * S.n_states;
     double acc = 0.0;
-    for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
+    for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
+        if ((f & (ROT_ROWS - 1)) >= rows) continue;
         const Cx<double> x = tl.value(f);
         acc += x.re * x.re + x.im * x.im;
     }
@@ -263,7 +326,7 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, in
         double re = 0.0, im = 0.0;
         const int jj = threadIdx.x;
         if (jj < rows && ls < nl) {
-            const Cx<double> x = tl.value(ls * rows + jj);
+            const Cx<double> x = tl.value(ls * ROT_ROWS + jj);
             const double* sg = S.state_g + (int64_t(s) * S.n_r + j0 + jj) * 2;
             const double ar = sg[0], ai = -sg[1];  // conj(state)
             re = ar * x.re - ai * x.im;
@@ -284,7 +347,7 @@ __host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode) {
+__global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode, int pf_dist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int si = plan.rot_items[2 * blockIdx.x];
     const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
@@ -314,7 +377,7 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode)
     }
 
     const int nr = S.n_r, nl = S.n_l;
-    const int rows_max = plan.rot_rows;
+    constexpr int rows_max = ROT_ROWS;
     const int j0 = tile_idx * rows_max;
     const int rows = min(rows_max, nr - j0);
     if (rows <= 0) return;
@@ -330,23 +393,30 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode)
         scratch = reinterpret_cast<double*>(hi + tile_elems);
     }
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
-    for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
-        const int l = f / rows, jj = f - l * rows;
-        hi[f] = ld(g + int64_t(l) * nr + j0 + jj);
-        if constexpr (Tile<R>::comp) tl.lo[f] = Cx<R>{R(0), R(0)};
+#pragma unroll 4
+    for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
+        const int l = f >> 5, jj = f & (ROT_ROWS - 1);
+        if (jj < rows) {
+            hi[f] = ld(g + int64_t(l) * nr + j0 + jj);
+            if constexpr (Tile<R>::comp) tl.lo[f] = Cx<R>{R(0), R(0)};
+        }
     }
+    if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
     __syncthreads();
 
     const RotTab<R> tb = RotTab<R>::make(S);
-    const int jj = threadIdx.x % rows_max, lane = threadIdx.x / rows_max;
-    const int lanes = blockDim.x / rows_max;
+    const int jj = threadIdx.x & (ROT_ROWS - 1), lane = threadIdx.x >> 5;
+    const int lanes = blockDim.x >> 5;
     if (post) {
         const R tau = R(S.tau[n_post]), ef = R(S.efield[n_post]);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
     }
     if (do_mask) {
-        for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) tl.scale(f, tb.mask[j0 + f % rows]);
+        for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
+            const int jm = f & (ROT_ROWS - 1);
+            if (jm < rows) tl.scale(f, tb.mask[j0 + jm]);
+        }
         __syncthreads();
     }
     if (reduce) {
@@ -359,9 +429,10 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode)
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
     }
     if (post || pre || do_mask) {
-        for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
-            const int l = f / rows, j2 = f - l * rows;
-            st(g + int64_t(l) * nr + j0 + j2, tl.out(f));
+#pragma unroll 4
+        for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
+            const int l = f >> 5, j2 = f & (ROT_ROWS - 1);
+            if (j2 < rows) st(g + int64_t(l) * nr + j0 + j2, tl.out(f));
         }
     }
 }
@@ -429,6 +500,23 @@ static int sh_validate(const ion_sh_plan* p) {
         set_error("ion_sh: invalid plan");
         return ION_ERR_INVALID_ARGUMENT;
     }
+    if (p->n_cn_buckets < 0 || p->n_cn_buckets > 8) {
+        set_error("ion_sh: invalid bucket count");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    for (int b = 0, prev = 0; b < p->n_cn_buckets; ++b) {
+        const int th = p->cn_bucket_threads[b];
+        if (p->cn_bucket_end[b] < prev || p->cn_bucket_end[b] > p->n_cn_items || th <= 0 ||
+            th > ShCfg<R>::MAX_T || (th & 31) || th > p->cn_threads) {
+            set_error("ion_sh: invalid bucket %d", b);
+            return ION_ERR_INVALID_ARGUMENT;
+        }
+        prev = p->cn_bucket_end[b];
+    }
+    if (p->n_cn_buckets > 0 && p->cn_bucket_end[p->n_cn_buckets - 1] != p->n_cn_items) {
+        set_error("ion_sh: buckets do not cover the items");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
     const int rows = sh_rows<R>(p);
     if (int64_t(p->max_n_r) > int64_t(rows) * ShCfg<R>::MAX_T ||
         sh_line_threads(p->max_n_r, rows) > p->cn_threads) {
@@ -440,7 +528,7 @@ static int sh_validate(const ion_sh_plan* p) {
 
 template <typename R>
 static size_t rot_smem(const ion_sh_plan* p) {
-    return rot_smem_bytes<R>(p->max_n_l, p->rot_rows);
+    return rot_smem_bytes<R>(p->max_n_l, ROT_ROWS);
 }
 
 template <typename R>
@@ -452,24 +540,40 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
         cudaFuncSetAttribute(sh_rot_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    sh_rot_kernel<R><<<p->n_rot_items, p->rot_rows * ROT_LANES, smem, s>>>(*p, mode);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
+    sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
     return check_launch("sh_rot_kernel");
 }
 
 template <typename R, int MAXM>
 static int sh_launch_cn_m(const ion_sh_plan* p, cudaStream_t s) {
-    const size_t smem = sh_cn_smem<R>(p->cn_threads, MAXM);
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(sh_cn_kernel<R, MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
-    if (smem > 200 * 1024) {
-        set_error("ion_sh: radial line too long for shared memory");
-        return ION_ERR_UNSUPPORTED;
+    const int nb = p->n_cn_buckets;
+    int begin = 0;
+    for (int b = 0; b < (nb > 0 ? nb : 1); ++b) {
+        const int end = nb > 0 ? p->cn_bucket_end[b] : p->n_cn_items;
+        const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
+        if (end > begin) {
+            const size_t smem = sh_cn_smem<R>(threads, MAXM);
+            if (smem > 200 * 1024) {
+                set_error("ion_sh: radial line too long for shared memory");
+                return ION_ERR_UNSUPPORTED;
+            }
+            // prefetch distance: the CTAs resident on the whole GPU at once
+            int per_sm = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_cn_kernel<R, MAXM>, threads, smem);
+            const int pf_dist = per_sm * num_sms();
+            sh_cn_kernel<R, MAXM><<<end - begin, threads, smem, s>>>(*p, begin, end, pf_dist);
+            if (int e = check_launch("sh_cn_kernel")) return e;
+        }
+        begin = end;
     }
-    sh_cn_kernel<R, MAXM><<<p->n_cn_items, p->cn_threads, smem, s>>>(*p);
-    return check_launch("sh_cn_kernel");
+    return ION_OK;
 }
 
 template <typename R>
