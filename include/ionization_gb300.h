@@ -76,6 +76,26 @@ int ion_tdma_c128(int64_t n, const void *sub, const void *diag, const void *sup,
 int ion_tdma_c64(int64_t n, const void *sub, const void *diag, const void *sup, const void *d,
                  void *x, void *scratch, int64_t scratch_bytes, void *stream);
 
+/* One system of n rows, like ion_tdma_c128, but taking no scratch argument and
+ * allocating nothing.  This entry point has no counterpart in the reference.
+ * It is for callers that cannot call cudaMalloc around the solve, for example
+ * a host code that runs under a fixed device-memory budget handed out once at
+ * start-up, or a time-stepping loop that must not pay the implicit device
+ * synchronisation an allocation can cause.  The partition scratch lives in a
+ * file-scope device array of 5 MiB (5242880 bytes), enough for
+ * n <= ion_tdma_noalloc_max_n_c128() = 65536; larger n is rejected with
+ * ION_ERR_INVALID_ARGUMENT.  Every GPU that loads this library holds that
+ * array until the process exits.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and caches it; make that first
+ * call before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (two streams, or two host threads) race on it and
+ * must be serialised by the caller.  The array keeps whatever the last call
+ * left in it; nothing in it has to start at zero, because each call writes
+ * every scratch word before reading it. */
+int ion_tdma_noalloc_c128(int64_t n, const void *sub, const void *diag, const void *sup, const void *d,
+                          void *x, void *stream);
+int64_t ion_tdma_noalloc_max_n_c128(void);
+
 /* nsys independent systems of n rows each, flattened back to back as the mesh
  * operators hand them to cy.tdma (system s = rows [s*n, (s+1)*n) of one long
  * vector of nsys*n rows; sub/sup hold nsys*n-1 entries).  The entries that

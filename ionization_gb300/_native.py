@@ -148,6 +148,8 @@ _SIGS = {
     "ion_tdma_scratch_bytes_c64": (c_i64, [c_i64]),
     "ion_tdma_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
     "ion_tdma_c64": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp]),
+    "ion_tdma_noalloc_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ion_tdma_noalloc_max_n_c128": (c_i64, []),
     "ion_tdma_batched_c128": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ion_tdma_batched_c64": (ctypes.c_int, [c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ion_tdma_batched_max_n_c128": (c_i64, []),

@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "ion_common.cuh"
 #include "ion_solver.cuh"
@@ -358,9 +359,78 @@ static int tdma_batched_impl(int64_t nsys, int64_t n, const void* sub, const voi
 
 }  // namespace ion
 
+// ---------------------------------------------------------------------------
+// Scratch-free entry point: the single-system solve with its partition
+// scratch in a fixed, file-scope device array rather than caller memory.
+// ---------------------------------------------------------------------------
+namespace ion {
+
+// Largest system it accepts, and the scratch that size needs
+// (ion_tdma_scratch_bytes_c128(65536); the need grows with n up to there).
+constexpr int64_t NOALLOC_MAX_N = 65536;
+constexpr int64_t NOALLOC_SCRATCH_BYTES = 5242880;
+
+// Held by every GPU that loads this library, until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// The array's name is only a host-side stand-in; its device address is
+// looked up once per device, with that device current, and cached.
+static void* g_noalloc_addr[64] = {nullptr};
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch_address(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        set_error("ion_tdma_noalloc_c128: no usable current device (%s)", cudaGetErrorString(e));
+        return ION_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_addr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error("ion_tdma_noalloc_c128: cudaGetSymbolAddress failed (%s)", cudaGetErrorString(e));
+            return ION_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return ION_OK;
+}
+
+static int tdma_noalloc_c128(int64_t n, const void* sub, const void* diag, const void* sup, const void* d,
+                             void* x, void* stream) {
+    if (n < 1 || n > NOALLOC_MAX_N) {
+        set_error("ion_tdma_noalloc_c128: n = %lld is outside 1..%lld (the size of its fixed scratch)",
+                  (long long)n, (long long)NOALLOC_MAX_N);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    const int64_t need = scratch_elems<double>(n) * int64_t(sizeof(Cx<double>));
+    if (need > NOALLOC_SCRATCH_BYTES) {
+        set_error("ion_tdma_noalloc_c128: n = %lld needs %lld scratch bytes, more than the %lld held",
+                  (long long)n, (long long)need, (long long)NOALLOC_SCRATCH_BYTES);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    void* scratch = nullptr;
+    if (need > 0)
+        if (int e = noalloc_scratch_address(&scratch)) return e;
+    // every scratch word the partition reads is written earlier in the same
+    // call, so nothing has to be cleared between calls
+    return tdma_impl<double>(n, sub, diag, sup, d, x, scratch, NOALLOC_SCRATCH_BYTES, stream);
+}
+
+}  // namespace ion
+
 using namespace ion;
 
 extern "C" {
+
+int ion_tdma_noalloc_c128(int64_t n, const void* sub, const void* diag, const void* sup, const void* d, void* x,
+                          void* stream) {
+    return tdma_noalloc_c128(n, sub, diag, sup, d, x, stream);
+}
+int64_t ion_tdma_noalloc_max_n_c128(void) { return NOALLOC_MAX_N; }
 
 const char* ion_last_error(void) { return g_err; }
 int ion_version(void) { return 100; }
