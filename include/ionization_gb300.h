@@ -215,10 +215,15 @@ int64_t ion_sh_max_n_r_c64(void);
  *     (1 + i tau H)^-1 (1 - i tau H),  H = H0 + diag(zq * E(times[t+1]))
  * method ION_LINE_SPLIT — SplitInteractionOperator (evolution_methods.py:80-123):
  *     S (1 + i tau H0)^-1 (1 - i tau H0) S,  S = diag(exp(-i tau zq E(times[t+1])))
+ * method ION_LINE_FFT — Fourier split-step, no counterpart in the reference:
+ *     P F^-1 K F P,  P = diag(exp(-i tau (vstat + zq E(times[t+1])))),
+ *     K = diag(exp(-i 2 tau kin)), F the discrete Fourier transform;
+ *     periodic in z, n a power of two.
  * followed by g *= mask (meshes.py:256-257).  One CTA advances one
- * simulation; data reductions are fused into the same pass.
+ * simulation; data reductions are fused into the same pass.  Simulations of
+ * different methods may share one plan.
  * ------------------------------------------------------------------------ */
-enum { ION_LINE_ADI = 0, ION_LINE_SPLIT = 1 };
+enum { ION_LINE_ADI = 0, ION_LINE_SPLIT = 1, ION_LINE_FFT = 2 };
 
 typedef struct ion_line_sim {
     void *g;          /* device psi [n], complex128 or complex64 */
@@ -241,6 +246,12 @@ typedef struct ion_line_sim {
     double weight;         /* delta z */
     double *out_norm;      /* [n_data] */
     double *out_ip;        /* [n_data*n_states*2] */
+    /* ION_LINE_FFT only (NULL otherwise) */
+    const double *vstat;   /* [n] static potential V(z) */
+    const double *kin;     /* [n] kinetic energy hbar^2 k^2 / (2 m) of the Fourier mode that the
+                              forward transform leaves at position i (bit-reversed order) */
+    const void *twiddle;   /* [n] exp(-2 pi i m / n), complex128 for _c128, complex64 for _c64 */
+    const float *vstat32;
 } ion_line_sim;
 
 typedef struct ion_line_plan {
@@ -248,13 +259,17 @@ typedef struct ion_line_plan {
     int32_t n_sims;
     int32_t max_n;
     int32_t threads; /* CTA size (multiple of 32) */
-    int32_t pad_;
+    int32_t cluster; /* CTAs per simulation.  0 or 1: one CTA, n <= ion_line_max_n_*().
+                        2..8: a thread-block cluster, the line split into equal
+                        segments, n <= cluster * ion_line_max_n_*(); Crank-Nicolson
+                        methods only (ION_LINE_FFT simulations are left untouched) */
 } ion_line_plan;
 
 int ion_line_run_c128(const ion_line_plan *plan, int64_t n_steps, void *stream);
 int ion_line_run_c64(const ion_line_plan *plan, int64_t n_steps, void *stream);
 int ion_line_reduce_c128(const ion_line_plan *plan, void *stream);
 int ion_line_reduce_c64(const ion_line_plan *plan, void *stream);
+/* Longest line one CTA holds (a cluster of C CTAs holds C times as much). */
 int64_t ion_line_max_n_c128(void);
 int64_t ion_line_max_n_c64(void);
 

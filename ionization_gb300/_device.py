@@ -283,7 +283,7 @@ class ShBatch:
 @dataclasses.dataclass
 class LineTables:
     n: int
-    method: int  # nat.ION_LINE_ADI or nat.ION_LINE_SPLIT
+    method: int  # nat.ION_LINE_ADI, ION_LINE_SPLIT or ION_LINE_FFT
     hd: np.ndarray
     hoff: np.ndarray
     zq: np.ndarray
@@ -296,11 +296,28 @@ class LineTables:
     t0: int
     t_final: int
     store_every: int
+    vstat: Optional[np.ndarray] = None  # ION_LINE_FFT: static potential
+    kin: Optional[np.ndarray] = None  # ION_LINE_FFT: kinetic energies in bit-reversed order
+    twiddle: Optional[np.ndarray] = None  # ION_LINE_FFT: exp(-2 pi i m / n)
 
 
 def line_threads(n: int, precision) -> int:
     maxm = 8 if Precision(precision) == Precision.C128 else 16
     return (n + maxm - 1) // maxm  # the line is padded to whole chunks
+
+
+LINE_MAX_CLUSTER = 8
+
+
+def line_cta_max_n(precision) -> int:
+    """Longest line one CTA of the line kernel holds."""
+    return int(nat.value("ion_line_max_n_" + Precision(precision).value))
+
+
+def line_cluster(n: int, precision, cta_max: Optional[int] = None) -> int:
+    """CTAs (a thread-block cluster when > 1) that advance a line of n points."""
+    cta_max = line_cta_max_n(precision) if cta_max is None else cta_max
+    return max(1, -(-int(n) // int(cta_max)))
 
 
 class LineDeviceSim:
@@ -318,6 +335,11 @@ class LineDeviceSim:
         self.d_tau, self.d_ef = to_dev(tab.tau, f64), to_dev(tab.efield, f64)
         self.d_hd32, self.d_hoff32, self.d_zq32 = to_dev(tab.hd, f32), to_dev(tab.hoff, f32), to_dev(tab.zq, f32)
         self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
+        self.d_vstat = self.d_vstat32 = self.d_kin = self.d_twiddle = None
+        if tab.method == nat.ION_LINE_FFT:
+            self.d_vstat, self.d_vstat32 = to_dev(tab.vstat, f64), to_dev(tab.vstat, f32)
+            self.d_kin = to_dev(tab.kin, f64)
+            self.d_twiddle = to_dev(np.asarray(tab.twiddle, np.complex128)).to(complex_dtype(precision))
         sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(-1, self.n)
         self.n_states = sg.shape[0]
         self.d_state_g = to_dev(sg.view(np.float64).reshape(-1)) if self.n_states else to_dev(np.zeros(2))
@@ -341,6 +363,7 @@ class LineDeviceSim:
         d.state_g = ptr(self.d_state_g)
         d.weight = float(self.tab.weight)
         d.out_norm, d.out_ip = ptr(self.d_norm), ptr(self.d_ip)
+        d.vstat, d.kin, d.twiddle, d.vstat32 = ptr(self.d_vstat), ptr(self.d_kin), ptr(self.d_twiddle), ptr(self.d_vstat32)
         return d
 
     def data(self):
@@ -353,38 +376,66 @@ class LineDeviceSim:
 
 
 class LineBatch:
+    """Line simulations advanced together: one launch per cluster size (lines
+    up to one CTA's capacity in one launch, longer ones in thread-block
+    clusters of 2..8 CTAs), any mix of methods, sizes and step counts."""
+
     def __init__(self, precision, sims: Optional[List[LineDeviceSim]] = None):
         self.precision = Precision(precision)
         self.sims: List[LineDeviceSim] = list(sims or [])
-        self._plan = None
+        self._plans = None
         self._keep = None
+        self._cta_max = None
 
     def add(self, sim):
         self.sims.append(sim)
-        self._plan = None
+        self._plans = None
 
     def remove(self, sim):
         self.sims.remove(sim)
-        self._plan = None
+        self._plans = None
 
     def invalidate(self):
-        self._plan = None
+        self._plans = None
+
+    def _cluster_of(self, sim) -> int:
+        if self._cta_max is None:
+            self._cta_max = line_cta_max_n(self.precision)
+        return line_cluster(sim.n, self.precision, self._cta_max)
+
+    @property
+    def plans(self):
+        if self._plans is None:
+            groups = {}
+            for s in self.sims:
+                groups.setdefault(self._cluster_of(s), []).append(s)
+            plans, keep = [], []
+            maxm = 8 if self.precision == Precision.C128 else 16
+            for c in sorted(groups):
+                sims = groups[c]
+                descs = (nat.LineSim * len(sims))()
+                for i, s in enumerate(sims):
+                    descs[i] = s.descriptor()
+                d = to_dev(np.frombuffer(bytes(descs), dtype=np.uint8).copy())
+                p = nat.LinePlan()
+                p.sims = ptr(d)
+                p.n_sims = len(sims)
+                p.max_n = max(s.n for s in sims)
+                p.threads = _round32(max(-(-s.n // (c * maxm)) for s in sims))
+                p.cluster = c
+                plans.append(p)
+                keep.append(d)
+            self._plans = plans
+            self._keep = keep
+        return self._plans
 
     @property
     def plan(self):
-        if self._plan is None:
-            descs = (nat.LineSim * max(len(self.sims), 1))()
-            for i, s in enumerate(self.sims):
-                descs[i] = s.descriptor()
-            d = to_dev(np.frombuffer(bytes(descs), dtype=np.uint8).copy())
-            p = nat.LinePlan()
-            p.sims = ptr(d)
-            p.n_sims = len(self.sims)
-            p.max_n = max([s.n for s in self.sims] + [2])
-            p.threads = _round32(max([line_threads(s.n, self.precision) for s in self.sims] + [1]))
-            self._plan = p
-            self._keep = d
-        return self._plan
+        """The single plan of a batch whose lines all take the same cluster size."""
+        plans = self.plans
+        if len(plans) != 1:
+            raise ValueError("batch spans several cluster sizes; use .plans")
+        return plans[0]
 
     def _fn(self, base):
         return base + ("_c128" if self.precision == Precision.C128 else "_c64")
@@ -392,13 +443,17 @@ class LineBatch:
     def run(self, n_steps: int):
         if n_steps <= 0 or not self.sims:
             return
-        nat.call(self._fn("ion_line_run"), ctypes.byref(self.plan), int(n_steps), stream_ptr())
+        fn = self._fn("ion_line_run")
+        for p in self.plans:
+            nat.call(fn, ctypes.byref(p), int(n_steps), stream_ptr())
         for s in self.sims:
             s.t = min(s.t + int(n_steps), s.t_final)
 
     def reduce(self):
         if self.sims:
-            nat.call(self._fn("ion_line_reduce"), ctypes.byref(self.plan), stream_ptr())
+            fn = self._fn("ion_line_reduce")
+            for p in self.plans:
+                nat.call(fn, ctypes.byref(p), stream_ptr())
 
 
 # ==========================================================================

@@ -22,6 +22,7 @@ c_i32, c_i64, c_f32, c_f64, c_vp = (
 ION_OK = 0
 ION_LINE_ADI = 0
 ION_LINE_SPLIT = 1
+ION_LINE_FFT = 2
 
 
 class NativeLibraryError(RuntimeError):
@@ -112,6 +113,10 @@ class LineSim(ctypes.Structure):
         ("weight", c_f64),
         ("out_norm", c_vp),
         ("out_ip", c_vp),
+        ("vstat", c_vp),
+        ("kin", c_vp),
+        ("twiddle", c_vp),
+        ("vstat32", c_vp),
     ]
 
 
@@ -121,7 +126,7 @@ class LinePlan(ctypes.Structure):
         ("n_sims", c_i32),
         ("max_n", c_i32),
         ("threads", c_i32),
-        ("pad_", c_i32),
+        ("cluster", c_i32),
     ]
 
 

@@ -157,3 +157,38 @@ def autotune(specs, precision="c64", graph_steps=(32,), steps=32, tables=None):
             del b
     best = min(timings, key=timings.get)
     return best, timings
+
+
+def _main(argv=None):
+    """Run the first ``--sims`` simulations of the seeded uneven sweep for a
+    few steps and print the time per step: a small, self-contained case of
+    the batched kernels (``python -m ionization_gb300.batch --sims 200``)."""
+    import argparse
+
+    from . import workloads as wl
+
+    ap = argparse.ArgumentParser(prog="python -m ionization_gb300.batch")
+    ap.add_argument("--sims", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", default="c64", choices=["c64", "c128"])
+    ap.add_argument("--rows", type=int, default=None, help="rows per thread of the radial solve")
+    ap.add_argument("--graphs", action="store_true", help="capture the steps in CUDA graphs")
+    a = ap.parse_args(argv)
+    specs = wl.uneven_sh_sweep(512, steps=10000, precision=a.precision)[: a.sims]
+    b = BatchedSphericalHarmonicSimulation(specs, precision=a.precision, use_graphs=a.graphs, cn_rows=a.rows or 0)
+    b.step(a.warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    b.step(a.steps)
+    e1.record()
+    torch.cuda.synchronize()
+    pts = b.total_mesh_points
+    ms = e0.elapsed_time(e1) / max(a.steps, 1)
+    print(f"{len(specs)} simulations, {pts} mesh points, {a.precision}: {ms:.4f} ms/step, "
+          f"{pts / ms * 1e3:.4g} point-steps/s")
+
+
+if __name__ == "__main__":
+    _main()

@@ -70,10 +70,27 @@ struct NoExtra {
     }
 };
 
-template <typename R, int M, class Coef, class Extra>
+// Rows next to a chunk that another thread owns.  LocalHalo: the line ends
+// at the first and last thread of the CTA.  ClusterHalo (the long-line
+// kernel) continues the line into the neighbouring CTAs of a cluster.
+struct LocalHalo {
+    __device__ __forceinline__ bool has_left(int t) const { return t > 0; }
+    __device__ __forceinline__ bool has_right(int t, int T) const { return t + 1 < T; }
+    template <typename R, int M>
+    __device__ __forceinline__ Cx<R> left(const Cx<R>* psi, int T, int t) const {
+        return psi[(M - 1) * T + t - 1];
+    }
+    template <typename R>
+    __device__ __forceinline__ Cx<R> right(const Cx<R>* psi, int T, int t) const {
+        return psi[t + 1];
+    }
+};
+
+template <typename R, int M, class Coef, class Extra, class Halo = LocalHalo>
 __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R>* psi, const Coef& coef,
                                                    const Extra& extra, Cx<R> (&al)[M], Cx<R> (&be)[M],
-                                                   Cx<R> (&ga)[M], RedRow<R>& rowS, RedRow<R>& rowE) {
+                                                   Cx<R> (&ga)[M], RedRow<R>& rowS, RedRow<R>& rowE,
+                                                   const Halo& halo = Halo{}) {
     static_assert(M >= 3, "chunks need an interior");
     const Cx<R> zero = {R(0), R(0)};
     const int s = t * M;
@@ -81,13 +98,14 @@ __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R
 #pragma unroll
     for (int k = 0; k < M; ++k) coef(s + k, bo[k], bd[k]);
     R bom1 = R(0);
-    if (t > 0) {
+    const bool hl = halo.has_left(t);
+    if (hl) {
         R d_;
         coef(s - 1, bom1, d_);
     }
     // psi of the chunk with one neighbour on each side
-    const Cx<R> pm1 = (t > 0) ? psi[(M - 1) * T + t - 1] : zero;
-    const Cx<R> pM = (t + 1 < T) ? psi[t + 1] : zero;
+    const Cx<R> pm1 = hl ? halo.template left<R, M>(psi, T, t) : zero;
+    const Cx<R> pM = halo.has_right(t, T) ? halo.template right<R>(psi, T, t) : zero;
     auto P = [&](int k) -> Cx<R> { return k < 0 ? pm1 : (k >= M ? pM : psi[k * T + t]); };
     auto ao = [&](int k) -> R { return k == 0 ? bom1 : bo[k - 1]; };
     // y_k = -i (w (B psi)_k + X_k)

@@ -10,8 +10,12 @@
 // the split-operator phase factors and the mask are applied on the way in and
 // out, and at data times the norm / inner products are reduced from shared
 // memory before psi is stored.
+#include <cooperative_groups.h>
+
 #include "ion_common.cuh"
 #include "ion_cn_solver.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ion {
 
@@ -97,13 +101,18 @@ __device__ __forceinline__ double block_sum_l(double v, double* scratch) {
     return r;
 }
 
-// norm and inner products of the line held in shared memory (FP64)
+// norm and inner products of the line held in shared memory (FP64).  The
+// first ``stride`` threads (a count fixed by the simulation alone) take rows
+// i = thread + k stride, so the sums do not depend on the CTA size of the
+// launch, i.e. on the other simulations of a plan.
 template <typename R, int M>
-__device__ void line_reduce(const ion_line_sim& S, const Cx<R>* line, int T, int64_t t, double* scratch) {
+__device__ void line_reduce(const ion_line_sim& S, const Cx<R>* line, int T, int stride, int64_t t,
+                            double* scratch) {
     const int n = S.n;
     const int64_t slot = line_slot(t, S.t_final, S.store_every);
+    const int i0 = int(threadIdx.x) < stride ? int(threadIdx.x) : n;
     double acc = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = i0; i < n; i += stride) {
         const Cx<R> x = line[islot<M>(i, T)];
         acc += double(x.re) * double(x.re) + double(x.im) * double(x.im);
     }
@@ -112,7 +121,7 @@ __device__ void line_reduce(const ion_line_sim& S, const Cx<R>* line, int T, int
     for (int s = 0; s < S.n_states; ++s) {
         const double* sg = S.state_g + int64_t(s) * n * 2;
         double re = 0.0, im = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int i = i0; i < n; i += stride) {
             const Cx<R> x = line[islot<M>(i, T)];
             const double ar = sg[2 * i], ai = -sg[2 * i + 1];
             re += ar * double(x.re) - ai * double(x.im);
@@ -132,6 +141,143 @@ __host__ __device__ inline size_t line_smem(int threads, int M) {
     return size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads) + 32 * sizeof(double);
 }
 
+// ---------------------------------------------------------------------------
+// Fourier split-step (ION_LINE_FFT; the reference evolves lines only with
+// Crank-Nicolson):
+//   psi <- mask * P F^-1 K F P psi,
+//   P = exp(-i tau (V + zq E(t_{n+1}))),  K = exp(-i 2 tau E_kin(k)) / n,
+// periodic in z.  F is an in-place radix-4 decimation-in-frequency FFT of the
+// line held in shared memory (n = 2^k, a final radix-2 stage when k is odd).
+// Every radix-4 butterfly stores its outputs in the order of two radix-2
+// stages, so the spectrum comes out in bit-reversed order; K is tabulated in
+// that order and the inverse applies the exact inverse of each forward
+// butterfly in reverse order, which gives back natural order (times n, folded
+// into K).  No reordering pass is needed.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ Cx<R> ldg_cx(const Cx<R>* p) {
+    const typename Vec2<R>::type v = __ldg(reinterpret_cast<const typename Vec2<R>::type*>(p));
+    return {v.x, v.y};
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_conj(Cx<R> a, Cx<R> w) {  // a * conj(w)
+    return {a.re * w.re + a.im * w.im, a.im * w.re - a.re * w.im};
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_minus_i(Cx<R> a) { return {a.im, -a.re}; }
+template <typename R>
+__device__ __forceinline__ Cx<R> mul_plus_i(Cx<R> a) { return {-a.im, a.re}; }
+
+// forward radix-4 stage over blocks of 4q points, q = 2^lq; tw[m] = exp(-2 pi i m / n)
+template <typename R>
+__device__ __forceinline__ void fft_dif4(Cx<R>* x, int n, int lq, const Cx<R>* __restrict__ tw) {
+    const int q = 1 << lq;
+    const int s = n >> (lq + 2);  // w_{4q}^j = tw[j s]
+    for (int b = threadIdx.x; b < (n >> 2); b += blockDim.x) {
+        const int k = b & (q - 1);
+        const int i0 = ((b >> lq) << (lq + 2)) + k;
+        const Cx<R> a0 = x[i0], a1 = x[i0 + q], a2 = x[i0 + 2 * q], a3 = x[i0 + 3 * q];
+        const Cx<R> t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_minus_i(a1 - a3);
+        x[i0] = t0 + t2;
+        x[i0 + q] = (t0 - t2) * ldg_cx(tw + 2 * k * s);
+        x[i0 + 2 * q] = (t1 + t3) * ldg_cx(tw + k * s);
+        x[i0 + 3 * q] = (t1 - t3) * ldg_cx(tw + 3 * k * s);
+    }
+}
+
+// inverse of fft_dif4 (times 4)
+template <typename R>
+__device__ __forceinline__ void fft_dif4_inverse(Cx<R>* x, int n, int lq, const Cx<R>* __restrict__ tw) {
+    const int q = 1 << lq;
+    const int s = n >> (lq + 2);
+    for (int b = threadIdx.x; b < (n >> 2); b += blockDim.x) {
+        const int k = b & (q - 1);
+        const int i0 = ((b >> lq) << (lq + 2)) + k;
+        const Cx<R> y0 = x[i0];
+        const Cx<R> u2 = mul_conj(x[i0 + q], ldg_cx(tw + 2 * k * s));
+        const Cx<R> u1 = mul_conj(x[i0 + 2 * q], ldg_cx(tw + k * s));
+        const Cx<R> u3 = mul_conj(x[i0 + 3 * q], ldg_cx(tw + 3 * k * s));
+        const Cx<R> t0 = y0 + u2, t2 = y0 - u2, t1 = u1 + u3, t3 = mul_plus_i(u1 - u3);
+        x[i0] = t0 + t1;
+        x[i0 + 2 * q] = t0 - t1;
+        x[i0 + q] = t2 + t3;
+        x[i0 + 3 * q] = t2 - t3;
+    }
+}
+
+// radix-2 stage over blocks of 2 points (its own inverse, times 2)
+template <typename R>
+__device__ __forceinline__ void fft_pairs(Cx<R>* x, int n) {
+    for (int j = threadIdx.x; j < (n >> 1); j += blockDim.x) {
+        const Cx<R> a = x[2 * j], b = x[2 * j + 1];
+        x[2 * j] = a + b;
+        x[2 * j + 1] = a - b;
+    }
+}
+
+template <typename R> struct FftTab;
+template <> struct FftTab<double> {
+    const double *v, *zq, *mask;
+    __device__ static FftTab make(const ion_line_sim& S) { return {S.vstat, S.zq, S.mask}; }
+};
+template <> struct FftTab<float> {
+    const float *v, *zq, *mask;
+    __device__ static FftTab make(const ion_line_sim& S) { return {S.vstat32, S.zq32, S.mask32}; }
+};
+
+// the kinetic phase angle 2 tau E_kin is formed in FP64; the FP32 path reduces
+// it to [-pi, pi] first so that its rounding is relative to the reduced angle
+template <typename R> __device__ __forceinline__ R kinetic_angle(double a);
+template <> __device__ __forceinline__ double kinetic_angle<double>(double a) { return a; }
+template <> __device__ __forceinline__ float kinetic_angle<float>(double a) {
+    const double turns = rint(a * 0.15915494309189535);  // a / (2 pi), to the nearest integer
+    return float(fma(-turns, 6.283185307179586, a));
+}
+
+template <typename R>
+__device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, double* scratch) {
+    const int n = S.n;
+    const int lg = 31 - __clz(n);
+    const FftTab<R> tb = FftTab<R>::make(S);
+    const Cx<R>* tw = static_cast<const Cx<R>*>(S.twiddle);
+    Cx<R>* g = static_cast<Cx<R>*>(S.g);
+    const double tau = S.tau[t + 1];
+    const R taur = R(tau), ef = R(S.efield[t + 1]);
+
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = phase(ld(g + i), taur * (tb.v[i] + tb.zq[i] * ef));
+    __syncthreads();
+    for (int lq = lg - 2; lq >= 0; lq -= 2) {
+        fft_dif4(x, n, lq, tw);
+        __syncthreads();
+    }
+    if (lg & 1) {
+        fft_pairs(x, n);
+        __syncthreads();
+    }
+    const R inv_n = R(1) / R(n);  // exact: n is a power of two
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        x[i] = scale(phase(x[i], kinetic_angle<R>(2.0 * tau * S.kin[i])), inv_n);
+    __syncthreads();
+    if (lg & 1) {
+        fft_pairs(x, n);
+        __syncthreads();
+    }
+    for (int lq = lg & 1; lq <= lg - 2; lq += 2) {
+        fft_dif4_inverse(x, n, lq, tw);
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        Cx<R> y = phase(x[i], taur * (tb.v[i] + tb.zq[i] * ef));
+        if (tb.mask) y = Cx<R>{y.re * tb.mask[i], y.im * tb.mask[i]};
+        x[i] = y;
+        st(g + i, y);
+    }
+    __syncthreads();
+    if (line_is_data(t + 1, S.t_final, S.store_every)) line_reduce<R, 1>(S, x, n, stride, t + 1, scratch);
+    __syncthreads();
+    if (threadIdx.x == 0) S.t = t + 1;
+}
+
 // mode 0: one step (t -> t+1) then reduce if data time; mode 1: reduce at t only
 template <typename R, int M>
 __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int mode) {
@@ -146,15 +292,20 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     double* scratch = reinterpret_cast<double*>(red + 12 * plan.threads);
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
     const Cx<R> zero = {R(0), R(0)};
+    if (n < 2 || n > plan.max_n) return;  // the plan's shared memory is sized for max_n
 
     if (mode == 1) {
         if (!line_is_data(t, tf, S.store_every)) return;
         for (int i = threadIdx.x; i < n; i += blockDim.x) line[islot<M>(i, T)] = ld(g + i);
         __syncthreads();
-        line_reduce<R, M>(S, line, T, t, scratch);
+        line_reduce<R, M>(S, line, T, T, t, scratch);
         return;
     }
     if (t >= tf) return;
+    if (S.method == ION_LINE_FFT) {
+        line_fft_step<R>(S, t, line, T, scratch);
+        return;
+    }
     const LineTab<R> tb = LineTab<R>::make(S);
     const R tau = R(S.tau[t + 1]);
     const R ef = R(S.efield[t + 1]);
@@ -184,20 +335,278 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
         st(g + i, x);
     }
     __syncthreads();
-    if (line_is_data(t + 1, tf, S.store_every)) line_reduce<R, M>(S, line, T, t + 1, scratch);
+    if (line_is_data(t + 1, tf, S.store_every)) line_reduce<R, M>(S, line, T, T, t + 1, scratch);
     __syncthreads();
     if (threadIdx.x == 0) S.t = t + 1;
 }
+
+// ---------------------------------------------------------------------------
+// Lines longer than one CTA holds: one thread-block cluster of C CTAs per
+// simulation.  CTA r holds rows [r T M, (r+1) T M) of the line in its shared
+// memory, with the same per-thread chunks as the one-CTA kernel.  The chunk
+// halos at a segment edge are read from the neighbouring CTA's shared memory
+// (DSMEM), and the PCR of the 2 T C reduced rows runs across the cluster, the
+// rows of other CTAs read through DSMEM, one cluster barrier per level.  Data
+// reductions are summed per CTA, gathered on rank 0 and added in rank order.
+// Every CTA of a cluster works on the same simulation, so every early return
+// is taken by the whole cluster.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct ClusterHalo {
+    const Cx<R>* prev;  // line of the previous CTA (DSMEM), nullptr on rank 0
+    const Cx<R>* next;  // line of the next CTA, nullptr on the last rank
+    __device__ __forceinline__ bool has_left(int t) const { return t > 0 || prev != nullptr; }
+    __device__ __forceinline__ bool has_right(int t, int T) const { return t + 1 < T || next != nullptr; }
+    template <typename RR, int M>
+    __device__ __forceinline__ Cx<RR> left(const Cx<RR>* psi, int T, int t) const {
+        return t > 0 ? psi[(M - 1) * T + t - 1] : reinterpret_cast<const Cx<RR>*>(prev)[(M - 1) * T + T - 1];
+    }
+    template <typename RR>
+    __device__ __forceinline__ Cx<RR> right(const Cx<RR>* psi, int T, int t) const {
+        return t + 1 < T ? psi[t + 1] : reinterpret_cast<const Cx<RR>*>(next)[0];
+    }
+};
+
+template <typename R>
+struct OffsetCoef {
+    LineCnCoef<R> c;
+    int off;
+    __device__ __forceinline__ void operator()(int i, R& bo, R& bd) const { c(off + i, bo, bd); }
+};
+
+// PCR over the C * 2T reduced rows of a cluster; row k of CTA r is global
+// row r 2T + k, stored as in pcr_solve_cn.  Called by every thread of every
+// CTA of the cluster.
+template <typename R>
+__device__ __forceinline__ void pcr_solve_cluster(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2],
+                                                  int rank, int C) {
+    cg::cluster_group cl = cg::this_cluster();
+    const Cx<R> zero = {R(0), R(0)};
+    const int N = 2 * T, NT = N * C;
+    Cx<R>* Ab = red;
+    Cx<R>* Cb = red + 2 * N;
+    Cx<R>* Db = red + 4 * N;
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            Ab[q * T + t] = r[q].a;
+            Cb[q * T + t] = r[q].c;
+            Db[q * T + t] = r[q].d;
+        }
+    }
+    cl.sync();
+    const int levels = pcr_levels(NT);
+    int p = 0;
+    for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
+        if (active) {
+            const int base = p * N;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int k = rank * N + 2 * t + q;
+                Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
+                const int km = k - sig, kp = k + sig;
+                if (km >= 0) {
+                    const int o = km / N, l = km - o * N;
+                    const int sl = base + (l & 1) * T + (l >> 1);
+                    const Cx<R>* A_ = o == rank ? Ab : cl.map_shared_rank(Ab, o);
+                    const Cx<R>* C_ = o == rank ? Cb : cl.map_shared_rank(Cb, o);
+                    const Cx<R>* D_ = o == rank ? Db : cl.map_shared_rank(Db, o);
+                    am = A_[sl];
+                    cm = C_[sl];
+                    dm = D_[sl];
+                }
+                if (kp < NT) {
+                    const int o = kp / N, l = kp - o * N;
+                    const int sl = base + (l & 1) * T + (l >> 1);
+                    const Cx<R>* A_ = o == rank ? Ab : cl.map_shared_rank(Ab, o);
+                    const Cx<R>* C_ = o == rank ? Cb : cl.map_shared_rank(Cb, o);
+                    const Cx<R>* D_ = o == rank ? Db : cl.map_shared_rank(Db, o);
+                    ap = A_[sl];
+                    cpp = C_[sl];
+                    dp = D_[sl];
+                }
+                const Cx<R> a = r[q].a, c = r[q].c, d = r[q].d;
+                const Cx<R> nb = Cx<R>{R(1), R(0)} - cm * a - ap * c;
+                const Cx<R> inv = crecip_fast(nb);
+                r[q].a = -(am * a) * inv;
+                r[q].c = -(cpp * c) * inv;
+                r[q].d = (d - dm * a - dp * c) * inv;
+            }
+            const int wb = (p ^ 1) * N;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                Ab[wb + q * T + t] = r[q].a;
+                Cb[wb + q * T + t] = r[q].c;
+                Db[wb + q * T + t] = r[q].d;
+            }
+        }
+        p ^= 1;
+        cl.sync();
+    }
+}
+
+// sum of one or two doubles (valid in thread 0 of each CTA) over the cluster,
+// added in rank order on rank 0; ``part`` is 32 doubles of shared memory,
+// double-buffered by ``round`` so one cluster barrier per round suffices
+__device__ __forceinline__ void cluster_sum2(double& a, double& b, double* part, int round, int rank, int C) {
+    cg::cluster_group cl = cg::this_cluster();
+    double* buf = part + (round & 1) * 16;
+    if (threadIdx.x == 0) {
+        double* dst = cl.map_shared_rank(buf, 0);
+        dst[2 * rank] = a;
+        dst[2 * rank + 1] = b;
+    }
+    cl.sync();
+    if (rank == 0 && threadIdx.x == 0) {
+        a = 0.0;
+        b = 0.0;
+        for (int k = 0; k < C; ++k) {
+            a += buf[2 * k];
+            b += buf[2 * k + 1];
+        }
+    }
+}
+
+template <typename R, int M>
+__device__ void line_reduce_cluster(const ion_line_sim& S, const Cx<R>* line, int T, int off, int64_t t,
+                                    double* scratch, double* part, int rank, int C) {
+    const int n = S.n;
+    const int L = T * M;
+    const int64_t slot = line_slot(t, S.t_final, S.store_every);
+    const int i0 = int(threadIdx.x) < T ? int(threadIdx.x) : L;  // see line_reduce
+    double acc = 0.0;
+    for (int i = i0; i < L && off + i < n; i += T) {
+        const Cx<R> x = line[islot<M>(i, T)];
+        acc += double(x.re) * double(x.re) + double(x.im) * double(x.im);
+    }
+    double nrm = block_sum_l(acc, scratch), unused = 0.0;
+    cluster_sum2(nrm, unused, part, 0, rank, C);
+    if (rank == 0 && threadIdx.x == 0) S.out_norm[slot] = nrm * S.weight;
+    for (int s = 0; s < S.n_states; ++s) {
+        const double* sg = S.state_g + int64_t(s) * n * 2;
+        double re = 0.0, im = 0.0;
+        for (int i = i0; i < L && off + i < n; i += T) {
+            const Cx<R> x = line[islot<M>(i, T)];
+            const double ar = sg[2 * (off + i)], ai = -sg[2 * (off + i) + 1];
+            re += ar * double(x.re) - ai * double(x.im);
+            im += ar * double(x.im) + ai * double(x.re);
+        }
+        double tr = block_sum_l(re, scratch);
+        double ti = block_sum_l(im, scratch);
+        cluster_sum2(tr, ti, part, s + 1, rank, C);
+        if (rank == 0 && threadIdx.x == 0) {
+            S.out_ip[(slot * S.n_states + s) * 2] = tr * S.weight;
+            S.out_ip[(slot * S.n_states + s) * 2 + 1] = ti * S.weight;
+        }
+    }
+}
+
+template <typename R>
+__host__ __device__ inline size_t line_cluster_smem(int threads, int M) {
+    return line_smem<R>(threads, M) + 32 * sizeof(double);
+}
+
+// Crank-Nicolson methods only (ION_LINE_ADI / ION_LINE_SPLIT); a simulation of
+// another method in a cluster plan is left untouched.
+template <typename R, int M>
+__global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = int(cl.num_blocks());
+    const int rank = int(cl.block_rank());
+    ion_line_sim& S = plan.sims[blockIdx.x / C];
+    const int64_t t = S.t, tf = S.t_final;
+    const int n = S.n;
+    const int T = (n + C * M - 1) / (C * M);
+    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT) return;
+    const int L = T * M, off = rank * L;
+    Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
+    Cx<R>* red = line + plan.threads * M;
+    double* scratch = reinterpret_cast<double*>(red + 12 * plan.threads);
+    double* part = scratch + 32;
+    Cx<R>* g = static_cast<Cx<R>*>(S.g);
+    const Cx<R> zero = {R(0), R(0)};
+
+    if (mode == 1) {
+        if (!line_is_data(t, tf, S.store_every)) return;
+        for (int i = threadIdx.x; i < L; i += blockDim.x) line[islot<M>(i, T)] = off + i < n ? ld(g + off + i) : zero;
+        __syncthreads();
+        line_reduce_cluster<R, M>(S, line, T, off, t, scratch, part, rank, C);
+        return;
+    }
+    if (t >= tf) return;
+    const LineTab<R> tb = LineTab<R>::make(S);
+    const R tau = R(S.tau[t + 1]);
+    const R ef = R(S.efield[t + 1]);
+    const bool split = S.method == ION_LINE_SPLIT;
+
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+        const int i = threadIdx.x + k * blockDim.x;
+        if (i >= L) continue;
+        const int gi = off + i;
+        Cx<R> x = zero;
+        if (gi < n) {
+            x = ld(g + gi);
+            if (split) x = phase(x, (tb.zq[gi] * ef) * tau);
+        }
+        line[islot<M>(i, T)] = x;
+    }
+    cl.sync();  // the neighbours' halo rows are staged
+    const OffsetCoef<R> coef{LineCnCoef<R>{tb, tau, ef, !split, n}, off};
+    const ClusterHalo<R> halo{rank > 0 ? cl.map_shared_rank(line, rank - 1) : nullptr,
+                              rank + 1 < C ? cl.map_shared_rank(line, rank + 1) : nullptr};
+    {
+        const int tid = threadIdx.x;
+        const bool active = tid < T;
+        Cx<R> al[M], be[M], ga[M];
+        RedRow<R> r[2];
+        if (active) cn_chunk_eliminate<R, M>(T, tid, R(2), line, coef, NoExtra{}, al, be, ga, r[0], r[1], halo);
+        pcr_solve_cluster<R>(T, tid, active, red, r, rank, C);
+        if (active) {
+            const LineAddOut<R, M> out{line, T};
+            const int s = tid * M;
+            const Cx<R> xs = r[0].d, xe = r[1].d;
+            out(s, xs);
+#pragma unroll
+            for (int k = 1; k < M - 1; ++k) out(s + k, al[k] + be[k] * xs + ga[k] * xe);
+            out(s + M - 1, xe);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < L && off + i < n; i += blockDim.x) {
+        const int gi = off + i;
+        Cx<R>* p = line + islot<M>(i, T);
+        Cx<R> x = *p;
+        if (split) x = phase(x, (tb.zq[gi] * ef) * tau);
+        if (tb.mask) x = Cx<R>{x.re * tb.mask[gi], x.im * tb.mask[gi]};
+        *p = x;
+        st(g + gi, x);
+    }
+    __syncthreads();
+    if (line_is_data(t + 1, tf, S.store_every))
+        line_reduce_cluster<R, M>(S, line, T, off, t + 1, scratch, part, rank, C);
+    // every CTA read S.t before the first cluster barrier above
+    if (rank == 0 && threadIdx.x == 0) S.t = t + 1;
+}
+
+constexpr int LINE_MAX_CLUSTER = 8;
+constexpr size_t LINE_SMEM_LIMIT = 200 * 1024;
 
 template <typename R>
 static int line_validate(const ion_line_plan* p) {
     constexpr int M = LineCfg<R>::M;
     if (!p || !p->sims || p->n_sims < 0 || p->max_n < 2 || p->threads <= 0 || p->threads > LineCfg<R>::MAX_T ||
-        (p->threads & 31) || line_threads(p->max_n, M) > p->threads) {
+        (p->threads & 31) || p->cluster < 0 || p->cluster > LINE_MAX_CLUSTER) {
         set_error("ion_line: invalid plan");
         return ION_ERR_INVALID_ARGUMENT;
     }
-    if (line_smem<R>(p->threads, M) > 200 * 1024) {
+    const int C = p->cluster > 1 ? p->cluster : 1;
+    if (line_threads(p->max_n, C * M) > p->threads) {
+        set_error("ion_line: max_n = %d needs more than %d threads x %d CTAs", p->max_n, p->threads, C);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (line_cluster_smem<R>(p->threads, M) > LINE_SMEM_LIMIT) {
         set_error("ion_line: line too long for shared memory");
         return ION_ERR_UNSUPPORTED;
     }
@@ -207,9 +616,38 @@ static int line_validate(const ion_line_plan* p) {
 template <typename R>
 static int line_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
     constexpr int M = LineCfg<R>::M;
+    if (p->cluster > 1) {
+        auto k = line_cluster_kernel<R, M>;
+        static bool cattr = false;
+        if (!cattr) {
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
+            cattr = true;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(unsigned(p->n_sims) * unsigned(p->cluster));
+        cfg.blockDim = dim3(unsigned(p->threads));
+        cfg.dynamicSmemBytes = line_cluster_smem<R>(p->threads, M);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = unsigned(p->cluster);
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int active = 0;
+        if (cudaOccupancyMaxActiveClusters(&active, k, &cfg) != cudaSuccess || active < 1) {
+            cudaGetLastError();
+            set_error("ion_line: a cluster of %d CTAs x %d threads does not fit on the device", p->cluster,
+                      p->threads);
+            return ION_ERR_UNSUPPORTED;
+        }
+        cudaLaunchKernelEx(&cfg, k, *p, mode);
+        return check_launch("line_cluster_kernel");
+    }
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(line_step_kernel<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(line_step_kernel<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
         attr = true;
     }
     line_step_kernel<R, M><<<p->n_sims, p->threads, line_smem<R>(p->threads, M), s>>>(*p, mode);
@@ -241,7 +679,7 @@ template <typename R>
 static int64_t line_max_n() {
     constexpr int M = LineCfg<R>::M;
     int T = LineCfg<R>::MAX_T;
-    while (T > 32 && line_smem<R>(T, M) > 200 * 1024) T -= 32;
+    while (T > 32 && line_cluster_smem<R>(T, M) > LINE_SMEM_LIMIT) T -= 32;
     return int64_t(T) * M;
 }
 

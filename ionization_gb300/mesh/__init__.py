@@ -9,7 +9,12 @@ from .data import (  # noqa: F401
     InnerProducts,
     Norm,
 )
-from .evolution_methods import AlternatingDirectionImplicit, EvolutionMethod, SplitInteractionOperator  # noqa: F401
+from .evolution_methods import (  # noqa: F401
+    AlternatingDirectionImplicit,
+    EvolutionMethod,
+    FourierSplitOperator,
+    SplitInteractionOperator,
+)
 from .mesh_operators import (  # noqa: F401
     CylindricalSliceLengthGaugeOperators,
     DotOperator,

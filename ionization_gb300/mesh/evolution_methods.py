@@ -76,3 +76,19 @@ class SplitInteractionOperator(EvolutionMethod):
             ),
             "split_interaction",
         )
+
+
+class FourierSplitOperator(EvolutionMethod):
+    """Fourier split-step for LineMesh (no counterpart in the reference, whose
+    line methods are the Crank-Nicolson ones above):
+
+        P F^-1 K F P,  P = exp(-i tau (V + V_int(t_{n+1}))),  K = exp(-i dt hbar k^2 / 2m)
+
+    with F the discrete Fourier transform over the z mesh, so the line is
+    periodic in z (the mask keeps the wavefunction away from the ends).  The
+    kinetic factor is exact for band-limited wavefunctions; the splitting error
+    is second order in dt.  Requires a power-of-two number of z points."""
+
+    def get_evolution_operators(self, mesh, time_step):
+        return ("potential_phase", "fourier_transform", "kinetic_phase", "inverse_fourier_transform",
+                "potential_phase")

@@ -148,6 +148,28 @@ class LineLengthGaugeOperators(MeshOperators):
         return hd, off.real.copy(), np.asarray(zq, dtype=np.float64)
 
     @_memo
+    def fourier_tables(self, mesh):
+        """(V, kin, twiddle) for FourierSplitOperator: the static potential on
+        the z mesh, the kinetic energy hbar^2 k^2 / (2 m) of each Fourier mode
+        (k = 2 pi fftfreq(n, dz)) placed at the position the device's in-place
+        transform leaves it (bit-reversed index), and exp(-2 pi i m / n)."""
+        spec = mesh.spec
+        n = len(mesh.z_mesh)
+        if n < 2 or n & (n - 1):
+            raise ValueError(f"FourierSplitOperator needs a power-of-two number of z points, not {n}")
+        V = np.asarray(spec.internal_potential(r=mesh.r_mesh, z=mesh.z_mesh, test_charge=spec.test_charge))
+        V = np.broadcast_to(V.real.astype(np.float64), (n,)).copy()
+        k = 2 * np.pi * np.fft.fftfreq(n, d=mesh.delta_z)
+        kin = (u.hbar ** 2) * (k ** 2) / (2 * spec.test_mass)
+        bits = n.bit_length() - 1
+        idx = np.arange(n)
+        rev = np.zeros(n, dtype=np.int64)
+        for b in range(bits):
+            rev |= ((idx >> b) & 1) << (bits - 1 - b)
+        twiddle = np.exp(-2j * np.pi * np.arange(n) / n)
+        return V, kin[rev].copy(), twiddle
+
+    @_memo
     def internal_hamiltonian(self, mesh):
         hd, hoff, _ = self.device_tables(mesh)
         m = sparse.diags((hoff.astype(np.complex128), hd.astype(np.complex128), hoff.astype(np.complex128)),

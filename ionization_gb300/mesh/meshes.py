@@ -172,9 +172,17 @@ class LineMesh(QuantumMesh):
             kind = nat.ION_LINE_ADI
         elif isinstance(method, em.SplitInteractionOperator):
             kind = nat.ION_LINE_SPLIT
+        elif isinstance(method, em.FourierSplitOperator):
+            kind = nat.ION_LINE_FFT
         else:
             raise exceptions.UnsupportedMesh(f"{type(method).__name__} has no device path on LineMesh")
         hd, hoff, zq = self.operators.device_tables(self)
+        vstat = kin = twiddle = None
+        if kind == nat.ION_LINE_FFT:
+            try:
+                vstat, kin, twiddle = self.operators.fourier_tables(self)
+            except ValueError as e:
+                raise exceptions.UnsupportedMesh(str(e)) from e
         mask = spec.mask(r=self.r_mesh)
         mask = None if np.isscalar(mask) and mask == 1 else np.broadcast_to(np.asarray(mask, np.float64), (self.mesh_points,))
         times = sim.times
@@ -184,13 +192,16 @@ class LineMesh(QuantumMesh):
         efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
         test_g = np.array([self.get_g_for_state(s) for s in spec.test_states], dtype=np.complex128).reshape(-1, self.mesh_points)
         g0 = self.get_g_for_state(spec.initial_state)
-        maxn = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_line_max_n_" + self.precision.value)
-        if self.mesh_points > maxn:
-            raise exceptions.UnsupportedMesh(f"line of {self.mesh_points} points exceeds the device limit {maxn}")
+        if not getattr(spec, "host_only", False):
+            cta = dev.line_cta_max_n(self.precision)
+            maxn = cta if kind == nat.ION_LINE_FFT else cta * dev.LINE_MAX_CLUSTER
+            if self.mesh_points > maxn:
+                raise exceptions.UnsupportedMesh(
+                    f"line of {self.mesh_points} points exceeds the device limit {maxn} for {type(method).__name__}")
         self.tables = dev.LineTables(
             n=self.mesh_points, method=kind, hd=hd, hoff=hoff, zq=zq, mask=mask, tau=self._tau_host.copy(),
             efield=efield, state_g=test_g, weight=self.inner_product_multiplier, g0=g0, t0=0,
-            t_final=len(times) - 1, store_every=spec.store_data_every,
+            t_final=len(times) - 1, store_every=spec.store_data_every, vstat=vstat, kin=kin, twiddle=twiddle,
         )
         if getattr(spec, "host_only", False):
             return

@@ -15,7 +15,11 @@
   0.125)), l_max ~ U{20..80}, E0 log-uniform [0.005, 0.1], w ~ U[0.03, 0.2],
   2..10 cycles, CEP ~ U[0, 2 pi); hydrogen 1s, dt 0.02 x 10000 steps, mask on
   the outer 25 a0, complex64 state.
-* ``poisson_scan_requests``: the served scan mix (see ionization_gb300.serve).
+* ``line_softcore``: soft-core lines of any length at the 4096-point line's
+  spacing.
+* ``poisson_scan_parameters``: the served scan mix (ionization_gb300.serve):
+  Poisson arrivals, lines of 2048-16384 points and SH meshes of Nr 1000-4000,
+  l_max 20-100, 2000-50000 steps, 80 % complex64.
 """
 
 import numpy as np
@@ -144,3 +148,58 @@ def uneven_sh_sweep(n_sims=512, seed=20261203, steps=10000, precision="c64", sto
                 p["cep"], steps, precision=precision, store_data_every=store_data_every, n_max=n_max, **kw)
         for p in params
     ]
+
+
+LINE_DZ = 200.0 / 4095  # the grid spacing of the 4096-point line on [-100, 100]
+
+
+def line_softcore(name, z_points, E0, omega, cycles, cep, steps, dt=0.05, precision="c128", store_data_every=-1,
+                  evolution_method=None, **kw):
+    """Soft-core line of ``z_points`` at the spacing of the 4096-point line
+    (z_bound grows with the point count), Gaussian start, sin^2 pulse, cos^(1/8)
+    mask on the outer 20 % of each side, Crank-Nicolson (ADI) by default."""
+    mesh, potentials, states = _mods()
+    z_bound = LINE_DZ * (z_points - 1) / 2
+    return mesh.LineSpecification(
+        name,
+        z_bound=z_bound,
+        z_points=z_points,
+        test_mass=1.0,
+        internal_potential=potentials.SoftCoulombPotential(softening_distance=np.sqrt(2)),
+        initial_state=states.GaussianState(width=1.0),
+        electric_potential=sin2_pulse(E0, omega, cycles, cep),
+        mask=potentials.AbsoluteRadialCosineMask(inner_radius=0.8 * z_bound, outer_radius=z_bound, smoothness=8),
+        time_initial=0.0,
+        time_final=steps * dt,
+        time_step=dt,
+        evolution_method=evolution_method or mesh.AlternatingDirectionImplicit(),
+        store_data_every=store_data_every,
+        precision=precision,
+        **kw,
+    )
+
+
+def poisson_scan_parameters(n_requests=100, rate=20.0, seed=20261204, line_fraction=0.5, c64_fraction=0.8):
+    """The served scan mix: Poisson arrivals at ``rate`` per second; each
+    request a soft-core line (2048-16384 points) or a hydrogen
+    spherical-harmonic mesh (Nr 1000-4000, l_max 20-100), with a pulse drawn
+    as in the uneven sweep, 2000-50000 steps, complex64 with probability
+    ``c64_fraction`` else complex128."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    for i in range(n_requests):
+        t += float(rng.exponential(1.0 / rate))
+        kind = "line" if rng.random() < line_fraction else "sh"
+        precision = "c64" if rng.random() < c64_fraction else "c128"
+        steps = int(rng.integers(2000, 50001))
+        E0 = float(np.exp(rng.uniform(np.log(0.005), np.log(0.1))))
+        omega = float(rng.uniform(0.03, 0.2))
+        cycles = int(rng.integers(2, 11))
+        cep = float(rng.uniform(0.0, 2 * np.pi))
+        if kind == "line":
+            points, l_bound = int(rng.integers(2048, 16385)), 0
+        else:
+            points, l_bound = int(rng.integers(1000, 4001)), int(rng.integers(20, 101)) + 1
+        out.append(dict(id=i, arrival=t, kind=kind, precision=precision, steps=steps, points=points,
+                        l_bound=l_bound, E0=E0, omega=omega, cycles=cycles, cep=cep))
+    return out

@@ -178,3 +178,5 @@ def test_full_cylindrical_workload_matches_reference(cuda):
     g = sim.mesh.g[::sz, ::sr]
     assert rel_l2(g, z["g_final"]) < TOL
     np.testing.assert_allclose(sim.data.norm, z["norm"], rtol=0, atol=TOL)
+    ips = np.array([sim.data.inner_products[s] for s in sim.spec.test_states])
+    np.testing.assert_allclose(ips, z["inner_products"], rtol=0, atol=TOL)

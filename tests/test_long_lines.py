@@ -1,0 +1,81 @@
+"""Lines longer than one CTA holds: the thread-block-cluster line kernel.
+
+Each case runs the product path (the line split across 2..8 CTAs of a
+cluster, halos and the reduced-system PCR exchanged through distributed
+shared memory) and the oracle (oracle/mesh.py, pinned to the reference's line
+fixtures) on the same inputs; complex128 must agree to relative L2 <= 1e-10
+on psi and 1e-10 absolute on the data."""
+
+import copy
+
+import numpy as np
+import pytest
+
+from oracle import mesh as om
+
+from .conftest import load_golden, rel_l2
+from .specs import product_spec
+
+pytestmark = pytest.mark.gpu
+
+
+def _params(n, method, z_bound=None, time_final=3.0):
+    params, _ = load_golden("line_split_small")
+    p = copy.deepcopy(params)
+    p["z_points"] = n
+    p["z_bound"] = z_bound if z_bound is not None else 40.0 * n / 2048
+    p["mask"] = {"inner_radius": 0.8 * p["z_bound"], "outer_radius": p["z_bound"], "smoothness": 8}
+    p["method"] = method
+    p["time_final"] = time_final
+    p["store_data_every"] = 20
+    return p
+
+
+LONG = [
+    (8192, "AlternatingDirectionImplicit"),
+    (8192, "SplitInteractionOperator"),
+    (12000, "SplitInteractionOperator"),  # three CTAs, ragged last segment
+    (16384, "AlternatingDirectionImplicit"),
+    (32768, "SplitInteractionOperator"),  # eight CTAs
+]
+
+
+@pytest.mark.parametrize("n,method", LONG)
+def test_long_line_c128_matches_oracle(cuda, n, method):
+    from ionization_gb300 import _device as dev
+
+    params = _params(n, method)
+    sim = product_spec("line", params).to_sim()
+    assert dev.line_cluster(n, "c128") > 1
+    want = om.run_from_params("line", params)
+    sim.run()
+    assert rel_l2(sim.mesh.g, want["g_final"]) < 1e-10
+    np.testing.assert_allclose(sim.data.norm, want["norm"], rtol=0, atol=1e-10)
+    ips = np.array([sim.data.inner_products[s] for s in sim.spec.test_states])
+    np.testing.assert_allclose(ips, want["inner_products"], rtol=0, atol=1e-10)
+
+
+def test_long_line_c64_close_to_oracle(cuda):
+    params = _params(16384, "SplitInteractionOperator")
+    want = om.run_from_params("line", params)
+    sim = product_spec("line", params, precision="c64").to_sim()
+    sim.run()
+    p64 = sim.data.initial_state_overlap[-1]
+    p128 = abs(want["inner_products"][0][-1]) ** 2
+    print(f"16384-point c64 line: |P_c64 - P_c128| = {abs(p64 - p128):.2e}")
+    assert abs(p64 - p128) < 1e-5
+    assert rel_l2(sim.mesh.g, want["g_final"]) < 1e-4
+
+
+def test_lines_of_every_cluster_size_share_one_batch(cuda):
+    from ionization_gb300 import _device as dev
+
+    cases = [_params(n, m) for n, m in [(512, "SplitInteractionOperator"), (6000, "AlternatingDirectionImplicit"),
+                                        (9000, "SplitInteractionOperator")]]
+    sims = [product_spec("line", p).to_sim() for p in cases]
+    batch = dev.LineBatch("c128", [s.mesh._dsim for s in sims])
+    assert len(batch.plans) == 3
+    batch.run(sims[0].mesh._dsim.t_final)
+    for p, s in zip(cases, sims):
+        want = om.run_from_params("line", p)
+        assert rel_l2(s.mesh._dsim.psi_host(), want["g_final"]) < 1e-10
