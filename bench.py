@@ -17,9 +17,12 @@ Prints one JSON line:
   cpu_baseline  the oracle (CPU restatement of the reference, complex128)
              on a bounded sample of the same workload on the host cores
   plain_c128 the single-simulation complex128 drop-in path (Nr 2000, l < 41)
-  accuracy   |P_ground(c64) - P_ground(c128)| and the same for the
-             ionization probability over the full 10000 steps, on a seeded
-             subset of the sweep
+  accuracy   |P_ground - P_ground(c128)| and the same for the ionization
+             probability over the full 10000 steps, on a seeded subset of the
+             sweep, for complex64 and for complex64 with a stored residual
+             (c64x)
+  serving    the served scan mix (Poisson arrivals, lines and SH meshes of
+             mixed sizes and precisions): p50/p99 latency, throughput
 
 ``--impl reference`` times the CPU oracle (the reference's algorithm,
 complex128) on the same workload with all host cores instead.
@@ -208,6 +211,7 @@ def run_ours(args, rank, world, local_rank):
     from ionization_gb300 import _device as dev
     from ionization_gb300 import _native as nat
     from ionization_gb300 import batch as bm
+    from ionization_gb300 import replicas
     from ionization_gb300 import workloads as wl
 
     torch.cuda.set_device(local_rank)
@@ -217,14 +221,11 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    barrier = replicas.barrier
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    # ---- the workload: this rank's seeded sweep ----
+    # ---- the workload: this rank's seeded sweep (replicas, weak scaling) ----
     t_setup = time.perf_counter()
-    specs = wl.uneven_sh_sweep(N_SIMS, seed=SEED + rank, steps=SIM_STEPS, precision="c64")
+    specs = wl.uneven_sh_sweep(N_SIMS, seed=replicas.sweep_seed(SEED, rank), steps=SIM_STEPS, precision="c64")
     tables = [bm._host_tables(s)[0] for s in specs]
     setup_host_s = time.perf_counter() - t_setup
     points = int(sum(t.n_r * t.n_l for t in tables))
@@ -262,11 +263,7 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     for s in b.sims:
         s.t = min(s.t + K, s.t_final)
-    elapsed_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(tt.item())
+    elapsed_ms = replicas.max_over_ranks(e0.elapsed_time(e1))
     cn_ms = float(np.mean([a.elapsed_time(c) for a, c in e_cn]))
     rot_ms = float(np.mean([e_cn[k][1].elapsed_time(e_rot[k][1]) for k in range(K)]))
     gpu_launches = 1 + 3 * K
@@ -279,7 +276,7 @@ def run_ours(args, rank, world, local_rank):
 
     peak, peak_kind = measured_peaks()
     alg_bytes = 16 * points  # complex64: psi read once and written once per kernel
-    dominant, dom_ms = ("sh_cn_kernel", cn_ms) if cn_ms >= rot_ms else ("sh_rot_kernel", rot_ms)
+    dominant, dom_ms = ("sh_cn_pipelined", cn_ms) if cn_ms >= rot_ms else ("sh_rot_kernel", rot_ms)
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     traffic = profile_traffic().get(dominant + "_c64_bytes_per_point")
     roofline = {
@@ -292,8 +289,8 @@ def run_ours(args, rank, world, local_rank):
         "frac": round(achieved / peak, 4),
         "traffic": None if traffic is None else int(traffic * points),
         "algorithmic_bytes": alg_bytes,
-        "kernel_ms": {"sh_cn_kernel": round(cn_ms, 4), "sh_rot_kernel": round(rot_ms, 4)},
-        "frac_by_kernel": {"sh_cn_kernel": round(alg_bytes / (cn_ms / 1e3) / 1e9 / peak, 4),
+        "kernel_ms": {"sh_cn_pipelined": round(cn_ms, 4), "sh_rot_kernel": round(rot_ms, 4)},
+        "frac_by_kernel": {"sh_cn_pipelined": round(alg_bytes / (cn_ms / 1e3) / 1e9 / peak, 4),
                            "sh_rot_kernel": round(alg_bytes / (rot_ms / 1e3) / 1e9 / peak, 4)},
     }
 
@@ -305,6 +302,9 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- accuracy on a seeded subset: c64 vs c128 over the full run ----
     acc = None if args.quick else run_accuracy()
+
+    # ---- the served form ----
+    serving = None if args.no_serve else run_serving(args)
 
     # ---- CPU oracle on a bounded sample ----
     cpu = None
@@ -349,6 +349,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "plain_c128": plain,
         "accuracy": acc,
+        "serving": serving,
     }
     if plain and plain.get("value"):
         out["vs_plain_c128"] = round(value / world / plain["value"], 2)
@@ -379,6 +380,40 @@ def run_e2e(args, specs, tables, rows, gs, points):
     del b, psis
     return {"value": points * K / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / K),
             "d2h_bytes_per_step": int(d2h / K), "steps": K, "wall_s": round(wall, 3)}
+
+
+def run_serving(args):
+    """The served scan mix: Poisson arrivals (20/s, seeded), lines of
+    2048-16384 points and SH meshes of Nr 1000-4000 x l_max 20-100,
+    2000-50000 steps, 80 % complex64, continuous batching under a 150 GB
+    budget.  Latency = arrival to results on the host.  Error: the complex64
+    requests with the least work rerun in complex128 (the path matched to the
+    reference), |P_ground(c64) - P_ground(c128)|."""
+    import torch
+
+    from ionization_gb300 import serve
+
+    reqs = serve.poisson_requests(args.serve_requests, rate=20.0, seed=20261204)
+    server = serve.Server()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    done = server.run(reqs)
+    makespan = time.perf_counter() - t0
+    out = serve.summarize(done, makespan)
+    out.update(workload=f"poisson_scan_parameters({args.serve_requests}, rate 20/s, seed 20261204)",
+               peak_active=server.peak_active, peak_reserved_bytes=server.peak_bytes,
+               mix={k: sum(1 for r in reqs if (r.kind, r.precision) == k)
+                    for k in {(r.kind, r.precision) for r in reqs}})
+    out["mix"] = {f"{k[0]}_{k[1]}": v for k, v in out["mix"].items()}
+    by_id = {c.request.id: c for c in done}
+    small = sorted((r for r in reqs if r.precision == "c64"), key=lambda r: r.mesh_points * r.steps)[:6]
+    errs = []
+    for r in small:
+        r128 = serve.Request(**{**r.__dict__, "precision": "c128"})
+        (ref,) = serve.Server().run([r128], realtime=False)
+        errs.append(abs(by_id[r.id].ground_population - ref.ground_population))
+    out["c64_vs_c128_ground_population_err"] = {"requests": [r.id for r in small], "max": float(max(errs)) if errs else None}
+    return out
 
 
 def run_plain_c128(args):
@@ -412,19 +447,23 @@ def run_accuracy(subset=(0, 37, 101, 163, 255, 300, 411, 500)):
     from ionization_gb300 import workloads as wl
 
     out = {}
-    for prec in ("c128", "c64"):
+    for prec in ("c128", "c64", "c64x"):
         specs = wl.uneven_sh_sweep(N_SIMS, seed=SEED, steps=SIM_STEPS, precision=prec, subset=list(subset))
         b = bm.BatchedSphericalHarmonicSimulation(specs, precision=prec)
         b.run()
         out[prec] = b.results()
         del b
         torch.cuda.synchronize()
-    dg = [abs(a["initial_state_overlap"][-1] - c["initial_state_overlap"][-1]) for a, c in zip(out["c64"], out["c128"])]
-    di = [abs((1 - a["bound_state_overlap"][-1]) - (1 - c["bound_state_overlap"][-1]))
-          for a, c in zip(out["c64"], out["c128"])]
-    return {"subset": list(subset), "steps": SIM_STEPS, "max_abs_err_ground_population": float(max(dg)),
-            "max_abs_err_ionization_probability": float(max(di)),
-            "ground_population_c128": [float(c["initial_state_overlap"][-1]) for c in out["c128"]]}
+    res = {"subset": list(subset), "steps": SIM_STEPS,
+           "ground_population_c128": [float(c["initial_state_overlap"][-1]) for c in out["c128"]]}
+    for prec in ("c64", "c64x"):
+        dg = [abs(a["initial_state_overlap"][-1] - c["initial_state_overlap"][-1])
+              for a, c in zip(out[prec], out["c128"])]
+        di = [abs((1 - a["bound_state_overlap"][-1]) - (1 - c["bound_state_overlap"][-1]))
+              for a, c in zip(out[prec], out["c128"])]
+        res[prec] = {"max_abs_err_ground_population": float(max(dg)),
+                     "max_abs_err_ionization_probability": float(max(di))}
+    return res
 
 
 # --------------------------------------------------------------------------
@@ -504,13 +543,13 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the 10000-step accuracy run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle sample")
     ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-mix run")
+    ap.add_argument("--serve-requests", type=int, default=100)
     args = ap.parse_args()
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if "WORLD_SIZE" not in os.environ:
-        world = 1
+    from ionization_gb300 import replicas
+
+    rank, world, local_rank = replicas.rank_world()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
     else:

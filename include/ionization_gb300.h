@@ -162,6 +162,12 @@ typedef struct ion_sh_sim {
     double *partials;       /* [n_tiles * (1 + 2*n_states)] device scratch for reductions */
     int32_t n_tiles;        /* number of row tiles of this simulation */
     int32_t pad_;
+    /* _c64 entry points only, or NULL: the rounding residual of psi,
+     * complex64 (n_l, n_r) like g.  With it psi = g + g_lo carries about 48
+     * significant bits: the arithmetic stays FP32, each step's increment is
+     * added to (g, g_lo) with an exact two-sum and the pair is renormalised
+     * when stored, so storing psi no longer rounds it to FP32 precision. */
+    void *g_lo;
 } ion_sh_sim;
 
 typedef struct ion_sh_plan {

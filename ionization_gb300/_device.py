@@ -67,6 +67,13 @@ def _round32(x: int) -> int:
     return (x + 31) // 32 * 32
 
 
+def _pad16(a) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float64).reshape(-1)
+    out = np.zeros((a.size + 16) // 16 * 16, dtype=np.float64)
+    out[: a.size] = a
+    return out
+
+
 # ==========================================================================
 # spherical-harmonic split operator
 # ==========================================================================
@@ -100,7 +107,7 @@ class ShTables:
 SH_ROT_ROWS = 32
 
 
-SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8)}  # default first
+SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8), Precision.C64X: (16, 8)}  # default first
 
 
 def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
@@ -120,7 +127,12 @@ class ShDeviceSim:
         self.store_every = int(tab.store_every)
         f64 = np.float64
         f32 = np.float32
-        self.g = to_dev(tab.g0.astype(np.complex128)).to(complex_dtype(precision))
+        g0 = np.asarray(tab.g0, dtype=np.complex128)
+        self.g = to_dev(g0).to(complex_dtype(precision))
+        self.g_lo = None
+        if self.precision == Precision.C64X:  # psi = g + g_lo
+            hi = g0.astype(np.complex64)
+            self.g_lo = to_dev((g0 - hi.astype(np.complex128)).astype(np.complex64))
         c128 = self.precision == Precision.C128
         self.d_hd = to_dev(tab.hd, f64) if c128 else None
         self.d_hoff = to_dev(tab.hoff, f64)
@@ -129,9 +141,11 @@ class ShDeviceSim:
         self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
         self.d_tau = to_dev(tab.tau, f64)
         self.d_ef = to_dev(tab.efield, f64)
-        self.d_kinv32 = to_dev(tab.kinv, f32)
-        self.d_cent32 = to_dev(tab.cent, f32)
-        self.d_hoff32 = to_dev(tab.hoff, f32)
+        # per-r FP32 tables zero-padded to a multiple of 16 entries: the radial
+        # solve reads a chunk of 8 or 16 rows with 16-byte vector loads
+        self.d_kinv32 = to_dev(_pad16(tab.kinv), f32)
+        self.d_cent32 = to_dev(_pad16(tab.cent), f32)
+        self.d_hoff32 = to_dev(_pad16(tab.hoff), f32)
         self.d_rq32 = to_dev(tab.rq, f32)
         self.d_cl32 = to_dev(tab.cl, f32)
         self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
@@ -168,6 +182,7 @@ class ShDeviceSim:
         d.weight = float(self.tab.weight)
         d.out_norm, d.out_ip, d.partials = ptr(self.d_norm), ptr(self.d_ip), ptr(self.d_partials)
         d.n_tiles = self.n_tiles
+        d.g_lo = ptr(self.g_lo)
         return d
 
     def data(self):
@@ -177,7 +192,10 @@ class ShDeviceSim:
         return norm, ip.reshape(self.n_data, self.n_states).T.copy()
 
     def psi_host(self) -> np.ndarray:
-        return self.g.cpu().numpy().astype(np.complex128)
+        g = self.g.cpu().numpy().astype(np.complex128)
+        if self.g_lo is not None:
+            g = g + self.g_lo.cpu().numpy().astype(np.complex128)
+        return g
 
 
 class ShBatch:

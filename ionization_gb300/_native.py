@@ -66,6 +66,7 @@ class ShSim(ctypes.Structure):
         ("partials", c_vp),
         ("n_tiles", c_i32),
         ("pad_", c_i32),
+        ("g_lo", c_vp),
     ]
 
 

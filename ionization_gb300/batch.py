@@ -171,7 +171,7 @@ def _main(argv=None):
     ap.add_argument("--sims", type=int, default=200)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--precision", default="c64", choices=["c64", "c128"])
+    ap.add_argument("--precision", default="c64", choices=["c64", "c64x", "c128"])
     ap.add_argument("--rows", type=int, default=None, help="rows per thread of the radial solve")
     ap.add_argument("--graphs", action="store_true", help="capture the steps in CUDA graphs")
     a = ap.parse_args(argv)

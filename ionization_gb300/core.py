@@ -21,7 +21,15 @@ class Gauge(StrEnum):
 
 
 class Precision(StrEnum):
-    """Arithmetic of the wavefunction and its sweeps on the device."""
+    """Arithmetic of the wavefunction and its sweeps on the device.
+
+    C128: complex128 state and FP64 arithmetic (matches the reference).
+    C64: complex64 state, FP32 sweeps, FP64 fields, coefficients and
+    reductions.
+    C64X: as C64, with the rounding residual of the state kept in a second
+    complex64 array (spherical-harmonic meshes): storing the state no longer
+    rounds it to FP32, which removes the dominant error of C64."""
 
     C128 = "c128"
     C64 = "c64"
+    C64X = "c64x"

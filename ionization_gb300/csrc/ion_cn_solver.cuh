@@ -63,6 +63,14 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Coefficients of the M rows [s, s + M) of one chunk; a coefficient type with
+// a faster whole-chunk load provides its own overload.
+template <int M, class Coef, typename R>
+__device__ __forceinline__ void load_chunk(const Coef& coef, int s, R (&bo)[M], R (&bd)[M]) {
+#pragma unroll
+    for (int k = 0; k < M; ++k) coef(s + k, bo[k], bd[k]);
+}
+
 struct NoExtra {
     template <typename R>
     __device__ __forceinline__ Cx<R> get(int) const {
@@ -95,8 +103,7 @@ __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R
     const Cx<R> zero = {R(0), R(0)};
     const int s = t * M;
     R bo[M], bd[M];
-#pragma unroll
-    for (int k = 0; k < M; ++k) coef(s + k, bo[k], bd[k]);
+    load_chunk<M>(coef, s, bo, bd);
     R bom1 = R(0);
     const bool hl = halo.has_left(t);
     if (hl) {

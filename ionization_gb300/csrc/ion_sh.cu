@@ -7,9 +7,11 @@
 // once per step of MeshSimulation.run (ionization/mesh/sims.py:289-333).
 //
 // Per step three kernels run on the whole batch:
-//   sh_cn_kernel   one CTA per (simulation, l) radial line: the line is staged
-//                  in shared memory, y = (1 - i tau H0) psi is formed on the
-//                  fly and (1 + i tau H0) x = y is solved by the block
+//   sh_cn_pipelined  the radial solves: persistent CTAs, each walking the
+//                  (simulation, l) lines of one bucket of equal CTA size with
+//                  the next line's psi streaming into shared memory while the
+//                  current one is solved; y = (1 - i tau H0) psi is formed on
+//                  the fly and (1 + i tau H0) x = y is solved by the block
 //                  partition + PCR solver;
 //   sh_rot_kernel  one CTA per (simulation, tile of r rows) holding all l of
 //                  those rows: the rotations after the radial solve of step
@@ -19,6 +21,8 @@
 //   sh_advance_kernel  finishes the reductions (compensated sum over tiles)
 //                  and advances each simulation's time index.
 #include <cstdio>
+
+#include <algorithm>
 
 #include "ion_common.cuh"
 #include <type_traits>
@@ -113,35 +117,40 @@ struct AddOut {
     }
 };
 
+// psi + delta, or delta alone (``add`` false), into the interleaved line
 template <typename R, int M>
-struct SmemCoef {  // (bo, bd) of every row staged in shared memory, interleaved
-    const Cx<R>* cf;
+struct AddOrSetOut {
+    Cx<R>* line;
     int T;
-    __device__ __forceinline__ void operator()(int i, R& bo, R& bd) const {
-        const Cx<R> v = cf[islot<M>(i, T)];
-        bo = v.re;
-        bd = v.im;
+    bool add;
+    __device__ __forceinline__ void operator()(int i, Cx<R> d) const {
+        Cx<R>* p = line + islot<M>(i, T);
+        *p = add ? *p + d : d;
     }
 };
 
+// (h + d) with the residual lo: h + d is formed exactly (Knuth's TwoSum), its
+// rounding error joins lo, and the pair is renormalised (Fast2Sum).  Returns
+// the new h; lo is updated in place.
 template <typename R>
-__host__ __device__ inline size_t sh_cn_smem(int threads, int M) {
-    return 2 * size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
+__device__ __forceinline__ R add_exact1(R h, R d, R& lo) {
+    const R s = h + d;
+    const R bb = s - h;
+    const R e = (h - (s - bb)) + (d - bb);
+    const R l = lo + e;
+    const R r = s + l;
+    lo = l - (r - s);
+    return r;
 }
+template <typename R>
+__device__ __forceinline__ Cx<R> add_exact(Cx<R> h, Cx<R> d, Cx<R>& lo) {
+    return Cx<R>{add_exact1(h.re, d.re, lo.re), add_exact1(h.im, d.im, lo.im)};
+}
+
+
 
 __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
-}
-
-// L2 prefetch of the psi line of radial item ``item`` (128-byte lines)
-template <typename R>
-__device__ __forceinline__ void prefetch_cn_item(const ion_sh_plan& plan, int item) {
-    const int si = plan.cn_items[2 * item];
-    const int l = plan.cn_items[2 * item + 1];
-    const ion_sh_sim& S = plan.sims[si];
-    const char* p = reinterpret_cast<const char*>(static_cast<const Cx<R>*>(S.g) + int64_t(l) * S.n_r);
-    const int bytes = S.n_r * int(sizeof(Cx<R>));
-    for (int o = threadIdx.x * 128; o < bytes; o += blockDim.x * 128) prefetch_l2(p + o);
 }
 
 // L2 prefetch of the rows of rotation tile ``item`` (n_l segments of
@@ -160,48 +169,165 @@ __device__ __forceinline__ void prefetch_rot_item(const ion_sh_plan& plan, int i
     }
 }
 
-// One CTA per (simulation, l) item of plan.cn_items[item0 + blockIdx.x].
-// The line and its tau-scaled coefficients are staged in shared memory in
-// one pass (all global loads issued together), then solved.  Each CTA first
-// asks L2 for the line of the item ``pf_dist`` ahead (about one resident
-// wave later), so later CTAs start from L2 instead of HBM.
+// ---------------------------------------------------------------------------
+// Pipelined radial solve: a persistent CTA walks the items of one bucket
+// (item0 + blockIdx.x, then every gridDim.x-th).  While it solves one line,
+// the psi of its next line is already streaming into the other of two
+// shared-memory buffers (cp.async, no registers held), so the global-load
+// latency of the staging overlaps the solve instead of stalling it.  The
+// coefficients are formed in the chunk elimination from the per-r tables,
+// which every line of a simulation shares (they stay in L1); the complex64
+// tables are padded with zeros to a multiple of 16 entries, so a chunk of
+// M = 8 or 16 rows is read with 16-byte vector loads.
+// ---------------------------------------------------------------------------
+struct ShCnCoef32 {
+    const float* kinv;
+    const float* cent;
+    const float* hoff;
+    float ll1, corr0, tau;
+    int n;
+    __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const {
+        if (i < 0 || i >= n) {
+            bo = 0.f;
+            bd = 0.f;
+            return;
+        }
+        float h = kinv[i] + ll1 * cent[i];
+        if (i == 0) h = h + corr0;
+        bd = tau * h;
+        bo = (i < n - 1) ? tau * hoff[i] : 0.f;
+    }
+};
+
+template <int M>
+__device__ __forceinline__ void load_chunk(const ShCnCoef32& c, int s, float (&bo)[M], float (&bd)[M]) {
+    static_assert(M % 4 == 0, "whole float4 groups");
+#pragma unroll
+    for (int q = 0; q < M / 4; ++q) {
+        const float4 kv = __ldg(reinterpret_cast<const float4*>(c.kinv + s) + q);
+        const float4 cv = __ldg(reinterpret_cast<const float4*>(c.cent + s) + q);
+        const float4 hv = __ldg(reinterpret_cast<const float4*>(c.hoff + s) + q);
+        const float kk[4] = {kv.x, kv.y, kv.z, kv.w}, cc[4] = {cv.x, cv.y, cv.z, cv.w},
+                    hh[4] = {hv.x, hv.y, hv.z, hv.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int k = 4 * q + e, i = s + k;
+            float h = kk[e] + c.ll1 * cc[e];
+            if (i == 0) h = h + c.corr0;
+            bd[k] = i < c.n ? c.tau * h : 0.f;
+            bo[k] = i < c.n - 1 ? c.tau * hh[e] : 0.f;
+        }
+    }
+}
+
+template <typename R> struct ShCnCoefFor;
+template <> struct ShCnCoefFor<double> {
+    using type = ShCnCoef<double>;
+    __device__ static type make(const ion_sh_sim& S, int l, double tau) {
+        return type{ShH<double>::make(S, l), tau, S.n_r};
+    }
+};
+template <> struct ShCnCoefFor<float> {
+    using type = ShCnCoef32;
+    __device__ static type make(const ion_sh_sim& S, int l, float tau) {
+        return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r};
+    }
+};
+
+// psi of item ``item`` into ``dst`` (interleaved, zero padding), asynchronously
 template <typename R, int M>
-__global__ void __launch_bounds__(512) sh_cn_kernel(ion_sh_plan plan, int item0, int item_end, int pf_dist) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int item = item0 + blockIdx.x;
-    if (pf_dist > 0 && item + pf_dist < item_end) prefetch_cn_item<R>(plan, item + pf_dist);
+__device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int item, Cx<R>* dst) {
     const int si = plan.cn_items[2 * item];
     const int l = plan.cn_items[2 * item + 1];
     const ion_sh_sim& S = plan.sims[si];
-    const int64_t t = S.t;
-    if (t >= S.t_final) return;  // whole CTA leaves together
+    if (S.t >= S.t_final) return;
     const int nr = S.n_r;
     const int T = (nr + M - 1) / M;
     const int npad = T * M;
-    const int cap = blockDim.x * M;
-    Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* cf = line + cap;
-    Cx<R>* red = cf + cap;
-    Cx<R>* g = static_cast<Cx<R>*>(S.g) + int64_t(l) * nr;
-    const R tau = R(S.tau[t + 1]);
-    const ShCnCoef<R> coef{ShH<R>::make(S, l), tau, nr};
-    const Cx<R> zero = {R(0), R(0)};
-#pragma unroll 4
+    const Cx<R>* g = static_cast<const Cx<R>*>(S.g) + int64_t(l) * nr;
     for (int i = threadIdx.x; i < npad; i += blockDim.x) {
-        const int sl = islot<M>(i, T);
-        line[sl] = (i < nr) ? ld(g + i) : zero;
-        R bo, bd;
-        coef(i, bo, bd);
-        cf[sl] = Cx<R>{bo, bd};
+        Cx<R>* d = dst + islot<M>(i, T);
+        if (i < nr) {
+            if (sizeof(Cx<R>) == 16)
+                cp_async16(d, g + i);
+            else
+                cp_async8(d, g + i);
+        } else {
+            *d = Cx<R>{R(0), R(0)};
+        }
     }
-    __syncthreads();
-    block_cn_solve<R, M>(T, threadIdx.x, R(2), line, red, SmemCoef<R, M>{cf, T}, NoExtra{}, AddOut<R, M>{line, T});
-    __syncthreads();
+}
+
+// ``dbuf`` 0: one line buffer (lines too long for two), staged at the top of
+// each iteration without overlap.
+template <typename R, int M>
+__global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int item0, int item_end, int dbuf) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int cap = blockDim.x * M;
+    Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
+    Cx<R>* buf1 = buf0 + cap;
+    Cx<R>* red = buf0 + (dbuf ? 2 : 1) * cap;
+    int item = item0 + blockIdx.x;
+    if (item >= item_end) return;
+    if (dbuf) {
+        sh_cn_stage_async<R, M>(plan, item, buf0);
+        cp_async_commit();
+    }
+    for (int j = 0; item < item_end; item += gridDim.x, ++j) {
+        Cx<R>* cur = (dbuf && (j & 1)) ? buf1 : buf0;
+        if (dbuf) {
+            const int next = item + gridDim.x;
+            if (next < item_end) sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1);
+            cp_async_commit();
+            cp_async_wait<1>();  // this item's psi has landed; the next one stays in flight
+        } else {
+            sh_cn_stage_async<R, M>(plan, item, buf0);
+            cp_async_commit();
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const int si = plan.cn_items[2 * item];
+        const int l = plan.cn_items[2 * item + 1];
+        const ion_sh_sim& S = plan.sims[si];
+        const int64_t t = S.t;
+        if (t < S.t_final) {  // the same for every thread of the CTA
+            const int nr = S.n_r;
+            const int T = (nr + M - 1) / M;
+            const R tau = R(S.tau[t + 1]);
+            const auto coef = ShCnCoefFor<R>::make(S, l, tau);
+            // with a stored residual the solve leaves the increment in ``cur``
+            Cx<R>* glo = sizeof(R) == 4 && S.g_lo ? static_cast<Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
+            block_cn_solve<R, M>(T, threadIdx.x, R(2), cur, red, coef, NoExtra{},
+                                 AddOrSetOut<R, M>{cur, T, glo == nullptr});
+            __syncthreads();
+            Cx<R>* g = static_cast<Cx<R>*>(S.g) + int64_t(l) * nr;
+            if (glo) {
 #pragma unroll
-    for (int k = 0; k < M; ++k) {
-        const int i = threadIdx.x + k * blockDim.x;
-        if (i < nr) st(g + i, line[islot<M>(i, T)]);
+                for (int k = 0; k < M; ++k) {
+                    const int i = threadIdx.x + k * blockDim.x;
+                    if (i < nr) {
+                        Cx<R> lo = ld(glo + i);
+                        const Cx<R> h = add_exact(ld(g + i), cur[islot<M>(i, T)], lo);
+                        st(g + i, h);
+                        st(glo + i, lo);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < M; ++k) {
+                    const int i = threadIdx.x + k * blockDim.x;
+                    if (i < nr) st(g + i, cur[islot<M>(i, T)]);
+                }
+            }
+        }
+        __syncthreads();  // every read of ``cur`` is done before it is refilled
     }
+    cp_async_wait<0>();
+}
+
+template <typename R>
+__host__ __device__ inline size_t sh_cn_pipelined_smem(int threads, int M, int buffers) {
+    return size_t(buffers) * threads * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
 }
 
 // ---------------------------------------------------------------------------
@@ -245,6 +371,7 @@ template <> struct Tile<double> {
     }
     __device__ void scale(int k, double m) const { hi[k] = Cx<double>{hi[k].re * m, hi[k].im * m}; }
     __device__ Cx<double> out(int k) const { return hi[k]; }
+    __device__ __forceinline__ void store(int k, Cx<double>* g, Cx<double>*, int64_t at) const { st(g + at, hi[k]); }
 };
 template <> struct Tile<float> {
     Cx<float>* hi;
@@ -265,11 +392,21 @@ template <> struct Tile<float> {
         lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.im) + e0r, l0.im + (cm1 * l0.im - s * l1.re) + e0i};
         lo[k1] = Cx<float>{l1.re + (cm1 * l1.re + s * l0.im) + e1r, l1.im + (cm1 * l1.im - s * l0.re) + e1i};
     }
-    __device__ void scale(int k, float m) const {
-        hi[k] = Cx<float>{hi[k].re * m, hi[k].im * m};
-        lo[k] = Cx<float>{lo[k].re * m, lo[k].im * m};
+    __device__ void scale(int k, float m) const {  // the product's rounding error goes to lo
+        const Cx<float> h = hi[k], l = lo[k];
+        const float pr = h.re * m, pi = h.im * m;
+        hi[k] = Cx<float>{pr, pi};
+        lo[k] = Cx<float>{fmaf(l.re, m, fmaf(h.re, m, -pr)), fmaf(l.im, m, fmaf(h.im, m, -pi))};
     }
     __device__ Cx<float> out(int k) const { return Cx<float>{hi[k].re + lo[k].re, hi[k].im + lo[k].im}; }
+    // element k to g[at]: hi + lo folded, or, with a stored residual, hi + lo
+    // renormalised (Fast2Sum, |hi| >= |lo|) into g[at] and glo[at]
+    __device__ __forceinline__ void store(int k, Cx<float>* g, Cx<float>* glo, int64_t at) const {
+        const Cx<float> h = hi[k], l = lo[k];
+        const float sr = h.re + l.re, si = h.im + l.im;
+        st(g + at, Cx<float>{sr, si});
+        if (glo) st(glo + at, Cx<float>{l.re - (sr - h.re), l.im - (si - h.im)});
+    }
 };
 
 // One rotation operator (parity 0: pairs at even F index, 1: odd) of time
@@ -347,7 +484,7 @@ __host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode, int pf_dist) {
+__global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf_dist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int si = plan.rot_items[2 * blockIdx.x];
     const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
@@ -393,12 +530,16 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode,
         scratch = reinterpret_cast<double*>(hi + tile_elems);
     }
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
+    // complex64 with a stored residual: the tile's compensation word starts
+    // from it and is stored back renormalised instead of folded into g
+    Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
 #pragma unroll 4
     for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
         const int l = f >> 5, jj = f & (ROT_ROWS - 1);
         if (jj < rows) {
-            hi[f] = ld(g + int64_t(l) * nr + j0 + jj);
-            if constexpr (Tile<R>::comp) tl.lo[f] = Cx<R>{R(0), R(0)};
+            const int64_t at = int64_t(l) * nr + j0 + jj;
+            hi[f] = ld(g + at);
+            if constexpr (Tile<R>::comp) tl.lo[f] = glo ? ld(glo + at) : Cx<R>{R(0), R(0)};
         }
     }
     if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
@@ -432,7 +573,7 @@ __global__ void __launch_bounds__(256) sh_rot_kernel(ion_sh_plan plan, int mode,
 #pragma unroll 4
         for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
             const int l = f >> 5, j2 = f & (ROT_ROWS - 1);
-            if (j2 < rows) st(g + int64_t(l) * nr + j0 + j2, tl.out(f));
+            if (j2 < rows) tl.store(f, g, glo, int64_t(l) * nr + j0 + j2);
         }
     }
 }
@@ -477,7 +618,7 @@ __global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
 // host side
 // ---------------------------------------------------------------------------
 // rows per thread of the radial solve: the compile-time register capacity
-// of sh_cn_kernel; plan.cn_rows = 0 selects the default
+// of sh_cn_pipelined; plan.cn_rows = 0 selects the default
 template <typename R> struct ShRows;
 template <> struct ShRows<double> {
     static bool ok(int r) { return r == 4 || r == 8; }
@@ -547,10 +688,10 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
 }
 
 template <typename R, int MAXM>
-static int sh_launch_cn_m(const ion_sh_plan* p, cudaStream_t s) {
+static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(sh_cn_kernel<R, MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr = true;
     }
     const int nb = p->n_cn_buckets;
@@ -559,17 +700,21 @@ static int sh_launch_cn_m(const ion_sh_plan* p, cudaStream_t s) {
         const int end = nb > 0 ? p->cn_bucket_end[b] : p->n_cn_items;
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
         if (end > begin) {
-            const size_t smem = sh_cn_smem<R>(threads, MAXM);
+            int dbuf = 1;
+            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2);
+            if (smem > 200 * 1024) {
+                dbuf = 0;
+                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1);
+            }
             if (smem > 200 * 1024) {
                 set_error("ion_sh: radial line too long for shared memory");
                 return ION_ERR_UNSUPPORTED;
             }
-            // prefetch distance: the CTAs resident on the whole GPU at once
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_cn_kernel<R, MAXM>, threads, smem);
-            const int pf_dist = per_sm * num_sms();
-            sh_cn_kernel<R, MAXM><<<end - begin, threads, smem, s>>>(*p, begin, end, pf_dist);
-            if (int e = check_launch("sh_cn_kernel")) return e;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_cn_pipelined<R, MAXM>, threads, smem);
+            const int grid = std::min(end - begin, std::max(per_sm, 1) * num_sms());
+            sh_cn_pipelined<R, MAXM><<<grid, threads, smem, s>>>(*p, begin, end, dbuf);
+            if (int e = check_launch("sh_cn_pipelined")) return e;
         }
         begin = end;
     }
@@ -582,13 +727,13 @@ static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s);
 template <>
 int sh_launch_cn<double>(const ion_sh_plan* p, cudaStream_t s) {
     if (p->n_cn_items == 0) return ION_OK;
-    return sh_rows<double>(p) == 4 ? sh_launch_cn_m<double, 4>(p, s) : sh_launch_cn_m<double, 8>(p, s);
+    return sh_rows<double>(p) == 4 ? sh_launch_cn_pipelined<double, 4>(p, s) : sh_launch_cn_pipelined<double, 8>(p, s);
 }
 
 template <>
 int sh_launch_cn<float>(const ion_sh_plan* p, cudaStream_t s) {
     if (p->n_cn_items == 0) return ION_OK;
-    return sh_rows<float>(p) == 8 ? sh_launch_cn_m<float, 8>(p, s) : sh_launch_cn_m<float, 16>(p, s);
+    return sh_rows<float>(p) == 8 ? sh_launch_cn_pipelined<float, 8>(p, s) : sh_launch_cn_pipelined<float, 16>(p, s);
 }
 
 template <typename R>

@@ -59,15 +59,27 @@ class QuantumMesh:
         return vector if order is None else np.reshape(vector, self.mesh_shape, order)
 
     # ---- wavefunction ----
+    def _psi_residual(self):
+        """The device residual of psi (precision c64x), else None."""
+        return None
+
     @property
     def g(self) -> np.ndarray:
-        return self._psi_device().cpu().numpy().astype(np.complex128).reshape(self.mesh_shape)
+        g = self._psi_device().cpu().numpy().astype(np.complex128)
+        lo = self._psi_residual()
+        if lo is not None:
+            g = g + lo.cpu().numpy().astype(np.complex128)
+        return g.reshape(self.mesh_shape)
 
     @g.setter
     def g(self, value):
         d = self._psi_device()
-        d.copy_(torch.from_numpy(np.ascontiguousarray(np.asarray(value, dtype=np.complex128).reshape(d.shape))).to(
-            d.device, d.dtype))
+        v = np.ascontiguousarray(np.asarray(value, dtype=np.complex128).reshape(d.shape))
+        d.copy_(torch.from_numpy(v).to(d.device, d.dtype))
+        lo = self._psi_residual()
+        if lo is not None:
+            hi = v.astype(np.complex64).astype(np.complex128)
+            lo.copy_(torch.from_numpy((v - hi).astype(np.complex64)).to(lo.device))
 
     @property
     def psi(self):
@@ -168,6 +180,9 @@ class LineMesh(QuantumMesh):
         method = spec.evolution_method
         if not isinstance(self.operators, mo.LineLengthGaugeOperators):
             raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on LineMesh")
+        if self.precision == core.Precision.C64X:
+            raise exceptions.UnsupportedMesh("precision c64x (complex64 with a stored residual) is implemented for "
+                                             "spherical-harmonic meshes only")
         if isinstance(method, em.AlternatingDirectionImplicit):
             kind = nat.ION_LINE_ADI
         elif isinstance(method, em.SplitInteractionOperator):
@@ -304,7 +319,8 @@ class SphericalHarmonicMesh(QuantumMesh):
             raise exceptions.UnsupportedMesh(
                 f"{type(spec.evolution_method).__name__} has no device path on SphericalHarmonicMesh"
             )
-        maxr = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_sh_max_n_r_" + self.precision.value)
+        suffix = "c128" if self.precision == core.Precision.C128 else "c64"
+        maxr = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_sh_max_n_r_" + suffix)
         if spec.r_points > maxr:
             raise exceptions.UnsupportedMesh(f"r_points {spec.r_points} exceeds the device limit {maxr}")
         tb = self.operators.device_tables(self)
@@ -339,6 +355,9 @@ class SphericalHarmonicMesh(QuantumMesh):
 
     def _psi_device(self):
         return self._dsim.g
+
+    def _psi_residual(self):
+        return self._dsim.g_lo
 
     def _tau_dev(self):
         return self._dsim.d_tau

@@ -16,11 +16,18 @@ share the GPU:
   their device memory fits the HBM budget, and finished ones are retired: their
   data are copied to the host and their buffers freed;
 * at most two chunks per batch are in flight, so admission and retirement
-  follow the GPU closely without the host waiting on every chunk.
+  follow the GPU closely; a batch whose queue is full does not hold up the
+  others, and a new request's buffers are uploaded on a separate stream.
 
 A request's results do not depend on which other requests shared its
-launches (per-simulation tables, chunking, tiles and reduction order), so a
-request served in a mix is bit-identical to the same request run alone.
+launches (per-simulation tables, solver chunking, tiles and reduction order),
+and every simulation meets chunk boundaries at the same steps of its own run
+(multiples of ``chunk_steps`` from its admission), so a request served in a
+mix is bit-identical to the same request served alone with the same chunk
+length.  complex128 results do not depend on the chunk length either (they
+equal the plain mesh path); complex64 ones do in the last bit, because the
+rotation pass carries a compensation word across a step boundary only inside
+one chunk.
 """
 
 import collections
@@ -101,7 +108,7 @@ def device_bytes(req: Request, precision: Optional[str] = None) -> int:
     """Device memory a request holds while it runs (psi, coefficient and field
     tables, test states, data buffers)."""
     prec = Precision(precision or req.precision)
-    c = 16 if prec == Precision.C128 else 8
+    c = 8 if prec == Precision.C64 else 16  # complex64 + residual counts twice
     n_t = req.steps + 1
     if req.kind == "sh":
         nr, nl, ns = req.points, req.l_bound, 15
@@ -128,8 +135,11 @@ class Server:
         self.chunk_steps = int(chunk_steps)
         self.keep_psi = keep_psi
         self.groups: Dict[tuple, _Group] = {}
-        self.used_bytes = 0
+        self._upload = None
+        self.used_bytes = 0  # reserved: device_bytes() of every active request
         self.peak_bytes = 0
+        self.allocated_bytes = 0  # what the active requests' buffers actually hold
+        self.peak_allocated_bytes = 0
         self.peak_active = 0
 
     def _group(self, req: Request) -> _Group:
@@ -140,8 +150,13 @@ class Server:
         return g
 
     def _admit(self, req: Request, tables):
+        """Upload a request on the upload stream (so the copies do not wait
+        behind the group's running chunks); the group's stream waits for it on
+        the device before its next chunk."""
         g = self._group(req)
-        with torch.cuda.stream(g.stream):
+        if self._upload is None:
+            self._upload = torch.cuda.Stream()
+        with torch.cuda.stream(self._upload):
             if req.kind == "sh":
                 dsim = dev.ShDeviceSim(tables, g.precision)
                 first = dev.ShBatch(g.precision, [dsim])
@@ -149,7 +164,10 @@ class Server:
                 dsim = dev.LineDeviceSim(tables, g.precision)
                 first = dev.LineBatch(g.precision, [dsim])
             first.reduce()  # data at t = 0
-            g.batch.add(dsim)
+            ready = torch.cuda.Event()
+            ready.record(self._upload)
+        g.stream.wait_event(ready)
+        g.batch.add(dsim)
         return g, dsim
 
     def run(self, requests: List[Request], realtime: bool = True) -> List[Completion]:
@@ -176,18 +194,23 @@ class Server:
                     break
                 waiting.popleft()
                 g, dsim = self._admit(req, tables)
-                nbytes = dsim.nbytes()
-                self.used_bytes += nbytes
-                active[req.id] = (req, g, dsim, clock(), nbytes)
+                self.used_bytes += need
+                self.allocated_bytes += dsim.nbytes()
+                active[req.id] = (req, g, dsim, clock(), need)
             self.peak_bytes = max(self.peak_bytes, self.used_bytes)
+            self.peak_allocated_bytes = max(self.peak_allocated_bytes, self.allocated_bytes)
             self.peak_active = max(self.peak_active, len(active))
 
-            # one chunk for every group with unfinished simulations
+            # a chunk for every group with unfinished simulations and room in
+            # its queue (two chunks in flight at most); a full group does not
+            # hold up the others
+            moved = False
             for g in self.groups.values():
-                if not any(s.t < s.t_final for s in g.batch.sims):
+                while g.inflight and g.inflight[0].query():
+                    g.inflight.popleft()
+                if len(g.inflight) >= 2 or not any(s.t < s.t_final for s in g.batch.sims):
                     continue
-                while len(g.inflight) >= 2:
-                    g.inflight.popleft().synchronize()
+                moved = True
                 with torch.cuda.stream(g.stream):
                     g.batch.run(self.chunk_steps)
                     ev = torch.cuda.Event()
@@ -202,11 +225,13 @@ class Server:
             still = []
             for ev, rid in retiring:
                 if ev.query():
+                    moved = True
                     req, g, dsim, adm, nb = active.pop(rid)
                     norm, ips = dsim.data()
                     psi = dsim.psi_host() if self.keep_psi else None
                     g.batch.remove(dsim)
                     self.used_bytes -= nb
+                    self.allocated_bytes -= dsim.nbytes()
                     done.append(Completion(req, adm, clock(), norm, ips, psi))
                 else:
                     still.append((ev, rid))
@@ -214,8 +239,8 @@ class Server:
 
             if not active and not waiting and pending and realtime:
                 time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.05)))
-            elif retiring and not any(any(s.t < s.t_final for s in g.batch.sims) for g in self.groups.values()):
-                retiring[0][0].synchronize()  # nothing left to enqueue: wait for the GPU
+            elif not moved:
+                time.sleep(0.0005)  # every queue is full: let the GPU catch up
         torch.cuda.synchronize()
         return done
 
@@ -249,7 +274,8 @@ def _main(argv=None):
     done = server.run(reqs)
     out = summarize(done, time.perf_counter() - t)
     out["peak_active"] = server.peak_active
-    out["peak_device_bytes"] = server.peak_bytes
+    out["peak_reserved_bytes"] = server.peak_bytes
+    out["peak_allocated_bytes"] = server.peak_allocated_bytes
     print(json.dumps(out))
 
 

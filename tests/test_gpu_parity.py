@@ -127,6 +127,25 @@ def test_mesh_c64_population_error(cuda, kind, name):
     assert rel_l2(sim.mesh.g, z["g_final"]) < 1e-4
 
 
+@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] == "sh"])
+def test_mesh_c64x_population_error(cuda, kind, name):
+    """complex64 arithmetic with the state's rounding residual kept: the final
+    population is within 1e-6 of the reference (the target of the complex64
+    forms).  psi itself stays near 1e-5 relative L2 (measured 1.05e-5 on the
+    even-L case): what remains is the FP32 rounding of the coefficients and
+    rotation angles, a small systematic change of H that moves the phase, not
+    the populations."""
+    params, z = load_golden(name)
+    sim = product_spec(kind, params, precision="c64x").to_sim()
+    sim.run()
+    p64 = sim.data.initial_state_overlap[-1]
+    p128 = z["initial_state_overlap"][-1]
+    err = rel_l2(sim.mesh.g, z["g_final"])
+    print(f"{name} c64x: |P - P_ref| = {abs(p64 - p128):.2e}, psi rel L2 = {err:.2e}")
+    assert abs(p64 - p128) < 1e-6
+    assert err < 1e-4
+
+
 def test_run_with_callback_and_resume(cuda):
     """Per-step callbacks and max_steps/resume give the same result."""
     params, z = load_golden("sh_split_small_oddL")
