@@ -278,7 +278,9 @@ def run_ours(args, rank, world, local_rank):
     alg_bytes = 16 * points  # complex64: psi read once and written once per kernel
     dominant, dom_ms = ("sh_cn_pipelined", cn_ms) if cn_ms >= rot_ms else ("sh_rot_kernel", rot_ms)
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
-    traffic = profile_traffic().get(dominant + "_c64_bytes_per_point")
+    pt = profile_traffic()
+    traffic = pt.get(dominant + "_c64_bytes_per_point")
+    step_traffic = pt.get("step_total_c64_bytes_per_point")
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -288,6 +290,10 @@ def run_ours(args, rank, world, local_rank):
         "unit": "GB/s",
         "frac": round(achieved / peak, 4),
         "traffic": None if traffic is None else int(traffic * points),
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 240-simulation case, "
+                          "bytes per point scaled to this workload (profiles/sh_dram_traffic_c64_uneven.md)",
+        "step_traffic": None if step_traffic is None else int(step_traffic * points),
+        "step_algorithmic_bytes": 2 * alg_bytes,
         "algorithmic_bytes": alg_bytes,
         "kernel_ms": {"sh_cn_pipelined": round(cn_ms, 4), "sh_rot_kernel": round(rot_ms, 4)},
         "frac_by_kernel": {"sh_cn_pipelined": round(alg_bytes / (cn_ms / 1e3) / 1e9 / peak, 4),

@@ -168,6 +168,12 @@ typedef struct ion_sh_sim {
      * added to (g, g_lo) with an exact two-sum and the pair is renormalised
      * when stored, so storing psi no longer rounds it to FP32 precision. */
     void *g_lo;
+    /* _c64 entry points: kinv + hoff[j-1] + hoff[j] (zero outside the line),
+     * summed in FP64 and rounded once, [n_r] (or NULL), zero-padded to a
+     * multiple of 16 entries.  With it the explicit half of the radial step is
+     * formed from neighbour differences and this row sum, which avoids the
+     * cancellation of the kinetic terms in FP32. */
+    const float *ksum32;
 } ion_sh_sim;
 
 typedef struct ion_sh_plan {

@@ -67,6 +67,7 @@ class ShSim(ctypes.Structure):
         ("n_tiles", c_i32),
         ("pad_", c_i32),
         ("g_lo", c_vp),
+        ("ksum32", c_vp),
     ]
 
 

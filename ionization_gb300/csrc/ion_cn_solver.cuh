@@ -71,6 +71,13 @@ __device__ __forceinline__ void load_chunk(const Coef& coef, int s, R (&bo)[M], 
     for (int k = 0; k < M; ++k) coef(s + k, bo[k], bd[k]);
 }
 
+// (B psi)_i = a0 psi_{i-1} + bd psi_i + bo psi_{i+1}; a coefficient type that
+// can form it without cancellation provides its own overload.
+template <class Coef, typename R>
+__device__ __forceinline__ Cx<R> stencil_row(const Coef&, int, R a0, R bd, R bo, Cx<R> p0, Cx<R> p1, Cx<R> p2) {
+    return Cx<R>{a0 * p0.re + bd * p1.re + bo * p2.re, a0 * p0.im + bd * p1.im + bo * p2.im};
+}
+
 struct NoExtra {
     template <typename R>
     __device__ __forceinline__ Cx<R> get(int) const {
@@ -118,8 +125,7 @@ __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R
     // y_k = -i (w (B psi)_k + X_k)
     auto Y = [&](int k) -> Cx<R> {
         const Cx<R> p0 = P(k - 1), p1 = P(k), p2 = P(k + 1);
-        const R a0 = ao(k);
-        Cx<R> v = {a0 * p0.re + bd[k] * p1.re + bo[k] * p2.re, a0 * p0.im + bd[k] * p1.im + bo[k] * p2.im};
+        Cx<R> v = stencil_row(coef, s + k, ao(k), bd[k], bo[k], p0, p1, p2);
         const Cx<R> X = extra.template get<R>(s + k);
         v = Cx<R>{w * v.re + X.re, w * v.im + X.im};
         return Cx<R>{v.im, -v.re};  // -i v
@@ -171,63 +177,85 @@ __device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R
     rowE.d = DE * iE;
 }
 
-// PCR over 2T normalised rows; row k = 2u + q is stored at slot q T + u of
-// double-buffered A, C, D arrays (pcr_smem_bytes<R>(T) bytes).
+// The reduced system of the 2T chunk-end unknowns, solved on T rows.
+// Thread t holds two normalised rows: r[0] for the first unknown of its
+// chunk, xs_t = d - a xe_{t-1} - c xe_t, and r[1] for the last one,
+// a xs_t + xe_t + c xs_{t+1} = d.  Substituting the first-row equations of
+// threads t and t+1 into r[1] leaves one tridiagonal row in xe per thread
+// (one step of odd-even reduction); PCR solves those T rows (ceil(log2 T)
+// levels of one row per thread), and xs_t follows from r[0].  Uses
+// 10 T complex words of ``red`` (pcr_smem_bytes<R>(T) holds 12 T).  On
+// return r[0].d = xs_t and r[1].d = xe_t.
 template <typename R>
 __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2]) {
-    const Cx<R> zero = {R(0), R(0)};
-    const int N = 2 * T;
-    Cx<R>* Ab = red;
-    Cx<R>* Cb = red + 2 * N;
-    Cx<R>* Db = red + 4 * N;
+    const Cx<R> zero = {R(0), R(0)}, one = {R(1), R(0)};
+    Cx<R>* Sa = red;
+    Cx<R>* Sc = red + T;
+    Cx<R>* Sd = red + 2 * T;
+    Cx<R>* Ab = red + 3 * T;  // double-buffered [2][T]
+    Cx<R>* Cb = red + 5 * T;
+    Cx<R>* Db = red + 7 * T;
+    Cx<R>* Xe = red + 9 * T;
     if (active) {
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            Ab[q * T + t] = r[q].a;
-            Cb[q * T + t] = r[q].c;
-            Db[q * T + t] = r[q].d;
-        }
+        Sa[t] = r[0].a;
+        Sc[t] = r[0].c;
+        Sd[t] = r[0].d;
     }
     __syncthreads();
-    const int levels = pcr_levels(N);
+    RedRow<R> e = {zero, zero, zero};
+    if (active) {
+        Cx<R> an = zero, cn = zero, dn = zero;  // the next thread's first row
+        if (t + 1 < T) {
+            an = Sa[t + 1];
+            cn = Sc[t + 1];
+            dn = Sd[t + 1];
+        }
+        const RedRow<R>& S = r[0];
+        const RedRow<R>& E = r[1];
+        const Cx<R> inv = crecip_fast(one - E.a * S.c - E.c * an);
+        e.a = -(E.a * S.a) * inv;
+        e.c = -(E.c * cn) * inv;
+        e.d = (E.d - E.a * S.d - E.c * dn) * inv;
+        Ab[t] = e.a;
+        Cb[t] = e.c;
+        Db[t] = e.d;
+    }
+    __syncthreads();
+    const int levels = pcr_levels(T);
     int p = 0;
     for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
         if (active) {
-            const int base = p * N;
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int k = 2 * t + q;
-                Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
-                const int km = k - sig, kp = k + sig;
-                if (km >= 0) {
-                    const int sl = base + (km & 1) * T + (km >> 1);
-                    am = Ab[sl];
-                    cm = Cb[sl];
-                    dm = Db[sl];
-                }
-                if (kp < N) {
-                    const int sl = base + (kp & 1) * T + (kp >> 1);
-                    ap = Ab[sl];
-                    cpp = Cb[sl];
-                    dp = Db[sl];
-                }
-                const Cx<R> a = r[q].a, c = r[q].c, d = r[q].d;
-                const Cx<R> nb = Cx<R>{R(1), R(0)} - cm * a - ap * c;
-                const Cx<R> inv = crecip_fast(nb);
-                r[q].a = -(am * a) * inv;
-                r[q].c = -(cpp * c) * inv;
-                r[q].d = (d - dm * a - dp * c) * inv;
+            const int base = p * T;
+            Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
+            if (t - sig >= 0) {
+                am = Ab[base + t - sig];
+                cm = Cb[base + t - sig];
+                dm = Db[base + t - sig];
             }
-            const int wb = (p ^ 1) * N;
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                Ab[wb + q * T + t] = r[q].a;
-                Cb[wb + q * T + t] = r[q].c;
-                Db[wb + q * T + t] = r[q].d;
+            if (t + sig < T) {
+                ap = Ab[base + t + sig];
+                cpp = Cb[base + t + sig];
+                dp = Db[base + t + sig];
             }
+            const Cx<R> a = e.a, c = e.c, d = e.d;
+            const Cx<R> inv = crecip_fast(one - cm * a - ap * c);
+            e.a = -(am * a) * inv;
+            e.c = -(cpp * c) * inv;
+            e.d = (d - dm * a - dp * c) * inv;
+            const int wb = (p ^ 1) * T;
+            Ab[wb + t] = e.a;
+            Cb[wb + t] = e.c;
+            Db[wb + t] = e.d;
         }
         p ^= 1;
         __syncthreads();
+    }
+    if (active) Xe[t] = e.d;
+    __syncthreads();
+    if (active) {
+        const Cx<R> xem1 = t > 0 ? Xe[t - 1] : zero;
+        r[0].d = r[0].d - r[0].a * xem1 - r[0].c * e.d;
+        r[1].d = e.d;
     }
 }
 

@@ -147,8 +147,6 @@ __device__ __forceinline__ Cx<R> add_exact(Cx<R> h, Cx<R> d, Cx<R>& lo) {
     return Cx<R>{add_exact1(h.re, d.re, lo.re), add_exact1(h.im, d.im, lo.im)};
 }
 
-
-
 __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
 }
@@ -184,6 +182,7 @@ struct ShCnCoef32 {
     const float* kinv;
     const float* cent;
     const float* hoff;
+    const float* ksum;  // kinv + hoff[i-1] + hoff[i], summed in FP64 (may be NULL)
     float ll1, corr0, tau;
     int n;
     __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const {
@@ -220,6 +219,25 @@ __device__ __forceinline__ void load_chunk(const ShCnCoef32& c, int s, float (&b
     }
 }
 
+// The explicit half-step of the complex64 radial solve.  Its kinetic terms
+// are ~1/dr^2 times psi and cancel to ~E psi, so forming a0 psi_{i-1} +
+// bd psi_i + bo psi_{i+1} in FP32 leaves a random error of ~1e-8 |psi| per
+// step, which sums to the dominant complex64 error over 10^4 steps.  Written
+// with neighbour differences and the row sum of B (tabulated in FP64 and
+// rounded once),
+//   (B psi)_i = a0 (psi_{i-1} - psi_i) + bo (psi_{i+1} - psi_i) + rowsum_i psi_i,
+// each product is of a small quantity and the cancellation is gone.
+__device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32& c, int i, float a0, float bd, float bo,
+                                                  Cx<float> p0, Cx<float> p1, Cx<float> p2) {
+    if (c.ksum == nullptr || i >= c.n)
+        return Cx<float>{a0 * p0.re + bd * p1.re + bo * p2.re, a0 * p0.im + bd * p1.im + bo * p2.im};
+    float h = c.ksum[i] + c.ll1 * c.cent[i];
+    if (i == 0) h = h + c.corr0;
+    const float rs = c.tau * h;
+    const Cx<float> dm = p0 - p1, dp = p2 - p1;
+    return Cx<float>{a0 * dm.re + bo * dp.re + rs * p1.re, a0 * dm.im + bo * dp.im + rs * p1.im};
+}
+
 template <typename R> struct ShCnCoefFor;
 template <> struct ShCnCoefFor<double> {
     using type = ShCnCoef<double>;
@@ -230,7 +248,8 @@ template <> struct ShCnCoefFor<double> {
 template <> struct ShCnCoefFor<float> {
     using type = ShCnCoef32;
     __device__ static type make(const ion_sh_sim& S, int l, float tau) {
-        return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r};
+        return type{S.kinv32, S.cent32, S.hoff32, S.ksum32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f,
+                    tau, S.n_r};
     }
 };
 
