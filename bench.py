@@ -2,11 +2,14 @@
 """Benchmark: batched uneven spherical-harmonic sweep on one GB300.
 
 Workload ``uneven_sh_sweep``: 512 spherical-harmonic split-operator
-simulations (Nr 800-3200 at dr 0.125, l_max 20-80, seeded pulses), complex64
-psi with FP64 fields, coefficients and reductions, 52.3 M mesh points,
-419 MB of psi (larger than L2).  A step advances all 512 simulations by one
-time step: three kernel launches (radial solve, rotation/mask/reduction pass,
-time-index advance).
+simulations (Nr 800-3200 at dr 0.125, l_max 20-80, seeded pulses), 52.3 M
+mesh points.  The headline configuration is c64x: complex64 arithmetic with
+FP64 fields, coefficients and reductions, psi stored as complex64 plus its
+complex64 rounding residual (837 MB, larger than L2) and refined radial
+solves, which keeps the final populations within 1e-6 of complex128 (see
+``accuracy``); plain complex64 is timed beside it (``c64_plain``).  A step
+advances all 512 simulations by one time step: three kernel launches (radial
+solve, rotation/mask/reduction pass, time-index advance).
 
 Prints one JSON line:
   value      mesh-point-steps/s over the timed steps, psi resident in HBM
@@ -204,12 +207,58 @@ class Clocks:
 # --------------------------------------------------------------------------
 
 
+HEADLINE = "c64x"  # complex64 arithmetic, residual-compensated state: meets the 1e-6 bound
+
+
+def time_batch(specs, tables, precision, K, warmup, rows, gs, local_rank, barrier):
+    """K steps of the whole batch with per-kernel CUDA events on the launching
+    stream (ion_sh_split_phase: rotations before the first solve, then per step
+    radial solve / rotation pass / advance) and the clocks sampled meanwhile."""
+    import torch
+
+    from ionization_gb300 import _native as nat
+    from ionization_gb300 import batch as bm
+
+    b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows,
+                                              tables=tables)
+    b.step(max(warmup, 3))
+    torch.cuda.synchronize()
+    plan = b.batch.plan
+    fn = "ion_sh_split_phase_c128" if precision == "c128" else "ion_sh_split_phase_c64"
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    e_cn = [(ev(), ev()) for _ in range(K)]
+    e_rot = [ev() for _ in range(K)]
+    e0, e1 = ev(), ev()
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local_rank) as clk:
+        e0.record(stream)
+        nat.call(fn, nat.ctypes.byref(plan), 1, sp)  # rotations before the first solve
+        for k in range(K):
+            e_cn[k][0].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 2, sp)
+            e_cn[k][1].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 4 if k + 1 < K else 3, sp)
+            e_rot[k].record(stream)
+            nat.call(fn, nat.ctypes.byref(plan), 5, sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    out = dict(elapsed_ms=e0.elapsed_time(e1),
+               cn_ms=float(np.mean([a.elapsed_time(c) for a, c in e_cn])),
+               rot_ms=float(np.mean([e_cn[k][1].elapsed_time(e_rot[k]) for k in range(K)])),
+               clocks=clk.summary(), launches=1 + 3 * K)
+    del b
+    torch.cuda.synchronize()
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
     import ionization_gb300 as ig
-    from ionization_gb300 import _device as dev
-    from ionization_gb300 import _native as nat
     from ionization_gb300 import batch as bm
     from ionization_gb300 import replicas
     from ionization_gb300 import workloads as wl
@@ -225,48 +274,22 @@ def run_ours(args, rank, world, local_rank):
 
     # ---- the workload: this rank's seeded sweep (replicas, weak scaling) ----
     t_setup = time.perf_counter()
-    specs = wl.uneven_sh_sweep(N_SIMS, seed=replicas.sweep_seed(SEED, rank), steps=SIM_STEPS, precision="c64")
+    specs = wl.uneven_sh_sweep(N_SIMS, seed=replicas.sweep_seed(SEED, rank), steps=SIM_STEPS, precision=HEADLINE)
     tables = [bm._host_tables(s)[0] for s in specs]
     setup_host_s = time.perf_counter() - t_setup
     points = int(sum(t.n_r * t.n_l for t in tables))
 
-    (best_rows, best_gs), tune = bm.autotune(specs, "c64", graph_steps=(32,), steps=16, tables=tables)
-    b = bm.BatchedSphericalHarmonicSimulation(specs, precision="c64", graph_steps=best_gs, cn_rows=best_rows,
-                                              tables=tables)
-    b.step(max(args.warmup, 3))
-    torch.cuda.synchronize()
+    (best_rows, best_gs), tune = bm.autotune(specs, HEADLINE, graph_steps=(32,), steps=16, tables=tables)
 
-    # ---- timed region: K steps, per-kernel events on the launching stream ----
+    # ---- timed region: K steps of the headline configuration ----
     K = args.steps
-    plan = b.batch.plan
-    fn = "ion_sh_split_phase_c64"
-    stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
-    e_cn = [(ev(), ev()) for _ in range(K)]
-    e_rot = [(ev(), ev()) for _ in range(K)]
-    e0, e1 = ev(), ev()
-    barrier()
-    torch.cuda.synchronize()
-    with Clocks(local_rank) as clk:
-        e0.record(stream)
-        nat.call(fn, nat.ctypes.byref(plan), 1, sp)  # rotations before the first solve
-        for k in range(K):
-            e_cn[k][0].record(stream)
-            nat.call(fn, nat.ctypes.byref(plan), 2, sp)
-            e_cn[k][1].record(stream)
-            nat.call(fn, nat.ctypes.byref(plan), 4 if k + 1 < K else 3, sp)
-            e_rot[k][1].record(stream)
-            nat.call(fn, nat.ctypes.byref(plan), 5, sp)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    for s in b.sims:
-        s.t = min(s.t + K, s.t_final)
-    elapsed_ms = replicas.max_over_ranks(e0.elapsed_time(e1))
-    cn_ms = float(np.mean([a.elapsed_time(c) for a, c in e_cn]))
-    rot_ms = float(np.mean([e_cn[k][1].elapsed_time(e_rot[k][1]) for k in range(K)]))
-    gpu_launches = 1 + 3 * K
+    main = time_batch(specs, tables, HEADLINE, K, args.warmup, best_rows, best_gs, local_rank, barrier)
+    elapsed_ms = replicas.max_over_ranks(main["elapsed_ms"])
+    cn_ms, rot_ms, clk_summary, gpu_launches = main["cn_ms"], main["rot_ms"], main["clocks"], main["launches"]
+    # plain complex64 (no stored residual): faster, above the 1e-6 bound
+    K64 = min(K, 100)
+    t64 = time_batch(specs, tables, "c64", K64, args.warmup, 16, best_gs, local_rank, barrier)
+    t64_ms = replicas.max_over_ranks(t64["elapsed_ms"])
 
     value = world * points * K / (elapsed_ms / 1e3)
     if rank != 0:
@@ -275,12 +298,13 @@ def run_ours(args, rank, world, local_rank):
         return None
 
     peak, peak_kind = measured_peaks()
-    alg_bytes = 16 * points  # complex64: psi read once and written once per kernel
+    state_bytes = 16  # complex64 psi + its complex64 residual per point
+    alg_bytes = 2 * state_bytes * points  # the state read once and written once per kernel
     dominant, dom_ms = ("sh_cn_pipelined", cn_ms) if cn_ms >= rot_ms else ("sh_rot_kernel", rot_ms)
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
     pt = profile_traffic()
-    traffic = pt.get(dominant + "_c64_bytes_per_point")
-    step_traffic = pt.get("step_total_c64_bytes_per_point")
+    traffic = pt.get(dominant + "_c64x_bytes_per_point")
+    step_traffic = pt.get("step_total_c64x_bytes_per_point")
     roofline = {
         "bound": "hbm",
         "kernel": dominant,
@@ -290,8 +314,8 @@ def run_ours(args, rank, world, local_rank):
         "unit": "GB/s",
         "frac": round(achieved / peak, 4),
         "traffic": None if traffic is None else int(traffic * points),
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 240-simulation case, "
-                          "bytes per point scaled to this workload (profiles/sh_dram_traffic_c64_uneven.md)",
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on a 240-simulation case of the "
+                          "sweep, bytes per point scaled to this workload (profiles/)",
         "step_traffic": None if step_traffic is None else int(step_traffic * points),
         "step_algorithmic_bytes": 2 * alg_bytes,
         "algorithmic_bytes": alg_bytes,
@@ -299,9 +323,17 @@ def run_ours(args, rank, world, local_rank):
         "frac_by_kernel": {"sh_cn_pipelined": round(alg_bytes / (cn_ms / 1e3) / 1e9 / peak, 4),
                            "sh_rot_kernel": round(alg_bytes / (rot_ms / 1e3) / 1e9 / peak, 4)},
     }
+    c64_plain = {
+        "dtype": "c64", "value": world * points * K64 / (t64_ms / 1e3), "unit": UNIT, "steps": K64,
+        "ms_per_step": t64_ms / K64,
+        "kernel_ms": {"sh_cn_pipelined": round(t64["cn_ms"], 4), "sh_rot_kernel": round(t64["rot_ms"], 4)},
+        "frac_by_kernel": {k: round(16 * points / (v / 1e3) / 1e9 / peak, 4)
+                           for k, v in (("sh_cn_pipelined", t64["cn_ms"]), ("sh_rot_kernel", t64["rot_ms"]))},
+        "note": "complex64 state without the stored residual: above the 1e-6 population bound (see accuracy)",
+    }
 
     # ---- e2e through the public API from host buffers ----
-    e2e = run_e2e(args, specs, tables, best_rows, best_gs, points)
+    e2e = run_e2e(args, specs, tables, best_rows, best_gs, points, HEADLINE)
 
     # ---- plain complex128 drop-in path, single simulation ----
     plain = run_plain_c128(args)
@@ -323,7 +355,7 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"first {len(sample)} simulations of the sweep x {args.cpu_steps} steps on {cores} "
                          f"processes (complex128 oracle), {wall:.1f} s wall"}
 
-    clocks = clk.summary()
+    clocks = clk_summary
     out = {
         "metric": METRIC,
         "value": value,
@@ -339,10 +371,12 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic",
         "config": {
             "workload": "uneven_sh_sweep: 512 spherical-harmonic sims, Nr 800-3200, l_max 20-80, split operator",
+            "precision": "c64x: complex64 arithmetic, FP64 fields / tables / reductions, psi stored as complex64 "
+                         "+ complex64 rounding residual, refined radial solves",
             "n_sims": N_SIMS,
             "mesh_points": points,
-            "psi_bytes": points * 8,
-            "l2": "inputs larger than L2 (psi 419 MB)",
+            "state_bytes": points * state_bytes,
+            "l2": "inputs larger than L2 (state 837 MB)",
             "parallelism": f"replicas x{world}",
             "autotune": {"chosen": {"cn_rows_per_thread": best_rows, "graph_steps": best_gs},
                          "ms_per_step": {f"rows{r}_graph{g}": round(v, 4) for (r, g), v in tune.items()}},
@@ -354,6 +388,7 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": gpu_launches,
         "clocks": clocks,
         "plain_c128": plain,
+        "c64_plain": c64_plain,
         "accuracy": acc,
         "serving": serving,
     }
@@ -364,7 +399,7 @@ def run_ours(args, rank, world, local_rank):
     return out
 
 
-def run_e2e(args, specs, tables, rows, gs, points):
+def run_e2e(args, specs, tables, rows, gs, points, precision):
     """Public API from host buffers: build the batch (H2D of psi, tables and
     field tables), K steps, then read back every simulation's data and psi."""
     import torch
@@ -374,15 +409,15 @@ def run_e2e(args, specs, tables, rows, gs, points):
     K = args.steps
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b = bm.BatchedSphericalHarmonicSimulation(specs, precision="c64", graph_steps=gs, cn_rows=rows, tables=tables)
+    b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
     b.step(K)
     res = b.results()
-    psis = [s.g.cpu() for s in b.sims]
+    psis = [s.psi_host() for s in b.sims]  # g (+ its residual) to the host
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     h2d = sum(s.nbytes() for s in b.sims) - sum(int(s.d_partials.numel()) * 8 for s in b.sims)
-    d2h = sum(int(p.numel()) * 8 for p in psis) + sum(r["norm"].nbytes + 16 * len(r["inner_products"]) * len(r["norm"])
-                                                       for r in res)
+    d2h = sum(s.g.numel() * s.g.element_size() * (1 if s.g_lo is None else 2) for s in b.sims)
+    d2h += sum(r["norm"].nbytes + 16 * len(r["inner_products"]) * len(r["norm"]) for r in res)
     del b, psis
     return {"value": points * K / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / K),
             "d2h_bytes_per_step": int(d2h / K), "steps": K, "wall_s": round(wall, 3)}

@@ -30,6 +30,10 @@
  *                         (evolution_methods.py:46-77, mesh_operators.py:550-640)
  *   ion_reduce_*          QuantumMesh.inner_product / norm (meshes.py:195-217) and the
  *                         SphericalHarmonicMesh inner-product shortcut (meshes.py:1099-1131)
+ *   ion_weighted_norms_*, ion_sh_observables_*
+ *                         QuantumMesh.z/r_expectation_value (meshes.py:231-237),
+ *                         SphericalHarmonicMesh.norm_by_l (meshes.py:1133-1136),
+ *                         NormWithinRadius (data.py:407-425)
  */
 #ifndef IONIZATION_GB300_H
 #define IONIZATION_GB300_H
@@ -166,22 +170,30 @@ typedef struct ion_sh_sim {
      * complex64 (n_l, n_r) like g.  With it psi = g + g_lo carries about 48
      * significant bits: the arithmetic stays FP32, each step's increment is
      * added to (g, g_lo) with an exact two-sum and the pair is renormalised
-     * when stored, so storing psi no longer rounds it to FP32 precision. */
+     * when stored, so storing psi no longer rounds it to FP32 precision; the
+     * explicit half of the radial step is then formed from neighbour
+     * differences and an exact row sum of the same FP32 coefficients, which
+     * removes the cancellation of the kinetic terms and keeps the step
+     * unitary. */
     void *g_lo;
-    /* _c64 entry points: kinv + hoff[j-1] + hoff[j] (zero outside the line),
-     * summed in FP64 and rounded once, [n_r] (or NULL), zero-padded to a
-     * multiple of 16 entries.  With it the explicit half of the radial step is
-     * formed from neighbour differences and this row sum, which avoids the
-     * cancellation of the kinetic terms in FP32. */
-    const float *ksum32;
 } ion_sh_sim;
+
+/* ion_sh_plan.flags: with it, the radial solve of every simulation that carries a
+ * stored residual is followed by one step of iterative refinement.  The matrix
+ * 1 + i tau H0 is the same at every step, so the FP32 rounding of its
+ * elimination is too; unrefined, that fixed error makes the step slightly
+ * non-unitary and the norm drifts by ~2e-10 per step.  The refinement solves for
+ * the correction with the residual formed from the first solution (about twice
+ * the radial-solve time). */
+enum { ION_SH_REFINE = 1 };
 
 typedef struct ion_sh_plan {
     ion_sh_sim *sims;         /* device array [n_sims] */
     int32_t n_sims;
     int32_t max_n_l;          /* largest n_l of the batch */
     int32_t max_n_r;          /* largest n_r of the batch */
-    int32_t pad_;
+    int32_t flags;            /* ION_SH_REFINE: refine the radial solves of the simulations
+                                 that carry a stored residual (g_lo) */
     const int32_t *cn_items;  /* device [n_cn_items*2]: (sim, l) handled by one CTA */
     int32_t n_cn_items;
     int32_t cn_threads;       /* CTA size of the radial solve (multiple of 32) */
@@ -323,6 +335,38 @@ int ion_reduce_c128(int64_t M, const void *g, int32_t n_states, const void *stat
                     double *out_norm, double *out_ip, void *partials, void *stream);
 int ion_reduce_c64(int64_t M, const void *g, int32_t n_states, const void *states, double weight,
                    double *out_norm, double *out_ip, void *partials, void *stream);
+
+/* ------------------------------------------------------------------------
+ * Position expectation values and partial norms (the ZExpectationValue,
+ * RExpectationValue, NormWithinRadius and NormBySphericalHarmonic datastores,
+ * ionization/mesh/data.py:344-464).  FP64 two-stage sums with a compensated
+ * second stage; the complex64 forms accept the stored residual g_lo (or NULL).
+ *
+ * ion_weighted_norms_*: out[k] = weight * sum_i w[k * n + i] |g_i|^2 for
+ *   1 <= n_w <= 8 weight vectors (element-wise operators on line and
+ *   cylindrical meshes: w = z, r or the indicator r <= R; QuantumMesh.
+ *   expectation_value, meshes.py:206-237).
+ * ion_sh_observables_*: on the (n_l, n_r) spherical-harmonic mesh,
+ *   out[0] = <r>, out[1] = <z> (the F-order off-diagonal z operator of
+ *   SphericalHarmonicLengthGaugeOperators.z, mesh_operators.py:1086-1104,
+ *   with c_l = cl[l] and r_j = r[j]), out[2 + l] = norm of line l
+ *   (SphericalHarmonicMesh.norm_by_l, meshes.py:1133-1136) and
+ *   out[2 + n_l + k] = norm of the rows r_j <= radii[k], 0 <= n_radii <= 8;
+ *   every entry times ``weight`` (dr).
+ * ``scratch`` holds the matching *_scratch_bytes query.
+ * ------------------------------------------------------------------------ */
+int64_t ion_weighted_norms_scratch_bytes(int64_t n, int32_t n_w);
+int ion_weighted_norms_c128(int64_t n, const void *g, int32_t n_w, const double *w, double weight, double *out,
+                            void *scratch, int64_t scratch_bytes, void *stream);
+int ion_weighted_norms_c64(int64_t n, const void *g, const void *g_lo, int32_t n_w, const double *w,
+                           double weight, double *out, void *scratch, int64_t scratch_bytes, void *stream);
+int64_t ion_sh_observables_scratch_bytes(int32_t n_r, int32_t n_l, int32_t n_radii);
+int ion_sh_observables_c128(const void *g, int32_t n_r, int32_t n_l, const double *r, const double *cl,
+                            int32_t n_radii, const double *radii, double weight, double *out, void *scratch,
+                            int64_t scratch_bytes, void *stream);
+int ion_sh_observables_c64(const void *g, const void *g_lo, int32_t n_r, int32_t n_l, const double *r,
+                           const double *cl, int32_t n_radii, const double *radii, double weight, double *out,
+                           void *scratch, int64_t scratch_bytes, void *stream);
 
 #ifdef __cplusplus
 }

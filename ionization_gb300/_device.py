@@ -146,12 +146,7 @@ class ShDeviceSim:
         self.d_kinv32 = to_dev(_pad16(tab.kinv), f32)
         self.d_cent32 = to_dev(_pad16(tab.cent), f32)
         self.d_hoff32 = to_dev(_pad16(tab.hoff), f32)
-        # row sums of the radial operator's kinetic + potential part, in FP64
-        hoff = np.asarray(tab.hoff, dtype=np.float64)
-        ksum = np.asarray(tab.kinv, dtype=np.float64).copy()
-        ksum[1:] += hoff
-        ksum[:-1] += hoff
-        self.d_ksum32 = to_dev(_pad16(ksum), f32)
+
         self.d_rq32 = to_dev(tab.rq, f32)
         self.d_cl32 = to_dev(tab.cl, f32)
         self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
@@ -189,9 +184,6 @@ class ShDeviceSim:
         d.out_norm, d.out_ip, d.partials = ptr(self.d_norm), ptr(self.d_ip), ptr(self.d_partials)
         d.n_tiles = self.n_tiles
         d.g_lo = ptr(self.g_lo)
-        # the cancellation-free explicit stencil pays off once the stored
-        # residual has removed the state's own FP32 rounding (c64x)
-        d.ksum32 = ptr(self.d_ksum32) if self.precision == Precision.C64X else None
         return d
 
     def data(self):
@@ -255,6 +247,7 @@ class ShBatch:
         plan.n_sims = len(sims)
         plan.max_n_l = max([s.n_l for s in sims] + [1])
         plan.max_n_r = max([s.n_r for s in sims] + [2])
+        plan.flags = nat.ION_SH_REFINE if any(s.g_lo is not None for s in sims) else 0
         plan.cn_items = ptr(d_cn)
         plan.n_cn_items = len(cn)
         plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, self.cn_rows) for s in sims] + [1]))

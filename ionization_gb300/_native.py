@@ -23,6 +23,7 @@ ION_OK = 0
 ION_LINE_ADI = 0
 ION_LINE_SPLIT = 1
 ION_LINE_FFT = 2
+ION_SH_REFINE = 1
 
 
 class NativeLibraryError(RuntimeError):
@@ -67,7 +68,6 @@ class ShSim(ctypes.Structure):
         ("n_tiles", c_i32),
         ("pad_", c_i32),
         ("g_lo", c_vp),
-        ("ksum32", c_vp),
     ]
 
 
@@ -77,7 +77,7 @@ class ShPlan(ctypes.Structure):
         ("n_sims", c_i32),
         ("max_n_l", c_i32),
         ("max_n_r", c_i32),
-        ("pad_", c_i32),
+        ("flags", c_i32),
         ("cn_items", c_vp),
         ("n_cn_items", c_i32),
         ("cn_threads", c_i32),
@@ -180,6 +180,14 @@ _SIGS = {
     "ion_reduce_scratch_bytes": (c_i64, [c_i64, c_i32]),
     "ion_reduce_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
     "ion_reduce_c64": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
+    "ion_weighted_norms_scratch_bytes": (c_i64, [c_i64, c_i32]),
+    "ion_weighted_norms_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
+    "ion_weighted_norms_c64": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
+    "ion_sh_observables_scratch_bytes": (c_i64, [c_i32, c_i32, c_i32]),
+    "ion_sh_observables_c128": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp,
+                                                c_i64, c_vp]),
+    "ion_sh_observables_c64": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp,
+                                               c_vp, c_i64, c_vp]),
 }
 
 _lock = threading.Lock()

@@ -33,3 +33,15 @@ class Precision(StrEnum):
     C128 = "c128"
     C64 = "c64"
     C64X = "c64x"
+
+
+@dataclasses.dataclass(frozen=True)
+class SphericalHarmonic:
+    """Y_l^m, the key of the per-l datastores (simulacra's SphericalHarmonic
+    in the reference; only l and m matter here)."""
+
+    l: int = 0
+    m: int = 0
+
+    def __str__(self):
+        return f"Y_{self.l}^{self.m}"

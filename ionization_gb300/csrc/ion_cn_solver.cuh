@@ -32,9 +32,8 @@ __host__ __device__ __forceinline__ int islot(int i, int T) {
     return (i % M) * T + i / M;
 }
 
-// complex64 pivots: the hardware reciprocal (MUFU, ~1 ulp) is ample for FP32
-// sweeps; complex128 keeps the correctly rounded reciprocal
-__device__ __forceinline__ float rcp_ieee(float x) { return __fdividef(1.0f, x); }
+// pivots use the correctly rounded reciprocal
+__device__ __forceinline__ float rcp_ieee(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double rcp_ieee(double x) { return __drcp_rn(x); }
 
 template <typename R>

@@ -1,0 +1,238 @@
+// Position expectation values and partial norms of a mesh wavefunction, for
+// the ZExpectationValue, RExpectationValue, NormWithinRadius and
+// NormBySphericalHarmonic datastores (ionization/mesh/data.py:344-464).
+//
+//   ion_weighted_norms_*  out[k] = weight * sum_i w[k][i] |g_i|^2 for a few
+//                         FP64 weight vectors (line and cylindrical meshes:
+//                         w = z, r, or the indicator r <= R, as
+//                         QuantumMesh.expectation_value with an element-wise
+//                         operator and NormWithinRadius.store compute them,
+//                         meshes.py:206-237, data.py:407-425).
+//   ion_sh_observables_*  on the (l, r) spherical-harmonic mesh, in one pass:
+//                         <r> = dr sum |g|^2 r_j;
+//                         <z> = dr sum 2 Re(conj(g_{l,j}) g_{l+1,j}) c_l r_j, the
+//                           F-order off-diagonal z operator of
+//                           SphericalHarmonicLengthGaugeOperators.z
+//                           (mesh_operators.py:1086-1104);
+//                         the norm of each l (SphericalHarmonicMesh.norm_by_l,
+//                         meshes.py:1133-1136);
+//                         the norm within each radius R_k (rows r_j <= R_k).
+// The complex64 state may carry its stored residual (g + g_lo).  Stage 1
+// writes FP64 partials per CTA (per row tile for the SH form); stage 2 adds
+// them in CTA order with Neumaier compensation, so results do not depend on
+// scheduling.
+#include "ion_common.cuh"
+
+namespace ion {
+
+constexpr int OBS_THREADS = 256;
+constexpr int OBS_BLOCKS = 304;
+constexpr int OBS_MAX_W = 8;      // weight vectors per call
+constexpr int OBS_MAX_RADII = 8;  // radii per SH call
+constexpr int OBS_ROWS = 32;      // r rows per SH tile
+
+__device__ __forceinline__ double obs_warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block sum, valid in thread 0; every thread calls it
+__device__ __forceinline__ double obs_block_sum(double v, double* sh) {
+    v = obs_warp_sum(v);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < int(blockDim.x >> 5); ++i) r += sh[i];
+    return r;
+}
+
+template <typename R>
+__device__ __forceinline__ double abs2_at(const Cx<R>* g, const Cx<R>* glo, int64_t k) {
+    const Cx<R> x = ld(g + k);
+    double re = double(x.re), im = double(x.im);
+    if (glo) {
+        const Cx<R> e = ld(glo + k);
+        re += double(e.re);
+        im += double(e.im);
+    }
+    return re * re + im * im;
+}
+
+template <typename R>
+__device__ __forceinline__ Cx<double> value_at(const Cx<R>* g, const Cx<R>* glo, int64_t k) {
+    const Cx<R> x = ld(g + k);
+    Cx<double> v = {double(x.re), double(x.im)};
+    if (glo) {
+        const Cx<R> e = ld(glo + k);
+        v.re += double(e.re);
+        v.im += double(e.im);
+    }
+    return v;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(OBS_THREADS) weighted_stage1(int64_t n, const Cx<R>* g, const Cx<R>* glo, int nw,
+                                                               const double* w, double* part) {
+    __shared__ double sh[32];
+    double acc[OBS_MAX_W];
+#pragma unroll
+    for (int k = 0; k < OBS_MAX_W; ++k) acc[k] = 0.0;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double p = abs2_at(g, glo, i);
+#pragma unroll
+        for (int k = 0; k < OBS_MAX_W; ++k)
+            if (k < nw) acc[k] += w[int64_t(k) * n + i] * p;
+    }
+    for (int k = 0; k < nw; ++k) {
+        const double t = obs_block_sum(acc[k], sh);
+        if (threadIdx.x == 0) part[int64_t(blockIdx.x) * nw + k] = t;
+    }
+}
+
+// sum of the per-CTA (or per-tile) partials in CTA order, Neumaier-compensated
+__global__ void obs_stage2(int nparts, int nq, const double* part, double weight, double* out) {
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        double sum = 0.0, comp = 0.0;
+        for (int b = 0; b < nparts; ++b) {
+            const double v = part[int64_t(b) * nq + q];
+            const double t = sum + v;
+            comp += (fabs(sum) >= fabs(v)) ? (sum - t) + v : (v - t) + sum;
+            sum = t;
+        }
+        out[q] = (sum + comp) * weight;
+    }
+}
+
+// one CTA per tile of OBS_ROWS rows x all l; warp w takes l = w, w + 8, ...
+// and lane jj the row j0 + jj, so a warp's loads are one contiguous segment
+template <typename R>
+__global__ void __launch_bounds__(OBS_THREADS) sh_obs_stage1(const Cx<R>* g, const Cx<R>* glo, int nr, int nl,
+                                                             const double* r, const double* cl, int nrad,
+                                                             const double* radii, double* part) {
+    __shared__ double sh[32];
+    const int nq = 2 + nl + nrad;
+    const int tile = blockIdx.x;
+    const int jj = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int j = tile * OBS_ROWS + jj;
+    const bool row_ok = j < nr;
+    const double rj = row_ok ? r[j] : 0.0;
+    double acc_r = 0.0, acc_z = 0.0, acc_in[OBS_MAX_RADII];
+#pragma unroll
+    for (int k = 0; k < OBS_MAX_RADII; ++k) acc_in[k] = 0.0;
+    for (int l = warp; l < nl; l += nwarp) {
+        double p = 0.0;
+        if (row_ok) {
+            const Cx<double> x = value_at(g, glo, int64_t(l) * nr + j);
+            p = x.re * x.re + x.im * x.im;
+            acc_r += p * rj;
+#pragma unroll
+            for (int k = 0; k < OBS_MAX_RADII; ++k)
+                if (k < nrad && rj <= radii[k]) acc_in[k] += p;
+            if (l + 1 < nl) {
+                const Cx<double> y = value_at(g, glo, int64_t(l + 1) * nr + j);
+                acc_z += 2.0 * (x.re * y.re + x.im * y.im) * (cl[l] * rj);
+            }
+        }
+        const double pl = obs_warp_sum(p);  // this tile's rows of line l
+        if (jj == 0) part[int64_t(tile) * nq + 2 + l] = pl;
+    }
+    const double tr = obs_block_sum(acc_r, sh);
+    const double tz = obs_block_sum(acc_z, sh);
+    if (threadIdx.x == 0) {
+        part[int64_t(tile) * nq] = tr;
+        part[int64_t(tile) * nq + 1] = tz;
+    }
+    for (int k = 0; k < nrad; ++k) {
+        const double t = obs_block_sum(acc_in[k], sh);
+        if (threadIdx.x == 0) part[int64_t(tile) * nq + 2 + nl + k] = t;
+    }
+}
+
+static int weighted_blocks(int64_t n) {
+    const int64_t b = (n + OBS_THREADS - 1) / OBS_THREADS;
+    return int(b < OBS_BLOCKS ? b : OBS_BLOCKS);
+}
+
+template <typename R>
+static int weighted_impl(int64_t n, const void* g, const void* g_lo, int32_t nw, const double* w, double weight,
+                         double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+    if (n < 1 || !g || nw < 1 || nw > OBS_MAX_W || !w || !out || !scratch) {
+        set_error("ion_weighted_norms: invalid argument (n >= 1, 1 <= n_w <= %d, pointers set)", OBS_MAX_W);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    const int blocks = weighted_blocks(n);
+    if (scratch_bytes < int64_t(blocks) * nw * int64_t(sizeof(double))) {
+        set_error("ion_weighted_norms: scratch too small");
+        return ION_ERR_SCRATCH_TOO_SMALL;
+    }
+    cudaStream_t s = as_stream(stream);
+    double* part = static_cast<double*>(scratch);
+    weighted_stage1<R><<<blocks, OBS_THREADS, 0, s>>>(n, static_cast<const Cx<R>*>(g),
+                                                      static_cast<const Cx<R>*>(g_lo), nw, w, part);
+    if (int e = check_launch("weighted_stage1")) return e;
+    obs_stage2<<<1, 32, 0, s>>>(blocks, nw, part, weight, out);
+    return check_launch("obs_stage2");
+}
+
+template <typename R>
+static int sh_obs_impl(const void* g, const void* g_lo, int32_t nr, int32_t nl, const double* r, const double* cl,
+                       int32_t nrad, const double* radii, double weight, double* out, void* scratch,
+                       int64_t scratch_bytes, void* stream) {
+    if (!g || nr < 1 || nl < 1 || !r || !cl || nrad < 0 || nrad > OBS_MAX_RADII || (nrad > 0 && !radii) || !out ||
+        !scratch) {
+        set_error("ion_sh_observables: invalid argument (n_r, n_l >= 1, 0 <= n_radii <= %d, pointers set)",
+                  OBS_MAX_RADII);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    const int tiles = (nr + OBS_ROWS - 1) / OBS_ROWS;
+    const int nq = 2 + nl + nrad;
+    if (scratch_bytes < int64_t(tiles) * nq * int64_t(sizeof(double))) {
+        set_error("ion_sh_observables: scratch too small");
+        return ION_ERR_SCRATCH_TOO_SMALL;
+    }
+    cudaStream_t s = as_stream(stream);
+    double* part = static_cast<double*>(scratch);
+    sh_obs_stage1<R><<<tiles, OBS_THREADS, 0, s>>>(static_cast<const Cx<R>*>(g), static_cast<const Cx<R>*>(g_lo),
+                                                   nr, nl, r, cl, nrad, radii, part);
+    if (int e = check_launch("sh_obs_stage1")) return e;
+    obs_stage2<<<1, 128, 0, s>>>(tiles, nq, part, weight, out);
+    return check_launch("obs_stage2");
+}
+
+}  // namespace ion
+
+using namespace ion;
+
+extern "C" {
+int64_t ion_weighted_norms_scratch_bytes(int64_t n, int32_t n_w) {
+    return n < 1 || n_w < 1 ? 0 : int64_t(weighted_blocks(n)) * n_w * int64_t(sizeof(double));
+}
+int ion_weighted_norms_c128(int64_t n, const void* g, int32_t n_w, const double* w, double weight, double* out,
+                            void* scratch, int64_t scratch_bytes, void* stream) {
+    return weighted_impl<double>(n, g, nullptr, n_w, w, weight, out, scratch, scratch_bytes, stream);
+}
+int ion_weighted_norms_c64(int64_t n, const void* g, const void* g_lo, int32_t n_w, const double* w, double weight,
+                           double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+    return weighted_impl<float>(n, g, g_lo, n_w, w, weight, out, scratch, scratch_bytes, stream);
+}
+int64_t ion_sh_observables_scratch_bytes(int32_t n_r, int32_t n_l, int32_t n_radii) {
+    if (n_r < 1 || n_l < 1 || n_radii < 0) return 0;
+    return int64_t((n_r + OBS_ROWS - 1) / OBS_ROWS) * (2 + n_l + n_radii) * int64_t(sizeof(double));
+}
+int ion_sh_observables_c128(const void* g, int32_t n_r, int32_t n_l, const double* r, const double* cl,
+                            int32_t n_radii, const double* radii, double weight, double* out, void* scratch,
+                            int64_t scratch_bytes, void* stream) {
+    return sh_obs_impl<double>(g, nullptr, n_r, n_l, r, cl, n_radii, radii, weight, out, scratch, scratch_bytes,
+                               stream);
+}
+int ion_sh_observables_c64(const void* g, const void* g_lo, int32_t n_r, int32_t n_l, const double* r,
+                           const double* cl, int32_t n_radii, const double* radii, double weight, double* out,
+                           void* scratch, int64_t scratch_bytes, void* stream) {
+    return sh_obs_impl<float>(g, g_lo, n_r, n_l, r, cl, n_radii, radii, weight, out, scratch, scratch_bytes, stream);
+}
+}

@@ -178,13 +178,16 @@ __device__ __forceinline__ void prefetch_rot_item(const ion_sh_plan& plan, int i
 // tables are padded with zeros to a multiple of 16 entries, so a chunk of
 // M = 8 or 16 rows is read with 16-byte vector loads.
 // ---------------------------------------------------------------------------
+// RES: the explicit half is formed in the residual form below (with a stored
+// residual ``lo``, which may still be NULL); otherwise plainly.
+template <bool RES>
 struct ShCnCoef32 {
     const float* kinv;
     const float* cent;
     const float* hoff;
-    const float* ksum;  // kinv + hoff[i-1] + hoff[i], summed in FP64 (may be NULL)
     float ll1, corr0, tau;
     int n;
+    const Cx<float>* lo;  // the line's stored residual (c64x), or NULL
     __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const {
         if (i < 0 || i >= n) {
             bo = 0.f;
@@ -198,8 +201,8 @@ struct ShCnCoef32 {
     }
 };
 
-template <int M>
-__device__ __forceinline__ void load_chunk(const ShCnCoef32& c, int s, float (&bo)[M], float (&bd)[M]) {
+template <int M, bool RES>
+__device__ __forceinline__ void load_chunk(const ShCnCoef32<RES>& c, int s, float (&bo)[M], float (&bd)[M]) {
     static_assert(M % 4 == 0, "whole float4 groups");
 #pragma unroll
     for (int q = 0; q < M / 4; ++q) {
@@ -219,37 +222,61 @@ __device__ __forceinline__ void load_chunk(const ShCnCoef32& c, int s, float (&b
     }
 }
 
-// The explicit half-step of the complex64 radial solve.  Its kinetic terms
-// are ~1/dr^2 times psi and cancel to ~E psi, so forming a0 psi_{i-1} +
-// bd psi_i + bo psi_{i+1} in FP32 leaves a random error of ~1e-8 |psi| per
-// step, which sums to the dominant complex64 error over 10^4 steps.  Written
-// with neighbour differences and the row sum of B (tabulated in FP64 and
-// rounded once),
-//   (B psi)_i = a0 (psi_{i-1} - psi_i) + bo (psi_{i+1} - psi_i) + rowsum_i psi_i,
-// each product is of a small quantity and the cancellation is gone.
-__device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32& c, int i, float a0, float bd, float bo,
-                                                  Cx<float> p0, Cx<float> p1, Cx<float> p2) {
-    if (c.ksum == nullptr || i >= c.n)
-        return Cx<float>{a0 * p0.re + bd * p1.re + bo * p2.re, a0 * p0.im + bd * p1.im + bo * p2.im};
-    float h = c.ksum[i] + c.ll1 * c.cent[i];
-    if (i == 0) h = h + c.corr0;
-    const float rs = c.tau * h;
-    const Cx<float> dm = p0 - p1, dp = p2 - p1;
-    return Cx<float>{a0 * dm.re + bo * dp.re + rs * p1.re, a0 * dm.im + bo * dp.im + rs * p1.im};
+// The explicit half-step of the complex64 radial solve, with a stored residual.
+// Its kinetic terms are ~1/dr^2 times psi and cancel to ~E psi, so forming
+// a0 psi_{i-1} + bd psi_i + bo psi_{i+1} in FP32 leaves a random error of
+// ~1e-8 |psi| per step, which once the state's own rounding is gone is the
+// dominant error over 10^4 steps.  The same FP32 coefficients are used as
+//   a0 (psi_{i-1} - psi_i) + bo (psi_{i+1} - psi_i) + (a0 + bd + bo) psi_i,
+// with the row sum a0 + bd + bo formed exactly as a two-float (TwoSum), so
+// the explicit operator equals the implicit one exactly (the step stays
+// unitary) and no product is of a large, cancelling quantity.
+__device__ __forceinline__ float two_sum_err(float a, float b, float& e) {
+    const float s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+    return s;
 }
 
-template <typename R> struct ShCnCoefFor;
-template <> struct ShCnCoefFor<double> {
+// The residual itself enters B psi as well: most of a step's sub-ulp
+// increment is what lands in the residual, so leaving B lo out of the right
+// side would bias every step the same way (a steady norm drift).  B lo is
+// tiny and formed plainly.
+template <bool RES>
+__device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i, float a0, float bd, float bo,
+                                                  Cx<float> p0, Cx<float> p1, Cx<float> p2) {
+    if (!RES || c.lo == nullptr)
+        return Cx<float>{a0 * p0.re + bd * p1.re + bo * p2.re, a0 * p0.im + bd * p1.im + bo * p2.im};
+    float e1, e2;
+    const float s1 = two_sum_err(bd, a0, e1);
+    const float rs = two_sum_err(s1, bo, e2);
+    const float rl = e1 + e2;  // rs + rl = a0 + bd + bo to ~2^-48
+    const Cx<float> dm = p0 - p1, dp = p2 - p1;
+    Cx<float> v = {a0 * dm.re + bo * dp.re + (rs * p1.re + rl * p1.re),
+                   a0 * dm.im + bo * dp.im + (rs * p1.im + rl * p1.im)};
+    if (i < c.n) {  // padding rows carry no residual
+        const Cx<float> l1 = ld(c.lo + i);
+        const Cx<float> l0 = i > 0 ? ld(c.lo + i - 1) : Cx<float>{0.f, 0.f};
+        const Cx<float> l2 = i + 1 < c.n ? ld(c.lo + i + 1) : Cx<float>{0.f, 0.f};
+        v.re += a0 * l0.re + bd * l1.re + bo * l2.re;
+        v.im += a0 * l0.im + bd * l1.im + bo * l2.im;
+    }
+    return v;
+}
+
+template <typename R, bool RES> struct ShCnCoefFor;
+template <bool RES> struct ShCnCoefFor<double, RES> {
     using type = ShCnCoef<double>;
     __device__ static type make(const ion_sh_sim& S, int l, double tau) {
         return type{ShH<double>::make(S, l), tau, S.n_r};
     }
 };
-template <> struct ShCnCoefFor<float> {
-    using type = ShCnCoef32;
+template <bool RES> struct ShCnCoefFor<float, RES> {
+    using type = ShCnCoef32<RES>;
     __device__ static type make(const ion_sh_sim& S, int l, float tau) {
-        return type{S.kinv32, S.cent32, S.hoff32, S.ksum32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f,
-                    tau, S.n_r};
+        const Cx<float>* lo = S.g_lo ? static_cast<const Cx<float>*>(S.g_lo) + int64_t(l) * S.n_r : nullptr;
+        return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r,
+                    lo};
     }
 };
 
@@ -277,15 +304,36 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
     }
 }
 
-// ``dbuf`` 0: one line buffer (lines too long for two), staged at the top of
-// each iteration without overlap.
+// X_i = -i d_i with d read from an interleaved line buffer, or 0 (``on`` false)
 template <typename R, int M>
+struct MinusIExtra {
+    const Cx<R>* d;
+    int T;
+    bool on;
+    template <typename RR>
+    __device__ __forceinline__ Cx<RR> get(int i) const {
+        if (!on) return Cx<RR>{RR(0), RR(0)};
+        const Cx<R> v = d[islot<M>(i, T)];
+        return Cx<RR>{v.im, -v.re};
+    }
+};
+
+// ``dbuf`` 0: one line buffer (lines too long for two), staged at the top of
+// each iteration without overlap.  ``refine`` 1: a third line buffer holds the
+// increment, and the simulations with a stored residual refine their solve:
+// with Delta1 from A Delta1 = Y, the correction solves
+//   A delta = Y - A Delta1 = -i B (2 psi + Delta1) - Delta1,
+// i.e. the same solver on phi = psi + Delta1 / 2 with X = -i Delta1, so the
+// fixed rounding of the elimination of A acts only on the small residual.
+template <typename R, int M, bool REFINE>
 __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int item0, int item_end, int dbuf) {
+    constexpr int refine = REFINE ? 1 : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cap = blockDim.x * M;
     Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* buf1 = buf0 + cap;
-    Cx<R>* red = buf0 + (dbuf ? 2 : 1) * cap;
+    Cx<R>* ext = buf0 + (dbuf ? 2 : 1) * cap;
+    Cx<R>* red = ext + (refine ? cap : 0);
     int item = item0 + blockIdx.x;
     if (item >= item_end) return;
     if (dbuf) {
@@ -313,12 +361,33 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
             const int nr = S.n_r;
             const int T = (nr + M - 1) / M;
             const R tau = R(S.tau[t + 1]);
-            const auto coef = ShCnCoefFor<R>::make(S, l, tau);
-            // with a stored residual the solve leaves the increment in ``cur``
+            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau);
+            // with a stored residual the solve leaves the increment in ``inc``
             Cx<R>* glo = sizeof(R) == 4 && S.g_lo ? static_cast<Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
-            block_cn_solve<R, M>(T, threadIdx.x, R(2), cur, red, coef, NoExtra{},
-                                 AddOrSetOut<R, M>{cur, T, glo == nullptr});
-            __syncthreads();
+            Cx<R>* inc = cur;
+            if constexpr (REFINE) {
+                // two solves through one call site: delta1 into ext, then
+                // phi = psi + delta1 / 2 in cur and delta1 + delta into ext
+                const bool two = glo != nullptr;
+                if (two) inc = ext;
+                for (int pass = 0; pass < (two ? 2 : 1); ++pass) {
+                    block_cn_solve<R, M>(T, threadIdx.x, R(2), cur, red, coef, MinusIExtra<R, M>{ext, T, pass == 1},
+                                         AddOrSetOut<R, M>{inc, T, pass == 1 || !two});
+                    __syncthreads();
+                    if (two && pass == 0) {
+                        for (int i = threadIdx.x; i < T * M; i += blockDim.x) {
+                            const int sl = islot<M>(i, T);
+                            cur[sl] = cur[sl] + scale(ext[sl], R(0.5));
+                        }
+                        __syncthreads();
+                    }
+                }
+            } else {
+                // plain: psi + delta into cur; with a residual: delta into cur
+                block_cn_solve<R, M>(T, threadIdx.x, R(2), cur, red, coef, NoExtra{},
+                                     AddOrSetOut<R, M>{cur, T, glo == nullptr});
+                __syncthreads();
+            }
             Cx<R>* g = static_cast<Cx<R>*>(S.g) + int64_t(l) * nr;
             if (glo) {
 #pragma unroll
@@ -326,7 +395,7 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                     const int i = threadIdx.x + k * blockDim.x;
                     if (i < nr) {
                         Cx<R> lo = ld(glo + i);
-                        const Cx<R> h = add_exact(ld(g + i), cur[islot<M>(i, T)], lo);
+                        const Cx<R> h = add_exact(ld(g + i), inc[islot<M>(i, T)], lo);
                         st(g + i, h);
                         st(glo + i, lo);
                     }
@@ -710,7 +779,10 @@ template <typename R, int MAXM>
 static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
         attr = true;
     }
     const int nb = p->n_cn_buckets;
@@ -719,20 +791,22 @@ static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
         const int end = nb > 0 ? p->cn_bucket_end[b] : p->n_cn_items;
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
         if (end > begin) {
+            const int refine = (p->flags & ION_SH_REFINE) && sizeof(R) == 4 ? 1 : 0;
             int dbuf = 1;
-            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2);
+            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2 + refine);
             if (smem > 200 * 1024) {
                 dbuf = 0;
-                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1);
+                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1 + refine);
             }
             if (smem > 200 * 1024) {
                 set_error("ion_sh: radial line too long for shared memory");
                 return ION_ERR_UNSUPPORTED;
             }
+            auto kern = refine ? sh_cn_pipelined<R, MAXM, true> : sh_cn_pipelined<R, MAXM, false>;
             int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_cn_pipelined<R, MAXM>, threads, smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
             const int grid = std::min(end - begin, std::max(per_sm, 1) * num_sms());
-            sh_cn_pipelined<R, MAXM><<<grid, threads, smem, s>>>(*p, begin, end, dbuf);
+            kern<<<grid, threads, smem, s>>>(*p, begin, end, dbuf);
             if (int e = check_launch("sh_cn_pipelined")) return e;
         }
         begin = end;

@@ -1,9 +1,12 @@
-"""Datastores (ionization/mesh/data.py:14-275): Fields, Norm, InnerProducts.
+"""Datastores (ionization/mesh/data.py:14-464): Fields, Norm, InnerProducts,
+ZExpectationValue, RExpectationValue, NormWithinRadius, NormBySphericalHarmonic.
 
 Norm and InnerProducts are filled from the FP64 device reductions made at the
 data times of the run (fused into the step kernels, or a reduction kernel at
 the data time); ``Fields`` is evaluated on the host from the pulse.  The
-attribute names on ``sim.data`` are the reference's.
+position expectation values and partial norms are device reductions of the
+current wavefunction launched at each data time (``store``).  The attribute
+names on ``sim.data`` are the reference's.
 """
 
 import numpy as np
@@ -31,6 +34,9 @@ DATA_NAME_TO_DATASTORE_TYPE = {}
 
 
 class Datastore:
+    # True: ``store`` runs at every data time (the run loop stops there)
+    stores_at_data_times = False
+
     def init(self, sim):
         self.sim = sim
         self.spec = sim.spec
@@ -155,5 +161,96 @@ DATA_NAME_TO_DATASTORE_TYPE.update(
         "total_state_overlap": InnerProducts,
     }
 )
+
+class ZExpectationValue(Datastore):
+    """<z> at the data times (data.py:344-375): on the device, the F-order
+    dipole operator on a spherical-harmonic mesh, z |g|^2 on line and
+    cylindrical meshes."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        self.z_expectation_value = sim.get_blank_data()
+        super().init(sim)
+
+    def store(self):
+        self.z_expectation_value[self.sim.data_time_index] = self.sim.mesh.z_expectation_value()
+
+    def attach(self):
+        self.sim.data.z_expectation_value = self.z_expectation_value
+
+    def z_dipole_moment_expectation_value(self):
+        return self.spec.test_charge * self.z_expectation_value
+
+
+Data.z_dipole_moment_expectation_value = link_property_to_data(
+    ZExpectationValue, ZExpectationValue.z_dipole_moment_expectation_value)
+DATA_NAME_TO_DATASTORE_TYPE.update({"z_expectation_value": ZExpectationValue,
+                                    "z_dipole_moment_expectation_value": ZExpectationValue})
+
+
+class RExpectationValue(Datastore):
+    """<r> at the data times (data.py:378-395)."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        self.r_expectation_value = sim.get_blank_data()
+        super().init(sim)
+
+    def store(self):
+        self.r_expectation_value[self.sim.data_time_index] = self.sim.mesh.r_expectation_value()
+
+    def attach(self):
+        self.sim.data.r_expectation_value = self.r_expectation_value
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"r_expectation_value": RExpectationValue})
+
+
+class NormWithinRadius(Datastore):
+    """The norm of the part of the mesh with r <= R for each R (data.py:398-429;
+    on a line r is the signed z coordinate, as the reference's r_mesh)."""
+
+    stores_at_data_times = True
+
+    def __init__(self, radii=()):
+        self.radii = tuple(sorted(radii))
+
+    def init(self, sim):
+        self.norm_within_radius = {r: sim.get_blank_data() for r in self.radii}
+        super().init(sim)
+
+    def store(self):
+        vals = self.sim.mesh.norm_within_radius(self.radii)
+        for r, v in zip(self.radii, vals):
+            self.norm_within_radius[r][self.sim.data_time_index] = v
+
+    def attach(self):
+        self.sim.data.norm_within_radius = self.norm_within_radius
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"norm_within_radius": NormWithinRadius})
+
+
+class NormBySphericalHarmonic(Datastore):
+    """The norm in each spherical harmonic (data.py:432-454), keyed like the
+    specification's ``spherical_harmonics``."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        self.norm_by_l = {sph: sim.get_blank_data() for sph in sim.spec.spherical_harmonics}
+        super().init(sim)
+
+    def store(self):
+        for sph, v in zip(self.spec.spherical_harmonics, self.sim.mesh.norm_by_l()):
+            self.norm_by_l[sph][self.sim.data_time_index] = v
+
+    def attach(self):
+        self.sim.data.norm_by_sph_harm = self.norm_by_l
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"norm_by_l": NormBySphericalHarmonic})
 
 DEFAULT_DATASTORE_TYPES = (Fields, Norm, InnerProducts)

@@ -110,6 +110,46 @@ class QuantumMesh:
     def norm(self, state=None):
         return self.inner_product(state, state).real
 
+    # ---- position expectation values and partial norms (device reductions) ----
+    def _weighted_norms(self, weights):
+        """weight * sum w |g|^2 for each weight array (mesh shape), on the device."""
+        import torch
+
+        out = []
+        g = self._psi_device()
+        lo = self._psi_residual()
+        n = int(np.prod(self.mesh_shape))
+        for k0 in range(0, len(weights), 8):
+            chunk = weights[k0:k0 + 8]
+            w = np.stack([np.broadcast_to(np.asarray(x, dtype=np.float64), self.mesh_shape).reshape(-1)
+                          for x in chunk])
+            d_w = dev.to_dev(w)
+            nbytes = nat.value("ion_weighted_norms_scratch_bytes", n, len(chunk))
+            scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=g.device)
+            res = torch.empty(len(chunk), dtype=torch.float64, device=g.device)
+            if g.dtype == torch.complex128:
+                nat.call("ion_weighted_norms_c128", n, dev.ptr(g), len(chunk), dev.ptr(d_w),
+                         float(self.inner_product_multiplier), dev.ptr(res), dev.ptr(scratch), int(nbytes),
+                         dev.stream_ptr())
+            else:
+                nat.call("ion_weighted_norms_c64", n, dev.ptr(g), dev.ptr(lo), len(chunk), dev.ptr(d_w),
+                         float(self.inner_product_multiplier), dev.ptr(res), dev.ptr(scratch), int(nbytes),
+                         dev.stream_ptr())
+            out.extend(res.cpu().numpy().tolist())
+        return out
+
+    def z_expectation_value(self):
+        """<z> of the current wavefunction (meshes.py:231-233)."""
+        return self._weighted_norms([self.z_mesh])[0]
+
+    def r_expectation_value(self):
+        """<r> of the current wavefunction (meshes.py:235-237)."""
+        return self._weighted_norms([self.r_mesh])[0]
+
+    def norm_within_radius(self, radii):
+        """The norm of the mesh points with r <= R, for each R (data.py:420-425)."""
+        return self._weighted_norms([(self.r_mesh <= R).astype(np.float64) for R in radii])
+
     # ---- stepping ----
     def _method_supported(self):
         raise NotImplementedError
@@ -358,6 +398,49 @@ class SphericalHarmonicMesh(QuantumMesh):
 
     def _psi_residual(self):
         return self._dsim.g_lo
+
+    def _sh_observables(self, radii=()):
+        """(<r>, <z>, norm by l, norm within radii) in one device pass."""
+        import torch
+
+        radii = tuple(radii)
+        if len(radii) > 8:
+            head = self._sh_observables(radii[:8])
+            return head[0], head[1], head[2], list(head[3]) + list(self._sh_observables(radii[8:])[3])
+        if not hasattr(self, "_d_obs_tables"):
+            cl = np.asarray(self.operators.c_l(np.arange(self.spec.l_bound)), dtype=np.float64)
+            self._d_obs_tables = (dev.to_dev(np.asarray(self.r, dtype=np.float64)), dev.to_dev(cl))
+        d_r, d_cl = self._d_obs_tables
+        g = self._psi_device()
+        lo = self._psi_residual()
+        nr, nl = self.spec.r_points, self.spec.l_bound
+        d_radii = dev.to_dev(np.asarray(radii if radii else [0.0], dtype=np.float64))
+        nbytes = nat.value("ion_sh_observables_scratch_bytes", nr, nl, len(radii))
+        scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=g.device)
+        res = torch.empty(2 + nl + len(radii), dtype=torch.float64, device=g.device)
+        w = float(self.inner_product_multiplier)
+        if g.dtype == torch.complex128:
+            nat.call("ion_sh_observables_c128", dev.ptr(g), nr, nl, dev.ptr(d_r), dev.ptr(d_cl), len(radii),
+                     dev.ptr(d_radii), w, dev.ptr(res), dev.ptr(scratch), int(nbytes), dev.stream_ptr())
+        else:
+            nat.call("ion_sh_observables_c64", dev.ptr(g), dev.ptr(lo), nr, nl, dev.ptr(d_r), dev.ptr(d_cl),
+                     len(radii), dev.ptr(d_radii), w, dev.ptr(res), dev.ptr(scratch), int(nbytes), dev.stream_ptr())
+        v = res.cpu().numpy()
+        return float(v[0]), float(v[1]), v[2:2 + nl].copy(), v[2 + nl:].tolist()
+
+    def z_expectation_value(self):
+        """<z>: the F-order dipole operator (mesh_operators.py:1086-1104)."""
+        return self._sh_observables()[1]
+
+    def r_expectation_value(self):
+        return self._sh_observables()[0]
+
+    def norm_by_l(self):
+        """SphericalHarmonicMesh.norm_by_l (meshes.py:1133-1136)."""
+        return self._sh_observables()[2]
+
+    def norm_within_radius(self, radii):
+        return self._sh_observables(radii)[3]
 
     def _tau_dev(self):
         return self._dsim.d_tau

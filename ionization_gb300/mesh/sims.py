@@ -102,11 +102,22 @@ class MeshSimulation:
                 msg = f"Wavefunction norm ({n[k]}) grew by more than 0.1% at data index {k} for {self}"
                 self.warnings.setdefault("norm_growth", []).append(core.WarningRecord(k, msg))
 
+    @property
+    def _stores_at_data_times(self):
+        return [ds for ds in self.datastores_by_type.values() if ds.stores_at_data_times]
+
+    def _store_data_time(self):
+        """Datastores that read the wavefunction at a data time."""
+        if self.data_mask[self.time_index]:
+            self.data_time_index = int(np.sum(self.data_indices < self.time_index))
+            for ds in self._stores_at_data_times:
+                ds.store()
+
     def _next_stop(self, callback_given):
         last = self.time_steps - 1
         if callback_given:
             return self.time_index + 1
-        if not self.mesh.fused_data:
+        if not self.mesh.fused_data or self._stores_at_data_times:
             later = self.data_indices[self.data_indices > self.time_index]
             return int(later[0]) if len(later) else last
         return last
@@ -119,6 +130,7 @@ class MeshSimulation:
         last = self.time_steps - 1
         if not self._initial_data_done:
             self.mesh._reduce_current()  # data of time index 0
+            self._store_data_time()
             self._initial_data_done = True
         if callback is not None:
             callback(self)
@@ -131,6 +143,7 @@ class MeshSimulation:
             self.time_index = nxt
             if not self.mesh.fused_data and self.data_mask[self.time_index]:
                 self.mesh._reduce_current()
+            self._store_data_time()
             if callback is not None:
                 self._pull_data()
                 callback(self)
@@ -349,6 +362,7 @@ class SphericalHarmonicSpecification(MeshSpecification):
         self.r_bound = r_bound
         self.r_points = int(r_points)
         self.l_bound = int(l_bound)
+        self.spherical_harmonics = tuple(core.SphericalHarmonic(l, 0) for l in range(self.l_bound))
         self.theta_points = theta_points
         self.use_numeric_eigenstates = False
         self.numeric_eigenstate_max_angular_momentum = min(self.l_bound - 1, numeric_eigenstate_max_angular_momentum)

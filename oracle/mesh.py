@@ -80,13 +80,14 @@ def apply_implicit(op, g, shape):
     return _wrap(tdma(op.sub, op.diag, op.sup, _flat(g, op.order)), shape, op.order)
 
 
-def run(stepper, times, store_data_every, max_steps=None):
+def run(stepper, times, store_data_every, max_steps=None, observe=None):
     """The data/evolve skeleton of MeshSimulation.run, sims.py:289-333.
 
     ``stepper`` exposes ``evolve(dt, t_now)``, ``norm()`` and
-    ``inner_products()``.  Returns data-time norms and inner products."""
+    ``inner_products()``.  Returns data-time norms and inner products, and
+    ``observe(stepper)`` at each data time under "observed" when given."""
     mask = data_mask(len(times), store_data_every)
-    norms, ips, dtimes = [], [], []
+    norms, ips, dtimes, obs = [], [], [], []
     time_index = 0
     steps = 0
     while True:
@@ -94,6 +95,8 @@ def run(stepper, times, store_data_every, max_steps=None):
             norms.append(stepper.norm())
             ips.append(stepper.inner_products())
             dtimes.append(times[time_index])
+            if observe is not None:
+                obs.append(observe(stepper))
         if time_index == len(times) - 1:
             break
         if max_steps is not None and steps >= max_steps:
@@ -106,7 +109,41 @@ def run(stepper, times, store_data_every, max_steps=None):
         norm=np.array(norms),
         inner_products=np.array(ips).T if ips else np.zeros((0, 0)),
         steps=steps,
+        observed=obs,
     )
+
+
+# --------------------------------------------------------------------------
+# position expectation values and partial norms
+# --------------------------------------------------------------------------
+
+def observables(stepper, kind, radii):
+    """<z>, <r>, the norm within each radius and (SH) the norm of each l of the
+    stepper's current g:
+      QuantumMesh.expectation_value with the mesh's z / r operator
+        (meshes.py:206-237): element-wise z_mesh, r_mesh on line and cylinder
+        meshes (mesh_operators.py:344-349, 634-639); on the SH mesh z is the
+        F-order off-diagonal c_l r operator (mesh_operators.py:1086-1104);
+      NormWithinRadius.store: norm of where(r_mesh <= R, g, 0) (data.py:420-425);
+      SphericalHarmonicMesh.norm_by_l (meshes.py:1133-1136)."""
+    g = stepper.g
+    p = (np.conj(g) * g).real
+    if kind == "line":
+        w, zw, rw = stepper.dz, stepper.z, stepper.z  # a line's r_mesh is z
+        within = [np.sum(np.where(stepper.z <= R, p, 0.0)) * w for R in radii]
+        return dict(z=np.sum(zw * p) * w, r=np.sum(rw * p) * w, within=within)
+    if kind == "cyl":
+        w = stepper.dz * stepper.drho
+        within = [np.sum(np.where(stepper.r_mesh <= R, p, 0.0)) * w for R in radii]
+        return dict(z=np.sum(stepper.z_mesh * p) * w, r=np.sum(stepper.r_mesh * p) * w, within=within)
+    if kind == "sh":
+        w = stepper.dr
+        r = stepper.r[None, :]
+        cl = np.array([_c_l(l) for l in range(stepper.L - 1)])[:, None]
+        z = np.sum(2 * (np.conj(g[:-1]) * g[1:]).real * cl * r) * w
+        within = [np.sum(np.where(stepper.r_mesh <= R, p, 0.0)) * w for R in radii]
+        return dict(z=z, r=np.sum(p * r) * w, within=within, by_l=np.sum(p, axis=1) * w)
+    raise ValueError(kind)
 
 
 # --------------------------------------------------------------------------
@@ -427,11 +464,12 @@ def build_from_params(kind, params):
     raise ValueError(kind)
 
 
-def run_from_params(kind, params, max_steps=None):
+def run_from_params(kind, params, max_steps=None, radii=None):
     stepper = build_from_params(kind, params)
     times = get_times(params["time_initial"], params["time_final"], params["time_step"])
     g0 = stepper.g.copy()
-    out = run(stepper, times, params["store_data_every"], max_steps=max_steps)
+    observe = None if radii is None else (lambda st: observables(st, kind, radii))
+    out = run(stepper, times, params["store_data_every"], max_steps=max_steps, observe=observe)
     out["times"] = times
     out["g_initial"] = g0
     out["g_final"] = stepper.g

@@ -19,6 +19,9 @@ Cases (reference call sites in parentheses):
                    (optional --full-sh, ~10 min single core)
   cyl_cfg3_full    the full cylindrical workload: 2000 x 1000, 5000 steps
                    (optional --full-cyl, ~1 h single core; psi stored subsampled)
+  *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
+                   RExpectationValue, NormWithinRadius and (SH)
+                   NormBySphericalHarmonic datastores
 
 Each npz holds the spec parameters (``params`` JSON string), the time grid,
 the initial and final ``g``, and the Norm / InnerProducts datastore arrays.
@@ -328,10 +331,65 @@ def gen_cyl(ion, full=False):
         save("cyl_cfg3_full", params, out)
 
 
+OBS_RADII = {"line": (-5.0, 0.0, 12.5), "sh": (2.0, 5.0, 12.0), "cyl": (3.0, 7.5)}
+
+
+def _observable_datastores(ion, kind):
+    d = ion.mesh.data if hasattr(ion.mesh, "data") else __import__("ionization.mesh.data").mesh.data
+    stores = [d.Fields(), d.Norm(), d.InnerProducts(), d.NormWithinRadius(radii=OBS_RADII[kind])]
+    if kind != "line":  # LineLengthGaugeOperators.z/r return tuples: the reference's line <z> raises
+        stores += [d.ZExpectationValue(), d.RExpectationValue()]
+    # NormBySphericalHarmonic.init reads self.spec before Datastore.init sets
+    # it, so the reference cannot run that datastore; its per-l norm is taken
+    # from SphericalHarmonicMesh.norm_by_l (meshes.py:1133-1136) after the run
+    return stores
+
+
+def _observable_arrays(sim, kind):
+    out = dict(
+        radii=np.asarray(OBS_RADII[kind]),
+        norm_within_radius=np.array([sim.data.norm_within_radius[r] for r in OBS_RADII[kind]]),
+    )
+    if kind != "line":
+        out["z_expectation_value"] = np.asarray(sim.data.z_expectation_value)
+        out["r_expectation_value"] = np.asarray(sim.data.r_expectation_value)
+    if kind == "sh":
+        out["norm_by_l_final"] = np.asarray(sim.mesh.norm_by_l())
+    return out
+
+
+def gen_observables(ion):
+    """ZExpectationValue, RExpectationValue, NormWithinRadius and (SH)
+    NormBySphericalHarmonic datastores (ionization/mesh/data.py:344-464) on
+    small line, SH and cylindrical runs."""
+    fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+    spec, params = line_spec(ion, "line_observables_small", 512, 40.0, 300, 0.05, _pulse_kwargs(0.1, 0.5, 2, 0.3),
+                             "SplitInteractionOperator", dict(inner_radius=30.0, outer_radius=40.0, smoothness=8), 25)
+    spec.datastores = _observable_datastores(ion, "line")
+    spec.datastore_types = tuple(type(ds) for ds in spec.datastores)
+    sim, out = run_and_collect(spec)
+    out.update(_observable_arrays(sim, "line"))
+    save("line_observables_small", params, out)
+
+    spec, params = sh_spec(ion, "sh_observables_small", 160, 11, 500, 0.02, fast_pulse, 5.0, 50)
+    spec.datastores = _observable_datastores(ion, "sh")
+    spec.datastore_types = tuple(type(ds) for ds in spec.datastores)
+    sim, out = run_and_collect(spec)
+    out.update(_observable_arrays(sim, "sh"))
+    save("sh_observables_small", params, out)
+
+    spec, params = cyl_spec(ion, "cyl_observables_small", 120, 15.0, 60, 15.0, 200, 0.05, fast_pulse, 25)
+    spec.datastores = _observable_datastores(ion, "cyl")
+    spec.datastore_types = tuple(type(ds) for ds in spec.datastores)
+    sim, out = run_and_collect(spec)
+    out.update(_observable_arrays(sim, "cyl"))
+    save("cyl_observables_small", params, out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -340,7 +398,7 @@ def main():
     from loader import import_reference
 
     ion = import_reference(args.ref)
-    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl"}
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -349,6 +407,8 @@ def main():
         gen_sh(ion)
     if "cyl" in only:
         gen_cyl(ion)
+    if "obs" in only:
+        gen_observables(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:
