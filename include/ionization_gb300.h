@@ -276,6 +276,9 @@ typedef struct ion_line_sim {
                               forward transform leaves at position i (bit-reversed order) */
     const void *twiddle;   /* [n] exp(-2 pi i m / n), complex128 for _c128, complex64 for _c64 */
     const float *vstat32;
+    /* _c64 entry points with ION_LINE_RESIDUAL: the rounding residual of psi
+     * (complex64 [n], psi = g + g_lo), or NULL */
+    void *g_lo;
 } ion_line_sim;
 
 typedef struct ion_line_plan {
@@ -287,15 +290,25 @@ typedef struct ion_line_plan {
                         2..8: a thread-block cluster, the line split into equal
                         segments, n <= cluster * ion_line_max_n_*(); Crank-Nicolson
                         methods only (ION_LINE_FFT simulations are left untouched) */
+    int32_t flags;   /* ION_LINE_RESIDUAL (_c64 only): every simulation carries g_lo and
+                        is advanced in the residual form: 8 rows per thread,
+                        n <= cluster * ion_line_max_n_c64x(), Crank-Nicolson methods,
+                        the explicit half in exact-row-sum difference form, one step of
+                        iterative refinement of each solve */
+    int32_t pad2_;
 } ion_line_plan;
+
+enum { ION_LINE_RESIDUAL = 1 };
 
 int ion_line_run_c128(const ion_line_plan *plan, int64_t n_steps, void *stream);
 int ion_line_run_c64(const ion_line_plan *plan, int64_t n_steps, void *stream);
 int ion_line_reduce_c128(const ion_line_plan *plan, void *stream);
 int ion_line_reduce_c64(const ion_line_plan *plan, void *stream);
-/* Longest line one CTA holds (a cluster of C CTAs holds C times as much). */
+/* Longest line one CTA holds (a cluster of C CTAs holds C times as much);
+ * _c64x: in the residual form (ION_LINE_RESIDUAL). */
 int64_t ion_line_max_n_c128(void);
 int64_t ion_line_max_n_c64(void);
+int64_t ion_line_max_n_c64x(void);
 
 /* ------------------------------------------------------------------------
  * Cylindrical slice mesh, length gauge, ADI (CylindricalSliceLengthGaugeOperators,

@@ -321,8 +321,14 @@ class LineTables:
     twiddle: Optional[np.ndarray] = None  # ION_LINE_FFT: exp(-2 pi i m / n)
 
 
+def line_rows(precision) -> int:
+    """Rows per thread of the line kernels (8 for complex128 and the residual
+    form, 16 for complex64)."""
+    return 16 if Precision(precision) == Precision.C64 else 8
+
+
 def line_threads(n: int, precision) -> int:
-    maxm = 8 if Precision(precision) == Precision.C128 else 16
+    maxm = line_rows(precision)
     return (n + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
@@ -332,6 +338,12 @@ LINE_MAX_CLUSTER = 8
 def line_cta_max_n(precision) -> int:
     """Longest line one CTA of the line kernel holds."""
     return int(nat.value("ion_line_max_n_" + Precision(precision).value))
+
+
+def line_cluster_for(n: int, precision, cta_max: int) -> int:
+    """Cluster size of a line: the residual form always runs as a cluster (of 1
+    or more CTAs)."""
+    return max(1, -(-int(n) // int(cta_max)))
 
 
 def line_cluster(n: int, precision, cta_max: Optional[int] = None) -> int:
@@ -349,7 +361,12 @@ class LineDeviceSim:
         self.t_final = int(tab.t_final)
         self.store_every = int(tab.store_every)
         f64, f32 = np.float64, np.float32
-        self.g = to_dev(tab.g0.astype(np.complex128)).to(complex_dtype(precision))
+        g0 = np.asarray(tab.g0, dtype=np.complex128)
+        self.g = to_dev(g0).to(complex_dtype(precision))
+        self.g_lo = None
+        if self.precision == Precision.C64X:  # psi = g + g_lo
+            hi = g0.astype(np.complex64)
+            self.g_lo = to_dev((g0 - hi.astype(np.complex128)).astype(np.complex64))
         self.d_hd, self.d_hoff, self.d_zq = to_dev(tab.hd, f64), to_dev(tab.hoff, f64), to_dev(tab.zq, f64)
         self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
         self.d_tau, self.d_ef = to_dev(tab.tau, f64), to_dev(tab.efield, f64)
@@ -384,6 +401,7 @@ class LineDeviceSim:
         d.weight = float(self.tab.weight)
         d.out_norm, d.out_ip = ptr(self.d_norm), ptr(self.d_ip)
         d.vstat, d.kin, d.twiddle, d.vstat32 = ptr(self.d_vstat), ptr(self.d_kin), ptr(self.d_twiddle), ptr(self.d_vstat32)
+        d.g_lo = ptr(self.g_lo)
         return d
 
     def data(self):
@@ -392,7 +410,10 @@ class LineDeviceSim:
         return norm, ip.reshape(self.n_data, self.n_states).T.copy()
 
     def psi_host(self) -> np.ndarray:
-        return self.g.cpu().numpy().astype(np.complex128)
+        g = self.g.cpu().numpy().astype(np.complex128)
+        if self.g_lo is not None:
+            g = g + self.g_lo.cpu().numpy().astype(np.complex128)
+        return g
 
 
 class LineBatch:
@@ -430,7 +451,7 @@ class LineBatch:
             for s in self.sims:
                 groups.setdefault(self._cluster_of(s), []).append(s)
             plans, keep = [], []
-            maxm = 8 if self.precision == Precision.C128 else 16
+            maxm = line_rows(self.precision)
             for c in sorted(groups):
                 sims = groups[c]
                 descs = (nat.LineSim * len(sims))()
@@ -443,6 +464,7 @@ class LineBatch:
                 p.max_n = max(s.n for s in sims)
                 p.threads = _round32(max(-(-s.n // (c * maxm)) for s in sims))
                 p.cluster = c
+                p.flags = nat.ION_LINE_RESIDUAL if self.precision == Precision.C64X else 0
                 plans.append(p)
                 keep.append(d)
             self._plans = plans

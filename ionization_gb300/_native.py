@@ -24,6 +24,7 @@ ION_LINE_ADI = 0
 ION_LINE_SPLIT = 1
 ION_LINE_FFT = 2
 ION_SH_REFINE = 1
+ION_LINE_RESIDUAL = 1
 
 
 class NativeLibraryError(RuntimeError):
@@ -119,6 +120,7 @@ class LineSim(ctypes.Structure):
         ("kin", c_vp),
         ("twiddle", c_vp),
         ("vstat32", c_vp),
+        ("g_lo", c_vp),
     ]
 
 
@@ -129,6 +131,8 @@ class LinePlan(ctypes.Structure):
         ("max_n", c_i32),
         ("threads", c_i32),
         ("cluster", c_i32),
+        ("flags", c_i32),
+        ("pad2_", c_i32),
     ]
 
 
@@ -175,6 +179,7 @@ _SIGS = {
     "ion_line_reduce_c64": (ctypes.c_int, [ctypes.POINTER(LinePlan), c_vp]),
     "ion_line_max_n_c128": (c_i64, []),
     "ion_line_max_n_c64": (c_i64, []),
+    "ion_line_max_n_c64x": (c_i64, []),
     "ion_cyl_adi_run_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
     "ion_cyl_max_points_c128": (c_i64, []),
     "ion_reduce_scratch_bytes": (c_i64, [c_i64, c_i32]),

@@ -12,6 +12,8 @@
 // memory before psi is stored.
 #include <cooperative_groups.h>
 
+#include <type_traits>
+
 #include "ion_common.cuh"
 #include "ion_cn_solver.cuh"
 
@@ -62,7 +64,7 @@ struct LineCnCoef {
             bd = R(0);
             return;
         }
-        const R h = with_field ? tb.hd[i] + tb.zq[i] * efield : tb.hd[i];
+        const R h = with_field ? fma(tb.zq[i], efield, tb.hd[i]) : tb.hd[i];
         bd = tau * h;
         bo = (i < n - 1) ? tau * tb.hoff[i] : R(0);
     }
@@ -590,12 +592,350 @@ __global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, i
     if (rank == 0 && threadIdx.x == 0) S.t = t + 1;
 }
 
+// ---------------------------------------------------------------------------
+// Complex64 with a stored residual (ion_line_sim.g_lo, plan flag
+// ION_LINE_RESIDUAL): psi = g + g_lo, FP32 arithmetic.  One kernel for every
+// line length, launched as a cluster of C >= 1 CTAs with 8 rows per thread
+// (three line buffers: psi, its residual, the increment).  Per step:
+//   stage (g, g_lo) with the split operator's phase applied to the pair;
+//   solve A Delta1 = -i 2 B psi with the explicit half in the exact-row-sum
+//   difference form plus B g_lo, then refine: A delta = -i B (2 psi + Delta1)
+//   - Delta1 (the same solver on phi = psi + Delta1 / 2, X = -i Delta1);
+//   add Delta = Delta1 + delta to (g, g_lo) exactly, apply the phase and the
+//   mask to the pair, store, and reduce g + g_lo in FP64 at data times.
+// ---------------------------------------------------------------------------
+constexpr int LINE_RES_M = 8;
+
+__device__ __forceinline__ float two_sum_full(float a, float b, float& e) {
+    const float s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+    return s;
+}
+
+// h + d with the residual lo: h + d formed exactly (Knuth's TwoSum), its
+// rounding error added to lo, the pair renormalised (Fast2Sum); returns the
+// new h and updates lo
+__device__ __forceinline__ float add_exact1_f(float h, float d, float& lo) {
+    float e;
+    const float s = two_sum_full(h, d, e);
+    const float l = lo + e;
+    const float r = s + l;
+    lo = l - (r - s);
+    return r;
+}
+__device__ __forceinline__ Cx<float> add_exact_f(Cx<float> h, Cx<float> d, Cx<float>& lo) {
+    return Cx<float>{add_exact1_f(h.re, d.re, lo.re), add_exact1_f(h.im, d.im, lo.im)};
+}
+
+// (hi + lo) * exp(-i theta), the rounding of hi's update kept in lo
+__device__ __forceinline__ void phase_res(Cx<float>& hi, Cx<float>& lo, float theta) {
+    float cm1, s;
+    rot_coeffs(theta, cm1, s);
+    float er, ei;
+    const float hr = two_sum_full(hi.re, cm1 * hi.re + s * hi.im, er);
+    const float hi_i = two_sum_full(hi.im, cm1 * hi.im - s * hi.re, ei);
+    lo = Cx<float>{lo.re + (cm1 * lo.re + s * lo.im) + er, lo.im + (cm1 * lo.im - s * lo.re) + ei};
+    hi = Cx<float>{hr, hi_i};
+}
+
+// (hi + lo) * m, the product's rounding kept in lo
+__device__ __forceinline__ void scale_res(Cx<float>& hi, Cx<float>& lo, float m) {
+    const float pr = hi.re * m, pi = hi.im * m;
+    lo = Cx<float>{fmaf(lo.re, m, fmaf(hi.re, m, -pr)), fmaf(lo.im, m, fmaf(hi.im, m, -pi))};
+    hi = Cx<float>{pr, pi};
+}
+
+// the line coefficients plus the staged residual (local rows; the rows just
+// outside this CTA's segment come from the neighbouring CTAs' buffers)
+template <int M>
+struct LineResCoef {
+    OffsetCoef<float> c;
+    const Cx<float>* lob;
+    const Cx<float>* prev;  // previous CTA's residual buffer (DSMEM) or nullptr
+    const Cx<float>* next;
+    const double* hd64;  // the FP64 diagonal of H0 that hd32 rounds
+    int T, L;
+    __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const { c(i, bo, bd); }
+    // bd_exact - bd for the diagonal bd = tau * fma(zq, E, hd32) of local row
+    // i: the rounding of hd32 from the FP64 diagonal (hd = -2p + V loses the
+    // low bits of V beside the kinetic term, a random potential of ~1e-8 of
+    // the kinetic diagonal) plus the rounding of the field term and of the
+    // product with tau, formed with error-free transforms.  The explicit half
+    // uses the exact diagonal; the refinement then solves with it.
+    __device__ __forceinline__ float bd_lo(int i) const {
+        const int gi = c.off + i;
+        const LineCnCoef<float>& k = c.c;
+        if (gi >= k.n) return 0.f;
+        const float hd = k.tb.hd[gi];
+        float h = hd, herr = float(hd64[gi] - double(hd));
+        if (k.with_field) {
+            const float zq = k.tb.zq[gi];
+            h = fmaf(zq, k.efield, hd);
+            const float p = zq * k.efield;
+            const float pe = fmaf(zq, k.efield, -p);
+            float se;
+            const float sm = two_sum_full(hd, p, se);
+            herr += ((sm - h) + se) + pe;
+        }
+        const float b = k.tau * h;
+        return fmaf(k.tau, h, -b) + k.tau * herr;
+    }
+    __device__ __forceinline__ Cx<float> lo_at(int i) const {
+        if (i < 0) return prev ? prev[islot<M>(L - 1, T)] : Cx<float>{0.f, 0.f};
+        if (i >= L) return next ? next[0] : Cx<float>{0.f, 0.f};
+        return lob[islot<M>(i, T)];
+    }
+};
+
+template <int M>
+__device__ __forceinline__ Cx<float> stencil_row(const LineResCoef<M>& c, int i, float a0, float bd, float bo,
+                                                  Cx<float> p0, Cx<float> p1, Cx<float> p2) {
+    float e1, e2;
+    const float s1 = two_sum_full(bd, a0, e1);
+    const float rs = two_sum_full(s1, bo, e2);
+    const float rl = (e1 + e2) + c.bd_lo(i);
+    const Cx<float> dm = p0 - p1, dp = p2 - p1;
+    const Cx<float> l0 = c.lo_at(i - 1), l1 = c.lo_at(i), l2 = c.lo_at(i + 1);
+    return Cx<float>{a0 * dm.re + bo * dp.re + (rs * p1.re + rl * p1.re) + (a0 * l0.re + bd * l1.re + bo * l2.re),
+                     a0 * dm.im + bo * dp.im + (rs * p1.im + rl * p1.im) + (a0 * l0.im + bd * l1.im + bo * l2.im)};
+}
+
+// X_i = -i d_i from an interleaved buffer, or 0
+template <int M>
+struct LineMinusIExtra {
+    const Cx<float>* d;
+    int T;
+    bool on;
+    template <typename RR>
+    __device__ __forceinline__ Cx<RR> get(int i) const {
+        if (!on) return Cx<RR>{RR(0), RR(0)};
+        const Cx<float> v = d[islot<M>(i, T)];
+        return Cx<RR>{v.im, -v.re};
+    }
+};
+
+template <int M>
+struct LineSetAddOut {
+    Cx<float>* line;
+    int T;
+    bool add;
+    __device__ __forceinline__ void operator()(int i, Cx<float> d) const {
+        Cx<float>* p = line + islot<M>(i, T);
+        *p = add ? *p + d : d;
+    }
+};
+
+// norm and inner products of hi + lo over the cluster
+template <int M>
+__device__ void line_reduce_res(const ion_line_sim& S, const Cx<float>* line, const Cx<float>* lob, int T, int off,
+                                int64_t t, double* scratch, double* part, int rank, int C) {
+    const int n = S.n;
+    const int L = T * M;
+    const int64_t slot = line_slot(t, S.t_final, S.store_every);
+    const int i0 = int(threadIdx.x) < T ? int(threadIdx.x) : L;
+    auto val = [&](int i) {
+        const Cx<float> h = line[islot<M>(i, T)], l = lob[islot<M>(i, T)];
+        return Cx<double>{double(h.re) + double(l.re), double(h.im) + double(l.im)};
+    };
+    double acc = 0.0;
+    for (int i = i0; i < L && off + i < n; i += T) {
+        const Cx<double> x = val(i);
+        acc += x.re * x.re + x.im * x.im;
+    }
+    double nrm = block_sum_l(acc, scratch), unused = 0.0;
+    cluster_sum2(nrm, unused, part, 0, rank, C);
+    if (rank == 0 && threadIdx.x == 0) S.out_norm[slot] = nrm * S.weight;
+    for (int s = 0; s < S.n_states; ++s) {
+        const double* sg = S.state_g + int64_t(s) * n * 2;
+        double re = 0.0, im = 0.0;
+        for (int i = i0; i < L && off + i < n; i += T) {
+            const Cx<double> x = val(i);
+            const double ar = sg[2 * (off + i)], ai = -sg[2 * (off + i) + 1];
+            re += ar * x.re - ai * x.im;
+            im += ar * x.im + ai * x.re;
+        }
+        double tr = block_sum_l(re, scratch);
+        double ti = block_sum_l(im, scratch);
+        cluster_sum2(tr, ti, part, s + 1, rank, C);
+        if (rank == 0 && threadIdx.x == 0) {
+            S.out_ip[(slot * S.n_states + s) * 2] = tr * S.weight;
+            S.out_ip[(slot * S.n_states + s) * 2 + 1] = ti * S.weight;
+        }
+    }
+}
+
+__host__ __device__ inline size_t line_res_smem(int threads) {
+    return 3 * size_t(threads) * LINE_RES_M * sizeof(Cx<float>) + pcr_smem_bytes<float>(threads) +
+           64 * sizeof(double);
+}
+
+// Crank-Nicolson methods (ION_LINE_ADI / ION_LINE_SPLIT) with a residual; a
+// simulation of another method, or without g_lo, is left untouched.
+__global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int mode) {
+    constexpr int M = LINE_RES_M;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = int(cl.num_blocks());
+    const int rank = int(cl.block_rank());
+    ion_line_sim& S = plan.sims[blockIdx.x / C];
+    const int64_t t = S.t, tf = S.t_final;
+    const int n = S.n;
+    const int T = (n + C * M - 1) / (C * M);
+    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT || S.g_lo == nullptr) return;
+    const int L = T * M, off = rank * L;
+    const int cap = plan.threads * M;
+    Cx<float>* line = reinterpret_cast<Cx<float>*>(smem_raw);
+    Cx<float>* lob = line + cap;
+    Cx<float>* ext = lob + cap;
+    Cx<float>* red = ext + cap;
+    double* scratch = reinterpret_cast<double*>(red + 12 * plan.threads);
+    double* part = scratch + 32;
+    Cx<float>* g = static_cast<Cx<float>*>(S.g);
+    Cx<float>* glo = static_cast<Cx<float>*>(S.g_lo);
+    const Cx<float> zero = {0.f, 0.f};
+
+    if (mode == 1) {
+        if (!line_is_data(t, tf, S.store_every)) return;
+        for (int i = threadIdx.x; i < L; i += blockDim.x) {
+            const bool in = off + i < n;
+            line[islot<M>(i, T)] = in ? ld(g + off + i) : zero;
+            lob[islot<M>(i, T)] = in ? ld(glo + off + i) : zero;
+        }
+        __syncthreads();
+        line_reduce_res<M>(S, line, lob, T, off, t, scratch, part, rank, C);
+        return;
+    }
+    if (t >= tf) return;
+    const LineTab<float> tb = LineTab<float>::make(S);
+    const float tau = float(S.tau[t + 1]);
+    const float ef = float(S.efield[t + 1]);
+    const bool split = S.method == ION_LINE_SPLIT;
+    // the pair at global row gi as staged: (g, g_lo) with the first phase
+    auto staged = [&](int gi, Cx<float>& h, Cx<float>& lw) {
+        h = ld(g + gi);
+        lw = ld(glo + gi);
+        if (split) phase_res(h, lw, (tb.zq[gi] * ef) * tau);
+    };
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        Cx<float> h = zero, lw = zero;
+        if (off + i < n) staged(off + i, h, lw);
+        line[islot<M>(i, T)] = h;
+        lob[islot<M>(i, T)] = lw;
+    }
+    cl.sync();  // the neighbours' halo rows are staged
+    const LineResCoef<M> coef{OffsetCoef<float>{LineCnCoef<float>{tb, tau, ef, !split, n}, off}, lob,
+                              rank > 0 ? cl.map_shared_rank(lob, rank - 1) : nullptr,
+                              rank + 1 < C ? cl.map_shared_rank(lob, rank + 1) : nullptr, S.hd, T, L};
+    const ClusterHalo<float> halo{rank > 0 ? cl.map_shared_rank(line, rank - 1) : nullptr,
+                                  rank + 1 < C ? cl.map_shared_rank(line, rank + 1) : nullptr};
+    const int tid = threadIdx.x;
+    const bool active = tid < T;
+    for (int pass = 0; pass < 2; ++pass) {
+        {
+            Cx<float> al[M], be[M], ga[M];
+            RedRow<float> r[2];
+            if (active)
+                cn_chunk_eliminate<float, M>(T, tid, 2.f, line, coef, LineMinusIExtra<M>{ext, T, pass == 1}, al, be,
+                                             ga, r[0], r[1], halo);
+            pcr_solve_cluster<float>(T, tid, active, red, r, rank, C);
+            if (active) {
+                const LineSetAddOut<M> out{ext, T, pass == 1};
+                const int s = tid * M;
+                const Cx<float> xs = r[0].d, xe = r[1].d;
+                out(s, xs);
+#pragma unroll
+                for (int k = 1; k < M - 1; ++k) out(s + k, al[k] + be[k] * xs + ga[k] * xe);
+                out(s + M - 1, xe);
+            }
+        }
+        __syncthreads();
+        if (pass == 0) {  // phi = psi + Delta1 / 2
+            for (int i = threadIdx.x; i < L; i += blockDim.x) {
+                const int sl = islot<M>(i, T);
+                line[sl] = line[sl] + scale(ext[sl], 0.5f);
+            }
+            cl.sync();  // the neighbours read this CTA's phi as their halo
+        }
+    }
+    for (int i = threadIdx.x; i < L && off + i < n; i += blockDim.x) {
+        const int gi = off + i;
+        const int sl = islot<M>(i, T);
+        Cx<float> h, lw;
+        staged(gi, h, lw);
+        h = add_exact_f(h, ext[sl], lw);
+        if (split) phase_res(h, lw, (tb.zq[gi] * ef) * tau);
+        if (tb.mask) scale_res(h, lw, tb.mask[gi]);
+        line[sl] = h;
+        lob[sl] = lw;
+        st(g + gi, h);
+        st(glo + gi, lw);
+    }
+    __syncthreads();
+    if (line_is_data(t + 1, tf, S.store_every)) line_reduce_res<M>(S, line, lob, T, off, t + 1, scratch, part, rank, C);
+    // every CTA read S.t before the first cluster barrier above
+    if (rank == 0 && threadIdx.x == 0) S.t = t + 1;
+}
+
 constexpr int LINE_MAX_CLUSTER = 8;
 constexpr size_t LINE_SMEM_LIMIT = 200 * 1024;
 
 template <typename R>
+static bool line_residual(const ion_line_plan* p) {
+    return std::is_same<R, float>::value && p && (p->flags & ION_LINE_RESIDUAL);
+}
+
+static int line_res_validate(const ion_line_plan* p) {
+    if (!p->sims || p->n_sims < 0 || p->max_n < 2 || p->threads <= 0 || p->threads > 512 || (p->threads & 31) ||
+        p->cluster < 0 || p->cluster > LINE_MAX_CLUSTER) {
+        set_error("ion_line: invalid plan");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    const int C = p->cluster > 1 ? p->cluster : 1;
+    if (line_threads(p->max_n, C * LINE_RES_M) > p->threads) {
+        set_error("ion_line: max_n = %d needs more than %d threads x %d CTAs", p->max_n, p->threads, C);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (line_res_smem(p->threads) > LINE_SMEM_LIMIT) {
+        set_error("ion_line: line too long for shared memory");
+        return ION_ERR_UNSUPPORTED;
+    }
+    return ION_OK;
+}
+
+static int line_res_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(line_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
+        attr = true;
+    }
+    const unsigned C = unsigned(p->cluster > 1 ? p->cluster : 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(p->n_sims) * C);
+    cfg.blockDim = dim3(unsigned(p->threads));
+    cfg.dynamicSmemBytes = line_res_smem(p->threads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int active = 0;
+    if (cudaOccupancyMaxActiveClusters(&active, line_res_kernel, &cfg) != cudaSuccess || active < 1) {
+        cudaGetLastError();
+        set_error("ion_line: a cluster of %u CTAs x %d threads does not fit on the device", C, p->threads);
+        return ION_ERR_UNSUPPORTED;
+    }
+    cudaLaunchKernelEx(&cfg, line_res_kernel, *p, mode);
+    return check_launch("line_res_kernel");
+}
+
+template <typename R>
 static int line_validate(const ion_line_plan* p) {
     constexpr int M = LineCfg<R>::M;
+    if (line_residual<R>(p)) return line_res_validate(p);
     if (!p || !p->sims || p->n_sims < 0 || p->max_n < 2 || p->threads <= 0 || p->threads > LineCfg<R>::MAX_T ||
         (p->threads & 31) || p->cluster < 0 || p->cluster > LINE_MAX_CLUSTER) {
         set_error("ion_line: invalid plan");
@@ -616,6 +956,7 @@ static int line_validate(const ion_line_plan* p) {
 template <typename R>
 static int line_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
     constexpr int M = LineCfg<R>::M;
+    if (line_residual<R>(p)) return line_res_launch(p, mode, s);
     if (p->cluster > 1) {
         auto k = line_cluster_kernel<R, M>;
         static bool cattr = false;
@@ -698,4 +1039,9 @@ int ion_line_reduce_c128(const ion_line_plan* plan, void* stream) { return line_
 int ion_line_reduce_c64(const ion_line_plan* plan, void* stream) { return line_reduce_only<float>(plan, stream); }
 int64_t ion_line_max_n_c128(void) { return line_max_n<double>(); }
 int64_t ion_line_max_n_c64(void) { return line_max_n<float>(); }
+int64_t ion_line_max_n_c64x(void) {
+    int T = 512;
+    while (T > 32 && line_res_smem(T) > LINE_SMEM_LIMIT) T -= 32;
+    return int64_t(T) * LINE_RES_M;
+}
 }

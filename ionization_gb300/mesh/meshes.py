@@ -220,9 +220,7 @@ class LineMesh(QuantumMesh):
         method = spec.evolution_method
         if not isinstance(self.operators, mo.LineLengthGaugeOperators):
             raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on LineMesh")
-        if self.precision == core.Precision.C64X:
-            raise exceptions.UnsupportedMesh("precision c64x (complex64 with a stored residual) is implemented for "
-                                             "spherical-harmonic meshes only")
+
         if isinstance(method, em.AlternatingDirectionImplicit):
             kind = nat.ION_LINE_ADI
         elif isinstance(method, em.SplitInteractionOperator):
@@ -233,6 +231,8 @@ class LineMesh(QuantumMesh):
             raise exceptions.UnsupportedMesh(f"{type(method).__name__} has no device path on LineMesh")
         hd, hoff, zq = self.operators.device_tables(self)
         vstat = kin = twiddle = None
+        if kind == nat.ION_LINE_FFT and self.precision == core.Precision.C64X:
+            raise exceptions.UnsupportedMesh("FourierSplitOperator has no c64x (stored residual) form")
         if kind == nat.ION_LINE_FFT:
             try:
                 vstat, kin, twiddle = self.operators.fourier_tables(self)
@@ -265,6 +265,9 @@ class LineMesh(QuantumMesh):
 
     def _psi_device(self):
         return self._dsim.g
+
+    def _psi_residual(self):
+        return self._dsim.g_lo
 
     def _tau_dev(self):
         return self._dsim.d_tau

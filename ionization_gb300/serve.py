@@ -50,7 +50,7 @@ class Request:
     id: int
     arrival: float  # seconds after the start of the run
     kind: str  # "line" or "sh"
-    precision: str  # "c64" or "c128"
+    precision: str  # "c64x", "c64" or "c128"
     steps: int
     points: int  # z points of a line, radial points of a spherical-harmonic mesh
     l_bound: int = 0

@@ -19,7 +19,7 @@
   spacing.
 * ``poisson_scan_parameters``: the served scan mix (ionization_gb300.serve):
   Poisson arrivals, lines of 2048-16384 points and SH meshes of Nr 1000-4000,
-  l_max 20-100, 2000-50000 steps, 80 % complex64.
+  l_max 20-100, 2000-50000 steps, 80 % complex64 arithmetic (residual form).
 """
 
 import numpy as np
@@ -179,18 +179,21 @@ def line_softcore(name, z_points, E0, omega, cycles, cep, steps, dt=0.05, precis
     )
 
 
-def poisson_scan_parameters(n_requests=100, rate=20.0, seed=20261204, line_fraction=0.5, c64_fraction=0.8):
+def poisson_scan_parameters(n_requests=100, rate=20.0, seed=20261204, line_fraction=0.5, c64_fraction=0.8,
+                            c64_precision="c64x"):
     """The served scan mix: Poisson arrivals at ``rate`` per second; each
     request a soft-core line (2048-16384 points) or a hydrogen
     spherical-harmonic mesh (Nr 1000-4000, l_max 20-100), with a pulse drawn
-    as in the uneven sweep, 2000-50000 steps, complex64 with probability
-    ``c64_fraction`` else complex128."""
+    as in the uneven sweep, 2000-50000 steps, complex64 arithmetic with
+    probability ``c64_fraction`` else complex128.  The complex64 requests use
+    ``c64_precision``: "c64x" (the residual-compensated state that holds the
+    1e-6 population bound) or "c64"."""
     rng = np.random.default_rng(seed)
     out, t = [], 0.0
     for i in range(n_requests):
         t += float(rng.exponential(1.0 / rate))
         kind = "line" if rng.random() < line_fraction else "sh"
-        precision = "c64" if rng.random() < c64_fraction else "c128"
+        precision = c64_precision if rng.random() < c64_fraction else "c128"
         steps = int(rng.integers(2000, 50001))
         E0 = float(np.exp(rng.uniform(np.log(0.005), np.log(0.1))))
         omega = float(rng.uniform(0.03, 0.2))

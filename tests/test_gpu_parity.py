@@ -127,7 +127,7 @@ def test_mesh_c64_population_error(cuda, kind, name):
     assert rel_l2(sim.mesh.g, z["g_final"]) < 1e-4
 
 
-@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] == "sh"])
+@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] != "cyl"])
 def test_mesh_c64x_population_error(cuda, kind, name):
     """complex64 arithmetic with the state's rounding residual kept: the final
     population is within 1e-6 of the reference (the target of the complex64

@@ -82,3 +82,18 @@ def test_lines_of_every_cluster_size_share_one_batch(cuda):
     for p, s in zip(cases, sims):
         want = om.run_from_params("line", p)
         assert rel_l2(s.mesh._dsim.psi_host(), want["g_final"]) < 1e-10
+
+
+@pytest.mark.parametrize("n,method", [(4096, "SplitInteractionOperator"), (8192, "AlternatingDirectionImplicit"),
+                                      (12000, "SplitInteractionOperator"), (16384, "SplitInteractionOperator")])
+def test_long_line_c64x_close_to_oracle(cuda, n, method):
+    """The residual form on 1..4-CTA clusters: populations within 1e-6."""
+    params = _params(n, method)
+    want = om.run_from_params("line", params)
+    sim = product_spec("line", params, precision="c64x").to_sim()
+    sim.run()
+    p64 = sim.data.initial_state_overlap[-1]
+    p128 = abs(want["inner_products"][0][-1]) ** 2
+    print(f"{n}-point c64x line ({method}): |P_c64x - P_c128| = {abs(p64 - p128):.2e}")
+    assert abs(p64 - p128) < 1e-6
+    np.testing.assert_allclose(sim.data.norm, want["norm"], rtol=0, atol=1e-6)

@@ -24,7 +24,7 @@ def test_poisson_mix_is_seeded_and_in_range():
     assert all(2048 <= p["points"] <= 16384 for p in lines)
     assert all(1000 <= p["points"] <= 4000 and 21 <= p["l_bound"] <= 101 for p in shs)
     assert all(2000 <= p["steps"] <= 50000 for p in a)
-    frac64 = np.mean([p["precision"] == "c64" for p in a])
+    frac64 = np.mean([p["precision"] == "c64x" for p in a])
     assert 0.7 < frac64 < 0.9
 
 
@@ -38,6 +38,8 @@ def _small_requests():
         Request(3, 0.0, "line", "c64", 130, 9000, 0, 0.05, 0.057, 3, 0.0),  # a two-CTA cluster
         Request(4, 0.0, "sh", "c64", 40, 1000, 25, 0.08, 0.06, 2, 3.0),
         Request(5, 0.0, "line", "c128", 70, 5000, 0, 0.04, 0.12, 2, 0.5),  # a two-CTA cluster
+        Request(6, 0.0, "sh", "c64x", 50, 500, 15, 0.06, 0.09, 2, 1.5),
+        Request(7, 0.0, "line", "c64x", 60, 6000, 0, 0.05, 0.1, 2, 0.7),  # residual form, two-CTA cluster
     ]
 
 
