@@ -279,7 +279,10 @@ def run_ours(args, rank, world, local_rank):
     setup_host_s = time.perf_counter() - t_setup
     points = int(sum(t.n_r * t.n_l for t in tables))
 
-    (best_rows, best_gs), tune = bm.autotune(specs, HEADLINE, graph_steps=(32,), steps=16, tables=tables)
+    if args.rows:  # a fixed launch shape (e.g. for a profiler run, whose timings would mislead the autotuner)
+        (best_rows, best_gs), tune = (args.rows, 32), {}
+    else:
+        (best_rows, best_gs), tune = bm.autotune(specs, HEADLINE, graph_steps=(32,), steps=16, tables=tables)
 
     # ---- timed region: K steps of the headline configuration ----
     K = args.steps
@@ -587,6 +590,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=5)
     ap.add_argument("--no-serve", action="store_true", help="skip the served-mix run")
     ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--rows", type=int, default=0, choices=[0, 8, 16],
+                    help="rows per thread of the radial solve; 0 = autotune")
     args = ap.parse_args()
 
     from ionization_gb300 import replicas

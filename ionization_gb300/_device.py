@@ -340,16 +340,33 @@ def line_cta_max_n(precision) -> int:
     return int(nat.value("ion_line_max_n_" + Precision(precision).value))
 
 
-def line_cluster_for(n: int, precision, cta_max: int) -> int:
-    """Cluster size of a line: the residual form always runs as a cluster (of 1
-    or more CTAs)."""
-    return max(1, -(-int(n) // int(cta_max)))
+# Fewest points a CTA of a spread line keeps (measured on GB300, 10 lines of
+# 2048-16384 points): a complex128 step is bound by one SM's FP64 rate, so
+# down to one warp of chunks (256 points) more CTAs shorten it, 4096 points
+# from 150 to 49 us per step with 8.  A complex64 step gains little (c64x,
+# 16384 points: 53 -> 43 us with 8 CTAs) and loses below 2048 points per CTA,
+# where the cluster barriers cost more than the elimination they share out,
+# while each CTA of the residual form holds most of an SM's shared memory
+# that a served mix's spherical-harmonic batches would use: complex64 lines
+# keep 4096 points per CTA (c64x: no spreading beyond what the length needs).
+LINE_SPREAD_MIN_POINTS = {Precision.C128: 256, Precision.C64: 4096, Precision.C64X: 4096}
+# A line batch spreads every line this far by default.  The cluster size of a
+# line depends on its length and precision only, never on its batch-mates, so
+# a line's results are the same whichever lines share its launches.
+LINE_DEFAULT_SPREAD = 8
 
 
-def line_cluster(n: int, precision, cta_max: Optional[int] = None) -> int:
-    """CTAs (a thread-block cluster when > 1) that advance a line of n points."""
+def line_cluster(n: int, precision, cta_max: Optional[int] = None, spread: int = 1) -> int:
+    """CTAs (a thread-block cluster when > 1) that advance a line of n points:
+    as many as its length needs, or up to ``spread`` (at most 8) while each
+    CTA keeps LINE_SPREAD_MIN_POINTS.  Spreading a line over more SMs
+    shortens a step at the price of cluster barriers, so it pays where SMs
+    would otherwise idle, as in a served mix with few lines."""
+    precision = Precision(precision)
     cta_max = line_cta_max_n(precision) if cta_max is None else cta_max
-    return max(1, -(-int(n) // int(cta_max)))
+    need = max(1, -(-int(n) // int(cta_max)))
+    fit = max(1, int(n) // LINE_SPREAD_MIN_POINTS[precision])
+    return max(need, min(int(spread), fit, LINE_MAX_CLUSTER))
 
 
 class LineDeviceSim:
@@ -421,9 +438,10 @@ class LineBatch:
     up to one CTA's capacity in one launch, longer ones in thread-block
     clusters of 2..8 CTAs), any mix of methods, sizes and step counts."""
 
-    def __init__(self, precision, sims: Optional[List[LineDeviceSim]] = None):
+    def __init__(self, precision, sims: Optional[List[LineDeviceSim]] = None, spread: int = LINE_DEFAULT_SPREAD):
         self.precision = Precision(precision)
         self.sims: List[LineDeviceSim] = list(sims or [])
+        self.spread = int(spread)  # CTAs per line where the line is short enough (line_cluster)
         self._plans = None
         self._keep = None
         self._cta_max = None
@@ -442,7 +460,9 @@ class LineBatch:
     def _cluster_of(self, sim) -> int:
         if self._cta_max is None:
             self._cta_max = line_cta_max_n(self.precision)
-        return line_cluster(sim.n, self.precision, self._cta_max)
+        # the Fourier split-step runs in one CTA (cluster plans skip it)
+        spread = 1 if sim.tab.method == nat.ION_LINE_FFT else self.spread
+        return line_cluster(sim.n, self.precision, self._cta_max, spread)
 
     @property
     def plans(self):

@@ -277,15 +277,15 @@ __device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, 
     __syncthreads();
     if (line_is_data(t + 1, S.t_final, S.store_every)) line_reduce<R, 1>(S, x, n, stride, t + 1, scratch);
     __syncthreads();
-    if (threadIdx.x == 0) S.t = t + 1;
 }
 
-// mode 0: one step (t -> t+1) then reduce if data time; mode 1: reduce at t only
+// mode 0: up to n_steps steps (each followed by the reductions at a data
+// time), ending at t_final; mode 1: the reductions at t only
 template <typename R, int M>
-__global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int mode) {
+__global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int mode, int n_steps) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ion_line_sim& S = plan.sims[blockIdx.x];
-    const int64_t t = S.t, tf = S.t_final;
+    const int64_t t0 = S.t, tf = S.t_final;
     const int n = S.n;
     const int T = line_threads(n, M);
     const int npad = T * M;
@@ -297,16 +297,18 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     if (n < 2 || n > plan.max_n) return;  // the plan's shared memory is sized for max_n
 
     if (mode == 1) {
-        if (!line_is_data(t, tf, S.store_every)) return;
+        if (!line_is_data(t0, tf, S.store_every)) return;
         for (int i = threadIdx.x; i < n; i += blockDim.x) line[islot<M>(i, T)] = ld(g + i);
         __syncthreads();
-        line_reduce<R, M>(S, line, T, T, t, scratch);
+        line_reduce<R, M>(S, line, T, T, t0, scratch);
         return;
     }
-    if (t >= tf) return;
+    const int64_t tend = tf - t0 > n_steps ? t0 + n_steps : tf;
+    if (t0 >= tend) return;
+    for (int64_t t = t0; t < tend; ++t) {  // each step ends with a CTA barrier
     if (S.method == ION_LINE_FFT) {
         line_fft_step<R>(S, t, line, T, scratch);
-        return;
+        continue;
     }
     const LineTab<R> tb = LineTab<R>::make(S);
     const R tau = R(S.tau[t + 1]);
@@ -339,7 +341,8 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     __syncthreads();
     if (line_is_data(t + 1, tf, S.store_every)) line_reduce<R, M>(S, line, T, T, t + 1, scratch);
     __syncthreads();
-    if (threadIdx.x == 0) S.t = t + 1;
+    }
+    if (threadIdx.x == 0) S.t = tend;  // every thread read S.t before the first barrier
 }
 
 // ---------------------------------------------------------------------------
@@ -376,74 +379,108 @@ struct OffsetCoef {
     __device__ __forceinline__ void operator()(int i, R& bo, R& bd) const { c(off + i, bo, bd); }
 };
 
-// PCR over the C * 2T reduced rows of a cluster; row k of CTA r is global
-// row r 2T + k, stored as in pcr_solve_cn.  Called by every thread of every
-// CTA of the cluster.
+// The reduced system of a line split over the C CTAs of a cluster, in the
+// form pcr_solve_cn uses for one CTA: thread t of CTA r holds the two rows of
+// its chunk ends; one step of odd-even reduction leaves one row per thread
+// (the first row of thread t + 1 comes from the next CTA for t = T - 1), PCR
+// solves the T C rows of the cluster (global row r T + t; rows of other CTAs
+// through distributed shared memory, one cluster barrier per level), and the
+// chunk-start unknowns follow from the left neighbour's chunk-end unknown.
+// Uses 9 T complex words of ``red``.  The last read of another CTA's ``red``
+// comes after the last barrier here: the caller holds a cluster barrier
+// before ``red`` is written again or the CTA exits.  On return
+// r[0].d = xs_t and r[1].d = xe_t.
 template <typename R>
 __device__ __forceinline__ void pcr_solve_cluster(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2],
                                                   int rank, int C) {
     cg::cluster_group cl = cg::this_cluster();
-    const Cx<R> zero = {R(0), R(0)};
-    const int N = 2 * T, NT = N * C;
-    Cx<R>* Ab = red;
-    Cx<R>* Cb = red + 2 * N;
-    Cx<R>* Db = red + 4 * N;
+    const Cx<R> zero = {R(0), R(0)}, one = {R(1), R(0)};
+    Cx<R>* Sa = red;
+    Cx<R>* Sc = red + T;
+    Cx<R>* Sd = red + 2 * T;
+    Cx<R>* Ab = red + 3 * T;  // double-buffered [2][T]
+    Cx<R>* Cb = red + 5 * T;
+    Cx<R>* Db = red + 7 * T;
     if (active) {
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            Ab[q * T + t] = r[q].a;
-            Cb[q * T + t] = r[q].c;
-            Db[q * T + t] = r[q].d;
-        }
+        Sa[t] = r[0].a;
+        Sc[t] = r[0].c;
+        Sd[t] = r[0].d;
     }
     cl.sync();
+    RedRow<R> e = {zero, zero, zero};
+    if (active) {
+        Cx<R> an = zero, cn = zero, dn = zero;  // the next thread's first row
+        if (t + 1 < T) {
+            an = Sa[t + 1];
+            cn = Sc[t + 1];
+            dn = Sd[t + 1];
+        } else if (rank + 1 < C) {
+            an = cl.map_shared_rank(Sa, rank + 1)[0];
+            cn = cl.map_shared_rank(Sc, rank + 1)[0];
+            dn = cl.map_shared_rank(Sd, rank + 1)[0];
+        }
+        const RedRow<R>& S0 = r[0];
+        const RedRow<R>& E = r[1];
+        const Cx<R> inv = crecip_fast(one - E.a * S0.c - E.c * an);
+        e.a = -(E.a * S0.a) * inv;
+        e.c = -(E.c * cn) * inv;
+        e.d = (E.d - E.a * S0.d - E.c * dn) * inv;
+        Ab[t] = e.a;
+        Cb[t] = e.c;
+        Db[t] = e.d;
+    }
+    cl.sync();
+    const int NT = T * C;
     const int levels = pcr_levels(NT);
+    // owner CTA of global row k: floor(k / T) as (k + 1/2) * (1 / T) in FP32,
+    // exact here: the quotient stays >= 1/(2T) >= 2^-10 from an integer while
+    // k < 2^13 keeps the rounding below 2^-20
+    const float invT = 1.f / float(T);
+    // row k at level buffer ``base``: local rows through the shared window,
+    // other CTAs' rows through distributed shared memory
+    auto fetch = [&](int k, int base, Cx<R>& a_, Cx<R>& c_, Cx<R>& d_) {
+        const int o = int((float(k) + 0.5f) * invT);
+        const int sl = base + (k - o * T);
+        if (o == rank) {
+            a_ = Ab[sl];
+            c_ = Cb[sl];
+            d_ = Db[sl];
+        } else {
+            a_ = cl.map_shared_rank(Ab, o)[sl];
+            c_ = cl.map_shared_rank(Cb, o)[sl];
+            d_ = cl.map_shared_rank(Db, o)[sl];
+        }
+    };
+    const int k0 = rank * T + t;
     int p = 0;
     for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
         if (active) {
-            const int base = p * N;
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int k = rank * N + 2 * t + q;
-                Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
-                const int km = k - sig, kp = k + sig;
-                if (km >= 0) {
-                    const int o = km / N, l = km - o * N;
-                    const int sl = base + (l & 1) * T + (l >> 1);
-                    const Cx<R>* A_ = o == rank ? Ab : cl.map_shared_rank(Ab, o);
-                    const Cx<R>* C_ = o == rank ? Cb : cl.map_shared_rank(Cb, o);
-                    const Cx<R>* D_ = o == rank ? Db : cl.map_shared_rank(Db, o);
-                    am = A_[sl];
-                    cm = C_[sl];
-                    dm = D_[sl];
-                }
-                if (kp < NT) {
-                    const int o = kp / N, l = kp - o * N;
-                    const int sl = base + (l & 1) * T + (l >> 1);
-                    const Cx<R>* A_ = o == rank ? Ab : cl.map_shared_rank(Ab, o);
-                    const Cx<R>* C_ = o == rank ? Cb : cl.map_shared_rank(Cb, o);
-                    const Cx<R>* D_ = o == rank ? Db : cl.map_shared_rank(Db, o);
-                    ap = A_[sl];
-                    cpp = C_[sl];
-                    dp = D_[sl];
-                }
-                const Cx<R> a = r[q].a, c = r[q].c, d = r[q].d;
-                const Cx<R> nb = Cx<R>{R(1), R(0)} - cm * a - ap * c;
-                const Cx<R> inv = crecip_fast(nb);
-                r[q].a = -(am * a) * inv;
-                r[q].c = -(cpp * c) * inv;
-                r[q].d = (d - dm * a - dp * c) * inv;
-            }
-            const int wb = (p ^ 1) * N;
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                Ab[wb + q * T + t] = r[q].a;
-                Cb[wb + q * T + t] = r[q].c;
-                Db[wb + q * T + t] = r[q].d;
-            }
+            const int base = p * T;
+            Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
+            if (k0 - sig >= 0) fetch(k0 - sig, base, am, cm, dm);
+            if (k0 + sig < NT) fetch(k0 + sig, base, ap, cpp, dp);
+            const Cx<R> a = e.a, c = e.c, d = e.d;
+            const Cx<R> inv = crecip_fast(one - cm * a - ap * c);
+            e.a = -(am * a) * inv;
+            e.c = -(cpp * c) * inv;
+            e.d = (d - dm * a - dp * c) * inv;
+            const int wb = (p ^ 1) * T;
+            Ab[wb + t] = e.a;
+            Cb[wb + t] = e.c;
+            Db[wb + t] = e.d;
         }
         p ^= 1;
         cl.sync();
+    }
+    // Db[p T + .] holds every thread's chunk-end unknown
+    if (active) {
+        Cx<R> xem1 = zero;
+        if (t > 0)
+            xem1 = Db[p * T + t - 1];
+        else if (rank > 0)
+            xem1 = cl.map_shared_rank(Db, rank - 1)[p * T + T - 1];
+        r[0].d = r[0].d - r[0].a * xem1 - r[0].c * e.d;
+        r[1].d = e.d;
     }
 }
 
@@ -511,13 +548,13 @@ __host__ __device__ inline size_t line_cluster_smem(int threads, int M) {
 // Crank-Nicolson methods only (ION_LINE_ADI / ION_LINE_SPLIT); a simulation of
 // another method in a cluster plan is left untouched.
 template <typename R, int M>
-__global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, int mode) {
+__global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, int mode, int n_steps) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cg::cluster_group cl = cg::this_cluster();
     const int C = int(cl.num_blocks());
     const int rank = int(cl.block_rank());
     ion_line_sim& S = plan.sims[blockIdx.x / C];
-    const int64_t t = S.t, tf = S.t_final;
+    const int64_t t0 = S.t, tf = S.t_final;
     const int n = S.n;
     const int T = (n + C * M - 1) / (C * M);
     if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT) return;
@@ -530,13 +567,18 @@ __global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, i
     const Cx<R> zero = {R(0), R(0)};
 
     if (mode == 1) {
-        if (!line_is_data(t, tf, S.store_every)) return;
+        if (!line_is_data(t0, tf, S.store_every)) return;
         for (int i = threadIdx.x; i < L; i += blockDim.x) line[islot<M>(i, T)] = off + i < n ? ld(g + off + i) : zero;
         __syncthreads();
-        line_reduce_cluster<R, M>(S, line, T, off, t, scratch, part, rank, C);
+        line_reduce_cluster<R, M>(S, line, T, off, t0, scratch, part, rank, C);
         return;
     }
-    if (t >= tf) return;
+    const int64_t tend = tf - t0 > n_steps ? t0 + n_steps : tf;
+    if (t0 >= tend) return;
+    // Steps follow each other without a further cluster barrier: the
+    // neighbours read this CTA's rows (halo, reduced system) only before the
+    // barrier that ends each solve.
+    for (int64_t t = t0; t < tend; ++t) {
     const LineTab<R> tb = LineTab<R>::make(S);
     const R tau = R(S.tau[t + 1]);
     const R ef = R(S.efield[t + 1]);
@@ -575,7 +617,7 @@ __global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, i
             out(s + M - 1, xe);
         }
     }
-    __syncthreads();
+    cl.sync();  // the solve's reads of the other CTAs' shared memory are done
     for (int i = threadIdx.x; i < L && off + i < n; i += blockDim.x) {
         const int gi = off + i;
         Cx<R>* p = line + islot<M>(i, T);
@@ -588,8 +630,9 @@ __global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, i
     __syncthreads();
     if (line_is_data(t + 1, tf, S.store_every))
         line_reduce_cluster<R, M>(S, line, T, off, t + 1, scratch, part, rank, C);
+    }
     // every CTA read S.t before the first cluster barrier above
-    if (rank == 0 && threadIdx.x == 0) S.t = t + 1;
+    if (rank == 0 && threadIdx.x == 0) S.t = tend;
 }
 
 // ---------------------------------------------------------------------------
@@ -772,14 +815,14 @@ __host__ __device__ inline size_t line_res_smem(int threads) {
 
 // Crank-Nicolson methods (ION_LINE_ADI / ION_LINE_SPLIT) with a residual; a
 // simulation of another method, or without g_lo, is left untouched.
-__global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int mode) {
+__global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int mode, int n_steps) {
     constexpr int M = LINE_RES_M;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cg::cluster_group cl = cg::this_cluster();
     const int C = int(cl.num_blocks());
     const int rank = int(cl.block_rank());
     ion_line_sim& S = plan.sims[blockIdx.x / C];
-    const int64_t t = S.t, tf = S.t_final;
+    const int64_t t0 = S.t, tf = S.t_final;
     const int n = S.n;
     const int T = (n + C * M - 1) / (C * M);
     if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT || S.g_lo == nullptr) return;
@@ -796,17 +839,21 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     const Cx<float> zero = {0.f, 0.f};
 
     if (mode == 1) {
-        if (!line_is_data(t, tf, S.store_every)) return;
+        if (!line_is_data(t0, tf, S.store_every)) return;
         for (int i = threadIdx.x; i < L; i += blockDim.x) {
             const bool in = off + i < n;
             line[islot<M>(i, T)] = in ? ld(g + off + i) : zero;
             lob[islot<M>(i, T)] = in ? ld(glo + off + i) : zero;
         }
         __syncthreads();
-        line_reduce_res<M>(S, line, lob, T, off, t, scratch, part, rank, C);
+        line_reduce_res<M>(S, line, lob, T, off, t0, scratch, part, rank, C);
         return;
     }
-    if (t >= tf) return;
+    const int64_t tend = tf - t0 > n_steps ? t0 + n_steps : tf;
+    if (t0 >= tend) return;
+    // as in line_cluster_kernel, the neighbours are done with this CTA's rows
+    // at the barrier that ends the second solve of a step
+    for (int64_t t = t0; t < tend; ++t) {
     const LineTab<float> tb = LineTab<float>::make(S);
     const float tau = float(S.tau[t + 1]);
     const float ef = float(S.efield[t + 1]);
@@ -838,7 +885,10 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
             if (active)
                 cn_chunk_eliminate<float, M>(T, tid, 2.f, line, coef, LineMinusIExtra<M>{ext, T, pass == 1}, al, be,
                                              ga, r[0], r[1], halo);
-            pcr_solve_cluster<float>(T, tid, active, red, r, rank, C);
+            if (C == 1)  // one CTA: the halved block PCR with CTA barriers
+                pcr_solve_cn<float>(T, tid, active, red, r);
+            else
+                pcr_solve_cluster<float>(T, tid, active, red, r, rank, C);
             if (active) {
                 const LineSetAddOut<M> out{ext, T, pass == 1};
                 const int s = tid * M;
@@ -849,7 +899,10 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
                 out(s + M - 1, xe);
             }
         }
-        __syncthreads();
+        if (C > 1)
+            cl.sync();  // the solve's reads of the other CTAs' shared memory are done
+        else
+            __syncthreads();
         if (pass == 0) {  // phi = psi + Delta1 / 2
             for (int i = threadIdx.x; i < L; i += blockDim.x) {
                 const int sl = islot<M>(i, T);
@@ -873,8 +926,9 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     }
     __syncthreads();
     if (line_is_data(t + 1, tf, S.store_every)) line_reduce_res<M>(S, line, lob, T, off, t + 1, scratch, part, rank, C);
+    }
     // every CTA read S.t before the first cluster barrier above
-    if (rank == 0 && threadIdx.x == 0) S.t = t + 1;
+    if (rank == 0 && threadIdx.x == 0) S.t = tend;
 }
 
 constexpr int LINE_MAX_CLUSTER = 8;
@@ -903,7 +957,7 @@ static int line_res_validate(const ion_line_plan* p) {
     return ION_OK;
 }
 
-static int line_res_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
+static int line_res_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(line_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
@@ -928,7 +982,7 @@ static int line_res_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
         set_error("ion_line: a cluster of %u CTAs x %d threads does not fit on the device", C, p->threads);
         return ION_ERR_UNSUPPORTED;
     }
-    cudaLaunchKernelEx(&cfg, line_res_kernel, *p, mode);
+    cudaLaunchKernelEx(&cfg, line_res_kernel, *p, mode, n_steps);
     return check_launch("line_res_kernel");
 }
 
@@ -954,9 +1008,9 @@ static int line_validate(const ion_line_plan* p) {
 }
 
 template <typename R>
-static int line_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
+static int line_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream_t s) {
     constexpr int M = LineCfg<R>::M;
-    if (line_residual<R>(p)) return line_res_launch(p, mode, s);
+    if (line_residual<R>(p)) return line_res_launch(p, mode, n_steps, s);
     if (p->cluster > 1) {
         auto k = line_cluster_kernel<R, M>;
         static bool cattr = false;
@@ -983,7 +1037,7 @@ static int line_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
                       p->threads);
             return ION_ERR_UNSUPPORTED;
         }
-        cudaLaunchKernelEx(&cfg, k, *p, mode);
+        cudaLaunchKernelEx(&cfg, k, *p, mode, n_steps);
         return check_launch("line_cluster_kernel");
     }
     static bool attr = false;
@@ -991,7 +1045,7 @@ static int line_launch(const ion_line_plan* p, int mode, cudaStream_t s) {
         cudaFuncSetAttribute(line_step_kernel<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
         attr = true;
     }
-    line_step_kernel<R, M><<<p->n_sims, p->threads, line_smem<R>(p->threads, M), s>>>(*p, mode);
+    line_step_kernel<R, M><<<p->n_sims, p->threads, line_smem<R>(p->threads, M), s>>>(*p, mode, n_steps);
     return check_launch("line_step_kernel");
 }
 
@@ -1004,8 +1058,13 @@ static int line_run(const ion_line_plan* p, int64_t n_steps, void* stream) {
     }
     if (p->n_sims == 0) return ION_OK;
     cudaStream_t s = as_stream(stream);
-    for (int64_t k = 0; k < n_steps; ++k)
-        if (int e = line_launch<R>(p, 0, s)) return e;
+    // one launch advances every line by up to 2^30 steps (each CTA loops over
+    // the steps; a line that reaches t_final stops there)
+    for (int64_t done = 0; done < n_steps;) {
+        const int k = int(n_steps - done < (int64_t(1) << 30) ? n_steps - done : (int64_t(1) << 30));
+        if (int e = line_launch<R>(p, 0, k, s)) return e;
+        done += k;
+    }
     return ION_OK;
 }
 
@@ -1013,7 +1072,7 @@ template <typename R>
 static int line_reduce_only(const ion_line_plan* p, void* stream) {
     if (int e = line_validate<R>(p)) return e;
     if (p->n_sims == 0) return ION_OK;
-    return line_launch<R>(p, 1, as_stream(stream));
+    return line_launch<R>(p, 1, 0, as_stream(stream));
 }
 
 template <typename R>

@@ -15,14 +15,17 @@ share the GPU:
 * between chunks, arrived requests are admitted first come first served while
   their device memory fits the HBM budget, and finished ones are retired: their
   data are copied to the host and their buffers freed;
-* at most two chunks per batch are in flight, so admission and retirement
-  follow the GPU closely; a batch whose queue is full does not hold up the
-  others, and a new request's buffers are uploaded on a separate stream.
+* a chunk is ~10 ms of GPU work (32 steps of a spherical-harmonic batch, 256
+  of a line batch) and at most three per batch are in flight, so admission
+  and retirement follow the GPU closely; a batch whose queue is full does not
+  hold up the others, a new request's host tables are built on worker
+  threads and its buffers uploaded on a separate stream, and line batches run
+  on a higher-priority stream.
 
 A request's results do not depend on which other requests shared its
 launches (per-simulation tables, solver chunking, tiles and reduction order),
 and every simulation meets chunk boundaries at the same steps of its own run
-(multiples of ``chunk_steps`` from its admission), so a request served in a
+(multiples of its kind's chunk length from its admission), so a request served in a
 mix is bit-identical to the same request served alone with the same chunk
 length.  complex128 results do not depend on the chunk length either (they
 equal the plain mesh path); complex64 ones do in the last bit, because the
@@ -31,6 +34,7 @@ one chunk.
 """
 
 import collections
+import concurrent.futures
 import dataclasses
 import time
 from typing import Dict, List, Optional
@@ -122,7 +126,11 @@ class _Group:
     def __init__(self, kind: str, precision: Precision):
         self.kind = kind
         self.precision = precision
-        self.stream = torch.cuda.Stream()
+        # Line steps are short launches of a few CTAs each; on a stream of
+        # their own priority the block scheduler places them as soon as SMs
+        # free up, instead of behind the spherical-harmonic groups' whole-GPU
+        # launches.
+        self.stream = torch.cuda.Stream(priority=-1 if kind == "line" else 0)
         self.batch = dev.ShBatch(precision) if kind == "sh" else dev.LineBatch(precision)
         self.inflight = collections.deque()  # events of enqueued chunks
 
@@ -130,9 +138,15 @@ class _Group:
 class Server:
     """Continuous-batching server for ``Request`` objects on the current GPU."""
 
-    def __init__(self, hbm_budget: int = DEFAULT_HBM_BUDGET, chunk_steps: int = 32, keep_psi: bool = False):
+    def __init__(self, hbm_budget: int = DEFAULT_HBM_BUDGET, chunk_steps: int = 32, keep_psi: bool = False,
+                 line_chunk_steps: int = 256, max_inflight: int = 3, table_workers: int = 4):
         self.hbm_budget = int(hbm_budget)
+        # steps per chunk: a line step is ~30-100 us, a spherical-harmonic
+        # batch step ~0.1-1 ms, so both kinds queue ~10 ms of work per chunk
         self.chunk_steps = int(chunk_steps)
+        self.line_chunk_steps = int(line_chunk_steps)
+        self.max_inflight = int(max_inflight)
+        self.table_workers = int(table_workers)
         self.keep_psi = keep_psi
         self.groups: Dict[tuple, _Group] = {}
         self._upload = None
@@ -174,19 +188,29 @@ class Server:
         """Serve ``requests`` (arrival times in seconds from the start; with
         ``realtime`` False every request is available at once) and return
         their completions in finishing order."""
+        with concurrent.futures.ThreadPoolExecutor(max_workers=self.table_workers) as pool:
+            return self._run(requests, realtime, pool)
+
+    def _run(self, requests, realtime, pool) -> List[Completion]:
         pending = collections.deque(sorted(requests, key=lambda r: (r.arrival, r.id)))
-        waiting = collections.deque()  # arrived, host tables built
+        building = collections.deque()  # arrived, host tables being built (arrival order)
+        waiting = collections.deque()  # host tables built
         active = {}  # id -> (req, group, dsim, admitted, bytes)
         retiring = []  # (event, id)
         done: List[Completion] = []
         t0 = time.perf_counter()
         clock = lambda: time.perf_counter() - t0  # noqa: E731
 
-        while pending or waiting or active or retiring:
+        while pending or building or waiting or active or retiring:
             now = clock()
+            # host tables are built on worker threads (numpy, mostly outside
+            # the GIL), so this loop keeps feeding the GPU meanwhile
             while pending and (not realtime or pending[0].arrival <= now):
                 req = pending.popleft()
-                waiting.append((req, host_tables(req)))
+                building.append((req, pool.submit(host_tables, req)))
+            while building and building[0][1].done():
+                req, fut = building.popleft()
+                waiting.append((req, fut.result()))
             while waiting:
                 req, tables = waiting[0]
                 need = device_bytes(req)
@@ -202,17 +226,17 @@ class Server:
             self.peak_active = max(self.peak_active, len(active))
 
             # a chunk for every group with unfinished simulations and room in
-            # its queue (two chunks in flight at most); a full group does not
-            # hold up the others
+            # its queue (max_inflight chunks); a full group does not hold up
+            # the others
             moved = False
             for g in self.groups.values():
                 while g.inflight and g.inflight[0].query():
                     g.inflight.popleft()
-                if len(g.inflight) >= 2 or not any(s.t < s.t_final for s in g.batch.sims):
+                if len(g.inflight) >= self.max_inflight or not any(s.t < s.t_final for s in g.batch.sims):
                     continue
                 moved = True
                 with torch.cuda.stream(g.stream):
-                    g.batch.run(self.chunk_steps)
+                    g.batch.run(self.line_chunk_steps if g.kind == "line" else self.chunk_steps)
                     ev = torch.cuda.Event()
                     ev.record(g.stream)
                 g.inflight.append(ev)
@@ -237,7 +261,7 @@ class Server:
                     still.append((ev, rid))
             retiring = still
 
-            if not active and not waiting and pending and realtime:
+            if not active and not waiting and not building and pending and realtime:
                 time.sleep(max(0.0, min(pending[0].arrival - clock(), 0.05)))
             elif not moved:
                 time.sleep(0.0005)  # every queue is full: let the GPU catch up
@@ -248,11 +272,16 @@ class Server:
 def summarize(completions: List[Completion], makespan: float) -> dict:
     lat = np.array([c.latency for c in completions])
     pts = sum(c.request.mesh_points * c.request.steps for c in completions)
+    by_kind = collections.defaultdict(list)
+    for c in completions:
+        by_kind[f"{c.request.kind}_{c.request.precision}"].append(c.latency)
     return {
         "requests": len(completions),
         "makespan_s": round(makespan, 3),
         "latency_p50_s": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
         "latency_p99_s": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
+        "latency_by_kind": {k: {"n": len(v), "p50_s": round(float(np.percentile(v, 50)), 3),
+                                "p99_s": round(float(np.percentile(v, 99)), 3)} for k, v in sorted(by_kind.items())},
         "point_steps_per_s": pts / makespan if makespan > 0 else None,
         "requests_per_s": len(completions) / makespan if makespan > 0 else None,
     }

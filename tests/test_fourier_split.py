@@ -192,7 +192,8 @@ def test_fourier_and_crank_nicolson_share_one_plan(cuda):
 
     cases = [_fft_params("line_split_small"), _fft_params("line_split_small", 1024), load_golden("line_split_small")[0]]
     sims = [product_spec("line", p).to_sim() for p in cases]
-    batch = dev.LineBatch("c128", [s.mesh._dsim for s in sims])
+    batch = dev.LineBatch("c128", [s.mesh._dsim for s in sims], spread=1)
+    assert len(batch.plans) == 1
     steps = sims[0].mesh._dsim.t_final
     batch.run(steps)
     for p, s in zip(cases, sims):

@@ -76,7 +76,7 @@ def test_lines_of_every_cluster_size_share_one_batch(cuda):
     cases = [_params(n, m) for n, m in [(512, "SplitInteractionOperator"), (6000, "AlternatingDirectionImplicit"),
                                         (9000, "SplitInteractionOperator")]]
     sims = [product_spec("line", p).to_sim() for p in cases]
-    batch = dev.LineBatch("c128", [s.mesh._dsim for s in sims])
+    batch = dev.LineBatch("c128", [s.mesh._dsim for s in sims], spread=1)
     assert len(batch.plans) == 3
     batch.run(sims[0].mesh._dsim.t_final)
     for p, s in zip(cases, sims):
@@ -97,3 +97,36 @@ def test_long_line_c64x_close_to_oracle(cuda, n, method):
     print(f"{n}-point c64x line ({method}): |P_c64x - P_c128| = {abs(p64 - p128):.2e}")
     assert abs(p64 - p128) < 1e-6
     np.testing.assert_allclose(sim.data.norm, want["norm"], rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64x", "c64"])
+def test_spread_lines_match_oracle(cuda, precision):
+    """Lines spread over clusters of up to 8 CTAs (LineBatch(spread=8)),
+    beside a Fourier split-step line, which stays in one CTA: complex128 to
+    1e-10 of the oracle, the complex64 forms by their population bounds."""
+    from ionization_gb300 import _device as dev
+
+    # complex64 lines spread only from 2 x 4096 points up, c64x not at all
+    sizes = {"c128": (2048, 3000), "c64": (8192, 16384), "c64x": (6000, 8192)}[precision]
+    cases = [_params(sizes[0], "AlternatingDirectionImplicit"), _params(sizes[1], "SplitInteractionOperator")]
+    if precision != "c64x":  # the Fourier split-step has no residual form
+        cases.append(_params(2048, "FourierSplitOperator"))
+    sims = [product_spec("line", p, precision=precision).to_sim() for p in cases]
+    batch = dev.LineBatch(precision, [s.mesh._dsim for s in sims], spread=8)
+    clusters = [batch._cluster_of(s.mesh._dsim) for s in sims]
+    for p, c in zip(cases[:2], clusters):
+        need = dev.line_cluster(p["z_points"], precision)
+        assert c == need if precision == "c64x" else c > need  # more CTAs than the length needs
+    assert clusters[2:] in ([], [1])
+    batch.run(sims[0].mesh._dsim.t_final)
+    for p, s in zip(cases, sims):
+        want = om.run_from_params("line", p)
+        psi = s.mesh._dsim.psi_host()
+        if precision == "c128":
+            assert rel_l2(psi, want["g_final"]) < 1e-10
+            continue
+        dz = want["stepper"].dz
+        pop = abs(np.sum(np.conj(want["g_initial"]) * psi) * dz) ** 2
+        ref = abs(want["inner_products"][0][-1]) ** 2
+        print(f"{p['method']} n={p['z_points']} {precision} spread: |dP| = {abs(pop - ref):.2e}")
+        assert abs(pop - ref) < (1e-6 if precision == "c64x" else 1e-5)
