@@ -160,7 +160,10 @@ class LineLength:
     mesh."""
 
     def __init__(self, z_points, z_bound, test_mass, softening_distance, pulse, mask, method,
-                 gaussian_width=1.0):
+                 gaussian_width=1.0, gauge="length"):
+        self.gauge = gauge
+        self.times = None  # the time grid, for the velocity gauge's vector potential
+        self._index = 0
         self.z = np.linspace(-z_bound, z_bound, z_points)
         self.dz = np.abs(self.z[1] - self.z[0])
         self.shape = (z_points,)
@@ -207,6 +210,19 @@ class LineLength:
             g = p * g
             g = np.fft.ifft(np.exp(-1j * (2 * tau) * self.kin) * np.fft.fft(g))
             g = p * g
+        elif self.gauge == "velocity":
+            # LineVelocityGaugeOperators (mesh_operators.py:352-427) with
+            # SplitInteractionOperator: S = (even, odd) real pair rotations
+            self._index += 1
+            A = vector_potential(self.pulse, self.times[: self._index + 1])
+            off = ph.HBAR * (ph.ELECTRON_CHARGE / self.test_mass) / (2 * self.dz) * np.ones(len(self.z) - 1)
+            even, odd = pair_rotations(tau * A * off, len(self.z) % 2 != 0, "velocity", None)
+            g = apply_explicit(even, g, self.shape)
+            g = apply_explicit(odd, g, self.shape)
+            g = apply_explicit(self.H0.scaled_plus_identity(-1j * tau), g, self.shape)
+            g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
+            g = apply_explicit(odd, g, self.shape)
+            g = apply_explicit(even, g, self.shape)
         elif self.method == "AlternatingDirectionImplicit":
             H = Tridiag(self.H0.sub, self.H0.diag + 1.0 * vint, self.H0.sup, None)
             g = apply_explicit(H.scaled_plus_identity(-1j * tau), g, self.shape)
@@ -225,6 +241,48 @@ class LineLength:
 # --------------------------------------------------------------------------
 # spherical-harmonic mesh, length gauge, split-interaction operator
 # --------------------------------------------------------------------------
+
+def vector_potential(pulse, times):
+    """ElectricPotential.get_vector_potential_amplitude_numeric at times[-1]
+    (pulses.py:58-77): minus the Simpson integral of E over ``times`` (the
+    reference's ``integrate.simps`` is scipy's ``simpson``)."""
+    from scipy import integrate
+
+    return -integrate.simpson(y=np.asarray(pulse.field(times), dtype=np.float64), x=times)
+
+
+def pair_rotations(a, both_odd, gauge, order):
+    """The even and odd operators of a split interaction over a flattened
+    mesh with angles a[k] (pair (k, k+1)): mesh_operators.py:1037-1080
+    (length gauge, [[cos, -i sin], [-i sin, cos]]), :1234-1268 and :385-424
+    (velocity gauge, [[cos, sin], [-sin, cos]]).  ``both_odd``: the padding
+    branch (an odd number of points), where the even operator leaves the last
+    point alone and the odd one the first."""
+    a_even, a_odd = a[::2], a[1::2]
+    n = len(a) + 1
+    even_diag = np.zeros(n, dtype=np.complex128)
+    even_off = np.zeros(n - 1, dtype=np.complex128)
+    odd_diag = np.zeros(n, dtype=np.complex128)
+    odd_off = np.zeros(n - 1, dtype=np.complex128)
+    sin = (lambda x: -1j * np.sin(x)) if gauge == "length" else np.sin
+    if both_odd:
+        even_diag[:-1] = np.cos(a_even).repeat(2)
+        even_diag[-1] = 1
+        even_off[::2] = sin(a_even)
+        odd_diag[0] = 1
+        odd_diag[1:] = np.cos(a_odd).repeat(2)
+        odd_off[1::2] = sin(a_odd)
+    else:
+        even_diag[:] = np.cos(a_even).repeat(2)
+        even_off[::2] = sin(a_even)
+        odd_diag[0] = odd_diag[-1] = 1
+        odd_diag[1:-1] = np.cos(a_odd).repeat(2)
+        odd_off[1::2] = sin(a_odd)
+    if gauge == "length":  # symmetric
+        return Tridiag(even_off, even_diag, even_off, order), Tridiag(odd_off, odd_diag, odd_off, order)
+    # antisymmetric: diags((-off, diag, off), offsets=(-1, 0, 1))
+    return Tridiag(-even_off, even_diag, even_off, order), Tridiag(-odd_off, odd_diag, odd_off, order)
+
 
 def _alpha(j):
     x = (j ** 2) + (2 * j)
@@ -310,28 +368,7 @@ class SphericalHarmonicSplit:
     def split_operators(self, tau, efield):
         """split_interaction_operators, mesh_operators.py:1037-1080."""
         a = tau * (self.l_off * efield)
-        a_even, a_odd = a[::2], a[1::2]
-        len_a = len(a)
-        even_diag = np.zeros(len_a + 1, dtype=np.complex128)
-        even_off = np.zeros(len_a, dtype=np.complex128)
-        odd_diag = np.zeros(len_a + 1, dtype=np.complex128)
-        odd_off = np.zeros(len_a, dtype=np.complex128)
-        if self.Nr % 2 != 0 and self.L % 2 != 0:
-            even_diag[:-1] = np.cos(a_even).repeat(2)
-            even_diag[-1] = 1
-            even_off[::2] = -1j * np.sin(a_even)
-            odd_diag[0] = 1
-            odd_diag[1:] = np.cos(a_odd).repeat(2)
-            odd_off[1::2] = -1j * np.sin(a_odd)
-        else:
-            even_diag = np.cos(a_even).repeat(2)
-            even_off[::2] = -1j * np.sin(a_even)
-            odd_diag[0] = odd_diag[-1] = 1
-            odd_diag[1:-1] = np.cos(a_odd).repeat(2)
-            odd_off[1::2] = -1j * np.sin(a_odd)
-        even = Tridiag(even_off, even_diag, even_off, "F")
-        odd = Tridiag(odd_off, odd_diag, odd_off, "F")
-        return even, odd
+        return pair_rotations(a, self.Nr % 2 != 0 and self.L % 2 != 0, "length", "F")
 
     def evolve(self, dt, t_now):
         tau = dt / (2 * ph.HBAR)
@@ -344,6 +381,81 @@ class SphericalHarmonicSplit:
         g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
         g = apply_explicit(odd, g, self.shape)
         g = apply_explicit(even, g, self.shape)
+        if self.mask is not None:
+            g = g * self.mask
+        self.g = g
+
+
+class SphericalHarmonicVelocity(SphericalHarmonicSplit):
+    """SphericalHarmonicMesh with SphericalHarmonicVelocityGaugeOperators
+    (mesh_operators.py:1130-1408) and SplitInteractionOperator: per step
+    S = (h1 even, h1 odd, h2 even-even, even-odd, odd-even, odd-odd), the
+    radial Crank-Nicolson pair, reversed S, the mask.  The field enters as the
+    vector potential at the current time (times_to_current, sims.py:195-196)."""
+
+    def __init__(self, *args, test_mass=ph.ELECTRON_MASS_REDUCED, **kw):
+        super().__init__(*args, **kw)
+        self.times = None
+        self._index = 0
+        q_over_m = ph.ELECTRON_CHARGE / test_mass
+        kk = np.arange(self.M - 1)
+        l_of = kk % self.L
+        r_f = self.r_mesh.flatten("F")[:-1]
+        # h1 (mesh_operators.py:1143-1158) without i and the field:
+        # hbar (q/m) c_l (l+1) / r on F-order neighbours of one r
+        self.h1_off = np.where((kk + 1) % self.L != 0, _c_l(l_of) * (l_of + 1), 0.0) * (ph.HBAR * q_over_m) / r_f
+        # h2 = hbar (q/m) / (2 dr) kron(c_block, alpha_block) (:1160-1176)
+        self.h2_l = _c_l(np.arange(self.L - 1))
+        self.h2_r = (ph.HBAR * q_over_m / (2 * self.dr)) * _alpha(np.arange(self.Nr - 1))
+
+    def _similarity(self, g, parity):
+        """SimilarityOperator.u_even_g / u_odd_g (mesh_operators.py:166-189)
+        along l: rows (l, l+1) of each pair -> ((a + b), (a - b)) / sqrt 2, the
+        unpaired rows as sqrt(2) g / sqrt(2)."""
+        s2 = np.sqrt(2)
+        out = (s2 * g) / s2
+        first = np.arange(parity, self.L - 1, 2)
+        a, b = g[first], g[first + 1]
+        out[first] = (a + b) / s2
+        out[first + 1] = (a - b) / s2
+        return out
+
+    def _h2(self, g, tau, A, lpar, rpar):
+        """One SimilarityOperator of split_h2 (mesh_operators.py:1270-1408):
+        in the transformed rows of l-pair (l, l+1) the r-pairs (r, r+1) of
+        parity ``rpar`` turn by [[cos, sin], [-sin, cos]] with angle
+        tau A c_l alpha(r) hbar (q/m) / (2 dr), the (a - b) row by the
+        opposite angle; then the transform back."""
+        u = self._similarity(g, lpar)
+        first = np.arange(lpar, self.L - 1, 2)
+        rs = np.arange(rpar, self.Nr - 1, 2)
+        th = tau * A * self.h2_l[first][:, None] * self.h2_r[rs][None, :]
+        c, s = np.cos(th), np.sin(th)
+        for row, sign in ((first, 1.0), (first + 1, -1.0)):
+            x0, x1 = u[row][:, rs], u[row][:, rs + 1]
+            y0 = c * x0 + (sign * s) * x1
+            y1 = -(sign * s) * x0 + c * x1
+            blk = u[row]
+            blk[:, rs], blk[:, rs + 1] = y0, y1
+            u[row] = blk
+        return self._similarity(u, lpar)
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        self._index += 1
+        A = vector_potential(self.pulse, self.times[: self._index + 1])
+        h1e, h1o = pair_rotations(tau * A * self.h1_off, self.Nr % 2 != 0 and self.L % 2 != 0, "velocity", "F")
+        g = self.g
+        g = apply_explicit(h1e, g, self.shape)
+        g = apply_explicit(h1o, g, self.shape)
+        for lp, rp in ((0, 0), (0, 1), (1, 0), (1, 1)):
+            g = self._h2(g, tau, A, lp, rp)
+        g = apply_explicit(self.H0.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
+        for lp, rp in ((1, 1), (1, 0), (0, 1), (0, 0)):
+            g = self._h2(g, tau, A, lp, rp)
+        g = apply_explicit(h1o, g, self.shape)
+        g = apply_explicit(h1e, g, self.shape)
         if self.mask is not None:
             g = g * self.mask
         self.g = g
@@ -449,10 +561,11 @@ def build_from_params(kind, params):
         return LineLength(
             params["z_points"], params["z_bound"], params["test_mass"],
             params["softening_distance"], pulse, params.get("mask"), method,
-            params.get("gaussian_width", 1.0),
+            params.get("gaussian_width", 1.0), gauge=params.get("gauge", "length"),
         )
     if kind == "sh":
-        return SphericalHarmonicSplit(
+        cls = SphericalHarmonicVelocity if params.get("gauge", "length") == "velocity" else SphericalHarmonicSplit
+        return cls(
             params["r_points"], params["r_bound"], params["l_bound"], pulse, params.get("mask"),
             [tuple(s) for s in params["test_states"]], params["time_step"],
         )
@@ -467,6 +580,7 @@ def build_from_params(kind, params):
 def run_from_params(kind, params, max_steps=None, radii=None):
     stepper = build_from_params(kind, params)
     times = get_times(params["time_initial"], params["time_final"], params["time_step"])
+    stepper.times = times
     g0 = stepper.g.copy()
     observe = None if radii is None else (lambda st: observables(st, kind, radii))
     out = run(stepper, times, params["store_data_every"], max_steps=max_steps, observe=observe)

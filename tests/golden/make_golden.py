@@ -19,6 +19,10 @@ Cases (reference call sites in parentheses):
                    (optional --full-sh, ~10 min single core)
   cyl_cfg3_full    the full cylindrical workload: 2000 x 1000, 5000 steps
                    (optional --full-cyl, ~1 h single core; psi stored subsampled)
+  *_velocity_small  SH (even L; odd Nr and odd L; even Nr and odd L) and line
+                   (even and odd z_points) runs in the velocity gauge
+                   (SphericalHarmonicVelocityGaugeOperators,
+                   LineVelocityGaugeOperators) with SplitInteractionOperator
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
                    RExpectationValue, NormWithinRadius and (SH)
                    NormBySphericalHarmonic datastores
@@ -161,7 +165,7 @@ def gen_tdma(ion):
     save("tdma", {"sizes": sizes, "seed": 20261203}, cases)
 
 
-def line_spec(ion, name, z_points, z_bound, steps, dt, pulse, method, mask, store_every):
+def line_spec(ion, name, z_points, z_bound, steps, dt, pulse, method, mask, store_every, gauge="length"):
     GaussianState, AbsRadialCosineMask = build_helpers(ion)
     import simulacra.units as u
 
@@ -179,6 +183,8 @@ def line_spec(ion, name, z_points, z_bound, steps, dt, pulse, method, mask, stor
         store_data_every=store_every,
         gaussian_width=1.0,
     )
+    if gauge != "length":
+        params["gauge"] = gauge
     spec = ion.mesh.LineSpecification(
         name,
         z_bound=z_bound,
@@ -193,7 +199,7 @@ def line_spec(ion, name, z_points, z_bound, steps, dt, pulse, method, mask, stor
         time_initial=0.0,
         time_final=steps * dt,
         time_step=dt,
-        operators=ion.mesh.LineLengthGaugeOperators(),
+        operators=ion.mesh.LineVelocityGaugeOperators() if gauge == "velocity" else ion.mesh.LineLengthGaugeOperators(),
         evolution_method=getattr(ion.mesh, method)(),
         store_data_every=store_every,
     )
@@ -224,7 +230,7 @@ def gen_line(ion, full=False):
         save("line_cfg1_full", params, out)
 
 
-def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3):
+def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3, gauge="length"):
     from ionization import states
 
     r_bound = 0.125 * (r_points - 1)
@@ -243,6 +249,8 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
         store_data_every=store_every,
         test_states=[[s.n, s.l] for s in test_states],
     )
+    if gauge != "length":
+        params["gauge"] = gauge
     spec = ion.mesh.SphericalHarmonicSpecification(
         name,
         r_points=r_points,
@@ -256,7 +264,8 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
         time_initial=0.0,
         time_final=steps * dt,
         time_step=dt,
-        operators=ion.mesh.SphericalHarmonicLengthGaugeOperators(),
+        operators=(ion.mesh.SphericalHarmonicVelocityGaugeOperators() if gauge == "velocity"
+                   else ion.mesh.SphericalHarmonicLengthGaugeOperators()),
         evolution_method=ion.mesh.SplitInteractionOperator(),
         store_data_every=store_every,
     )
@@ -279,6 +288,27 @@ def gen_sh(ion, full=False):
         spec, params = sh_spec(ion, "sh_cfg2_full", 2000, 41, 20000, 0.02, pulse, 25.0, 1000, n_max=5)
         _, out = run_and_collect(spec)
         save("sh_cfg2_full", params, out)
+
+
+def gen_velocity(ion):
+    """Velocity-gauge split operators: SphericalHarmonicVelocityGaugeOperators
+    (mesh_operators.py:1130-1408: l-rotations h1, r/l similarity blocks h2)
+    and LineVelocityGaugeOperators (mesh_operators.py:352-427), with
+    SplitInteractionOperator; the vector potential is the reference's
+    Simpson integral of E over the times so far (pulses.py:58-77)."""
+    fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+    for name, nr, L in (("sh_velocity_small_evenL", 160, 8), ("sh_velocity_small_oddNr_oddL", 151, 7),
+                        ("sh_velocity_small_evenNr_oddL", 160, 11)):
+        spec, params = sh_spec(ion, name, nr, L, 500, 0.02, fast_pulse, 5.0, 50, gauge="velocity")
+        _, out = run_and_collect(spec)
+        save(name, params, out)
+    for name, nz in (("line_velocity_small", 512), ("line_velocity_small_odd", 511)):
+        spec, params = line_spec(
+            ion, name, nz, 40.0, 400, 0.05, _pulse_kwargs(0.1, 0.5, 2, 0.3), "SplitInteractionOperator",
+            dict(inner_radius=30.0, outer_radius=40.0, smoothness=8), 50, gauge="velocity",
+        )
+        _, out = run_and_collect(spec)
+        save(name, params, out)
 
 
 def cyl_spec(ion, name, z_points, z_bound, rho_points, rho_bound, steps, dt, pulse, store_every):
@@ -389,7 +419,7 @@ def gen_observables(ion):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -398,7 +428,7 @@ def main():
     from loader import import_reference
 
     ion = import_reference(args.ref)
-    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs"}
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -409,6 +439,8 @@ def main():
         gen_cyl(ion)
     if "obs" in only:
         gen_observables(ion)
+    if "vel" in only:
+        gen_velocity(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

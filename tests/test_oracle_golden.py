@@ -42,6 +42,12 @@ CASES = [
     ("sh", "sh_split_small_oddL"),
     ("sh", "sh_split_small_oddNr_oddL"),
     ("cyl", "cyl_adi_small"),
+    # velocity gauge (SphericalHarmonicVelocityGaugeOperators, LineVelocityGaugeOperators)
+    ("sh", "sh_velocity_small_evenL"),
+    ("sh", "sh_velocity_small_oddNr_oddL"),
+    ("sh", "sh_velocity_small_evenNr_oddL"),
+    ("line", "line_velocity_small"),
+    ("line", "line_velocity_small_odd"),
 ]
 
 
