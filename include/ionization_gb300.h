@@ -165,7 +165,7 @@ typedef struct ion_sh_sim {
     double *out_ip;         /* [n_data*n_states*2] complex128 */
     double *partials;       /* [n_tiles * (1 + 2*n_states)] device scratch for reductions */
     int32_t n_tiles;        /* number of row tiles of this simulation */
-    int32_t pad_;
+    int32_t gauge;          /* ION_GAUGE_LENGTH (0) or ION_GAUGE_VELOCITY, see below */
     /* _c64 entry points only, or NULL: the rounding residual of psi,
      * complex64 (n_l, n_r) like g.  With it psi = g + g_lo carries about 48
      * significant bits: the arithmetic stays FP32, each step's increment is
@@ -176,7 +176,20 @@ typedef struct ion_sh_sim {
      * removes the cancellation of the kinetic terms and keeps the step
      * unitary. */
     void *g_lo;
+    /* ION_GAUGE_VELOCITY (SphericalHarmonicVelocityGaugeOperators,
+     * mesh_operators.py:1130-1408): the split operators are h1, rotations of
+     * F-order l-neighbours at one r by tau A hbar (q/m) c_l (l+1) / r_j, and h2,
+     * rotations of the (l, r)-(l+1, r+1) and (l, r+1)-(l+1, r) pairs of each
+     * l-pair x r-pair block by tau A c_l h2r[j]; per step h1 even, h1 odd,
+     * h2 (even, even), (even, odd), (odd, even), (odd, odd) (l-pair, r-pair
+     * parities), the radial solve, the same in reverse.  In this gauge rq
+     * (rq32) holds hbar (q/m) / r_j, efield the vector potential A(times[t]),
+     * cl the plain c_l. */
+    const double *h2r;      /* [n_r-1] hbar (q/m) / (2 dr) alpha(j), or NULL */
+    const float *h2r32;
 } ion_sh_sim;
+
+enum { ION_GAUGE_LENGTH = 0, ION_GAUGE_VELOCITY = 1 };
 
 /* ion_sh_plan.flags: with it, the radial solve of every simulation that carries a
  * stored residual is followed by one step of iterative refinement.  The matrix
@@ -186,6 +199,9 @@ typedef struct ion_sh_sim {
  * the correction with the residual formed from the first solution (about twice
  * the radial-solve time). */
 enum { ION_SH_REFINE = 1 };
+/* ion_sh_plan.flags: some simulations are in the velocity gauge (their
+ * rotation pass runs in its own kernel), or all of them are. */
+enum { ION_SH_VELOCITY = 2, ION_SH_ONLY_VELOCITY = 4 };
 
 typedef struct ion_sh_plan {
     ion_sh_sim *sims;         /* device array [n_sims] */

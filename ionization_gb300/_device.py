@@ -102,6 +102,10 @@ class ShTables:
     t0: int
     t_final: int
     store_every: int
+    # velocity gauge: rq holds hbar (q/m) / r_j, efield the vector potential
+    # A(times[t]) and h2r [n_r - 1] the r factor of the h2 blocks
+    gauge: int = 0
+    h2r: Optional[np.ndarray] = None
 
 
 SH_ROT_ROWS = 32
@@ -150,6 +154,10 @@ class ShDeviceSim:
         self.d_rq32 = to_dev(tab.rq, f32)
         self.d_cl32 = to_dev(tab.cl, f32)
         self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
+        self.gauge = int(tab.gauge)
+        self.d_h2r = self.d_h2r32 = None
+        if self.gauge == nat.ION_GAUGE_VELOCITY:
+            self.d_h2r, self.d_h2r32 = to_dev(tab.h2r, f64), to_dev(tab.h2r, f32)
         self.n_states = len(tab.state_l)
         self.d_state_l = to_dev(np.asarray(tab.state_l, dtype=np.int32).reshape(-1))
         sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(self.n_states, self.n_r)
@@ -184,6 +192,8 @@ class ShDeviceSim:
         d.out_norm, d.out_ip, d.partials = ptr(self.d_norm), ptr(self.d_ip), ptr(self.d_partials)
         d.n_tiles = self.n_tiles
         d.g_lo = ptr(self.g_lo)
+        d.gauge = self.gauge
+        d.h2r, d.h2r32 = ptr(self.d_h2r), ptr(self.d_h2r32)
         return d
 
     def data(self):
@@ -248,6 +258,9 @@ class ShBatch:
         plan.max_n_l = max([s.n_l for s in sims] + [1])
         plan.max_n_r = max([s.n_r for s in sims] + [2])
         plan.flags = nat.ION_SH_REFINE if any(s.g_lo is not None for s in sims) else 0
+        n_vel = sum(1 for s in sims if s.gauge == nat.ION_GAUGE_VELOCITY)
+        if n_vel:
+            plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)
         plan.cn_items = ptr(d_cn)
         plan.n_cn_items = len(cn)
         plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, self.cn_rows) for s in sims] + [1]))

@@ -24,6 +24,10 @@ ION_LINE_ADI = 0
 ION_LINE_SPLIT = 1
 ION_LINE_FFT = 2
 ION_SH_REFINE = 1
+ION_SH_VELOCITY = 2
+ION_SH_ONLY_VELOCITY = 4
+ION_GAUGE_LENGTH = 0
+ION_GAUGE_VELOCITY = 1
 ION_LINE_RESIDUAL = 1
 
 
@@ -67,8 +71,10 @@ class ShSim(ctypes.Structure):
         ("out_ip", c_vp),
         ("partials", c_vp),
         ("n_tiles", c_i32),
-        ("pad_", c_i32),
+        ("gauge", c_i32),
         ("g_lo", c_vp),
+        ("h2r", c_vp),
+        ("h2r32", c_vp),
     ]
 
 

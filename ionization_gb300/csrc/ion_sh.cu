@@ -457,6 +457,12 @@ template <> struct Tile<double> {
         hi[k0] = Cx<double>{x0.re + (cm1 * x0.re + s * x1.im), x0.im + (cm1 * x0.im - s * x1.re)};
         hi[k1] = Cx<double>{x1.re + (cm1 * x1.re + s * x0.im), x1.im + (cm1 * x1.im - s * x0.re)};
     }
+    // velocity gauge: [[cos, sin], [-sin, cos]] in increment form
+    __device__ void rotate_real(int k0, int k1, double cm1, double s) const {
+        const Cx<double> x0 = hi[k0], x1 = hi[k1];
+        hi[k0] = Cx<double>{x0.re + (cm1 * x0.re + s * x1.re), x0.im + (cm1 * x0.im + s * x1.im)};
+        hi[k1] = Cx<double>{x1.re + (cm1 * x1.re - s * x0.re), x1.im + (cm1 * x1.im - s * x0.im)};
+    }
     __device__ void scale(int k, double m) const { hi[k] = Cx<double>{hi[k].re * m, hi[k].im * m}; }
     __device__ Cx<double> out(int k) const { return hi[k]; }
     __device__ __forceinline__ void store(int k, Cx<double>* g, Cx<double>*, int64_t at) const { st(g + at, hi[k]); }
@@ -479,6 +485,18 @@ template <> struct Tile<float> {
         hi[k1] = Cx<float>{h1r, h1i};
         lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.im) + e0r, l0.im + (cm1 * l0.im - s * l1.re) + e0i};
         lo[k1] = Cx<float>{l1.re + (cm1 * l1.re + s * l0.im) + e1r, l1.im + (cm1 * l1.im - s * l0.re) + e1i};
+    }
+    __device__ void rotate_real(int k0, int k1, float cm1, float s) const {
+        const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo[k0], l1 = lo[k1];
+        float e0r, e0i, e1r, e1i;
+        const float h0r = two_sum(x0.re, cm1 * x0.re + s * x1.re, e0r);
+        const float h0i = two_sum(x0.im, cm1 * x0.im + s * x1.im, e0i);
+        const float h1r = two_sum(x1.re, cm1 * x1.re - s * x0.re, e1r);
+        const float h1i = two_sum(x1.im, cm1 * x1.im - s * x0.im, e1i);
+        hi[k0] = Cx<float>{h0r, h0i};
+        hi[k1] = Cx<float>{h1r, h1i};
+        lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.re) + e0r, l0.im + (cm1 * l0.im + s * l1.im) + e0i};
+        lo[k1] = Cx<float>{l1.re + (cm1 * l1.re - s * l0.re) + e1r, l1.im + (cm1 * l1.im - s * l0.im) + e1i};
     }
     __device__ void scale(int k, float m) const {  // the product's rounding error goes to lo
         const Cx<float> h = hi[k], l = lo[k];
@@ -577,6 +595,7 @@ __global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf
     const int si = plan.rot_items[2 * blockIdx.x];
     const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
     const ion_sh_sim& S = plan.sims[si];
+    if (S.gauge != ION_GAUGE_LENGTH) return;  // sh_rot_vel_kernel
     const int64_t t = S.t;
     const int64_t tf = S.t_final;
 
@@ -666,6 +685,182 @@ __global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf
     }
 }
 
+// ---------------------------------------------------------------------------
+// Velocity gauge (ion_sh_sim.gauge == ION_GAUGE_VELOCITY): the same tiles of
+// ROT_ROWS r rows x all l, loaded with VEL_HALO rows on each side.  h2 couples
+// r and r +- 1, and a tile applies at most 8 such operators per launch (4
+// after the solve of step n, 4 before the solve of step n+1), each of which
+// leaves one more row at a cut edge wrong; so with 8 halo rows the interior
+// rows are exact, and only they are stored and reduced.
+// ---------------------------------------------------------------------------
+constexpr int VEL_HALO = 8;
+constexpr int VEL_ROWS = ROT_ROWS + 2 * VEL_HALO;
+
+// h1 of parity ``parity`` (F-order pairs of l at each r) on every loaded row
+template <typename R>
+__device__ __forceinline__ void vel_h1(const Tile<R>& tl, int jlo, int jhi, int nl, int r0, int parity,
+                                       const RotTab<R>& tb, R tau, R afield) {
+    const int span = jhi - jlo;
+    const int pairs = nl >> 1;
+    for (int idx = threadIdx.x; idx < span * pairs; idx += blockDim.x) {
+        const int jj = jlo + idx % span;
+        const int j = r0 + jj;  // mesh row
+        const int l = int((int64_t(j) * nl + parity) & 1) + 2 * (idx / span);
+        if (l + 1 >= nl) continue;
+        R cm1, s;
+        rot_coeffs(tau * ((tb.cl[l] * R(l + 1)) * (tb.rq[j] * afield)), cm1, s);
+        tl.rotate_real(l * VEL_ROWS + jj, (l + 1) * VEL_ROWS + jj, cm1, s);
+    }
+    __syncthreads();
+}
+
+// h2 of l-pair parity lp and r-pair parity rp: per block, the pairs
+// ((l, r), (l+1, r+1)) and ((l+1, r), (l, r+1)) turn by [[cos, sin], [-sin, cos]]
+template <typename R>
+__device__ __forceinline__ void vel_h2(const Tile<R>& tl, int jlo, int jhi, int nl, int r0, int lp, int rp,
+                                       const RotTab<R>& tb, const R* h2r, R tau, R afield) {
+    const int lpairs = (nl - lp) >> 1;
+    const int rpairs = (VEL_ROWS - rp) >> 1;
+    for (int idx = threadIdx.x; idx < lpairs * rpairs; idx += blockDim.x) {
+        const int jj = rp + 2 * (idx % rpairs);  // r0 is even, so row parity = jj parity
+        const int l = lp + 2 * (idx / rpairs);
+        if (jj < jlo || jj + 1 >= jhi) continue;
+        R cm1, s;
+        rot_coeffs(tau * ((tb.cl[l] * h2r[r0 + jj]) * afield), cm1, s);
+        tl.rotate_real(l * VEL_ROWS + jj, (l + 1) * VEL_ROWS + jj + 1, cm1, s);
+        tl.rotate_real((l + 1) * VEL_ROWS + jj, l * VEL_ROWS + jj + 1, cm1, s);
+    }
+    __syncthreads();
+}
+
+template <typename R> struct VelTab;
+template <> struct VelTab<double> {
+    __device__ static const double* h2r(const ion_sh_sim& S) { return S.h2r; }
+};
+template <> struct VelTab<float> {
+    __device__ static const float* h2r(const ion_sh_sim& S) { return S.h2r32; }
+};
+
+template <typename R>
+__global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh_plan plan, int mode) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int si = plan.rot_items[2 * blockIdx.x];
+    const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
+    const ion_sh_sim& S = plan.sims[si];
+    if (S.gauge != ION_GAUGE_VELOCITY) return;
+    const int64_t t = S.t;
+    const int64_t tf = S.t_final;
+    bool post = false, do_mask = false, reduce = false, pre = false;
+    int64_t n_post = 0, n_pre = 0;
+    if (mode == ROT_PRE_ONLY) {
+        if (t >= tf) return;
+        pre = true;
+        n_pre = t + 1;
+    } else if (mode == ROT_STEP || mode == ROT_STEP_PRE) {
+        if (t >= tf) return;
+        post = true;
+        n_post = t + 1;
+        do_mask = S.mask != nullptr;
+        reduce = is_data_time(t + 1, tf, S.store_every);
+        if (mode == ROT_STEP_PRE && t + 1 < tf) {
+            pre = true;
+            n_pre = t + 2;
+        }
+    } else if (mode == ROT_REDUCE_ONLY) {
+        reduce = is_data_time(t, tf, S.store_every);
+        if (!reduce) return;
+    }
+    const int nr = S.n_r, nl = S.n_l;
+    const int j0 = tile_idx * ROT_ROWS;
+    const int rows = min(ROT_ROWS, nr - j0);
+    if (rows <= 0) return;
+    const int r0 = j0 - VEL_HALO;  // mesh row of tile row 0
+    const int jlo = max(0, -r0), jhi = min(VEL_ROWS, nr - r0);
+    const size_t tile_elems = size_t(plan.max_n_l) * VEL_ROWS;
+    Cx<R>* hi = reinterpret_cast<Cx<R>*>(smem_raw);
+    Tile<R> tl;
+    tl.hi = hi;
+    double* scratch;
+    if constexpr (Tile<R>::comp) {
+        tl.lo = hi + tile_elems;
+        scratch = reinterpret_cast<double*>(hi + 2 * tile_elems);
+    } else {
+        scratch = reinterpret_cast<double*>(hi + tile_elems);
+    }
+    Cx<R>* g = static_cast<Cx<R>*>(S.g);
+    Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
+    const int span = jhi - jlo;
+    for (int f = threadIdx.x; f < nl * span; f += blockDim.x) {
+        const int l = f / span, jj = jlo + f % span;
+        const int64_t at = int64_t(l) * nr + r0 + jj;
+        hi[l * VEL_ROWS + jj] = ld(g + at);
+        if constexpr (Tile<R>::comp) tl.lo[l * VEL_ROWS + jj] = glo ? ld(glo + at) : Cx<R>{R(0), R(0)};
+    }
+    __syncthreads();
+    const RotTab<R> tb = RotTab<R>::make(S);
+    const R* h2r = VelTab<R>::h2r(S);
+    if (post) {  // reversed(S): h2 (odd, odd) ... (even, even), h1 odd, h1 even
+        const R tau = R(S.tau[n_post]), af = R(S.efield[n_post]);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 1, 1, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 1, 0, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 0, 1, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 0, 0, tb, h2r, tau, af);
+        vel_h1<R>(tl, jlo, jhi, nl, r0, 1, tb, tau, af);
+        vel_h1<R>(tl, jlo, jhi, nl, r0, 0, tb, tau, af);
+    }
+    if (do_mask) {
+        for (int f = threadIdx.x; f < nl * span; f += blockDim.x) {
+            const int l = f / span, jj = jlo + f % span;
+            tl.scale(l * VEL_ROWS + jj, tb.mask[r0 + jj]);
+        }
+        __syncthreads();
+    }
+    if (reduce) {  // interior rows
+        const int nq = 1 + 2 * S.n_states;
+        double acc = 0.0;
+        for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
+            const Cx<double> x = tl.value((f / rows) * VEL_ROWS + VEL_HALO + f % rows);
+            acc += x.re * x.re + x.im * x.im;
+        }
+        const double tot = block_sum(acc, scratch);
+        if (threadIdx.x == 0) S.partials[int64_t(tile_idx) * nq] = tot;
+        for (int q = 0; q < S.n_states; ++q) {
+            const int ls = S.state_l[q];
+            double re = 0.0, im = 0.0;
+            const int jj = threadIdx.x;
+            if (jj < rows && ls < nl) {
+                const Cx<double> x = tl.value(ls * VEL_ROWS + VEL_HALO + jj);
+                const double* sg = S.state_g + (int64_t(q) * nr + j0 + jj) * 2;
+                const double ar = sg[0], ai = -sg[1];
+                re = ar * x.re - ai * x.im;
+                im = ar * x.im + ai * x.re;
+            }
+            const double tr = block_sum(re, scratch);
+            const double ti = block_sum(im, scratch);
+            if (threadIdx.x == 0) {
+                S.partials[int64_t(tile_idx) * nq + 1 + 2 * q] = tr;
+                S.partials[int64_t(tile_idx) * nq + 2 + 2 * q] = ti;
+            }
+        }
+        __syncthreads();
+    }
+    if (pre) {  // S: h1 even, h1 odd, h2 (even, even) ... (odd, odd)
+        const R tau = R(S.tau[n_pre]), af = R(S.efield[n_pre]);
+        vel_h1<R>(tl, jlo, jhi, nl, r0, 0, tb, tau, af);
+        vel_h1<R>(tl, jlo, jhi, nl, r0, 1, tb, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 0, 0, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 0, 1, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 1, 0, tb, h2r, tau, af);
+        vel_h2<R>(tl, jlo, jhi, nl, r0, 1, 1, tb, h2r, tau, af);
+    }
+    if (post || pre || do_mask) {
+        for (int f = threadIdx.x; f < nl * rows; f += blockDim.x) {
+            const int l = f / rows, jr = f % rows;
+            tl.store(l * VEL_ROWS + VEL_HALO + jr, g, glo, int64_t(l) * nr + j0 + jr);
+        }
+    }
+}
+
 // Neumaier-compensated sum of the per-tile partials, then advance t
 __global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
     ion_sh_sim& S = plan.sims[blockIdx.x];
@@ -746,6 +941,11 @@ static int sh_validate(const ion_sh_plan* p) {
         set_error("ion_sh: buckets do not cover the items");
         return ION_ERR_INVALID_ARGUMENT;
     }
+    if ((p->flags & (ION_SH_VELOCITY | ION_SH_ONLY_VELOCITY)) &&
+        rot_smem_bytes<R>(p->max_n_l, VEL_ROWS) > 200 * 1024) {
+        set_error("ion_sh: l_bound %d too large for the velocity-gauge rotation tile", p->max_n_l);
+        return ION_ERR_UNSUPPORTED;
+    }
     const int rows = sh_rows<R>(p);
     if (int64_t(p->max_n_r) > int64_t(rows) * ShCfg<R>::MAX_T ||
         sh_line_threads(p->max_n_r, rows) > p->cn_threads) {
@@ -763,16 +963,29 @@ static size_t rot_smem(const ion_sh_plan* p) {
 template <typename R>
 static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     if (p->n_rot_items == 0) return ION_OK;
-    const size_t smem = rot_smem<R>(p);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(sh_rot_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
+    if (!(p->flags & ION_SH_ONLY_VELOCITY)) {
+        const size_t smem = rot_smem<R>(p);
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(sh_rot_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            attr = true;
+        }
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
+        sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
+        if (int e = check_launch("sh_rot_kernel")) return e;
     }
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
-    sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
-    return check_launch("sh_rot_kernel");
+    if (p->flags & (ION_SH_VELOCITY | ION_SH_ONLY_VELOCITY)) {
+        const size_t smem = rot_smem_bytes<R>(p->max_n_l, VEL_ROWS);
+        static bool vattr = false;
+        if (!vattr) {
+            cudaFuncSetAttribute(sh_rot_vel_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            vattr = true;
+        }
+        sh_rot_vel_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode);
+        if (int e = check_launch("sh_rot_vel_kernel")) return e;
+    }
+    return ION_OK;
 }
 
 template <typename R, int MAXM>

@@ -23,6 +23,7 @@ from .mesh_operators import (  # noqa: F401
     MeshOperator,
     MeshOperators,
     SphericalHarmonicLengthGaugeOperators,
+    SphericalHarmonicVelocityGaugeOperators,
     SumOfOperators,
     TDMAOperator,
     add_to_diagonal_sparse_matrix_diagonal,

@@ -291,6 +291,58 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
         return SumOfOperators(DotOperator(m, wrapping_direction="l"))
 
 
+class SphericalHarmonicVelocityGaugeOperators(SphericalHarmonicLengthGaugeOperators):
+    """mesh_operators.py:1130-1408: the radial Hamiltonian of the length-gauge
+    class; the interaction is h1 + h2 times the vector potential A(t) =
+    -integral of E over the times so far (pulses.py:58-77):
+      h1 = i hbar (q/m) c_l (l+1) / r between F-order l-neighbours at one r,
+      h2 = i hbar (q/m) / (2 dr) kron(c_block, alpha_block)."""
+
+    gauge = core.Gauge.VELOCITY
+
+    def __init__(self, hydrogen_zero_angular_momentum_correction: bool = True):
+        super().__init__(hydrogen_zero_angular_momentum_correction=hydrogen_zero_angular_momentum_correction)
+
+    def __repr__(self):
+        return (f"{self.__class__.__name__}(hydrogen_zero_angular_momentum_correction = "
+                f"{self.hydrogen_zero_angular_momentum_correction})")
+
+    @_memo
+    def velocity_tables(self, mesh):
+        """rq [Nr] = hbar (q/m) / r_j (h1 = A rq_j c_l (l+1) between l-neighbours)
+        and h2r [Nr-1] = hbar (q/m) / (2 dr) alpha(j) (h2 = A c_l h2r_j on the
+        (l, j)-(l+1, j+1) link)."""
+        spec = mesh.spec
+        q_over_m = spec.test_charge / spec.test_mass
+        rq = (u.hbar * q_over_m) / mesh.r
+        h2r = (u.hbar * q_over_m / (2 * mesh.delta_r)) * self.alpha(np.arange(spec.r_points - 1))
+        return dict(rq=np.asarray(rq, dtype=np.float64), h2r=np.asarray(h2r, dtype=np.float64))
+
+    @_memo
+    def interaction_hamiltonian_matrices_without_field(self, mesh):
+        """(h1, h2) as sparse matrices (mesh_operators.py:1143-1176); h1 acts on
+        the mesh flattened along l, h2 along r."""
+        spec = mesh.spec
+        L, nr = spec.l_bound, spec.r_points
+        q_over_m = spec.test_charge / spec.test_mass
+        rF = mesh.r_mesh.flatten("F")[:-1]
+        kk = np.arange(len(rF))
+        l_of = kk % L
+        h1_off = np.where((kk + 1) % L != 0, self.c_l(l_of) * (l_of + 1), 0) * (1j * u.hbar * q_over_m) / rF
+        h1 = sparse.diags((-h1_off, h1_off), offsets=(-1, 1))
+        alpha_vec = self.alpha(np.arange(nr - 1, dtype=np.complex128))
+        c_vec = self.c_l(np.arange(L - 1, dtype=np.complex128))
+        h2 = (1j * u.hbar * q_over_m / (2 * mesh.delta_r)) * sparse.kron(
+            sparse.diags((c_vec, c_vec), offsets=(-1, 1)), sparse.diags((-alpha_vec, alpha_vec), offsets=(-1, 1)),
+            format="dia")
+        return h1, h2
+
+    def interaction_hamiltonian(self, mesh):
+        h1, h2 = self.interaction_hamiltonian_matrices_without_field(mesh)
+        A = mesh.spec.electric_potential.get_vector_potential_amplitude_numeric(mesh.sim.times_to_current)
+        return SumOfOperators(DotOperator(A * h1, wrapping_direction="l"), DotOperator(A * h2, wrapping_direction="r"))
+
+
 # --------------------------------------------------------------------------
 # cylindrical slice mesh
 # --------------------------------------------------------------------------

@@ -16,7 +16,7 @@ import torch
 
 from .. import _device as dev
 from .. import _native as nat
-from .. import core, exceptions, states
+from .. import core, exceptions, potentials, states
 from .. import units as u
 from . import evolution_methods as em
 from . import mesh_operators as mo
@@ -373,9 +373,18 @@ class SphericalHarmonicMesh(QuantumMesh):
         self._tau_host = np.zeros(len(times))
         self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
         efield = np.zeros(len(times))
-        efield[1:] = np.asarray(
-            spec.electric_potential.get_electric_field_amplitude(times[1:] + (spec.time_step / 2)), np.float64
-        ) * np.ones(len(times) - 1)
+        gauge, h2r, rq = nat.ION_GAUGE_LENGTH, None, tb["rq"]
+        if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
+            # the velocity-gauge operators take A at the step's own time
+            # (times_to_current, sims.py:195-196); the tables carry its factors
+            gauge = nat.ION_GAUGE_VELOCITY
+            vt = self.operators.velocity_tables(self)
+            rq, h2r = vt["rq"], vt["h2r"]
+            efield[1:] = potentials.vector_potential_table(spec.electric_potential, times)[1:]
+        else:
+            efield[1:] = np.asarray(
+                spec.electric_potential.get_electric_field_amplitude(times[1:] + (spec.time_step / 2)), np.float64
+            ) * np.ones(len(times) - 1)
         sl, sg = [], []
         for s in spec.test_states:
             comps = list(s)
@@ -385,11 +394,11 @@ class SphericalHarmonicMesh(QuantumMesh):
             sg.append(self.get_radial_g_for_state(comps[0]) * 1)
         g0 = self.get_g_for_state(spec.initial_state)
         self.tables = dev.ShTables(
-            n_r=spec.r_points, n_l=spec.l_bound, hd=tb["hd"], hoff=tb["hoff"], rq=tb["rq"], cl=tb["cl"], mask=mask,
+            n_r=spec.r_points, n_l=spec.l_bound, hd=tb["hd"], hoff=tb["hoff"], rq=rq, cl=tb["cl"], mask=mask,
             tau=self._tau_host.copy(), efield=efield, kinv=tb["kinv"], cent=tb["cent"], corr0=tb["corr0"],
             state_l=sl, state_g=np.array(sg, dtype=np.complex128).reshape(len(sl), spec.r_points),
             weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
-            store_every=spec.store_data_every,
+            store_every=spec.store_data_every, gauge=gauge, h2r=h2r,
         )
         if getattr(spec, "host_only", False):
             return

@@ -252,6 +252,53 @@ def field_table(electric_potential, times):
     )
 
 
+def simpson_prefix_integrals(y, x):
+    """I[k] = the integral of y over x[:k+1] for every k, each by Simpson's rule
+    for irregularly spaced samples as ``get_vector_potential_amplitude_numeric``
+    evaluates it at every step (pulses.py:58-77 with ``integrate.simps``):
+    k = 1, the trapezoid; an odd number of samples, the composite rule over
+    pairs of intervals (h0, h1):
+        (h0 + h1)/6 [y0 (2 - h1/h0) + y1 (h0 + h1)^2/(h0 h1) + y2 (2 - h0/h1)];
+    an even number, the composite rule up to the last interval plus the
+    parabola through the last three samples integrated over the last interval
+    (Cartwright 2017):
+        (2 h1^2 + 3 h0 h1)/(6 (h0 + h1)) y2 + (h1^2 + 3 h0 h1)/(6 h0) y1
+        - h1^3/(6 h0 (h0 + h1)) y0.
+    All prefixes in O(n) (a running sum of the pair terms) instead of one
+    O(n) integral per step."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = len(x)
+    out = np.zeros(n)
+    if n < 2:
+        return out
+    h = np.diff(x)
+    out[1] = 0.5 * h[0] * (y[0] + y[1])
+    m = (n - 1) // 2  # whole pairs of intervals
+    if m == 0:
+        return out
+    h0, h1 = h[0 : 2 * m : 2], h[1 : 2 * m : 2]
+    hs, hp, q = h0 + h1, h0 * h1, h0 / h1
+    pair = hs / 6.0 * (y[0 : 2 * m : 2] * (2.0 - 1.0 / q) + y[1 : 2 * m : 2] * (hs * hs / hp) + y[2 : 2 * m + 1 : 2] * (2.0 - q))
+    cum = np.concatenate([[0.0], np.cumsum(pair)])
+    k = np.arange(2, n, 2)  # odd sample counts
+    out[k] = cum[k // 2]
+    k = np.arange(3, n, 2)  # even sample counts
+    a0, a1 = h[k - 2], h[k - 1]
+    alpha = (2 * a1 ** 2 + 3 * a0 * a1) / (6 * (a1 + a0))
+    beta = (a1 ** 2 + 3 * a0 * a1) / (6 * a0)
+    eta = a1 ** 3 / (6 * a0 * (a0 + a1))
+    out[k] = cum[(k - 1) // 2] + alpha * y[k] + beta * y[k - 1] - eta * y[k - 2]
+    return out
+
+
+def vector_potential_table(electric_potential, times):
+    """A(times[k]) for every k: minus the integral of E over times[:k+1], the
+    value the velocity-gauge operators take at step k (mesh_operators.py:
+    1186-1196, 371-380, with sims.py:195-196)."""
+    return -simpson_prefix_integrals(field_table(electric_potential, times), times)
+
+
 # --------------------------------------------------------------------------
 # masks (potentials/masks.py:11-113)
 # --------------------------------------------------------------------------

@@ -35,11 +35,14 @@ def product_spec(kind, params, **kw):
             internal_potential=potentials.SoftCoulombPotential(softening_distance=params["softening_distance"]),
             initial_state=states.GaussianState(width=params.get("gaussian_width", 1.0)),
             mask=potentials.AbsoluteRadialCosineMask(**params["mask"]),
-            operators=mesh.LineLengthGaugeOperators(),
+            operators=(mesh.LineVelocityGaugeOperators() if params.get("gauge", "length") == "velocity"
+                       else mesh.LineLengthGaugeOperators()),
             evolution_method=getattr(mesh, params["method"])(),
             **common,
         )
     if kind == "sh":
+        if params.get("gauge", "length") == "velocity":
+            common.setdefault("operators", mesh.SphericalHarmonicVelocityGaugeOperators())
         return mesh.SphericalHarmonicSpecification(
             "sh",
             r_points=params["r_points"],

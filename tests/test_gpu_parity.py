@@ -92,6 +92,10 @@ CASES = [
     ("sh", "sh_split_small_oddL"),
     ("sh", "sh_split_small_oddNr_oddL"),
     ("cyl", "cyl_adi_small"),
+    # velocity gauge (SphericalHarmonicVelocityGaugeOperators)
+    ("sh", "sh_velocity_small_evenL"),
+    ("sh", "sh_velocity_small_oddNr_oddL"),
+    ("sh", "sh_velocity_small_evenNr_oddL"),
 ]
 
 
