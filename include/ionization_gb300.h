@@ -281,7 +281,7 @@ typedef struct ion_line_sim {
     const float *zq32;
     const float *mask32;
     int32_t n_states;
-    int32_t pad_;
+    int32_t gauge;         /* ION_GAUGE_LENGTH, or ION_GAUGE_VELOCITY (ION_LINE_SPLIT, one CTA, see vcoef) */
     const double *state_g; /* [n_states*n*2] complex128 test states */
     double weight;         /* delta z */
     double *out_norm;      /* [n_data] */
@@ -295,6 +295,13 @@ typedef struct ion_line_sim {
     /* _c64 entry points with ION_LINE_RESIDUAL: the rounding residual of psi
      * (complex64 [n], psi = g + g_lo), or NULL */
     void *g_lo;
+    /* ION_GAUGE_VELOCITY (LineVelocityGaugeOperators, mesh_operators.py:352-427):
+     * the split operators are rotations [[cos, sin], [-sin, cos]] of the pairs
+     * (2k, 2k+1) (even) and (2k+1, 2k+2) (odd) by tau A vcoef, A = efield[t]
+     * the vector potential; per step even, odd, the Crank-Nicolson pair, odd,
+     * even.  vcoef = hbar (q/m) / (2 dz).  Runs in one CTA (cluster and
+     * residual plans leave such a line untouched). */
+    double vcoef;
 } ion_line_sim;
 
 typedef struct ion_line_plan {

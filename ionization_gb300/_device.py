@@ -332,6 +332,8 @@ class LineTables:
     vstat: Optional[np.ndarray] = None  # ION_LINE_FFT: static potential
     kin: Optional[np.ndarray] = None  # ION_LINE_FFT: kinetic energies in bit-reversed order
     twiddle: Optional[np.ndarray] = None  # ION_LINE_FFT: exp(-2 pi i m / n)
+    gauge: int = 0  # ION_GAUGE_VELOCITY: efield holds A(times[t]); vcoef = hbar (q/m) / (2 dz)
+    vcoef: float = 0.0
 
 
 def line_rows(precision) -> int:
@@ -432,6 +434,7 @@ class LineDeviceSim:
         d.out_norm, d.out_ip = ptr(self.d_norm), ptr(self.d_ip)
         d.vstat, d.kin, d.twiddle, d.vstat32 = ptr(self.d_vstat), ptr(self.d_kin), ptr(self.d_twiddle), ptr(self.d_vstat32)
         d.g_lo = ptr(self.g_lo)
+        d.gauge, d.vcoef = int(self.tab.gauge), float(self.tab.vcoef)
         return d
 
     def data(self):
@@ -473,8 +476,10 @@ class LineBatch:
     def _cluster_of(self, sim) -> int:
         if self._cta_max is None:
             self._cta_max = line_cta_max_n(self.precision)
-        # the Fourier split-step runs in one CTA (cluster plans skip it)
-        spread = 1 if sim.tab.method == nat.ION_LINE_FFT else self.spread
+        # the Fourier split-step and velocity-gauge lines run in one CTA
+        # (cluster plans skip them)
+        one_cta = sim.tab.method == nat.ION_LINE_FFT or sim.tab.gauge == nat.ION_GAUGE_VELOCITY
+        spread = 1 if one_cta else self.spread
         return line_cluster(sim.n, self.precision, self._cta_max, spread)
 
     @property

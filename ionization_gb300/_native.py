@@ -117,7 +117,7 @@ class LineSim(ctypes.Structure):
         ("zq32", c_vp),
         ("mask32", c_vp),
         ("n_states", c_i32),
-        ("pad_", c_i32),
+        ("gauge", c_i32),
         ("state_g", c_vp),
         ("weight", c_f64),
         ("out_norm", c_vp),
@@ -127,6 +127,7 @@ class LineSim(ctypes.Structure):
         ("twiddle", c_vp),
         ("vstat32", c_vp),
         ("g_lo", c_vp),
+        ("vcoef", c_f64),
     ]
 
 

@@ -279,6 +279,21 @@ __device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, 
     __syncthreads();
 }
 
+// The velocity gauge's split operator on a line held in shared memory: the
+// pairs (i, i+1) for i = parity, parity + 2, ... turn by [[cos, sin],
+// [-sin, cos]] (cm1 = cos - 1 for the increment form)
+template <typename R, int M>
+__device__ __forceinline__ void line_pair_rotations(Cx<R>* line, int n, int T, int parity, R cm1, R s) {
+    for (int i = parity + 2 * int(threadIdx.x); i + 1 < n; i += 2 * int(blockDim.x)) {
+        Cx<R>* p0 = line + islot<M>(i, T);
+        Cx<R>* p1 = line + islot<M>(i + 1, T);
+        const Cx<R> x0 = *p0, x1 = *p1;
+        *p0 = Cx<R>{x0.re + (cm1 * x0.re + s * x1.re), x0.im + (cm1 * x0.im + s * x1.im)};
+        *p1 = Cx<R>{x1.re + (cm1 * x1.re - s * x0.re), x1.im + (cm1 * x1.im - s * x0.im)};
+    }
+    __syncthreads();
+}
+
 // mode 0: up to n_steps steps (each followed by the reductions at a data
 // time), ending at t_final; mode 1: the reductions at t only
 template <typename R, int M>
@@ -313,7 +328,10 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     const LineTab<R> tb = LineTab<R>::make(S);
     const R tau = R(S.tau[t + 1]);
     const R ef = R(S.efield[t + 1]);
-    const bool split = S.method == ION_LINE_SPLIT;
+    const bool vel = S.gauge == ION_GAUGE_VELOCITY;  // ef is then A(t)
+    const bool split = S.method == ION_LINE_SPLIT && !vel;
+    R vcm1 = R(0), vs = R(0);
+    if (vel) rot_coeffs(R(S.tau[t + 1] * S.efield[t + 1] * S.vcoef), vcm1, vs);
 
 #pragma unroll
     for (int k = 0; k < M; ++k) {  // npad <= blockDim * M: loads issue together
@@ -327,9 +345,17 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
         line[islot<M>(i, T)] = x;
     }
     __syncthreads();
-    const LineCnCoef<R> coef{tb, tau, ef, !split, n};
+    if (vel) {
+        line_pair_rotations<R, M>(line, n, T, 0, vcm1, vs);
+        line_pair_rotations<R, M>(line, n, T, 1, vcm1, vs);
+    }
+    const LineCnCoef<R> coef{tb, tau, ef, S.method == ION_LINE_ADI, n};
     block_cn_solve<R, M>(T, threadIdx.x, R(2), line, red, coef, NoExtra{}, LineAddOut<R, M>{line, T});
     __syncthreads();
+    if (vel) {
+        line_pair_rotations<R, M>(line, n, T, 1, vcm1, vs);
+        line_pair_rotations<R, M>(line, n, T, 0, vcm1, vs);
+    }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         Cx<R>* p = line + islot<M>(i, T);
         Cx<R> x = *p;
@@ -557,7 +583,8 @@ __global__ void __launch_bounds__(512) line_cluster_kernel(ion_line_plan plan, i
     const int64_t t0 = S.t, tf = S.t_final;
     const int n = S.n;
     const int T = (n + C * M - 1) / (C * M);
-    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT) return;
+    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT || S.gauge != ION_GAUGE_LENGTH)
+        return;
     const int L = T * M, off = rank * L;
     Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* red = line + plan.threads * M;
@@ -825,7 +852,9 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     const int64_t t0 = S.t, tf = S.t_final;
     const int n = S.n;
     const int T = (n + C * M - 1) / (C * M);
-    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT || S.g_lo == nullptr) return;
+    if (n < 2 || n > plan.max_n || T > plan.threads || S.method == ION_LINE_FFT || S.g_lo == nullptr ||
+        S.gauge != ION_GAUGE_LENGTH)
+        return;
     const int L = T * M, off = rank * L;
     const int cap = plan.threads * M;
     Cx<float>* line = reinterpret_cast<Cx<float>*>(smem_raw);

@@ -20,6 +20,7 @@ from .mesh_operators import (  # noqa: F401
     DotOperator,
     KineticEnergyDerivation,
     LineLengthGaugeOperators,
+    LineVelocityGaugeOperators,
     MeshOperator,
     MeshOperators,
     SphericalHarmonicLengthGaugeOperators,

@@ -191,6 +191,30 @@ class LineLengthGaugeOperators(MeshOperators):
         )
 
 
+class LineVelocityGaugeOperators(LineLengthGaugeOperators):
+    """mesh_operators.py:352-427: the interaction is A(t) times the
+    antisymmetric nearest-neighbour coupling i hbar (q/m) / (2 dz); its split
+    operators are pair rotations.  ``gauge`` keeps the value the reference
+    class declares (mesh_operators.py:355)."""
+
+    gauge = core.Gauge.LENGTH
+
+    def velocity_coefficient(self, mesh):
+        """hbar (q/m) / (2 dz): the split angle is tau A times it."""
+        spec = mesh.spec
+        return float(u.hbar * (spec.test_charge / spec.test_mass) / (2 * mesh.delta_z))
+
+    @_memo
+    def interaction_hamiltonian_matrices_without_field(self, mesh):
+        off = 1j * self.velocity_coefficient(mesh) * np.ones(len(mesh.z_mesh) - 1, dtype=np.complex128)
+        return (sparse.diags((-off, off), offsets=(-1, 1)),)
+
+    def interaction_hamiltonian(self, mesh):
+        (m,) = self.interaction_hamiltonian_matrices_without_field(mesh)
+        A = mesh.spec.electric_potential.get_vector_potential_amplitude_numeric(mesh.sim.times_to_current)
+        return SumOfOperators(DotOperator(A * m, wrapping_direction=None))
+
+
 # --------------------------------------------------------------------------
 # spherical-harmonic mesh
 # --------------------------------------------------------------------------

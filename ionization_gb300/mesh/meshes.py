@@ -244,12 +244,21 @@ class LineMesh(QuantumMesh):
         self._tau_host = np.zeros(len(times))
         self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
         efield = np.zeros(len(times))
-        efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
+        gauge, vcoef = nat.ION_GAUGE_LENGTH, 0.0
+        if isinstance(self.operators, mo.LineVelocityGaugeOperators):
+            if kind != nat.ION_LINE_SPLIT:
+                raise exceptions.UnsupportedMesh("LineVelocityGaugeOperators have a device path with SplitInteractionOperator only")
+            if self.precision == core.Precision.C64X:
+                raise exceptions.UnsupportedMesh("LineVelocityGaugeOperators have no c64x (stored residual) form")
+            gauge, vcoef = nat.ION_GAUGE_VELOCITY, self.operators.velocity_coefficient(self)
+            efield[1:] = potentials.vector_potential_table(spec.electric_potential, times)[1:]
+        else:
+            efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
         test_g = np.array([self.get_g_for_state(s) for s in spec.test_states], dtype=np.complex128).reshape(-1, self.mesh_points)
         g0 = self.get_g_for_state(spec.initial_state)
         if not getattr(spec, "host_only", False):
             cta = dev.line_cta_max_n(self.precision)
-            maxn = cta if kind == nat.ION_LINE_FFT else cta * dev.LINE_MAX_CLUSTER
+            maxn = cta if kind == nat.ION_LINE_FFT or gauge == nat.ION_GAUGE_VELOCITY else cta * dev.LINE_MAX_CLUSTER
             if self.mesh_points > maxn:
                 raise exceptions.UnsupportedMesh(
                     f"line of {self.mesh_points} points exceeds the device limit {maxn} for {type(method).__name__}")
@@ -257,6 +266,7 @@ class LineMesh(QuantumMesh):
             n=self.mesh_points, method=kind, hd=hd, hoff=hoff, zq=zq, mask=mask, tau=self._tau_host.copy(),
             efield=efield, state_g=test_g, weight=self.inner_product_multiplier, g0=g0, t0=0,
             t_final=len(times) - 1, store_every=spec.store_data_every, vstat=vstat, kin=kin, twiddle=twiddle,
+            gauge=gauge, vcoef=vcoef,
         )
         if getattr(spec, "host_only", False):
             return

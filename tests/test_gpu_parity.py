@@ -96,6 +96,8 @@ CASES = [
     ("sh", "sh_velocity_small_evenL"),
     ("sh", "sh_velocity_small_oddNr_oddL"),
     ("sh", "sh_velocity_small_evenNr_oddL"),
+    ("line", "line_velocity_small"),  # LineVelocityGaugeOperators
+    ("line", "line_velocity_small_odd"),
 ]
 
 
@@ -131,7 +133,7 @@ def test_mesh_c64_population_error(cuda, kind, name):
     assert rel_l2(sim.mesh.g, z["g_final"]) < 1e-4
 
 
-@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] != "cyl"])
+@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] != "cyl" and not c[1].startswith("line_velocity")])
 def test_mesh_c64x_population_error(cuda, kind, name):
     """complex64 arithmetic with the state's rounding residual kept: the final
     population is within 1e-6 of the reference (the target of the complex64
