@@ -352,9 +352,17 @@ typedef struct ion_cyl_mesh {
     const double *mask;   /* [n_z*n_rho] or NULL */
     const double *tau;    /* indexed by time index */
     const double *efield; /* E(times[t]) indexed by time index */
+    /* [n_rho] or NULL.  When set, the off-diagonal of H_z between rows i and
+     * i+1 in column j is hz_off[i] * hz_off_col[j] * E(t): the interaction of
+     * the spherical-harmonic mesh under ADI (mesh_operators.py:1020-1035 with
+     * :988-1005), run on this kernel pair with z = l (hz_off = c_l,
+     * hz_off_col = -q r_j, hz_d and zq NULL) and rho = r (hr_d, hr_off = the
+     * radial H0). */
+    const double *hz_off_col;
 } ion_cyl_mesh;
 
-/* Advance psi from time index t0 by n_steps.  g_tmp is a psi-sized buffer. */
+/* Advance psi from time index t0 by n_steps.  g_tmp is a psi-sized buffer.
+ * hz_d and zq may be NULL (no such term). */
 int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t t0,
                          int64_t n_steps, void *stream);
 int64_t ion_cyl_max_points_c128(void);

@@ -155,6 +155,7 @@ class CylMesh(ctypes.Structure):
         ("mask", c_vp),
         ("tau", c_vp),
         ("efield", c_vp),
+        ("hz_off_col", c_vp),
     ]
 
 

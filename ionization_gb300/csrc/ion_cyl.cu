@@ -25,20 +25,32 @@ constexpr int CYL_MAX_T = 512;
 
 __host__ __device__ inline int cyl_threads(int n) { return (n + CYL_M - 1) / CYL_M; }
 
+// the optional diagonal terms: hz_d / hr_d and the field term 0.5 E zq
+__device__ __forceinline__ double cyl_field(const ion_cyl_mesh* m, int i, double hf) {
+    return m->zq ? hf * m->zq[i] : 0.0;
+}
+__device__ __forceinline__ double cyl_hz_d(const ion_cyl_mesh* m, int i, int j) {
+    return m->hz_d ? m->hz_d[int64_t(i) * m->n_rho + j] : 0.0;
+}
+// the z off-diagonal multiplier of column j (1, or hz_off_col[j] E)
+__device__ __forceinline__ double cyl_zcol(const ion_cyl_mesh* m, int j, double ef) {
+    return m->hz_off_col ? m->hz_off_col[j] * ef : 1.0;
+}
+
 // z column j: tau H_z and the H_rho stencil from global memory
 struct ZCoef {
     const ion_cyl_mesh* m;
     int j;
-    double tau, hf;  // hf = 0.5 * E
+    double tau, hf, zc;  // hf = 0.5 * E, zc = cyl_zcol(m, j, E)
     __device__ __forceinline__ void operator()(int i, double& bo, double& bd) const {
-        const int nz = m->n_z, nr = m->n_rho;
+        const int nz = m->n_z;
         if (i >= nz) {
             bo = 0.0;
             bd = 0.0;
             return;
         }
-        bd = tau * (m->hz_d[int64_t(i) * nr + j] + hf * m->zq[i]);
-        bo = (i < nz - 1) ? tau * m->hz_off[i] : 0.0;
+        bd = tau * (cyl_hz_d(m, i, j) + cyl_field(m, i, hf));
+        bo = (i < nz - 1) ? tau * (m->hz_off[i] * zc) : 0.0;
     }
 };
 
@@ -54,7 +66,7 @@ struct ZExtra {
         if (i >= nz) return Cx<double>{0.0, 0.0};
         const Cx<double>* row = g + int64_t(i) * nr;
         const Cx<double> p = line[islot<CYL_M>(i, T)];
-        const double hd = m->hr_d[int64_t(i) * nr + j] + hf * m->zq[i];
+        const double hd = m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, hf);
         Cx<double> v = {hd * p.re, hd * p.im};
         if (j > 0) {
             const Cx<double> q = ld(row + j - 1);
@@ -91,7 +103,8 @@ __global__ void __launch_bounds__(512) cyl_zpass_kernel(ion_cyl_mesh mesh, const
         line[islot<CYL_M>(i, T)] = (i < nz) ? ld(g + int64_t(i) * nr + j) : Cx<double>{0.0, 0.0};
     __syncthreads();
     const double tau = mesh.tau[tnext], hf = 0.5 * mesh.efield[tnext];
-    block_cn_solve<double, CYL_M>(T, threadIdx.x, 1.0, line, red, ZCoef{&mesh, j, tau, hf},
+    const double zc = cyl_zcol(&mesh, j, mesh.efield[tnext]);
+    block_cn_solve<double, CYL_M>(T, threadIdx.x, 1.0, line, red, ZCoef{&mesh, j, tau, hf, zc},
                                   ZExtra{&mesh, g, line, T, j, tau, hf}, CylAddOut{line, T});
     __syncthreads();
     for (int i = threadIdx.x; i < nz; i += blockDim.x) st(gout + int64_t(i) * nr + j, line[islot<CYL_M>(i, T)]);
@@ -109,7 +122,7 @@ struct RCoef {
             bd = 0.0;
             return;
         }
-        bd = tau * (m->hr_d[int64_t(i) * nr + j] + hf * m->zq[i]);
+        bd = tau * (m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, hf));
         bo = (j < nr - 1) ? tau * m->hr_off[j] : 0.0;
     }
 };
@@ -120,20 +133,21 @@ struct RExtra {
     const Cx<double>* down;  // row i+1
     const Cx<double>* line;  // row i (interleaved)
     int T, i;
-    double tau, hf;
+    double tau, hf, ef;
     template <typename R>
     __device__ __forceinline__ Cx<double> get(int j) const {
         const int nz = m->n_z, nr = m->n_rho;
         if (j >= nr) return Cx<double>{0.0, 0.0};
         const Cx<double> p = line[islot<CYL_M>(j, T)];
-        const double hd = m->hz_d[int64_t(i) * nr + j] + hf * m->zq[i];
+        const double hd = cyl_hz_d(m, i, j) + cyl_field(m, i, hf);
+        const double zc = cyl_zcol(m, j, ef);
         Cx<double> v = {hd * p.re, hd * p.im};
         if (i > 0) {
-            const double o = m->hz_off[i - 1];
+            const double o = m->hz_off[i - 1] * zc;
             v = Cx<double>{v.re + o * up[j].re, v.im + o * up[j].im};
         }
         if (i < nz - 1) {
-            const double o = m->hz_off[i];
+            const double o = m->hz_off[i] * zc;
             v = Cx<double>{v.re + o * down[j].re, v.im + o * down[j].im};
         }
         return Cx<double>{tau * v.re, tau * v.im};
@@ -161,7 +175,8 @@ __global__ void __launch_bounds__(512) cyl_rhopass_kernel(ion_cyl_mesh mesh, con
     __syncthreads();
     const double tau = mesh.tau[tnext], hf = 0.5 * mesh.efield[tnext];
     block_cn_solve<double, CYL_M>(T, threadIdx.x, 1.0, line, red, RCoef{&mesh, i, tau, hf},
-                                  RExtra{&mesh, up, down, line, T, i, tau, hf}, CylAddOut{line, T});
+                                  RExtra{&mesh, up, down, line, T, i, tau, hf, mesh.efield[tnext]},
+                                  CylAddOut{line, T});
     __syncthreads();
     for (int j = threadIdx.x; j < nr; j += blockDim.x) {
         Cx<double> x = line[islot<CYL_M>(j, T)];
@@ -179,8 +194,8 @@ static size_t rhopass_smem(int nr, int threads) {
 }
 
 static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int64_t n_steps, void* stream) {
-    if (!m || !g || !g_tmp || m->n_z < 2 || m->n_rho < 2 || n_steps < 0 || t0 < 0 || !m->hz_d || !m->hz_off ||
-        !m->hr_d || !m->hr_off || !m->zq || !m->tau || !m->efield) {
+    if (!m || !g || !g_tmp || m->n_z < 2 || m->n_rho < 2 || n_steps < 0 || t0 < 0 || !m->hz_off || !m->hr_d ||
+        !m->hr_off || !m->tau || !m->efield) {
         set_error("ion_cyl: invalid argument");
         return ION_ERR_INVALID_ARGUMENT;
     }

@@ -173,6 +173,51 @@ class QuantumMesh:
             self._tau_dev()[t_now] = tau
 
 
+class _AdiDevice:
+    """Device state of a mesh advanced by the two-direction ADI kernel pair
+    (``ion_cyl_adi_run_c128``: a pass implicit along the strided direction,
+    then one implicit along the contiguous one), with whole-mesh reductions
+    at data times.  Used by the cylindrical slice mesh (z, rho) and by the
+    spherical-harmonic mesh under AlternatingDirectionImplicit (l, r)."""
+
+    fused_data = False
+
+    def _adi_setup(self, n_strided, n_contig, arrays, g0, test_g):
+        """``arrays``: the ion_cyl_mesh tables by field name (FP64, or None)."""
+        f64 = np.float64
+        self._d = {k: (dev.to_dev(np.asarray(v).reshape(-1), f64) if v is not None else None) for k, v in arrays.items()}
+        self._g = dev.to_dev(np.asarray(g0, dtype=np.complex128))
+        self._gtmp = torch.empty_like(self._g)
+        cm = nat.CylMesh()
+        cm.n_z, cm.n_rho = int(n_strided), int(n_contig)
+        for k, v in self._d.items():
+            setattr(cm, k, dev.ptr(v))
+        self._cm = cm
+        self._reducer = dev.Reducer(self.mesh_points, test_g, self.inner_product_multiplier)
+        self._t = 0
+        times = self.sim.times
+        self.n_data = dev.n_data_slots(len(times) - 1, self.spec.store_data_every)
+        self._d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=dev.device())
+        self._d_ip = torch.full((self.n_data, max(len(test_g), 1), 2), float("nan"), dtype=torch.float64,
+                                device=dev.device())
+
+    def _adi_evolve_steps(self, n):
+        nat.call("ion_cyl_adi_run_c128", self._cm, dev.ptr(self._g), dev.ptr(self._gtmp), self._t, int(n),
+                 dev.stream_ptr())
+        self._t += int(n)
+
+    def _adi_reduce_current(self):
+        tf = len(self.sim.times) - 1
+        slot = dev.data_slot(self._t, tf, self.spec.store_data_every)
+        self._reducer(self._g, self._d_norm[slot:slot + 1], self._d_ip[slot])
+
+    def _adi_pull_data(self):
+        norm = self._d_norm.cpu().numpy()
+        ns = len(self.spec.test_states)
+        ip = self._d_ip.cpu().numpy()[:, :ns, :].copy().view(np.complex128)[..., 0]
+        return norm, ip.T.copy()
+
+
 # ==========================================================================
 # line
 # ==========================================================================
@@ -297,8 +342,9 @@ class LineMesh(QuantumMesh):
 # ==========================================================================
 
 
-class SphericalHarmonicMesh(QuantumMesh):
+class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
     mesh_storage_method = ("l", "r")
+    fused_data = True  # False under AlternatingDirectionImplicit
 
     def __init__(self, sim):
         super().__init__(sim)
@@ -366,8 +412,11 @@ class SphericalHarmonicMesh(QuantumMesh):
 
     def _init_device(self):
         spec, sim = self.spec, self.sim
+        self._adi = False
         if not isinstance(self.operators, mo.SphericalHarmonicLengthGaugeOperators):
             raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on SphericalHarmonicMesh")
+        if isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
+            return self._init_device_adi()
         if not isinstance(spec.evolution_method, em.SplitInteractionOperator):
             raise exceptions.UnsupportedMesh(
                 f"{type(spec.evolution_method).__name__} has no device path on SphericalHarmonicMesh"
@@ -415,11 +464,51 @@ class SphericalHarmonicMesh(QuantumMesh):
         self._dsim = dev.ShDeviceSim(self.tables, self.precision)
         self._batch = dev.ShBatch(self.precision, [self._dsim])
 
+    def _init_device_adi(self):
+        """AlternatingDirectionImplicit over total_hamiltonian
+        (evolution_methods.py:46-77, mesh_operators.py:1020-1035): per step
+        E(H0), I(H_int), E(H_int), I(H0), then the mask, with H0 the radial
+        Hamiltonian of each l and H_int = c_l (-q r_j) E(t + dt/2) between
+        l-neighbours at each r.  That is the cylindrical ADI step on the same
+        C-order layout with z = l (strided) and rho = r (contiguous), so it
+        runs on that kernel pair (complex128)."""
+        spec, sim = self.spec, self.sim
+        if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
+            raise exceptions.UnsupportedMesh("the velocity gauge's h2 is not tridiagonal: no ADI device path")
+        if self.precision != core.Precision.C128:
+            raise exceptions.UnsupportedMesh("the spherical-harmonic ADI device path is complex128")
+        self._adi = True
+        self.fused_data = False
+        nr, L = spec.r_points, spec.l_bound
+        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        if nr > cap or L > cap:
+            raise exceptions.UnsupportedMesh(f"mesh {L} x {nr} exceeds the ADI device limit {cap} per line")
+        tb = self.operators.device_tables(self)
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(
+            spec.electric_potential.get_electric_field_amplitude(times[1:] + (spec.time_step / 2)), np.float64
+        ) * np.ones(len(times) - 1)
+        mask = spec.mask(r=self.r)
+        mask = None if np.isscalar(mask) and mask == 1 else np.broadcast_to(
+            np.asarray(mask, dtype=np.float64) * np.ones(nr), (L, nr)).copy()
+        g0 = self.get_g_for_state(spec.initial_state)
+        test_g = np.array([self.get_g_for_state(s).reshape(-1) for s in spec.test_states], dtype=np.complex128)
+        arrays = dict(hz_d=None, hz_off=np.asarray(tb["cl"][: L - 1], dtype=np.float64), hr_d=tb["hd"],
+                      hr_off=tb["hoff"], zq=None, tau=self._tau_host, efield=efield, mask=mask,
+                      hz_off_col=tb["rq"])
+        self.tables = dict(arrays, g0=g0, state_g=test_g)
+        if getattr(spec, "host_only", False):
+            return
+        self._adi_setup(L, nr, arrays, g0, test_g)
+
     def _psi_device(self):
-        return self._dsim.g
+        return self._g if self._adi else self._dsim.g
 
     def _psi_residual(self):
-        return self._dsim.g_lo
+        return None if self._adi else self._dsim.g_lo
 
     def _sh_observables(self, radii=()):
         """(<r>, <z>, norm by l, norm within radii) in one device pass."""
@@ -465,16 +554,22 @@ class SphericalHarmonicMesh(QuantumMesh):
         return self._sh_observables(radii)[3]
 
     def _tau_dev(self):
-        return self._dsim.d_tau
+        return self._d["tau"] if self._adi else self._dsim.d_tau
 
     def _evolve_steps(self, n):
-        self._batch.run(n)
+        if self._adi:
+            self._adi_evolve_steps(n)
+        else:
+            self._batch.run(n)
 
     def _reduce_current(self):
-        self._batch.reduce()
+        if self._adi:
+            self._adi_reduce_current()
+        else:
+            self._batch.reduce()
 
     def _pull_data(self):
-        return self._dsim.data()
+        return self._adi_pull_data() if self._adi else self._dsim.data()
 
 
 # ==========================================================================
@@ -482,9 +577,8 @@ class SphericalHarmonicMesh(QuantumMesh):
 # ==========================================================================
 
 
-class CylindricalSliceMesh(QuantumMesh):
+class CylindricalSliceMesh(_AdiDevice, QuantumMesh):
     mesh_storage_method = ("z", "rho")
-    fused_data = False
 
     def __init__(self, sim):
         super().__init__(sim)
@@ -553,26 +647,9 @@ class CylindricalSliceMesh(QuantumMesh):
         self.tables = dict(tb, mask=mask, tau=self._tau_host.copy(), efield=efield, g0=g0, state_g=test_g)
         if getattr(spec, "host_only", False):
             return
-        f64 = np.float64
-        self._d = dict(
-            hz_d=dev.to_dev(tb["hz_d"], f64), hz_off=dev.to_dev(tb["hz_off"], f64),
-            hr_d=dev.to_dev(tb["hr_d"], f64), hr_off=dev.to_dev(tb["hr_off"], f64),
-            zq=dev.to_dev(tb["zq"], f64), tau=dev.to_dev(self._tau_host, f64), efield=dev.to_dev(efield, f64),
-            mask=dev.to_dev(mask.reshape(-1), f64) if mask is not None else None,
-        )
-        self._g = dev.to_dev(g0.astype(np.complex128))
-        self._gtmp = torch.empty_like(self._g)
-        cm = nat.CylMesh()
-        cm.n_z, cm.n_rho = spec.z_points, spec.rho_points
-        for k in ("hz_d", "hz_off", "hr_d", "hr_off", "zq", "mask", "tau", "efield"):
-            setattr(cm, k, dev.ptr(self._d[k]))
-        self._cm = cm
-        self._reducer = dev.Reducer(self.mesh_points, test_g, self.inner_product_multiplier)
-        self._t = 0
-        self.n_data = dev.n_data_slots(len(times) - 1, spec.store_data_every)
-        self._d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=dev.device())
-        self._d_ip = torch.full((self.n_data, max(len(test_g), 1), 2), float("nan"), dtype=torch.float64,
-                                device=dev.device())
+        self._adi_setup(spec.z_points, spec.rho_points, dict(
+            hz_d=tb["hz_d"], hz_off=tb["hz_off"], hr_d=tb["hr_d"], hr_off=tb["hr_off"], zq=tb["zq"],
+            tau=self._tau_host, efield=efield, mask=mask, hz_off_col=None), g0, test_g)
 
     def _psi_device(self):
         return self._g
@@ -581,17 +658,10 @@ class CylindricalSliceMesh(QuantumMesh):
         return self._d["tau"]
 
     def _evolve_steps(self, n):
-        nat.call("ion_cyl_adi_run_c128", self._cm, dev.ptr(self._g), dev.ptr(self._gtmp), self._t, int(n),
-                 dev.stream_ptr())
-        self._t += int(n)
+        self._adi_evolve_steps(n)
 
     def _reduce_current(self):
-        tf = len(self.sim.times) - 1
-        slot = dev.data_slot(self._t, tf, self.spec.store_data_every)
-        self._reducer(self._g, self._d_norm[slot:slot + 1], self._d_ip[slot])
+        self._adi_reduce_current()
 
     def _pull_data(self):
-        norm = self._d_norm.cpu().numpy()
-        ns = len(self.spec.test_states)
-        ip = self._d_ip.cpu().numpy()[:, :ns, :].copy().view(np.complex128)[..., 0]
-        return norm, ip.T.copy()
+        return self._adi_pull_data()

@@ -386,6 +386,29 @@ class SphericalHarmonicSplit:
         self.g = g
 
 
+class SphericalHarmonicADI(SphericalHarmonicSplit):
+    """SphericalHarmonicMesh with SphericalHarmonicLengthGaugeOperators and
+    AlternatingDirectionImplicit (evolution_methods.py:46-77): the operators of
+    total_hamiltonian (mesh_operators.py:1020-1035) are the radial H0 ("r",
+    C order) and the l-coupling interaction ("l", F order, field at
+    t + time_step / 2), taken explicit, implicit, explicit, implicit over
+    [H0, H_int, H_int, H0]; then the mask."""
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        efield = self.pulse.field(t_now + (self.time_step / 2))
+        off = self.l_off * efield
+        hint = Tridiag(off, np.zeros(self.M, dtype=np.complex128), off.copy(), "F")
+        g = self.g
+        g = apply_explicit(self.H0.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(hint.scaled_plus_identity(1j * tau), g, self.shape)
+        g = apply_explicit(hint.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(self.H0.scaled_plus_identity(1j * tau), g, self.shape)
+        if self.mask is not None:
+            g = g * self.mask
+        self.g = g
+
+
 class SphericalHarmonicVelocity(SphericalHarmonicSplit):
     """SphericalHarmonicMesh with SphericalHarmonicVelocityGaugeOperators
     (mesh_operators.py:1130-1408) and SplitInteractionOperator: per step
@@ -565,6 +588,8 @@ def build_from_params(kind, params):
         )
     if kind == "sh":
         cls = SphericalHarmonicVelocity if params.get("gauge", "length") == "velocity" else SphericalHarmonicSplit
+        if params.get("method", "SplitInteractionOperator") == "AlternatingDirectionImplicit":
+            cls = SphericalHarmonicADI
         return cls(
             params["r_points"], params["r_bound"], params["l_bound"], pulse, params.get("mask"),
             [tuple(s) for s in params["test_states"]], params["time_step"],

@@ -23,6 +23,8 @@ Cases (reference call sites in parentheses):
                    (even and odd z_points) runs in the velocity gauge
                    (SphericalHarmonicVelocityGaugeOperators,
                    LineVelocityGaugeOperators) with SplitInteractionOperator
+  sh_adi_small_*   SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators
+                   + AlternatingDirectionImplicit (even L; odd Nr and odd L)
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
                    RExpectationValue, NormWithinRadius and (SH)
                    NormBySphericalHarmonic datastores
@@ -230,7 +232,8 @@ def gen_line(ion, full=False):
         save("line_cfg1_full", params, out)
 
 
-def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3, gauge="length"):
+def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3, gauge="length",
+            method="SplitInteractionOperator"):
     from ionization import states
 
     r_bound = 0.125 * (r_points - 1)
@@ -251,6 +254,8 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
     )
     if gauge != "length":
         params["gauge"] = gauge
+    if method != "SplitInteractionOperator":
+        params["method"] = method
     spec = ion.mesh.SphericalHarmonicSpecification(
         name,
         r_points=r_points,
@@ -266,7 +271,7 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
         time_step=dt,
         operators=(ion.mesh.SphericalHarmonicVelocityGaugeOperators() if gauge == "velocity"
                    else ion.mesh.SphericalHarmonicLengthGaugeOperators()),
-        evolution_method=ion.mesh.SplitInteractionOperator(),
+        evolution_method=getattr(ion.mesh, method)(),
         store_data_every=store_every,
     )
     return spec, params
@@ -307,6 +312,19 @@ def gen_velocity(ion):
             ion, name, nz, 40.0, 400, 0.05, _pulse_kwargs(0.1, 0.5, 2, 0.3), "SplitInteractionOperator",
             dict(inner_radius=30.0, outer_radius=40.0, smoothness=8), 50, gauge="velocity",
         )
+        _, out = run_and_collect(spec)
+        save(name, params, out)
+
+
+def gen_sh_adi(ion):
+    """SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators with
+    AlternatingDirectionImplicit (evolution_methods.py:46-77 over
+    total_hamiltonian, mesh_operators.py:1020-1035): the radial H0 and the
+    l-coupling interaction alternate explicit / implicit halves."""
+    fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+    for name, nr, L in (("sh_adi_small_evenL", 160, 8), ("sh_adi_small_oddNr_oddL", 151, 7)):
+        spec, params = sh_spec(ion, name, nr, L, 500, 0.02, fast_pulse, 5.0, 50,
+                               method="AlternatingDirectionImplicit")
         _, out = run_and_collect(spec)
         save(name, params, out)
 
@@ -419,7 +437,7 @@ def gen_observables(ion):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -428,7 +446,7 @@ def main():
     from loader import import_reference
 
     ion = import_reference(args.ref)
-    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel"}
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -441,6 +459,8 @@ def main():
         gen_observables(ion)
     if "vel" in only:
         gen_velocity(ion)
+    if "shadi" in only:
+        gen_sh_adi(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

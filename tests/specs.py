@@ -43,6 +43,8 @@ def product_spec(kind, params, **kw):
     if kind == "sh":
         if params.get("gauge", "length") == "velocity":
             common.setdefault("operators", mesh.SphericalHarmonicVelocityGaugeOperators())
+        if "method" in params:
+            common.setdefault("evolution_method", getattr(mesh, params["method"])())
         return mesh.SphericalHarmonicSpecification(
             "sh",
             r_points=params["r_points"],

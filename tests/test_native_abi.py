@@ -54,4 +54,38 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(nat.ShPlan) == 8 + 4 * 4 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 16 * 4
     assert nat.ShSim.g.offset == 0 and nat.ShSim.t.offset == 16
     assert nat.LineSim.t.offset == 16
-    assert ctypes.sizeof(nat.CylMesh) == 8 + 8 * 8
+    assert ctypes.sizeof(nat.CylMesh) == 8 + 9 * 8
+
+
+def test_struct_offsets_match_the_c_compiler(tmp_path):
+    """Every field of every ctypes mirror sits where the C compiler puts the
+    header's field of the same name (sizes too)."""
+    import shutil
+    import subprocess
+
+    from ionization_gb300 import _native as nat
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"ion_sh_sim": nat.ShSim, "ion_sh_plan": nat.ShPlan, "ion_line_sim": nat.LineSim,
+               "ion_line_plan": nat.LinePlan, "ion_cyl_mesh": nat.CylMesh}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ionization_gb300.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    seen = 0
+    for line in filter(None, out):
+        cname, fname, value = line.split()
+        py = mirrors[cname]
+        got = ctypes.sizeof(py) if fname == "sizeof" else getattr(py, fname).offset
+        assert got == int(value), f"{cname}.{fname}: ctypes {got}, C {value}"
+        seen += 1
+    assert seen == sum(len(p._fields_) + 1 for p in mirrors.values())

@@ -48,6 +48,9 @@ CASES = [
     ("sh", "sh_velocity_small_evenNr_oddL"),
     ("line", "line_velocity_small"),
     ("line", "line_velocity_small_odd"),
+    # SphericalHarmonicMesh with AlternatingDirectionImplicit
+    ("sh", "sh_adi_small_evenL"),
+    ("sh", "sh_adi_small_oddNr_oddL"),
 ]
 
 
