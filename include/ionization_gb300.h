@@ -359,7 +359,15 @@ typedef struct ion_cyl_mesh {
      * hz_off_col = -q r_j, hz_d and zq NULL) and rho = r (hr_d, hr_off = the
      * radial H0). */
     const double *hz_off_col;
+    /* ION_ADI_STRIDED_FIRST (0): per step E(H_rho), I(H_z), E(H_z), I(H_rho)
+     * (the cylinder, whose kinetic operators come rho first); ION_ADI_CONTIG_FIRST:
+     * E(H_z), I(H_rho), E(H_rho), I(H_z) (the rectangle mesh, z first,
+     * mesh_operators.py:436-437).  The mask follows the step's last pass. */
+    int32_t order;
+    int32_t pad_;
 } ion_cyl_mesh;
+
+enum { ION_ADI_STRIDED_FIRST = 0, ION_ADI_CONTIG_FIRST = 1 };
 
 /* Advance psi from time index t0 by n_steps.  g_tmp is a psi-sized buffer.
  * hz_d and zq may be NULL (no such term). */

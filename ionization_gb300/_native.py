@@ -27,6 +27,8 @@ ION_SH_REFINE = 1
 ION_SH_VELOCITY = 2
 ION_SH_ONLY_VELOCITY = 4
 ION_GAUGE_LENGTH = 0
+ION_ADI_STRIDED_FIRST = 0
+ION_ADI_CONTIG_FIRST = 1
 ION_GAUGE_VELOCITY = 1
 ION_LINE_RESIDUAL = 1
 
@@ -156,6 +158,8 @@ class CylMesh(ctypes.Structure):
         ("tau", c_vp),
         ("efield", c_vp),
         ("hz_off_col", c_vp),
+        ("order", c_i32),
+        ("pad_", c_i32),
     ]
 
 

@@ -92,7 +92,7 @@ struct CylAddOut {
 };
 
 __global__ void __launch_bounds__(512) cyl_zpass_kernel(ion_cyl_mesh mesh, const Cx<double>* g,
-                                                        Cx<double>* gout, int64_t tnext, int bthreads) {
+                                                        Cx<double>* gout, int64_t tnext, int bthreads, int do_mask) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int j = blockIdx.x;
     const int nz = mesh.n_z, nr = mesh.n_rho;
@@ -107,7 +107,14 @@ __global__ void __launch_bounds__(512) cyl_zpass_kernel(ion_cyl_mesh mesh, const
     block_cn_solve<double, CYL_M>(T, threadIdx.x, 1.0, line, red, ZCoef{&mesh, j, tau, hf, zc},
                                   ZExtra{&mesh, g, line, T, j, tau, hf}, CylAddOut{line, T});
     __syncthreads();
-    for (int i = threadIdx.x; i < nz; i += blockDim.x) st(gout + int64_t(i) * nr + j, line[islot<CYL_M>(i, T)]);
+    for (int i = threadIdx.x; i < nz; i += blockDim.x) {
+        Cx<double> x = line[islot<CYL_M>(i, T)];
+        if (do_mask && mesh.mask) {
+            const double mk = mesh.mask[int64_t(i) * nr + j];
+            x = Cx<double>{x.re * mk, x.im * mk};
+        }
+        st(gout + int64_t(i) * nr + j, x);
+    }
 }
 
 // rho row i: tau H_rho and the H_z stencil from the staged neighbour rows
@@ -155,7 +162,7 @@ struct RExtra {
 };
 
 __global__ void __launch_bounds__(512) cyl_rhopass_kernel(ion_cyl_mesh mesh, const Cx<double>* gin, Cx<double>* g,
-                                                          int64_t tnext, int bthreads) {
+                                                          int64_t tnext, int bthreads, int do_mask) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int i = blockIdx.x;
     const int nz = mesh.n_z, nr = mesh.n_rho;
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(512) cyl_rhopass_kernel(ion_cyl_mesh mesh, con
     __syncthreads();
     for (int j = threadIdx.x; j < nr; j += blockDim.x) {
         Cx<double> x = line[islot<CYL_M>(j, T)];
-        if (mesh.mask) {
+        if (do_mask && mesh.mask) {
             const double mk = mesh.mask[int64_t(i) * nr + j];
             x = Cx<double>{x.re * mk, x.im * mk};
         }
@@ -195,7 +202,7 @@ static size_t rhopass_smem(int nr, int threads) {
 
 static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int64_t n_steps, void* stream) {
     if (!m || !g || !g_tmp || m->n_z < 2 || m->n_rho < 2 || n_steps < 0 || t0 < 0 || !m->hz_off || !m->hr_d ||
-        !m->hr_off || !m->tau || !m->efield) {
+        !m->hr_off || !m->tau || !m->efield || (m->order != ION_ADI_STRIDED_FIRST && m->order != ION_ADI_CONTIG_FIRST)) {
         set_error("ion_cyl: invalid argument");
         return ION_ERR_INVALID_ARGUMENT;
     }
@@ -214,12 +221,20 @@ static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int6
     cudaStream_t s = as_stream(stream);
     auto* gg = static_cast<Cx<double>*>(g);
     auto* gt = static_cast<Cx<double>*>(g_tmp);
+    const bool contig_first = m->order == ION_ADI_CONTIG_FIRST;
     for (int64_t k = 0; k < n_steps; ++k) {
         const int64_t tn = t0 + k + 1;
-        cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gg, gt, tn, bz);
-        if (int e = check_launch("cyl_zpass_kernel")) return e;
-        cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gt, gg, tn, br);
-        if (int e = check_launch("cyl_rhopass_kernel")) return e;
+        if (contig_first) {  // E(H_z) I(H_rho), then E(H_rho) I(H_z) and the mask
+            cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gg, gt, tn, br, 0);
+            if (int e = check_launch("cyl_rhopass_kernel")) return e;
+            cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gt, gg, tn, bz, 1);
+            if (int e = check_launch("cyl_zpass_kernel")) return e;
+        } else {  // E(H_rho) I(H_z), then E(H_z) I(H_rho) and the mask
+            cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gg, gt, tn, bz, 0);
+            if (int e = check_launch("cyl_zpass_kernel")) return e;
+            cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gt, gg, tn, br, 1);
+            if (int e = check_launch("cyl_rhopass_kernel")) return e;
+        }
     }
     return ION_OK;
 }

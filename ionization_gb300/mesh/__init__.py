@@ -23,6 +23,7 @@ from .mesh_operators import (  # noqa: F401
     LineVelocityGaugeOperators,
     MeshOperator,
     MeshOperators,
+    RectangleLengthGaugeOperators,
     SphericalHarmonicLengthGaugeOperators,
     SphericalHarmonicVelocityGaugeOperators,
     SumOfOperators,
@@ -30,12 +31,20 @@ from .mesh_operators import (  # noqa: F401
     add_to_diagonal_sparse_matrix_diagonal,
     apply_operators_sequentially,
 )
-from .meshes import CylindricalSliceMesh, LineMesh, QuantumMesh, SphericalHarmonicMesh, WrappingDirection  # noqa: F401
+from .meshes import (  # noqa: F401
+    CylindricalSliceMesh,
+    LineMesh,
+    QuantumMesh,
+    RectangleMesh,
+    SphericalHarmonicMesh,
+    WrappingDirection,
+)
 from .sims import (  # noqa: F401
     CylindricalSliceSpecification,
     LineSpecification,
     MeshSimulation,
     MeshSpecification,
+    RectangleSpecification,
     SphericalHarmonicSimulation,
     SphericalHarmonicSpecification,
 )

@@ -372,6 +372,31 @@ class SphericalHarmonicVelocityGaugeOperators(SphericalHarmonicLengthGaugeOperat
 # --------------------------------------------------------------------------
 
 
+class RectangleLengthGaugeOperators(MeshOperators):
+    """mesh_operators.py:430-505: kinetic energies along z then x (uniform
+    second differences), half of the internal potential and half of
+    -z q E(t) on each diagonal (mesh_operators.py:244-298)."""
+
+    gauge = core.Gauge.LENGTH
+
+    @_memo
+    def device_tables(self, mesh):
+        """Diagonals of the internal H_z and H_x in C order of the (z, x) mesh,
+        their (uniform) off-diagonals, and zq = -z * test_charge."""
+        spec = mesh.spec
+        nz, nx = spec.z_points, spec.x_points
+        m = spec.test_mass
+        pz = -(u.hbar ** 2) / (2 * m * (mesh.delta_z ** 2))
+        px = -(u.hbar ** 2) / (2 * m * (mesh.delta_x ** 2))
+        V = np.asarray(spec.internal_potential(r=mesh.r_mesh, z=mesh.z_mesh, x=mesh.x_mesh, test_charge=spec.test_charge),
+                       dtype=np.float64) * np.ones((nz, nx))
+        hz_d = (pz * (-2) + 0.5 * V).reshape(-1)
+        hr_d = (px * (-2) + 0.5 * V).reshape(-1)
+        zq = -mesh.z * spec.test_charge
+        return dict(hz_d=hz_d, hz_off=pz * np.ones(nz - 1), hr_d=hr_d, hr_off=px * np.ones(nx - 1),
+                    zq=np.asarray(zq, dtype=np.float64))
+
+
 class CylindricalSliceLengthGaugeOperators(MeshOperators):
     """mesh_operators.py:550-640."""
 

@@ -573,6 +573,104 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
 
 
 # ==========================================================================
+# rectangle
+# ==========================================================================
+
+
+class RectangleMesh(_AdiDevice, QuantumMesh):
+    """RectangleMesh (meshes.py:430-506): psi on (z, x), x contiguous.  Under
+    AlternatingDirectionImplicit each step is E(H_z), I(H_x), E(H_x), I(H_z),
+    then the mask: the two-direction ADI kernel pair with z strided, x
+    contiguous, the contiguous pass first (complex128)."""
+
+    mesh_storage_method = ("z", "x")
+
+    def __init__(self, sim):
+        super().__init__(sim)
+        self.z = np.linspace(-self.spec.z_bound, self.spec.z_bound, self.spec.z_points)
+        self.x = np.linspace(-self.spec.x_bound, self.spec.x_bound, self.spec.x_points)
+        self.delta_z = np.abs(self.z[1] - self.z[0])
+        self.delta_x = np.abs(self.x[1] - self.x[0])
+        self.inner_product_multiplier = self.delta_z * self.delta_x
+        self.g_factor = 1
+        self.z_center_index = int(self.spec.z_points // 2)
+        self.x_center_index = int(self.spec.x_points // 2)
+        self.z_mesh, self.x_mesh = np.meshgrid(self.z, self.x, indexing="ij")
+        self.r_mesh = np.sqrt((self.z_mesh ** 2) + (self.x_mesh ** 2))
+        self.mesh_points = len(self.z) * len(self.x)
+        self.mesh_shape = np.shape(self.r_mesh)
+        self._state_g_cache = {}
+        self._init_device()
+
+    @property
+    def theta_mesh(self):
+        return np.arctan2(self.x_mesh, self.z_mesh)
+
+    def wrapping_direction_to_order(self, wrapping_direction):
+        if wrapping_direction is None:
+            return None
+        if wrapping_direction == WrappingDirection.Z:
+            return "F"
+        if wrapping_direction == WrappingDirection.X:
+            return "C"
+        raise ValueError(f"{wrapping_direction} is not a valid specifier for flatten_mesh (valid specifiers: 'z', 'x')")
+
+    def get_g_for_state(self, state):
+        """meshes.py:487-493."""
+        if state in self._state_g_cache:
+            return self._state_g_cache[state]
+        g = np.asarray(state(self.r_mesh, self.theta_mesh), dtype=np.complex128)
+        g = g / np.sqrt(np.sum(np.conj(g) * g).real * self.inner_product_multiplier)
+        g = g * state.amplitude
+        self._state_g_cache[state] = g
+        return g
+
+    def _init_device(self):
+        spec, sim = self.spec, self.sim
+        if not isinstance(self.operators, mo.RectangleLengthGaugeOperators):
+            raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on RectangleMesh")
+        if not isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
+            raise exceptions.UnsupportedMesh(f"{type(spec.evolution_method).__name__} has no device path on RectangleMesh")
+        if self.precision != core.Precision.C128:
+            raise exceptions.UnsupportedMesh("the rectangle device path is complex128")
+        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        if spec.z_points > cap or spec.x_points > cap:
+            raise exceptions.UnsupportedMesh(f"mesh {spec.z_points} x {spec.x_points} exceeds {cap} points per line")
+        tb = self.operators.device_tables(self)
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
+        mask = spec.mask(r=self.r_mesh)
+        mask = None if np.isscalar(mask) and mask == 1 else np.asarray(mask, np.float64) * np.ones(self.mesh_shape)
+        g0 = self.get_g_for_state(spec.initial_state)
+        test_g = np.array([self.get_g_for_state(s).reshape(-1) for s in spec.test_states], dtype=np.complex128)
+        arrays = dict(hz_d=tb["hz_d"], hz_off=tb["hz_off"], hr_d=tb["hr_d"], hr_off=tb["hr_off"], zq=tb["zq"],
+                      tau=self._tau_host, efield=efield, mask=mask, hz_off_col=None)
+        self.tables = dict(arrays, g0=g0, state_g=test_g)
+        if getattr(spec, "host_only", False):
+            return
+        self._adi_setup(spec.z_points, spec.x_points, arrays, g0, test_g)
+        self._cm.order = nat.ION_ADI_CONTIG_FIRST
+
+    def _psi_device(self):
+        return self._g
+
+    def _tau_dev(self):
+        return self._d["tau"]
+
+    def _evolve_steps(self, n):
+        self._adi_evolve_steps(n)
+
+    def _reduce_current(self):
+        self._adi_reduce_current()
+
+    def _pull_data(self):
+        return self._adi_pull_data()
+
+
+# ==========================================================================
 # cylindrical slice
 # ==========================================================================
 

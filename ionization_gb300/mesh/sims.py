@@ -369,6 +369,34 @@ class SphericalHarmonicSpecification(MeshSpecification):
         self.numeric_eigenstate_max_energy = numeric_eigenstate_max_energy
 
 
+class RectangleSpecification(MeshSpecification):
+    """sims.py:765-833."""
+
+    mesh_type = meshes.RectangleMesh
+
+    def __init__(
+        self,
+        name,
+        internal_potential=potentials.NoPotentialEnergy(),
+        initial_state=None,
+        z_bound: float = 10 * u.nm,
+        z_points: int = 2 ** 9,
+        x_bound: float = 10 * u.nm,
+        x_points: int = 2 ** 9,
+        operators=mesh_operators.RectangleLengthGaugeOperators(),
+        evolution_method=evolution_methods.AlternatingDirectionImplicit(),
+        **kwargs,
+    ):
+        if initial_state is None:
+            initial_state = states.TwoDGaussianWavepacket()
+        super().__init__(name, internal_potential=internal_potential, initial_state=initial_state,
+                         operators=operators, evolution_method=evolution_method, **kwargs)
+        self.z_bound = z_bound
+        self.z_points = int(z_points)
+        self.x_bound = x_bound
+        self.x_points = int(x_points)
+
+
 class CylindricalSliceSpecification(MeshSpecification):
     mesh_type = meshes.CylindricalSliceMesh
 

@@ -202,3 +202,46 @@ class GaussianState(QuantumState):
 
     def __repr__(self):
         return f"GaussianState(width = {self.width}, center = {self.center})"
+
+
+class TwoDGaussianWavepacket(QuantumState):
+    """A free 2D Gaussian wavepacket in (z, x) (states/two_d.py:259-315):
+    exp(-(z - z0)^2 / (2 wz^2)) exp(-(x - x0)^2 / (2 wx^2)) exp(i (kz z + kx x))
+    / (sqrt(2 pi) sqrt(wz wx)), evaluated at (r, theta) as z = r cos theta,
+    x = r sin theta."""
+
+    eigenvalues = Eigenvalues.CONTINUOUS
+    binding = Binding.FREE
+    derivation = Derivation.ANALYTIC
+
+    def __init__(self, center_z=0, center_x=0, width_z=1 * u.nm, width_x=1 * u.nm, k_z=0, k_x=0,
+                 mass=u.electron_mass, amplitude=1):
+        if width_z <= 0:
+            raise exceptions.InvalidQuantumStateParameter("width_z must be positive")
+        if width_x <= 0:
+            raise exceptions.InvalidQuantumStateParameter("width_x must be positive")
+        self.center_z, self.center_x = center_z, center_x
+        self.width_z, self.width_x = width_z, width_x
+        self.k_z, self.k_x = k_z, k_x
+        self.mass = mass
+        super().__init__(amplitude=amplitude)
+
+    @property
+    def tuple(self):
+        return self.center_z, self.center_x, self.width_z, self.width_x
+
+    def eval_z_x(self, z, x):
+        norm = 1 / (np.sqrt(u.twopi) * np.sqrt(self.width_z * self.width_x))
+        gaussian = np.exp(-0.5 * (((z - self.center_z) / self.width_z) ** 2)) * np.exp(
+            -0.5 * (((x - self.center_x) / self.width_x) ** 2))
+        return norm * gaussian * (np.exp(1j * self.k_z * z) * np.exp(1j * self.k_x * x))
+
+    def eval_r_theta(self, r, theta):
+        return self.eval_z_x(r * np.cos(theta), r * np.sin(theta))
+
+    def __call__(self, r, theta):
+        return self.eval_r_theta(r, theta)
+
+    def __repr__(self):
+        return (f"TwoDGaussianWavepacket(center_z = {self.center_z}, center_x = {self.center_x}, width_z = "
+                f"{self.width_z}, width_x = {self.width_x}, k_z = {self.k_z}, k_x = {self.k_x})")

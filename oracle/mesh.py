@@ -567,6 +567,80 @@ class CylindricalSliceADI:
 # builders from fixture parameter dicts
 # --------------------------------------------------------------------------
 
+# --------------------------------------------------------------------------
+# rectangle mesh, length gauge, ADI
+# --------------------------------------------------------------------------
+
+class RectangleADI:
+    """RectangleMesh (meshes.py:430-506) with RectangleLengthGaugeOperators
+    (mesh_operators.py:430-505) and AlternatingDirectionImplicit
+    (evolution_methods.py:46-77): kinetic energies along z ("z", F order) and
+    x ("x", C order), in that order, each with half the internal potential
+    (mesh_operators.py:244-269) and half of -z q E(t_{n+1})
+    (mesh_operators.py:271-298); steps E(H_z), I(H_x), E(H_x), I(H_z), then
+    the mask.  The initial state is TwoDGaussianWavepacket (states/two_d.py:
+    259-315) evaluated through (r, theta = arctan2(x, z)) as
+    RectangleMesh.get_g_for_state does."""
+
+    def __init__(self, z_points, z_bound, x_points, x_bound, softening_distance, pulse, mask, state,
+                 test_mass=ph.ELECTRON_MASS_REDUCED):
+        self.z = np.linspace(-z_bound, z_bound, z_points)
+        self.x = np.linspace(-x_bound, x_bound, x_points)
+        self.dz, self.dx = abs(self.z[1] - self.z[0]), abs(self.x[1] - self.x[0])
+        self.shape = (z_points, x_points)
+        self.M = z_points * x_points
+        self.pulse = pulse
+        z_mesh, x_mesh = np.meshgrid(self.z, self.x, indexing="ij")
+        self.z_mesh, self.x_mesh = z_mesh, x_mesh
+        self.r_mesh = np.sqrt(z_mesh ** 2 + x_mesh ** 2)
+        self.theta_mesh = np.arctan2(x_mesh, z_mesh)
+        self.mask = ph.radial_cosine_mask(self.r_mesh, **mask) if mask is not None else None
+        V = ph.soft_coulomb(self.r_mesh, softening_distance)
+        self.H = []
+        for n_dir, d, order in ((z_points, self.dz, "F"), (x_points, self.dx, "C")):
+            p = -(ph.HBAR ** 2) / (2 * test_mass * d ** 2)
+            diag = -2 * p * np.ones(self.M, dtype=np.complex128)
+            kk = np.arange(self.M - 1)
+            off = p * np.where((kk + 1) % n_dir != 0, 1.0, 0.0).astype(np.complex128)
+            self.H.append(Tridiag(off, diag + 0.5 * V.flatten(order), off.copy(), order))
+        self.zq = {o: (-ph.ELECTRON_CHARGE * z_mesh).flatten(o) for o in ("F", "C")}
+        g = self._state(state)
+        self.g = g
+        self.test_g = [g.copy()]
+
+    def _state(self, st):
+        cz, cx, wz, wx, kz, kx = st
+        z = self.r_mesh * np.cos(self.theta_mesh)
+        x = self.r_mesh * np.sin(self.theta_mesh)
+        norm = 1 / (np.sqrt(ph.TWOPI) * np.sqrt(wz * wx))
+        g = norm * np.exp(-0.5 * (((z - cz) / wz) ** 2)) * np.exp(-0.5 * (((x - cx) / wx) ** 2)) \
+            * (np.exp(1j * kz * z) * np.exp(1j * kx * x))
+        return g / np.sqrt(self._norm(g))
+
+    def _norm(self, g):
+        return (np.sum(np.conj(g) * g) * self.dz * self.dx).real
+
+    def norm(self):
+        return self._norm(self.g)
+
+    def inner_products(self):
+        return [np.sum(np.conj(s) * self.g) * self.dz * self.dx for s in self.test_g]
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        E = self.pulse.field(t_now)
+        ops = [Tridiag(h.sub, h.diag + 0.5 * self.zq[h.order] * E, h.sup, h.order) for h in self.H]
+        hz, hx = ops
+        g = self.g
+        g = apply_explicit(hz.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(hx.scaled_plus_identity(1j * tau), g, self.shape)
+        g = apply_explicit(hx.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(hz.scaled_plus_identity(1j * tau), g, self.shape)
+        if self.mask is not None:
+            g = g * self.mask
+        self.g = g
+
+
 def pulse_from_params(p):
     return ph.CosSquaredPulse(
         amplitude=p["amplitude"],
@@ -593,6 +667,13 @@ def build_from_params(kind, params):
         return cls(
             params["r_points"], params["r_bound"], params["l_bound"], pulse, params.get("mask"),
             [tuple(s) for s in params["test_states"]], params["time_step"],
+        )
+    if kind == "rect":
+        st = (params["center_z"], params["center_x"], params["width_z"], params["width_x"], params["k_z"],
+              params.get("k_x", 0.0))
+        return RectangleADI(
+            params["z_points"], params["z_bound"], params["x_points"], params["x_bound"],
+            params["softening_distance"], pulse, params.get("mask"), st,
         )
     if kind == "cyl":
         return CylindricalSliceADI(

@@ -25,6 +25,7 @@ Cases (reference call sites in parentheses):
                    LineVelocityGaugeOperators) with SplitInteractionOperator
   sh_adi_small_*   SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators
                    + AlternatingDirectionImplicit (even L; odd Nr and odd L)
+  rect_adi_small*  RectangleMesh + RectangleLengthGaugeOperators + ADI (96 x 80; 81 x 64)
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
                    RExpectationValue, NormWithinRadius and (SH)
                    NormBySphericalHarmonic datastores
@@ -329,6 +330,32 @@ def gen_sh_adi(ion):
         save(name, params, out)
 
 
+def gen_rect(ion):
+    """RectangleMesh + RectangleLengthGaugeOperators + ADI (meshes.py:430-506,
+    mesh_operators.py:430-505): kinetic energies along z (F order) and x
+    (C order) in that order, soft-Coulomb V(r) and -z q E(t) split evenly
+    between them; a TwoDGaussianWavepacket initial state."""
+    from ionization import states
+
+    pulse = _pulse_kwargs(0.1, 0.5, 2, 0.3)
+    for name, nz, nx in (("rect_adi_small", 96, 80), ("rect_adi_small_odd", 81, 64)):
+        params = dict(z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0, time_initial=0.0, time_final=20.0,
+                      time_step=0.05, softening_distance=float(np.sqrt(2)), width_z=1.0, width_x=1.5,
+                      center_z=0.5, center_x=-0.25, k_z=0.3, pulse=pulse,
+                      mask=dict(inner_radius=12.0, outer_radius=16.0, smoothness=8), store_data_every=50)
+        init = states.TwoDGaussianWavepacket(center_z=0.5, center_x=-0.25, width_z=1.0, width_x=1.5, k_z=0.3)
+        spec = ion.mesh.RectangleSpecification(
+            name, z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0,
+            internal_potential=ion.potentials.SoftCoulombPotential(softening_distance=np.sqrt(2)),
+            initial_state=init, test_states=[init],
+            electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+            mask=ion.potentials.RadialCosineMask(inner_radius=12.0, outer_radius=16.0, smoothness=8),
+            time_initial=0.0, time_final=20.0, time_step=0.05, store_data_every=50,
+        )
+        _, out = run_and_collect(spec)
+        save(name, params, out)
+
+
 def cyl_spec(ion, name, z_points, z_bound, rho_points, rho_bound, steps, dt, pulse, store_every):
     from ionization import states
 
@@ -437,7 +464,7 @@ def gen_observables(ion):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -446,7 +473,7 @@ def main():
     from loader import import_reference
 
     ion = import_reference(args.ref)
-    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi"}
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -461,6 +488,8 @@ def main():
         gen_velocity(ion)
     if "shadi" in only:
         gen_sh_adi(ion)
+    if "rect" in only:
+        gen_rect(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

@@ -56,6 +56,22 @@ def product_spec(kind, params, **kw):
             mask=potentials.RadialCosineMask(**params["mask"]),
             **common,
         )
+    if kind == "rect":
+        init = states.TwoDGaussianWavepacket(center_z=params["center_z"], center_x=params["center_x"],
+                                             width_z=params["width_z"], width_x=params["width_x"],
+                                             k_z=params["k_z"], k_x=params.get("k_x", 0.0))
+        return mesh.RectangleSpecification(
+            "rect",
+            z_points=params["z_points"],
+            z_bound=params["z_bound"],
+            x_points=params["x_points"],
+            x_bound=params["x_bound"],
+            internal_potential=potentials.SoftCoulombPotential(softening_distance=params["softening_distance"]),
+            initial_state=init,
+            test_states=[init],
+            mask=potentials.RadialCosineMask(**params["mask"]),
+            **common,
+        )
     if kind == "cyl":
         return mesh.CylindricalSliceSpecification(
             "cyl",

@@ -101,6 +101,9 @@ CASES = [
     # SphericalHarmonicMesh with AlternatingDirectionImplicit (complex128)
     ("sh", "sh_adi_small_evenL"),
     ("sh", "sh_adi_small_oddNr_oddL"),
+    # RectangleMesh with AlternatingDirectionImplicit (complex128)
+    ("rect", "rect_adi_small"),
+    ("rect", "rect_adi_small_odd"),
 ]
 
 
@@ -121,7 +124,7 @@ def test_mesh_c128_matches_reference(cuda, kind, name):
     _check_against_golden(sim, z)
 
 
-COMPLEX64_CASES = [c for c in CASES if c[0] != "cyl" and not c[1].startswith("sh_adi")]
+COMPLEX64_CASES = [c for c in CASES if c[0] not in ("cyl", "rect") and not c[1].startswith("sh_adi")]
 
 
 @pytest.mark.parametrize("kind,name", COMPLEX64_CASES)

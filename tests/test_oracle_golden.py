@@ -51,6 +51,9 @@ CASES = [
     # SphericalHarmonicMesh with AlternatingDirectionImplicit
     ("sh", "sh_adi_small_evenL"),
     ("sh", "sh_adi_small_oddNr_oddL"),
+    # RectangleMesh with AlternatingDirectionImplicit
+    ("rect", "rect_adi_small"),
+    ("rect", "rect_adi_small_odd"),
 ]
 
 
