@@ -376,6 +376,30 @@ int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t
 int64_t ion_cyl_max_points_c128(void);
 
 /* ------------------------------------------------------------------------
+ * Eigenpairs of batched real symmetric tridiagonal matrices: the numeric
+ * eigenstate basis (SphericalHarmonicMesh.get_numeric_eigenstate_basis,
+ * meshes.py:1281-1356, and LineMesh._get_numeric_eigenstate_basis,
+ * meshes.py:343-387, which call scipy's eigsh on each single-l Hamiltonian).
+ * n_mat matrices of order n >= 2: diag [n_mat*n], off [n_mat*(n-1)], device.
+ *   ion_tridiag_count_below: counts[m] = number of eigenvalues of matrix m
+ *     below x[m] (Sturm sequence);
+ *   ion_tridiag_eigvals: vals[r] = the req_idx[r]-th smallest eigenvalue
+ *     (0-based) of matrix req_mat[r], by bisection to the last bits of FP64;
+ *   ion_tridiag_eigvecs: vecs[r*n ...] = the eigenvector of matrix req_mat[r]
+ *     for eigenvalue vals[r], by inverse iteration (partial pivoting, two
+ *     solves from a fixed start), unit 2-norm, sign such that its first
+ *     component above 1e-3 of the largest is positive; scratch holds
+ *     ion_tridiag_eig_scratch_doubles(n, n_req) doubles.
+ * ------------------------------------------------------------------------ */
+int64_t ion_tridiag_eig_scratch_doubles(int32_t n, int32_t n_req);
+int ion_tridiag_count_below(int32_t n_mat, int32_t n, const double *diag, const double *off, const double *x,
+                            int32_t *counts, void *stream);
+int ion_tridiag_eigvals(int32_t n_mat, int32_t n, const double *diag, const double *off, int32_t n_req,
+                        const int32_t *req_mat, const int32_t *req_idx, double *vals, void *stream);
+int ion_tridiag_eigvecs(int32_t n_mat, int32_t n, const double *diag, const double *off, int32_t n_req,
+                        const int32_t *req_mat, const double *vals, double *vecs, double *scratch, void *stream);
+
+/* ------------------------------------------------------------------------
  * Norm and inner products on a whole mesh (QuantumMesh.norm / inner_product,
  * meshes.py:195-217):  norm = weight * sum |g|^2,
  * ip[s] = weight * sum conj(states[s]) g, in FP64 with a compensated

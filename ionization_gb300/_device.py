@@ -537,6 +537,49 @@ class LineBatch:
 
 
 # ==========================================================================
+# batched symmetric tridiagonal eigenpairs (numeric eigenstate bases)
+# ==========================================================================
+
+
+def tridiagonal_eigenpairs(diags: np.ndarray, offs: np.ndarray, max_value: float, max_count: int):
+    """All eigenpairs with eigenvalue below ``max_value`` (at most
+    ``max_count`` per matrix, the smallest) of each real symmetric tridiagonal
+    matrix (rows of ``diags`` [n_mat, n], ``offs`` [n_mat, n-1]), on the
+    device: Sturm counts, bisection, inverse iteration.  Returns a list of
+    (values ascending, vectors [k, n] of unit 2-norm) per matrix."""
+    diags = np.ascontiguousarray(diags, dtype=np.float64)
+    offs = np.ascontiguousarray(offs, dtype=np.float64)
+    n_mat, n = diags.shape
+    d_d, d_o = to_dev(diags.reshape(-1)), to_dev(offs.reshape(-1))
+    d_x = to_dev(np.full(n_mat, float(max_value)))
+    d_cnt = torch.zeros(n_mat, dtype=torch.int32, device=device())
+    sp = stream_ptr()
+    nat.call("ion_tridiag_count_below", n_mat, n, ptr(d_d), ptr(d_o), ptr(d_x), ptr(d_cnt), sp)
+    counts = np.minimum(d_cnt.cpu().numpy(), int(max_count))
+    req_mat = np.concatenate([np.full(c, m, np.int32) for m, c in enumerate(counts)] + [np.zeros(0, np.int32)])
+    req_idx = np.concatenate([np.arange(c, dtype=np.int32) for c in counts] + [np.zeros(0, np.int32)])
+    n_req = len(req_mat)
+    out = [(np.zeros(0), np.zeros((0, n))) for _ in range(n_mat)]
+    if n_req == 0:
+        return out
+    d_rm, d_ri = to_dev(req_mat), to_dev(req_idx)
+    d_vals = torch.empty(n_req, dtype=torch.float64, device=device())
+    nat.call("ion_tridiag_eigvals", n_mat, n, ptr(d_d), ptr(d_o), n_req, ptr(d_rm), ptr(d_ri), ptr(d_vals), sp)
+    d_vecs = torch.empty(n_req * n, dtype=torch.float64, device=device())
+    d_scr = torch.empty(int(nat.value("ion_tridiag_eig_scratch_doubles", n, n_req)), dtype=torch.float64,
+                        device=device())
+    nat.call("ion_tridiag_eigvecs", n_mat, n, ptr(d_d), ptr(d_o), n_req, ptr(d_rm), ptr(d_vals), ptr(d_vecs),
+             ptr(d_scr), sp)
+    vals = d_vals.cpu().numpy()
+    vecs = d_vecs.cpu().numpy().reshape(n_req, n)
+    start = 0
+    for m, c in enumerate(counts):
+        out[m] = (vals[start:start + c].copy(), vecs[start:start + c].copy())
+        start += c
+    return out
+
+
+# ==========================================================================
 # whole-mesh reductions
 # ==========================================================================
 

@@ -293,6 +293,24 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
         return dict(hd=hd, hoff=hoff, rq=np.asarray(rq, dtype=np.float64), cl=cl, kinv=kinv, cent=cent,
                     corr0=float(corr0))
 
+    def single_l_hamiltonian(self, mesh, l):
+        """(diagonal, off-diagonal) of internal_hamiltonian_for_single_l
+        (mesh_operators.py:942-986): the Lagrangian radial kinetic energy of
+        one l, its centrifugal term, and V(r), in the reference's order."""
+        spec = mesh.spec
+        nr = spec.r_points
+        mu = u.electron_mass_reduced
+        p = -(u.hbar ** 2) / (2 * mu * (mesh.delta_r ** 2))
+        eff = ((u.hbar ** 2) / (2 * mu)) * l * (l + 1) / (mesh.r ** 2)
+        beta = self.beta(np.arange(nr, dtype=np.complex128))
+        if l == 0 and self.hydrogen_zero_angular_momentum_correction:
+            dr = mesh.delta_r / u.bohr_radius
+            beta[0] += dr * (1 + dr) / 8
+        diag = (-2 * p * beta) + eff
+        off = p * self.alpha(np.arange(nr - 1, dtype=np.complex128))
+        V = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge))
+        return (diag + V).real.astype(np.float64), off.real.astype(np.float64)
+
     @_memo
     def internal_hamiltonian(self, mesh):
         t = self.device_tables(mesh)

@@ -358,7 +358,46 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         self.l_mesh, self.r_mesh = np.meshgrid(self.l, self.r, indexing="ij")
         self.mesh_shape = np.shape(self.r_mesh)
         self._radial_cache = {}
+        if self.spec.use_numeric_eigenstates:  # meshes.py:1021-1033
+            self.analytic_to_numeric = self.get_numeric_eigenstate_basis(
+                self.spec.numeric_eigenstate_max_energy, self.spec.numeric_eigenstate_max_angular_momentum)
+            self.spec.test_states = sorted(self.analytic_to_numeric.values(), key=lambda x: x.energy)
+            if not self.spec.initial_state.numeric:
+                self.spec.initial_state = self.analytic_to_numeric[self.spec.initial_state]
         self._init_device()
+
+    def get_numeric_eigenstate_basis(self, max_energy, max_angular_momentum):
+        """meshes.py:1281-1356: for each l <= max_angular_momentum the
+        eigenpairs of the single-l Hamiltonian with energy <= max_energy (at
+        most r_points - 2, the smallest), normalised on the mesh and divided by
+        the g factor, labelled by the analytic state they approximate (bound:
+        HydrogenBoundState(n = int(sqrt(rydberg / |E|)), l); free:
+        HydrogenCoulombState(E, l)).  The reference takes them from scipy's
+        eigsh on each matrix in turn; here all l are solved together on the
+        device (batched Sturm bisection and inverse iteration).  Eigenvectors
+        are real with a fixed sign; the reference's carry an arbitrary phase."""
+        L = int(max_angular_momentum) + 1
+        mats = [self.operators.single_l_hamiltonian(self, l) for l in range(L)]
+        nr = self.spec.r_points
+        pairs = dev.tridiagonal_eigenpairs(np.array([m[0] for m in mats]), np.array([m[1] for m in mats]),
+                                           max_energy, nr - 2)
+        basis = {}
+        for l, (vals, vecs) in enumerate(pairs):
+            for energy, v in zip(vals, vecs):
+                v = v / np.sqrt(self.inner_product_multiplier * np.sum(np.abs(v) ** 2))
+                v = v / self.g_factor
+                if energy > max_energy:
+                    continue
+                if energy > 0:
+                    analytic = states.HydrogenCoulombState(energy=energy, l=l)
+                    binding = states.Binding.FREE
+                else:
+                    n_guess = max(1, int(np.sqrt(u.rydberg / np.abs(energy))))
+                    analytic = states.HydrogenBoundState(n=n_guess, l=l)
+                    binding = states.Binding.BOUND
+                basis[analytic] = states.NumericSphericalHarmonicState(
+                    g=v, l=l, m=0, energy=energy, corresponding_analytic_state=analytic, binding=binding)
+        return basis
 
     @property
     def g_factor(self):
@@ -390,6 +429,8 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
             raise NotImplementedError(
                 "States with non-definite angular momentum components are not currently supported by SphericalHarmonicMesh"
             )
+        if state.analytic and getattr(self.spec, "use_numeric_eigenstates", False):
+            state = getattr(self, "analytic_to_numeric", {}).get(state, state)
         g = np.zeros(self.mesh_shape, dtype=np.complex128)
         for s in state:
             g[s.l, :] += self.get_radial_g_for_state(s)

@@ -349,22 +349,18 @@ class SphericalHarmonicSpecification(MeshSpecification):
         theta_points: int = 180,
         operators=mesh_operators.SphericalHarmonicLengthGaugeOperators(),
         evolution_method=evolution_methods.SplitInteractionOperator(),
-        use_numeric_eigenstates: bool = False,
+        use_numeric_eigenstates: bool = True,
         numeric_eigenstate_max_energy: float = 20 * u.eV,
         numeric_eigenstate_max_angular_momentum: int = 5,
         **kwargs,
     ):
-        if use_numeric_eigenstates:
-            raise exceptions.UnsupportedMesh(
-                "numeric eigenstates are not part of the device path; pass use_numeric_eigenstates=False"
-            )
         super().__init__(name, operators=operators, evolution_method=evolution_method, **kwargs)
         self.r_bound = r_bound
         self.r_points = int(r_points)
         self.l_bound = int(l_bound)
         self.spherical_harmonics = tuple(core.SphericalHarmonic(l, 0) for l in range(self.l_bound))
         self.theta_points = theta_points
-        self.use_numeric_eigenstates = False
+        self.use_numeric_eigenstates = bool(use_numeric_eigenstates)
         self.numeric_eigenstate_max_angular_momentum = min(self.l_bound - 1, numeric_eigenstate_max_angular_momentum)
         self.numeric_eigenstate_max_energy = numeric_eigenstate_max_energy
 

@@ -180,6 +180,78 @@ class HydrogenBoundState(SphericalHarmonicState):
         return self.amplitude * normalization * r_dep * lag_poly
 
 
+def electron_wavenumber_from_energy(energy):
+    """core.py:19-20."""
+    return np.sqrt(2 * u.electron_mass * np.abs(energy)) / u.hbar
+
+
+class HydrogenCoulombState(SphericalHarmonicState):
+    """A hydrogen free state labelled by its energy (states/three_d.py:414-470);
+    here it names the free numeric eigenstates."""
+
+    eigenvalues = Eigenvalues.CONTINUOUS
+    binding = Binding.FREE
+    derivation = Derivation.ANALYTIC
+
+    def __init__(self, energy=1 * u.eV, l=0, m=0, amplitude=1.0):
+        if energy < 0:
+            raise exceptions.IllegalQuantumState("energy must be greater than zero")
+        self.energy = energy
+        super().__init__(l=l, m=m, amplitude=amplitude)
+
+    @property
+    def wavenumber(self):
+        return electron_wavenumber_from_energy(self.energy)
+
+    @property
+    def tuple(self):
+        return self.wavenumber, self.l, self.m, self.energy
+
+    def radial_function(self, r):
+        raise NotImplementedError("Coulomb radial functions are not evaluated here; use the numeric eigenbasis")
+
+    def __repr__(self):
+        return f"HydrogenCoulombState(energy = {self.energy}, l = {self.l}, m = {self.m})"
+
+
+class NumericSphericalHarmonicState(SphericalHarmonicState):
+    """A numerically derived radial state (states/three_d.py:543-630): its
+    radial function is the stored vector ``g``, labelled by the analytic
+    state it approximates."""
+
+    eigenvalues = Eigenvalues.DISCRETE
+    derivation = Derivation.NUMERIC
+
+    def __init__(self, *, g, l=0, m=0, energy, corresponding_analytic_state, binding, amplitude=1):
+        self.g = g
+        self.energy = energy
+        self.corresponding_analytic_state = corresponding_analytic_state
+        self.binding = binding
+        super().__init__(l=l, m=m, amplitude=amplitude)
+
+    @property
+    def n(self):
+        return self.corresponding_analytic_state.n
+
+    @property
+    def wavenumber(self):
+        return self.corresponding_analytic_state.wavenumber
+
+    @property
+    def tuple(self):
+        return self.corresponding_analytic_state.tuple
+
+    def radial_function(self, r):
+        return self.g
+
+    def __repr__(self):
+        return repr(self.corresponding_analytic_state) + "_n"
+
+    @property
+    def ket(self):
+        return self.corresponding_analytic_state.ket + "_n"
+
+
 class GaussianState(QuantumState):
     """exp(-(z - center)^2 / (2 width^2)), normalised on the mesh when
     projected (a 1D bound wavepacket; user-state extension)."""

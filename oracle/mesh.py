@@ -641,6 +641,47 @@ class RectangleADI:
         self.g = g
 
 
+# --------------------------------------------------------------------------
+# numeric eigenstate basis
+# --------------------------------------------------------------------------
+
+def single_l_hamiltonian(r_points, r_bound, l):
+    """internal_hamiltonian_for_single_l with the Lagrangian kinetic energy
+    (mesh_operators.py:942-986): (diagonal, off-diagonal), real."""
+    r = np.linspace(0, r_bound, r_points)
+    dr = r[1] - r[0]
+    r = r + dr / 2
+    mu = ph.ELECTRON_MASS_REDUCED
+    p = -(ph.HBAR ** 2) / (2 * mu * (dr ** 2))
+    eff = ((ph.HBAR ** 2) / (2 * mu)) * l * (l + 1) / (r ** 2)
+    beta = _beta(np.arange(r_points, dtype=np.complex128))
+    if l == 0:
+        d = dr / ph.BOHR_RADIUS
+        beta[0] += d * (1 + d) / 8
+    diag = (-2 * p * beta) + eff + ph.coulomb(r)
+    off = p * _alpha(np.arange(r_points - 1, dtype=np.complex128))
+    return diag.real, off.real, r, dr
+
+
+def numeric_eigenbasis(r_points, r_bound, max_energy, max_l):
+    """get_numeric_eigenstate_basis (meshes.py:1281-1356) with LAPACK's
+    tridiagonal eigensolver in place of eigsh: per l, the eigenpairs with
+    energy <= max_energy (at most r_points - 2, the smallest), each vector
+    normalised on the mesh (dr sum |v|^2 = 1).  Returns [(l, energy, v)]
+    sorted by energy; the vectors' signs are arbitrary."""
+    from scipy.linalg import eigh_tridiagonal
+
+    out = []
+    for l in range(max_l + 1):
+        d, e, r, dr = single_l_hamiltonian(r_points, r_bound, l)
+        w, v = eigh_tridiagonal(d, e, select="v", select_range=(-np.inf, max_energy))
+        w, v = w[: r_points - 2], v[:, : r_points - 2]
+        for k in range(len(w)):
+            vec = v[:, k] / np.sqrt(dr * np.sum(np.abs(v[:, k]) ** 2))
+            out.append((l, w[k], vec))
+    return sorted(out, key=lambda x: x[1])
+
+
 def pulse_from_params(p):
     return ph.CosSquaredPulse(
         amplitude=p["amplitude"],

@@ -26,6 +26,8 @@ Cases (reference call sites in parentheses):
   sh_adi_small_*   SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators
                    + AlternatingDirectionImplicit (even L; odd Nr and odd L)
   rect_adi_small*  RectangleMesh + RectangleLengthGaugeOperators + ADI (96 x 80; 81 x 64)
+  sh_numeric_small SH run with use_numeric_eigenstates=True (test states, initial
+                   state from eigsh; energies, l and radial vectors recorded)
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
                    RExpectationValue, NormWithinRadius and (SH)
                    NormBySphericalHarmonic datastores
@@ -330,6 +332,40 @@ def gen_sh_adi(ion):
         save(name, params, out)
 
 
+def gen_numeric(ion):
+    """SphericalHarmonicSpecification with use_numeric_eigenstates=True
+    (meshes.py:1021-1033, 1281-1356): the test states and the initial state
+    become numeric eigenstates of each single-l Hamiltonian found by eigsh.
+    Records each numeric state's energy, l and radial vector (as the mesh
+    uses it), with the run's data."""
+    from ionization import states
+
+    fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+    nr, L, steps, dt = 300, 6, 300, 0.02
+    r_bound = 0.125 * (nr - 1)
+    r_max = r_bound + 0.125 / 2
+    mask = dict(inner_radius=r_max - 5.0, outer_radius=r_max, smoothness=8)
+    params = dict(r_points=nr, r_bound=r_bound, l_bound=L, time_initial=0.0, time_final=steps * dt,
+                  time_step=dt, pulse=fast_pulse, mask=mask, store_data_every=50,
+                  numeric_eigenstate_max_energy=2.0, numeric_eigenstate_max_angular_momentum=3)
+    spec = ion.mesh.SphericalHarmonicSpecification(
+        "sh_numeric_small", r_points=nr, r_bound=r_bound, l_bound=L, use_numeric_eigenstates=True,
+        numeric_eigenstate_max_energy=2.0, numeric_eigenstate_max_angular_momentum=3,
+        initial_state=states.HydrogenBoundState(1, 0),
+        electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**fast_pulse),
+        mask=ion.potentials.RadialCosineMask(**mask), time_initial=0.0, time_final=steps * dt, time_step=dt,
+        operators=ion.mesh.SphericalHarmonicLengthGaugeOperators(),
+        evolution_method=ion.mesh.SplitInteractionOperator(), store_data_every=50,
+    )
+    sim, out = run_and_collect(spec)
+    ts = list(sim.spec.test_states)
+    out["numeric_energy"] = np.array([s.energy for s in ts])
+    out["numeric_l"] = np.array([s.l for s in ts])
+    out["numeric_bound"] = np.array([s.binding == states.Binding.BOUND for s in ts])
+    out["numeric_g"] = np.array([sim.mesh.get_radial_g_for_state(s) for s in ts])
+    save("sh_numeric_small", params, out)
+
+
 def gen_rect(ion):
     """RectangleMesh + RectangleLengthGaugeOperators + ADI (meshes.py:430-506,
     mesh_operators.py:430-505): kinetic energies along z (F order) and x
@@ -464,7 +500,7 @@ def gen_observables(ion):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -473,7 +509,8 @@ def main():
     from loader import import_reference
 
     ion = import_reference(args.ref)
-    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect"}
+    only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect",
+                                                        "num"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -490,6 +527,8 @@ def main():
         gen_sh_adi(ion)
     if "rect" in only:
         gen_rect(ion)
+    if "num" in only:
+        gen_numeric(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

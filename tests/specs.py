@@ -50,9 +50,9 @@ def product_spec(kind, params, **kw):
             r_points=params["r_points"],
             r_bound=params["r_bound"],
             l_bound=params["l_bound"],
-            use_numeric_eigenstates=False,
+            use_numeric_eigenstates=common.pop("use_numeric_eigenstates", False),
             initial_state=states.HydrogenBoundState(1, 0),
-            test_states=[states.HydrogenBoundState(n, l) for n, l in params["test_states"]],
+            test_states=[states.HydrogenBoundState(n, l) for n, l in params.get("test_states", [[1, 0]])],
             mask=potentials.RadialCosineMask(**params["mask"]),
             **common,
         )
