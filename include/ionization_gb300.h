@@ -365,6 +365,13 @@ typedef struct ion_cyl_mesh {
      * mesh_operators.py:436-437).  The mask follows the step's last pass. */
     int32_t order;
     int32_t pad_;
+    /* [n_z] or NULL: the rho off-diagonal of row i is hr_off[j] * hr_off_row[i]
+     * (the spherical slice's theta operator, whose coupling scales as
+     * 1/(j_r + 1/2)^2 along r) */
+    const double *hr_off_row;
+    /* [n_z*n_rho] or NULL: when set, the field term of point (i, j) is
+     * 0.5 E zq_pt[i*n_rho + j] instead of 0.5 E zq[i] (z varies along both axes) */
+    const double *zq_pt;
 } ion_cyl_mesh;
 
 enum { ION_ADI_STRIDED_FIRST = 0, ION_ADI_CONTIG_FIRST = 1 };

@@ -160,6 +160,8 @@ class CylMesh(ctypes.Structure):
         ("hz_off_col", c_vp),
         ("order", c_i32),
         ("pad_", c_i32),
+        ("hr_off_row", c_vp),
+        ("zq_pt", c_vp),
     ]
 
 

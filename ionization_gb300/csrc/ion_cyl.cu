@@ -26,8 +26,13 @@ constexpr int CYL_MAX_T = 512;
 __host__ __device__ inline int cyl_threads(int n) { return (n + CYL_M - 1) / CYL_M; }
 
 // the optional diagonal terms: hz_d / hr_d and the field term 0.5 E zq
-__device__ __forceinline__ double cyl_field(const ion_cyl_mesh* m, int i, double hf) {
+__device__ __forceinline__ double cyl_field(const ion_cyl_mesh* m, int i, int j, double hf) {
+    if (m->zq_pt) return hf * m->zq_pt[int64_t(i) * m->n_rho + j];
     return m->zq ? hf * m->zq[i] : 0.0;
+}
+// the rho off-diagonal multiplier of row i
+__device__ __forceinline__ double cyl_rrow(const ion_cyl_mesh* m, int i) {
+    return m->hr_off_row ? m->hr_off_row[i] : 1.0;
 }
 __device__ __forceinline__ double cyl_hz_d(const ion_cyl_mesh* m, int i, int j) {
     return m->hz_d ? m->hz_d[int64_t(i) * m->n_rho + j] : 0.0;
@@ -49,7 +54,7 @@ struct ZCoef {
             bd = 0.0;
             return;
         }
-        bd = tau * (cyl_hz_d(m, i, j) + cyl_field(m, i, hf));
+        bd = tau * (cyl_hz_d(m, i, j) + cyl_field(m, i, j, hf));
         bo = (i < nz - 1) ? tau * (m->hz_off[i] * zc) : 0.0;
     }
 };
@@ -66,16 +71,17 @@ struct ZExtra {
         if (i >= nz) return Cx<double>{0.0, 0.0};
         const Cx<double>* row = g + int64_t(i) * nr;
         const Cx<double> p = line[islot<CYL_M>(i, T)];
-        const double hd = m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, hf);
+        const double hd = m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, j, hf);
+        const double rr = cyl_rrow(m, i);
         Cx<double> v = {hd * p.re, hd * p.im};
         if (j > 0) {
             const Cx<double> q = ld(row + j - 1);
-            const double o = m->hr_off[j - 1];
+            const double o = m->hr_off[j - 1] * rr;
             v = Cx<double>{v.re + o * q.re, v.im + o * q.im};
         }
         if (j < nr - 1) {
             const Cx<double> q = ld(row + j + 1);
-            const double o = m->hr_off[j];
+            const double o = m->hr_off[j] * rr;
             v = Cx<double>{v.re + o * q.re, v.im + o * q.im};
         }
         return Cx<double>{tau * v.re, tau * v.im};
@@ -129,8 +135,8 @@ struct RCoef {
             bd = 0.0;
             return;
         }
-        bd = tau * (m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, hf));
-        bo = (j < nr - 1) ? tau * m->hr_off[j] : 0.0;
+        bd = tau * (m->hr_d[int64_t(i) * nr + j] + cyl_field(m, i, j, hf));
+        bo = (j < nr - 1) ? tau * (m->hr_off[j] * cyl_rrow(m, i)) : 0.0;
     }
 };
 
@@ -146,7 +152,7 @@ struct RExtra {
         const int nz = m->n_z, nr = m->n_rho;
         if (j >= nr) return Cx<double>{0.0, 0.0};
         const Cx<double> p = line[islot<CYL_M>(j, T)];
-        const double hd = cyl_hz_d(m, i, j) + cyl_field(m, i, hf);
+        const double hd = cyl_hz_d(m, i, j) + cyl_field(m, i, j, hf);
         const double zc = cyl_zcol(m, j, ef);
         Cx<double> v = {hd * p.re, hd * p.im};
         if (i > 0) {

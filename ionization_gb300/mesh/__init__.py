@@ -26,6 +26,7 @@ from .mesh_operators import (  # noqa: F401
     RectangleLengthGaugeOperators,
     SphericalHarmonicLengthGaugeOperators,
     SphericalHarmonicVelocityGaugeOperators,
+    SphericalSliceLengthGaugeOperators,
     SumOfOperators,
     TDMAOperator,
     add_to_diagonal_sparse_matrix_diagonal,
@@ -37,6 +38,7 @@ from .meshes import (  # noqa: F401
     QuantumMesh,
     RectangleMesh,
     SphericalHarmonicMesh,
+    SphericalSliceMesh,
     WrappingDirection,
 )
 from .sims import (  # noqa: F401
@@ -47,4 +49,5 @@ from .sims import (  # noqa: F401
     RectangleSpecification,
     SphericalHarmonicSimulation,
     SphericalHarmonicSpecification,
+    SphericalSliceSpecification,
 )

@@ -415,6 +415,46 @@ class RectangleLengthGaugeOperators(MeshOperators):
                     zq=np.asarray(zq, dtype=np.float64))
 
 
+class SphericalSliceLengthGaugeOperators(MeshOperators):
+    """mesh_operators.py:693-813: kinetic energies along theta (a
+    non-symmetric tridiagonal) then r, half of the internal potential and
+    half of -z q E(t) on each diagonal.  ``gauge`` keeps the value the
+    reference class declares (mesh_operators.py:696)."""
+
+    gauge = core.Gauge.VELOCITY
+
+    @_memo
+    def device_tables(self, mesh):
+        """The theta operator T = P_theta / (j + 1/2)^2 x [upper, -2, lower]
+        (mesh_operators.py:724-775) is D S D^-1 with S symmetric and D =
+        diag(d_k) in theta alone: d_{k+1}/d_k = sqrt(lower_k / upper_k) does
+        not depend on j, so D commutes with the r operator and with every
+        diagonal term, and the step runs on psi' = D^-1 g with S.  Returns
+        the r (strided) and theta (contiguous) tables of the two-direction ADI
+        kernels, the per-row theta factor 1/(j + 1/2)^2, z q per point, and D."""
+        spec = mesh.spec
+        nr, nth = spec.r_points, spec.theta_points
+        mu = u.electron_mass_reduced
+        dr, dth = mesh.delta_r, mesh.delta_theta
+        pt = -(u.hbar ** 2) / (2 * mu * ((dr * dth) ** 2))
+        pr = -(u.hbar ** 2) / (2 * mu * (dr ** 2))
+        j = np.arange(nr)
+        tjp = 1 / (j + 0.5) ** 2
+        k = np.arange(nth - 1)
+        c = lambda x: (dth / 2) / np.tan(x * dth)  # noqa: E731
+        sk = lambda x: np.sin(x * dth)  # noqa: E731
+        up = (1 + c(k + 0.5)) * np.sqrt(sk(k + 0.5) / sk(k + 1.5))
+        lo = (1 - c(k + 1.5)) * np.sqrt(sk(k + 1.5) / sk(k + 0.5))
+        d = np.concatenate([[1.0], np.cumprod(np.sqrt(lo / up))])
+        V = np.asarray(spec.internal_potential(r=mesh.r_mesh, test_charge=spec.test_charge), dtype=np.float64)
+        V = V * np.ones((nr, nth))
+        hr_d = ((-2 * pt) * tjp[:, None] + 0.5 * V).reshape(-1)  # theta diagonal, C order
+        hz_d = ((-2 * pr) + 0.5 * V).reshape(-1)  # r diagonal
+        zq_pt = (-spec.test_charge * mesh.r_mesh * np.cos(mesh.theta_mesh)).reshape(-1)
+        return dict(hz_d=hz_d, hz_off=pr * np.ones(nr - 1), hr_d=hr_d, hr_off=pt * np.sqrt(up * lo),
+                    hr_off_row=tjp, zq_pt=zq_pt, d=d)
+
+
 class CylindricalSliceLengthGaugeOperators(MeshOperators):
     """mesh_operators.py:550-640."""
 

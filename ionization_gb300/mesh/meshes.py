@@ -614,6 +614,140 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
 
 
 # ==========================================================================
+# spherical slice
+# ==========================================================================
+
+
+class SphericalSliceMesh(_AdiDevice, QuantumMesh):
+    """SphericalSliceMesh (meshes.py:887-983): g = sqrt(2 pi sin theta) r psi
+    on (r, theta), theta contiguous.  Under AlternatingDirectionImplicit each
+    step is E(H_theta), I(H_r), E(H_r), I(H_theta), then the mask, on the
+    two-direction ADI kernels with r strided (implicit first) and theta
+    contiguous.  The device holds psi' = D^-1 g, D the diagonal in theta that
+    symmetrises the theta operator (SphericalSliceLengthGaugeOperators.
+    device_tables); g, the norms and the overlaps are formed with D."""
+
+    mesh_storage_method = ("r", "theta")
+
+    def __init__(self, sim):
+        super().__init__(sim)
+        self.r = np.linspace(0, self.spec.r_bound, self.spec.r_points)
+        self.theta = np.delete(np.linspace(0, u.pi, self.spec.theta_points + 1), 0)
+        self.delta_r = self.r[1] - self.r[0]
+        self.delta_theta = self.theta[1] - self.theta[0]
+        self.inner_product_multiplier = self.delta_r * self.delta_theta
+        self.r = self.r + self.delta_r / 2
+        self.theta = self.theta - self.delta_theta / 2
+        self.r_max = np.max(self.r)
+        self.r_mesh, self.theta_mesh = np.meshgrid(self.r, self.theta, indexing="ij")
+        self.mesh_points = len(self.r) * len(self.theta)
+        self.mesh_shape = np.shape(self.r_mesh)
+        self._state_g_cache = {}
+        self._init_device()
+
+    @property
+    def z_mesh(self):
+        return self.r_mesh * np.cos(self.theta_mesh)
+
+    @property
+    def g_factor(self):
+        return np.sqrt(u.twopi * np.sin(self.theta_mesh)) * self.r_mesh
+
+    def wrapping_direction_to_order(self, wrapping_direction):
+        if wrapping_direction is None:
+            return None
+        if wrapping_direction == WrappingDirection.R:
+            return "F"
+        if wrapping_direction == WrappingDirection.THETA:
+            return "C"
+        raise ValueError(f"{wrapping_direction} is not a valid specifier for flatten_mesh (valid specifiers: 'r', 'theta')")
+
+    def get_g_for_state(self, state):
+        """meshes.py:961-967."""
+        if state in self._state_g_cache:
+            return self._state_g_cache[state]
+        g = self.g_factor * state(self.r_mesh, self.theta_mesh, 0)
+        g = np.asarray(g, dtype=np.complex128)
+        g = g / np.sqrt(np.sum(np.conj(g) * g).real * self.inner_product_multiplier)
+        g = g * state.amplitude
+        self._state_g_cache[state] = g
+        return g
+
+    def _init_device(self):
+        spec, sim = self.spec, self.sim
+        if not isinstance(self.operators, mo.SphericalSliceLengthGaugeOperators):
+            raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on SphericalSliceMesh")
+        if not isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
+            raise exceptions.UnsupportedMesh(
+                f"{type(spec.evolution_method).__name__} has no device path on SphericalSliceMesh")
+        if self.precision != core.Precision.C128:
+            raise exceptions.UnsupportedMesh("the spherical-slice device path is complex128")
+        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        if spec.r_points > cap or spec.theta_points > cap:
+            raise exceptions.UnsupportedMesh(f"mesh {spec.r_points} x {spec.theta_points} exceeds {cap} points per line")
+        tb = self.operators.device_tables(self)
+        self._D = np.asarray(tb["d"], dtype=np.float64)[None, :] * np.ones(self.mesh_shape)
+        times = sim.times
+        self._tau_host = np.zeros(len(times))
+        self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        efield = np.zeros(len(times))
+        efield[1:] = np.asarray(spec.electric_potential.get_electric_field_amplitude(times[1:]), np.float64) * np.ones(len(times) - 1)
+        mask = spec.mask(r=self.r_mesh)
+        mask = None if np.isscalar(mask) and mask == 1 else np.asarray(mask, np.float64) * np.ones(self.mesh_shape)
+        g0 = self.get_g_for_state(spec.initial_state)
+        # overlaps of g = D psi' are those of psi' with D s
+        test_g = np.array([(self.get_g_for_state(s) * self._D).reshape(-1) for s in spec.test_states],
+                          dtype=np.complex128)
+        arrays = dict(hz_d=tb["hz_d"], hz_off=tb["hz_off"], hr_d=tb["hr_d"], hr_off=tb["hr_off"], zq=None,
+                      tau=self._tau_host, efield=efield, mask=mask, hz_off_col=None, hr_off_row=tb["hr_off_row"],
+                      zq_pt=tb["zq_pt"])
+        self.tables = dict(arrays, g0=g0, state_g=test_g, d=tb["d"])
+        if getattr(spec, "host_only", False):
+            return
+        self._adi_setup(spec.r_points, spec.theta_points, arrays, g0 / self._D, test_g)
+        self._d_w2 = dev.to_dev((self._D ** 2).reshape(1, -1))
+        self._d_norm_scratch = torch.empty(1, dtype=torch.float64, device=dev.device())
+
+    @property
+    def g(self) -> np.ndarray:
+        return self._psi_device().cpu().numpy().astype(np.complex128).reshape(self.mesh_shape) * self._D
+
+    @g.setter
+    def g(self, value):
+        v = np.asarray(value, dtype=np.complex128).reshape(self.mesh_shape) / self._D
+        self._g.copy_(torch.from_numpy(np.ascontiguousarray(v)).to(self._g.device))
+
+    def _weighted_norms(self, weights):
+        return super()._weighted_norms([np.asarray(w, dtype=np.float64) * self._D ** 2 for w in weights])
+
+    def _psi_device(self):
+        return self._g
+
+    def _tau_dev(self):
+        return self._d["tau"]
+
+    def _evolve_steps(self, n):
+        self._adi_evolve_steps(n)
+
+    def _reduce_current(self):
+        """Overlaps through the reducer (states scaled by D); the norm with
+        the weights D^2."""
+        tf = len(self.sim.times) - 1
+        slot = dev.data_slot(self._t, tf, self.spec.store_data_every)
+        self._reducer(self._g, self._d_norm_scratch, self._d_ip[slot])
+        n = self.mesh_points
+        nbytes = nat.value("ion_weighted_norms_scratch_bytes", n, 1)
+        if not hasattr(self, "_d_wn_scratch") or self._d_wn_scratch.numel() * 8 < nbytes:
+            self._d_wn_scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=dev.device())
+        nat.call("ion_weighted_norms_c128", n, dev.ptr(self._g), 1, dev.ptr(self._d_w2),
+                 float(self.inner_product_multiplier), dev.ptr(self._d_norm[slot:slot + 1]),
+                 dev.ptr(self._d_wn_scratch), int(nbytes), dev.stream_ptr())
+
+    def _pull_data(self):
+        return self._adi_pull_data()
+
+
+# ==========================================================================
 # rectangle
 # ==========================================================================
 

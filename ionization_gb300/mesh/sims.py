@@ -365,6 +365,27 @@ class SphericalHarmonicSpecification(MeshSpecification):
         self.numeric_eigenstate_max_energy = numeric_eigenstate_max_energy
 
 
+class SphericalSliceSpecification(MeshSpecification):
+    """sims.py:907-950."""
+
+    mesh_type = meshes.SphericalSliceMesh
+
+    def __init__(
+        self,
+        name,
+        r_bound: float = 20 * u.bohr_radius,
+        r_points: int = 2 ** 10,
+        theta_points: int = 2 ** 10,
+        operators=mesh_operators.SphericalSliceLengthGaugeOperators(),
+        evolution_method=evolution_methods.AlternatingDirectionImplicit(),
+        **kwargs,
+    ):
+        super().__init__(name, operators=operators, evolution_method=evolution_method, **kwargs)
+        self.r_bound = r_bound
+        self.r_points = int(r_points)
+        self.theta_points = int(theta_points)
+
+
 class RectangleSpecification(MeshSpecification):
     """sims.py:765-833."""
 

@@ -642,6 +642,90 @@ class RectangleADI:
 
 
 # --------------------------------------------------------------------------
+# spherical slice mesh, length gauge, ADI
+# --------------------------------------------------------------------------
+
+class SphericalSliceADI:
+    """SphericalSliceMesh (meshes.py:887-983) with
+    SphericalSliceLengthGaugeOperators (mesh_operators.py:693-813) and
+    AlternatingDirectionImplicit: kinetic energies along theta ("theta",
+    C order, a non-symmetric tridiagonal) and r ("r", F order), in that
+    order, each with half of the Coulomb potential and half of -z q E(t_{n+1});
+    steps E(H_theta), I(H_r), E(H_r), I(H_theta), then the mask.  g = g_factor
+    psi with g_factor = sqrt(2 pi sin theta) r."""
+
+    def __init__(self, r_points, r_bound, theta_points, pulse, mask, test_states, initial_state=(1, 0)):
+        r = np.linspace(0, r_bound, r_points)
+        th = np.delete(np.linspace(0, np.pi, theta_points + 1), 0)
+        self.dr, self.dth = r[1] - r[0], th[1] - th[0]
+        self.r, self.theta = r + self.dr / 2, th - self.dth / 2
+        self.shape = (r_points, theta_points)
+        self.M = r_points * theta_points
+        self.pulse = pulse
+        r_mesh, th_mesh = np.meshgrid(self.r, self.theta, indexing="ij")
+        self.r_mesh, self.th_mesh = r_mesh, th_mesh
+        self.z_mesh = r_mesh * np.cos(th_mesh)
+        self.mask = ph.radial_cosine_mask(r_mesh, **mask) if mask is not None else None
+        mu = ph.ELECTRON_MASS_REDUCED
+        V = ph.coulomb(r_mesh)
+        nth = theta_points
+        # theta kinetic (mesh_operators.py:724-775), C order: index = j * nth + k
+        pt = -(ph.HBAR ** 2) / (2 * mu * ((self.dr * self.dth) ** 2))
+        idx = np.arange(self.M)
+        jj = idx // nth
+        tjp = lambda x: 1 / (x + 0.5) ** 2  # noqa: E731
+        sink = lambda x: np.sin(x * self.dth)  # noqa: E731
+        cotk = lambda x: 1 / np.tan(x * self.dth)  # noqa: E731
+        tdiag = (-2) * tjp(jj) * pt
+        kk = np.arange(self.M - 1)
+        j1, k1 = kk // nth, kk % nth
+        live = (kk + 1) % nth != 0
+        kp = k1 + 1
+        with np.errstate(invalid="ignore", divide="ignore"):  # the dead entries at block ends
+            upper = np.where(live, tjp(j1) * (1 + (self.dth / 2) * cotk(k1 + 0.5)) * np.sqrt(sink(k1 + 0.5) / sink(k1 + 1.5)), 0) * pt
+            lower = np.where(live, tjp(j1) * (1 - (self.dth / 2) * cotk(kp + 0.5)) * np.sqrt(sink(kp + 0.5) / sink(kp - 0.5)), 0) * pt
+        self.Hth = Tridiag(lower.astype(np.complex128), (tdiag + 0.5 * V.flatten("C")).astype(np.complex128),
+                           upper.astype(np.complex128), "C")
+        # r kinetic (:704-722), F order: index = k * nr + j
+        pr = -(ph.HBAR ** 2) / (2 * mu * (self.dr ** 2))
+        roff = pr * np.where((kk + 1) % r_points != 0, 1.0, 0.0)
+        self.Hr = Tridiag(roff.astype(np.complex128), (-2 * pr + 0.5 * V.flatten("F")).astype(np.complex128),
+                          roff.astype(np.complex128), "F")
+        self.zq = {o: (-ph.ELECTRON_CHARGE * self.z_mesh).flatten(o) for o in ("F", "C")}
+        self.g_factor = np.sqrt(2 * np.pi * np.sin(th_mesh)) * r_mesh
+        self.test_g = [self._state(n, l) for (n, l) in test_states]
+        self.g = self._state(*initial_state)
+
+    def _state(self, n, l):
+        psi = ph.hydrogen_radial(n, l, self.r_mesh) * ph.spherical_harmonic(l, 0, self.th_mesh, 0)
+        g = self.g_factor * psi
+        return g / np.sqrt(self._norm(g))
+
+    def _norm(self, g):
+        return (np.sum(np.conj(g) * g) * self.dr * self.dth).real
+
+    def norm(self):
+        return self._norm(self.g)
+
+    def inner_products(self):
+        return [np.sum(np.conj(s) * self.g) * self.dr * self.dth for s in self.test_g]
+
+    def evolve(self, dt, t_now):
+        tau = dt / (2 * ph.HBAR)
+        E = self.pulse.field(t_now)
+        hth = Tridiag(self.Hth.sub, self.Hth.diag + 0.5 * self.zq["C"] * E, self.Hth.sup, "C")
+        hr = Tridiag(self.Hr.sub, self.Hr.diag + 0.5 * self.zq["F"] * E, self.Hr.sup, "F")
+        g = self.g
+        g = apply_explicit(hth.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(hr.scaled_plus_identity(1j * tau), g, self.shape)
+        g = apply_explicit(hr.scaled_plus_identity(-1j * tau), g, self.shape)
+        g = apply_implicit(hth.scaled_plus_identity(1j * tau), g, self.shape)
+        if self.mask is not None:
+            g = g * self.mask
+        self.g = g
+
+
+# --------------------------------------------------------------------------
 # numeric eigenstate basis
 # --------------------------------------------------------------------------
 
@@ -708,6 +792,11 @@ def build_from_params(kind, params):
         return cls(
             params["r_points"], params["r_bound"], params["l_bound"], pulse, params.get("mask"),
             [tuple(s) for s in params["test_states"]], params["time_step"],
+        )
+    if kind == "slice":
+        return SphericalSliceADI(
+            params["r_points"], params["r_bound"], params["theta_points"], pulse, params.get("mask"),
+            [tuple(x) for x in params["test_states"]],
         )
     if kind == "rect":
         st = (params["center_z"], params["center_x"], params["width_z"], params["width_x"], params["k_z"],

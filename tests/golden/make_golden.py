@@ -26,6 +26,7 @@ Cases (reference call sites in parentheses):
   sh_adi_small_*   SphericalHarmonicMesh + SphericalHarmonicLengthGaugeOperators
                    + AlternatingDirectionImplicit (even L; odd Nr and odd L)
   rect_adi_small*  RectangleMesh + RectangleLengthGaugeOperators + ADI (96 x 80; 81 x 64)
+  slice_adi_small* SphericalSliceMesh + SphericalSliceLengthGaugeOperators + ADI
   sh_numeric_small SH run with use_numeric_eigenstates=True (test states, initial
                    state from eigsh; energies, l and radial vectors recorded)
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
@@ -366,6 +367,29 @@ def gen_numeric(ion):
     save("sh_numeric_small", params, out)
 
 
+def gen_slice(ion):
+    """SphericalSliceMesh + SphericalSliceLengthGaugeOperators + ADI
+    (meshes.py:887-983, mesh_operators.py:693-813): the theta kinetic
+    operator is a non-symmetric tridiagonal."""
+    from ionization import states
+
+    pulse = _pulse_kwargs(0.1, 0.5, 2, 0.3)
+    for name, nr, nth in (("slice_adi_small", 96, 64), ("slice_adi_small_odd", 81, 49)):
+        test = [states.HydrogenBoundState(1, 0), states.HydrogenBoundState(2, 0), states.HydrogenBoundState(2, 1)]
+        params = dict(r_points=nr, r_bound=20.0, theta_points=nth, time_initial=0.0, time_final=10.0,
+                      time_step=0.02, pulse=pulse, mask=dict(inner_radius=15.0, outer_radius=20.0, smoothness=8),
+                      store_data_every=50, test_states=[[st.n, st.l] for st in test])
+        spec = ion.mesh.SphericalSliceSpecification(
+            name, r_points=nr, r_bound=20.0, theta_points=nth,
+            initial_state=states.HydrogenBoundState(1, 0), test_states=test,
+            electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+            mask=ion.potentials.RadialCosineMask(inner_radius=15.0, outer_radius=20.0, smoothness=8),
+            time_initial=0.0, time_final=10.0, time_step=0.02, store_data_every=50,
+        )
+        _, out = run_and_collect(spec)
+        save(name, params, out)
+
+
 def gen_rect(ion):
     """RectangleMesh + RectangleLengthGaugeOperators + ADI (meshes.py:430-506,
     mesh_operators.py:430-505): kinetic energies along z (F order) and x
@@ -500,7 +524,7 @@ def gen_observables(ion):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num")
+    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -510,7 +534,7 @@ def main():
 
     ion = import_reference(args.ref)
     only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect",
-                                                        "num"}
+                                                        "num", "slice"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -529,6 +553,8 @@ def main():
         gen_rect(ion)
     if "num" in only:
         gen_numeric(ion)
+    if "slice" in only:
+        gen_slice(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

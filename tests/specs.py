@@ -56,6 +56,17 @@ def product_spec(kind, params, **kw):
             mask=potentials.RadialCosineMask(**params["mask"]),
             **common,
         )
+    if kind == "slice":
+        return mesh.SphericalSliceSpecification(
+            "slice",
+            r_points=params["r_points"],
+            r_bound=params["r_bound"],
+            theta_points=params["theta_points"],
+            initial_state=states.HydrogenBoundState(1, 0),
+            test_states=[states.HydrogenBoundState(n, l) for n, l in params["test_states"]],
+            mask=potentials.RadialCosineMask(**params["mask"]),
+            **common,
+        )
     if kind == "rect":
         init = states.TwoDGaussianWavepacket(center_z=params["center_z"], center_x=params["center_x"],
                                              width_z=params["width_z"], width_x=params["width_x"],

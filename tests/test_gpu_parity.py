@@ -104,6 +104,9 @@ CASES = [
     # RectangleMesh with AlternatingDirectionImplicit (complex128)
     ("rect", "rect_adi_small"),
     ("rect", "rect_adi_small_odd"),
+    # SphericalSliceMesh with AlternatingDirectionImplicit (complex128)
+    ("slice", "slice_adi_small"),
+    ("slice", "slice_adi_small_odd"),
 ]
 
 
@@ -124,7 +127,7 @@ def test_mesh_c128_matches_reference(cuda, kind, name):
     _check_against_golden(sim, z)
 
 
-COMPLEX64_CASES = [c for c in CASES if c[0] not in ("cyl", "rect") and not c[1].startswith("sh_adi")]
+COMPLEX64_CASES = [c for c in CASES if c[0] not in ("cyl", "rect", "slice") and not c[1].startswith("sh_adi")]
 
 
 @pytest.mark.parametrize("kind,name", COMPLEX64_CASES)

@@ -54,7 +54,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(nat.ShPlan) == 8 + 4 * 4 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 16 * 4
     assert nat.ShSim.g.offset == 0 and nat.ShSim.t.offset == 16
     assert nat.LineSim.t.offset == 16
-    assert ctypes.sizeof(nat.CylMesh) == 8 + 9 * 8 + 8
+    assert ctypes.sizeof(nat.CylMesh) == 8 + 9 * 8 + 8 + 2 * 8
 
 
 def test_struct_offsets_match_the_c_compiler(tmp_path):

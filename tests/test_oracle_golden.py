@@ -54,6 +54,9 @@ CASES = [
     # RectangleMesh with AlternatingDirectionImplicit
     ("rect", "rect_adi_small"),
     ("rect", "rect_adi_small_odd"),
+    # SphericalSliceMesh with AlternatingDirectionImplicit
+    ("slice", "slice_adi_small"),
+    ("slice", "slice_adi_small_odd"),
 ]
 
 
