@@ -415,7 +415,7 @@ def run_e2e(args, specs, tables, rows, gs, points, precision):
     b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
     b.step(K)
     res = b.results()
-    psis = [s.psi_host() for s in b.sims]  # g (+ its residual) to the host
+    psis = b.psi_all()  # g (+ its residual) to the host
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     h2d = sum(s.nbytes() for s in b.sims) - sum(int(s.d_partials.numel()) * 8 for s in b.sims)

@@ -119,55 +119,144 @@ def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
     return (n_r + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
-class ShDeviceSim:
-    """Device buffers of one spherical-harmonic simulation."""
+def _sh_host_arrays(tab: ShTables, precision) -> dict:
+    """The host arrays a spherical-harmonic simulation uploads (None where
+    absent), by attribute name, in their device dtype."""
+    precision = Precision(precision)
+    f64, f32 = np.float64, np.float32
+    g0 = np.asarray(tab.g0, dtype=np.complex128)
+    c128 = precision == Precision.C128
+    a = {}
+    a["g"] = g0 if c128 else g0.astype(np.complex64)
+    a["g_lo"] = None
+    if precision == Precision.C64X:  # psi = g + g_lo
+        a["g_lo"] = (g0 - g0.astype(np.complex64).astype(np.complex128)).astype(np.complex64)
+    a["d_hd"] = np.asarray(tab.hd, f64) if c128 else None
+    a["d_hoff"] = np.asarray(tab.hoff, f64)
+    a["d_rq"] = np.asarray(tab.rq, f64)
+    a["d_cl"] = np.asarray(tab.cl, f64)
+    a["d_mask"] = np.asarray(tab.mask, f64) if tab.mask is not None else None
+    a["d_tau"] = np.asarray(tab.tau, f64)
+    a["d_ef"] = np.asarray(tab.efield, f64)
+    # per-r FP32 tables zero-padded to a multiple of 16 entries: the radial
+    # solve reads a chunk of 8 or 16 rows with 16-byte vector loads
+    a["d_kinv32"] = _pad16(tab.kinv).astype(f32)
+    a["d_cent32"] = _pad16(tab.cent).astype(f32)
+    a["d_hoff32"] = _pad16(tab.hoff).astype(f32)
+    a["d_rq32"] = np.asarray(tab.rq, f32)
+    a["d_cl32"] = np.asarray(tab.cl, f32)
+    a["d_mask32"] = np.asarray(tab.mask, f32) if tab.mask is not None else None
+    vel = int(tab.gauge) == nat.ION_GAUGE_VELOCITY
+    a["d_h2r"] = np.asarray(tab.h2r, f64) if vel else None
+    a["d_h2r32"] = np.asarray(tab.h2r, f32) if vel else None
+    n_states = len(tab.state_l)
+    a["d_state_l"] = np.asarray(tab.state_l, dtype=np.int32).reshape(-1)
+    sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(n_states, tab.n_r)
+    a["d_state_g"] = sg.view(np.float64).reshape(-1) if n_states else np.zeros(2)
+    return a
 
-    def __init__(self, tab: ShTables, precision):
+
+def _sh_device_sizes(tab: ShTables):
+    """(n_data, n_states, n_tiles) of a simulation's device-only buffers."""
+    n_states = len(tab.state_l)
+    return n_data_slots(int(tab.t_final), int(tab.store_every)), n_states, (tab.n_r + SH_ROT_ROWS - 1) // SH_ROT_ROWS
+
+
+class _Arena:
+    """Arrays of one dtype packed into one pinned host buffer, uploaded with
+    one copy; each array becomes a view of the device buffer, starting on a
+    64-byte boundary (the radial solve's float4 table loads need 16)."""
+
+    def __init__(self, np_dtype):
+        self.np_dtype = np.dtype(np_dtype)
+        self.items = []  # (key, array, offset)
+        self.size = 0
+
+    def add(self, key, arr):
+        align = max(1, 64 // self.np_dtype.itemsize)
+        self.size = (self.size + align - 1) // align * align
+        self.items.append((key, arr, self.size))
+        self.size += arr.size
+
+    def upload(self) -> dict:
+        tdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
+               np.dtype(np.int32): torch.int32, np.dtype(np.complex64): torch.complex64,
+               np.dtype(np.complex128): torch.complex128}[self.np_dtype]
+        n = max(self.size, 1)
+        host = torch.empty(n, dtype=tdt, pin_memory=True)
+        hv = host.numpy()
+        for _, arr, off in self.items:
+            hv[off:off + arr.size] = arr.reshape(-1)
+        dev_buf = torch.empty(n, dtype=tdt, device=device())
+        dev_buf.copy_(host, non_blocking=True)
+        return {key: dev_buf[off:off + arr.size].view(arr.shape) for key, arr, off in self.items}
+
+
+class ShDeviceSim:
+    """Device buffers of one spherical-harmonic simulation.  ``arrays``: the
+    device tensors by attribute name, when built together with others
+    (``ShDeviceSim.bulk``); otherwise each host array is uploaded on its own."""
+
+    def __init__(self, tab: ShTables, precision, arrays: Optional[dict] = None):
         self.precision = Precision(precision)
         self.tab = tab
         self.n_r, self.n_l = tab.n_r, tab.n_l
         self.t = int(tab.t0)
         self.t_final = int(tab.t_final)
         self.store_every = int(tab.store_every)
-        f64 = np.float64
-        f32 = np.float32
-        g0 = np.asarray(tab.g0, dtype=np.complex128)
-        self.g = to_dev(g0).to(complex_dtype(precision))
-        self.g_lo = None
-        if self.precision == Precision.C64X:  # psi = g + g_lo
-            hi = g0.astype(np.complex64)
-            self.g_lo = to_dev((g0 - hi.astype(np.complex128)).astype(np.complex64))
-        c128 = self.precision == Precision.C128
-        self.d_hd = to_dev(tab.hd, f64) if c128 else None
-        self.d_hoff = to_dev(tab.hoff, f64)
-        self.d_rq = to_dev(tab.rq, f64)
-        self.d_cl = to_dev(tab.cl, f64)
-        self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
-        self.d_tau = to_dev(tab.tau, f64)
-        self.d_ef = to_dev(tab.efield, f64)
-        # per-r FP32 tables zero-padded to a multiple of 16 entries: the radial
-        # solve reads a chunk of 8 or 16 rows with 16-byte vector loads
-        self.d_kinv32 = to_dev(_pad16(tab.kinv), f32)
-        self.d_cent32 = to_dev(_pad16(tab.cent), f32)
-        self.d_hoff32 = to_dev(_pad16(tab.hoff), f32)
-
-        self.d_rq32 = to_dev(tab.rq, f32)
-        self.d_cl32 = to_dev(tab.cl, f32)
-        self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
         self.gauge = int(tab.gauge)
-        self.d_h2r = self.d_h2r32 = None
-        if self.gauge == nat.ION_GAUGE_VELOCITY:
-            self.d_h2r, self.d_h2r32 = to_dev(tab.h2r, f64), to_dev(tab.h2r, f32)
-        self.n_states = len(tab.state_l)
-        self.d_state_l = to_dev(np.asarray(tab.state_l, dtype=np.int32).reshape(-1))
-        sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(self.n_states, self.n_r)
-        self.d_state_g = to_dev(sg.view(np.float64).reshape(-1)) if self.n_states else to_dev(np.zeros(2))
-        self.n_data = n_data_slots(self.t_final, self.store_every)
-        self.d_norm = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
-        self.d_ip = torch.full((self.n_data * max(self.n_states, 1) * 2,), float("nan"), dtype=torch.float64,
-                               device=device())
-        self.n_tiles = (self.n_r + SH_ROT_ROWS - 1) // SH_ROT_ROWS
-        self.d_partials = torch.zeros(self.n_tiles * (1 + 2 * self.n_states), dtype=torch.float64, device=device())
+        if arrays is None:
+            arrays = {k: (to_dev(v) if v is not None else None) for k, v in _sh_host_arrays(tab, precision).items()}
+            self.n_data, n_states, self.n_tiles = _sh_device_sizes(tab)
+            arrays["d_norm"] = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
+            arrays["d_ip"] = torch.full((self.n_data * max(n_states, 1) * 2,), float("nan"), dtype=torch.float64,
+                                        device=device())
+            arrays["d_partials"] = torch.zeros(self.n_tiles * (1 + 2 * n_states), dtype=torch.float64,
+                                               device=device())
+        else:
+            self.n_data, n_states, self.n_tiles = _sh_device_sizes(tab)
+        for k, v in arrays.items():
+            setattr(self, k, v)
+        self.n_states = n_states
+
+    @classmethod
+    def bulk(cls, tables: List[ShTables], precision) -> List["ShDeviceSim"]:
+        """Many simulations with one pinned upload per dtype and one device
+        buffer per kind of array."""
+        arenas = {}
+        per = []
+        for i, tab in enumerate(tables):
+            host = _sh_host_arrays(tab, precision)
+            per.append(host)
+            for k, v in host.items():
+                if v is not None:
+                    arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
+        views = {}
+        for ar in arenas.values():
+            views.update(ar.upload())
+        torch.cuda.current_stream().synchronize()  # the pinned sources are released below
+        sizes = [_sh_device_sizes(tab) for tab in tables]
+        n_norm = sum(nd for nd, _, _ in sizes)
+        n_ip = sum(nd * max(ns, 1) * 2 for nd, ns, _ in sizes)
+        n_part = sum(nt * (1 + 2 * ns) for _, ns, nt in sizes)
+        d_norm = torch.full((max(n_norm, 1),), float("nan"), dtype=torch.float64, device=device())
+        d_ip = torch.full((max(n_ip, 1),), float("nan"), dtype=torch.float64, device=device())
+        d_part = torch.zeros(max(n_part, 1), dtype=torch.float64, device=device())
+        sims, o_norm, o_ip, o_part = [], 0, 0, 0
+        for i, tab in enumerate(tables):
+            nd, ns, nt = sizes[i]
+            arrays = {k: views.get((i, k)) for k in per[i]}
+            arrays["d_norm"] = d_norm[o_norm:o_norm + nd]
+            arrays["d_ip"] = d_ip[o_ip:o_ip + nd * max(ns, 1) * 2]
+            arrays["d_partials"] = d_part[o_part:o_part + nt * (1 + 2 * ns)]
+            sim = cls(tab, precision, arrays=arrays)
+            sim._bulk = dict(norm=(d_norm, o_norm, nd), ip=(d_ip, o_ip, nd * max(ns, 1) * 2))
+            o_norm += nd
+            o_ip += nd * max(ns, 1) * 2
+            o_part += nt * (1 + 2 * ns)
+            sims.append(sim)
+        return sims
+
 
     def nbytes(self) -> int:
         tot = 0
@@ -207,6 +296,55 @@ class ShDeviceSim:
         if self.g_lo is not None:
             g = g + self.g_lo.cpu().numpy().astype(np.complex128)
         return g
+
+
+def _host_copy(t: torch.Tensor) -> np.ndarray:
+    """One device-to-host copy through pinned memory."""
+    host = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    host.copy_(t)
+    return host.numpy()
+
+
+def sh_data_many(sims: List["ShDeviceSim"]):
+    """(norm, inner_products) of every simulation: with one copy per buffer
+    when they were built together (``ShDeviceSim.bulk``), else one by one."""
+    if not sims or not all(hasattr(s, "_bulk") for s in sims) or \
+            len({id(s._bulk["norm"][0]) for s in sims}) != 1:
+        return [s.data() for s in sims]
+    norm_all = _host_copy(sims[0]._bulk["norm"][0])
+    ip_all = _host_copy(sims[0]._bulk["ip"][0])
+    out = []
+    for s in sims:
+        _, on, nn = s._bulk["norm"]
+        _, oi, ni = s._bulk["ip"]
+        ip = ip_all[oi:oi + ni][: s.n_data * s.n_states * 2].view(np.complex128)
+        out.append((norm_all[on:on + nn].copy(), ip.reshape(s.n_data, s.n_states).T.copy()))
+    return out
+
+
+def sh_psi_many(sims: List["ShDeviceSim"]) -> List[np.ndarray]:
+    """psi (g + g_lo) of every simulation, complex128: one copy per storage
+    buffer when they share one, else one by one."""
+    bases = {}
+    for s in sims:
+        for t in (s.g, s.g_lo):
+            if t is not None:
+                b = t._base if t._base is not None else t
+                bases.setdefault(id(b), b)
+    host = {k: _host_copy(b).reshape(-1) for k, b in bases.items()}
+
+    def view(t):
+        b = t._base if t._base is not None else t
+        off = t.storage_offset() - b.storage_offset()
+        return host[id(b)][off:off + t.numel()].reshape(tuple(t.shape))
+
+    out = []
+    for s in sims:
+        g = view(s.g).astype(np.complex128)
+        if s.g_lo is not None:
+            g = g + view(s.g_lo).astype(np.complex128)
+        out.append(g)
+    return out
 
 
 class ShBatch:

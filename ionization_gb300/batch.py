@@ -47,7 +47,7 @@ class BatchedSphericalHarmonicSimulation:
         if tables is None:
             tables = [_host_tables(spec)[0] for spec in self.specs]
         self.tables = tables
-        dsims = [dev.ShDeviceSim(tab, self.precision) for tab in tables]
+        dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
         self.sims = dsims
         self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows)
         self.graph_steps = int(graph_steps)
@@ -112,8 +112,7 @@ class BatchedSphericalHarmonicSimulation:
     def results(self) -> List[dict]:
         torch.cuda.synchronize()
         out = []
-        for spec, s in zip(self.specs, self.sims):
-            norm, ips = s.data()
+        for spec, s, (norm, ips) in zip(self.specs, self.sims, dev.sh_data_many(self.sims)):
             ip = {st: ips[k] for k, st in enumerate(spec.test_states)}
             ov = {st: np.abs(v) ** 2 for st, v in ip.items()}
             out.append(dict(
@@ -128,6 +127,11 @@ class BatchedSphericalHarmonicSimulation:
 
     def psi(self, i) -> np.ndarray:
         return self.sims[i].psi_host()
+
+    def psi_all(self) -> List[np.ndarray]:
+        """psi of every simulation (complex128), read back together."""
+        torch.cuda.synchronize()
+        return dev.sh_psi_many(self.sims)
 
 
 def autotune(specs, precision="c64", graph_steps=(32,), steps=32, tables=None):
