@@ -187,7 +187,13 @@ struct ShCnCoef32 {
     const float* hoff;
     float ll1, corr0, tau;
     int n;
-    const Cx<float>* lo;  // the line's stored residual (c64x), or NULL
+    // the line's stored residual (c64x) staged in shared memory in the
+    // line's interleaved layout (slot (i mod 2^mshift) T + i >> mshift), or NULL
+    const Cx<float>* lob;
+    int T, mshift;
+    __device__ __forceinline__ Cx<float> lo_at(int i) const {
+        return lob[(i & ((1 << mshift) - 1)) * T + (i >> mshift)];
+    }
     __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const {
         if (i < 0 || i >= n) {
             bo = 0.f;
@@ -245,7 +251,7 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float& e) {
 template <bool RES>
 __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i, float a0, float bd, float bo,
                                                   Cx<float> p0, Cx<float> p1, Cx<float> p2) {
-    if (!RES || c.lo == nullptr)
+    if (!RES || c.lob == nullptr)
         return Cx<float>{a0 * p0.re + bd * p1.re + bo * p2.re, a0 * p0.im + bd * p1.im + bo * p2.im};
     float e1, e2;
     const float s1 = two_sum_err(bd, a0, e1);
@@ -255,9 +261,9 @@ __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i
     Cx<float> v = {a0 * dm.re + bo * dp.re + (rs * p1.re + rl * p1.re),
                    a0 * dm.im + bo * dp.im + (rs * p1.im + rl * p1.im)};
     if (i < c.n) {  // padding rows carry no residual
-        const Cx<float> l1 = ld(c.lo + i);
-        const Cx<float> l0 = i > 0 ? ld(c.lo + i - 1) : Cx<float>{0.f, 0.f};
-        const Cx<float> l2 = i + 1 < c.n ? ld(c.lo + i + 1) : Cx<float>{0.f, 0.f};
+        const Cx<float> l1 = c.lo_at(i);
+        const Cx<float> l0 = i > 0 ? c.lo_at(i - 1) : Cx<float>{0.f, 0.f};
+        const Cx<float> l2 = i + 1 < c.n ? c.lo_at(i + 1) : Cx<float>{0.f, 0.f};
         v.re += a0 * l0.re + bd * l1.re + bo * l2.re;
         v.im += a0 * l0.im + bd * l1.im + bo * l2.im;
     }
@@ -267,22 +273,25 @@ __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i
 template <typename R, bool RES> struct ShCnCoefFor;
 template <bool RES> struct ShCnCoefFor<double, RES> {
     using type = ShCnCoef<double>;
-    __device__ static type make(const ion_sh_sim& S, int l, double tau) {
+    __device__ static type make(const ion_sh_sim& S, int l, double tau, const void*, int, int) {
         return type{ShH<double>::make(S, l), tau, S.n_r};
     }
 };
 template <bool RES> struct ShCnCoefFor<float, RES> {
     using type = ShCnCoef32<RES>;
-    __device__ static type make(const ion_sh_sim& S, int l, float tau) {
-        const Cx<float>* lo = S.g_lo ? static_cast<const Cx<float>*>(S.g_lo) + int64_t(l) * S.n_r : nullptr;
+    // lob: the line's residual staged in shared memory, or NULL
+    __device__ static type make(const ion_sh_sim& S, int l, float tau, const void* lob, int T, int mshift) {
         return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r,
-                    lo};
+                    static_cast<const Cx<float>*>(lob), T, mshift};
     }
 };
 
-// psi of item ``item`` into ``dst`` (interleaved, zero padding), asynchronously
+// psi of item ``item`` into ``dst`` (interleaved, zero padding), and its
+// stored residual into ``lodst`` when given (complex64 with g_lo),
+// asynchronously
 template <typename R, int M>
-__device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int item, Cx<R>* dst) {
+__device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int item, Cx<R>* dst,
+                                                  Cx<R>* lodst = nullptr) {
     const int si = plan.cn_items[2 * item];
     const int l = plan.cn_items[2 * item + 1];
     const ion_sh_sim& S = plan.sims[si];
@@ -291,6 +300,7 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
     const int T = (nr + M - 1) / M;
     const int npad = T * M;
     const Cx<R>* g = static_cast<const Cx<R>*>(S.g) + int64_t(l) * nr;
+    const Cx<R>* glo = (lodst && S.g_lo) ? static_cast<const Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
     for (int i = threadIdx.x; i < npad; i += blockDim.x) {
         Cx<R>* d = dst + islot<M>(i, T);
         if (i < nr) {
@@ -298,8 +308,10 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
                 cp_async16(d, g + i);
             else
                 cp_async8(d, g + i);
+            if (glo) cp_async8(lodst + islot<M>(i, T), glo + i);
         } else {
             *d = Cx<R>{R(0), R(0)};
+            if (glo) lodst[islot<M>(i, T)] = Cx<R>{R(0), R(0)};
         }
     }
 }
@@ -330,25 +342,31 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
     constexpr int refine = REFINE ? 1 : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cap = blockDim.x * M;
+    // psi (double-buffered), with refinement the increment and the staged
+    // residual (double-buffered like psi), then the PCR scratch
     Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* buf1 = buf0 + cap;
     Cx<R>* ext = buf0 + (dbuf ? 2 : 1) * cap;
-    Cx<R>* red = ext + (refine ? cap : 0);
+    Cx<R>* lob0 = ext + (refine ? cap : 0);
+    Cx<R>* lob1 = lob0 + (dbuf ? cap : 0);
+    Cx<R>* red = lob0 + (refine ? (dbuf ? 2 : 1) * cap : 0);
     int item = item0 + blockIdx.x;
     if (item >= item_end) return;
     if (dbuf) {
-        sh_cn_stage_async<R, M>(plan, item, buf0);
+        sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr);
         cp_async_commit();
     }
     for (int j = 0; item < item_end; item += gridDim.x, ++j) {
         Cx<R>* cur = (dbuf && (j & 1)) ? buf1 : buf0;
+        Cx<R>* lob = (dbuf && (j & 1)) ? lob1 : lob0;
         if (dbuf) {
             const int next = item + gridDim.x;
-            if (next < item_end) sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1);
+            if (next < item_end)
+                sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1, refine ? ((j & 1) ? lob0 : lob1) : nullptr);
             cp_async_commit();
             cp_async_wait<1>();  // this item's psi has landed; the next one stays in flight
         } else {
-            sh_cn_stage_async<R, M>(plan, item, buf0);
+            sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr);
             cp_async_commit();
             cp_async_wait<0>();
         }
@@ -361,9 +379,10 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
             const int nr = S.n_r;
             const int T = (nr + M - 1) / M;
             const R tau = R(S.tau[t + 1]);
-            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau);
             // with a stored residual the solve leaves the increment in ``inc``
             Cx<R>* glo = sizeof(R) == 4 && S.g_lo ? static_cast<Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
+            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T,
+                                                           M == 16 ? 4 : (M == 8 ? 3 : 2));
             Cx<R>* inc = cur;
             if constexpr (REFINE) {
                 // two solves through one call site: delta1 into ext, then
@@ -394,7 +413,7 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                 for (int k = 0; k < M; ++k) {
                     const int i = threadIdx.x + k * blockDim.x;
                     if (i < nr) {
-                        Cx<R> lo = ld(glo + i);
+                        Cx<R> lo = refine ? lob[islot<M>(i, T)] : ld(glo + i);
                         const Cx<R> h = add_exact(ld(g + i), inc[islot<M>(i, T)], lo);
                         st(g + i, h);
                         st(glo + i, lo);
@@ -1005,11 +1024,12 @@ static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
         if (end > begin) {
             const int refine = (p->flags & ION_SH_REFINE) && sizeof(R) == 4 ? 1 : 0;
+            // psi x2, with refinement the increment and the staged residual x2
             int dbuf = 1;
-            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2 + refine);
+            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2 + 3 * refine);
             if (smem > 200 * 1024) {
                 dbuf = 0;
-                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1 + refine);
+                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1 + 2 * refine);
             }
             if (smem > 200 * 1024) {
                 set_error("ion_sh: radial line too long for shared memory");
