@@ -179,10 +179,11 @@ class _Arena:
         self.items.append((key, arr, self.size))
         self.size += arr.size
 
-    # one pageable copy per dtype: page-locking a gigabyte-sized staging
-    # buffer costs more than it saves on a one-shot upload (GB300: 0.72 s on
-    # first use against 0.34 s pageable for the 1.2 GB of a 512-simulation sweep)
-    pin = False
+    # staged through page-locked memory, which torch's host allocator keeps
+    # for reuse: the first batch of a size pays the page-locking (GB300, the
+    # 1.2 GB of a 512-simulation sweep: 0.72 s, later 0.31 s; one pageable
+    # copy instead: 0.33 s every time)
+    pin = True
 
     def upload(self) -> dict:
         tdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
