@@ -659,16 +659,28 @@ __global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf
     // complex64 with a stored residual: the tile's compensation word starts
     // from it and is stored back renormalised instead of folded into g
     Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
-#pragma unroll 4
+    // the tile by asynchronous copies: every thread's loads are in flight
+    // together without holding registers (register loads left the pass
+    // waiting on global memory at a third of the DRAM bandwidth)
     for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
         const int l = f >> 5, jj = f & (ROT_ROWS - 1);
         if (jj < rows) {
             const int64_t at = int64_t(l) * nr + j0 + jj;
-            hi[f] = ld(g + at);
-            if constexpr (Tile<R>::comp) tl.lo[f] = glo ? ld(glo + at) : Cx<R>{R(0), R(0)};
+            if constexpr (sizeof(Cx<R>) == 16)
+                cp_async16(hi + f, g + at);
+            else
+                cp_async8(hi + f, g + at);
+            if constexpr (Tile<R>::comp) {
+                if (glo)
+                    cp_async8(tl.lo + f, glo + at);
+                else
+                    tl.lo[f] = Cx<R>{R(0), R(0)};
+            }
         }
     }
+    cp_async_commit();
     if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
+    cp_async_wait<0>();
     __syncthreads();
 
     const RotTab<R> tb = RotTab<R>::make(S);
@@ -809,12 +821,22 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
     Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
     const int span = jhi - jlo;
-    for (int f = threadIdx.x; f < nl * span; f += blockDim.x) {
+    for (int f = threadIdx.x; f < nl * span; f += blockDim.x) {  // asynchronous, as in sh_rot_kernel
         const int l = f / span, jj = jlo + f % span;
         const int64_t at = int64_t(l) * nr + r0 + jj;
-        hi[l * VEL_ROWS + jj] = ld(g + at);
-        if constexpr (Tile<R>::comp) tl.lo[l * VEL_ROWS + jj] = glo ? ld(glo + at) : Cx<R>{R(0), R(0)};
+        if constexpr (sizeof(Cx<R>) == 16)
+            cp_async16(hi + l * VEL_ROWS + jj, g + at);
+        else
+            cp_async8(hi + l * VEL_ROWS + jj, g + at);
+        if constexpr (Tile<R>::comp) {
+            if (glo)
+                cp_async8(tl.lo + l * VEL_ROWS + jj, glo + at);
+            else
+                tl.lo[l * VEL_ROWS + jj] = Cx<R>{R(0), R(0)};
+        }
     }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     const RotTab<R> tb = RotTab<R>::make(S);
     const R* h2r = VelTab<R>::h2r(S);
