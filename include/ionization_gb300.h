@@ -124,6 +124,10 @@ int64_t ion_tdma_batched_max_n_c64(void);
  * E(times[t+1] + time_step/2) (mesh_operators.py:1011-1013, 1037-1080).  The
  * pairing of the rotations is over the F-order (r-major, l fastest) index of
  * the (l, r) mesh, exactly as the reference builds its even/odd matrices.
+ * Between two solves with no data stored in between, R_even(t+1), the mask
+ * and R_even(t+2) are applied to each pair in registers in one sweep, with
+ * the same arithmetic as three separate sweeps: results do not depend on
+ * how the steps are split into calls (complex128 bit for bit).
  *
  * psi of every simulation is stored (n_l, n_r) in C order (r contiguous),
  * the layout of the reference's ``mesh.g``, at its own device pointer.  A batch

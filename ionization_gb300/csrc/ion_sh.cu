@@ -465,16 +465,38 @@ __device__ __forceinline__ float two_sum(float a, float b, float& e) {
 
 // The tile holds psi as hi (+ lo for complex64: a compensation word that
 // collects the rounding of every update inside the pass, folded in once
-// when psi is stored).
+// when psi is stored).  The rotation and the mask are written once, on
+// register values, with every product-add an explicit fma: a launch that
+// chains several operators on one pair in registers does exactly the
+// arithmetic of one that goes through shared memory between them, so the
+// result does not depend on how steps are split into launches.
 template <typename R> struct Tile;
 template <> struct Tile<double> {
     Cx<double>* hi;
     static constexpr bool comp = false;
+    struct Pair {
+        Cx<double> x0, x1;
+    };
     __device__ Cx<double> value(int k) const { return hi[k]; }
+    __device__ __forceinline__ Pair load(int k0, int k1) const { return Pair{hi[k0], hi[k1]}; }
+    __device__ __forceinline__ void put(int k0, int k1, const Pair& p) const {
+        hi[k0] = p.x0;
+        hi[k1] = p.x1;
+    }
+    __device__ __forceinline__ static void rot(Pair& p, double cm1, double s) {
+        const Cx<double> x0 = p.x0, x1 = p.x1;
+        p.x0 = Cx<double>{x0.re + fma(cm1, x0.re, s * x1.im), x0.im + fma(cm1, x0.im, -(s * x1.re))};
+        p.x1 = Cx<double>{x1.re + fma(cm1, x1.re, s * x0.im), x1.im + fma(cm1, x1.im, -(s * x0.re))};
+    }
+    __device__ __forceinline__ static Cx<double> scaled(Cx<double> h, double m) { return Cx<double>{h.re * m, h.im * m}; }
+    __device__ __forceinline__ static void scale(Pair& p, double m) {
+        p.x0 = scaled(p.x0, m);
+        p.x1 = scaled(p.x1, m);
+    }
     __device__ void rotate(int k0, int k1, double cm1, double s) const {
-        const Cx<double> x0 = hi[k0], x1 = hi[k1];
-        hi[k0] = Cx<double>{x0.re + (cm1 * x0.re + s * x1.im), x0.im + (cm1 * x0.im - s * x1.re)};
-        hi[k1] = Cx<double>{x1.re + (cm1 * x1.re + s * x0.im), x1.im + (cm1 * x1.im - s * x0.re)};
+        Pair p = load(k0, k1);
+        rot(p, cm1, s);
+        put(k0, k1, p);
     }
     // velocity gauge: [[cos, sin], [-sin, cos]] in increment form
     __device__ void rotate_real(int k0, int k1, double cm1, double s) const {
@@ -482,7 +504,7 @@ template <> struct Tile<double> {
         hi[k0] = Cx<double>{x0.re + (cm1 * x0.re + s * x1.re), x0.im + (cm1 * x0.im + s * x1.im)};
         hi[k1] = Cx<double>{x1.re + (cm1 * x1.re - s * x0.re), x1.im + (cm1 * x1.im - s * x0.im)};
     }
-    __device__ void scale(int k, double m) const { hi[k] = Cx<double>{hi[k].re * m, hi[k].im * m}; }
+    __device__ void scale(int k, double m) const { hi[k] = scaled(hi[k], m); }
     __device__ Cx<double> out(int k) const { return hi[k]; }
     __device__ __forceinline__ void store(int k, Cx<double>* g, Cx<double>*, int64_t at) const { st(g + at, hi[k]); }
 };
@@ -490,20 +512,45 @@ template <> struct Tile<float> {
     Cx<float>* hi;
     Cx<float>* lo;
     static constexpr bool comp = true;
+    struct Pair {
+        Cx<float> x0, x1, l0, l1;
+    };
     __device__ Cx<double> value(int k) const {
         return Cx<double>{double(hi[k].re) + double(lo[k].re), double(hi[k].im) + double(lo[k].im)};
     }
-    __device__ void rotate(int k0, int k1, float cm1, float s) const {
-        const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo[k0], l1 = lo[k1];
+    __device__ __forceinline__ Pair load(int k0, int k1) const { return Pair{hi[k0], hi[k1], lo[k0], lo[k1]}; }
+    __device__ __forceinline__ void put(int k0, int k1, const Pair& p) const {
+        hi[k0] = p.x0;
+        hi[k1] = p.x1;
+        lo[k0] = p.l0;
+        lo[k1] = p.l1;
+    }
+    __device__ __forceinline__ static void rot(Pair& p, float cm1, float s) {
+        const Cx<float> x0 = p.x0, x1 = p.x1, l0 = p.l0, l1 = p.l1;
         float e0r, e0i, e1r, e1i;
-        const float h0r = two_sum(x0.re, cm1 * x0.re + s * x1.im, e0r);
-        const float h0i = two_sum(x0.im, cm1 * x0.im - s * x1.re, e0i);
-        const float h1r = two_sum(x1.re, cm1 * x1.re + s * x0.im, e1r);
-        const float h1i = two_sum(x1.im, cm1 * x1.im - s * x0.re, e1i);
-        hi[k0] = Cx<float>{h0r, h0i};
-        hi[k1] = Cx<float>{h1r, h1i};
-        lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.im) + e0r, l0.im + (cm1 * l0.im - s * l1.re) + e0i};
-        lo[k1] = Cx<float>{l1.re + (cm1 * l1.re + s * l0.im) + e1r, l1.im + (cm1 * l1.im - s * l0.re) + e1i};
+        const float h0r = two_sum(x0.re, fmaf(cm1, x0.re, s * x1.im), e0r);
+        const float h0i = two_sum(x0.im, fmaf(cm1, x0.im, -(s * x1.re)), e0i);
+        const float h1r = two_sum(x1.re, fmaf(cm1, x1.re, s * x0.im), e1r);
+        const float h1i = two_sum(x1.im, fmaf(cm1, x1.im, -(s * x0.re)), e1i);
+        p.x0 = Cx<float>{h0r, h0i};
+        p.x1 = Cx<float>{h1r, h1i};
+        p.l0 = Cx<float>{(l0.re + fmaf(cm1, l0.re, s * l1.im)) + e0r, (l0.im + fmaf(cm1, l0.im, -(s * l1.re))) + e0i};
+        p.l1 = Cx<float>{(l1.re + fmaf(cm1, l1.re, s * l0.im)) + e1r, (l1.im + fmaf(cm1, l1.im, -(s * l0.re))) + e1i};
+    }
+    // the product's rounding error goes to lo
+    __device__ __forceinline__ static void scaled(Cx<float>& h, Cx<float>& l, float m) {
+        const float pr = h.re * m, pi = h.im * m;
+        l = Cx<float>{fmaf(l.re, m, fmaf(h.re, m, -pr)), fmaf(l.im, m, fmaf(h.im, m, -pi))};
+        h = Cx<float>{pr, pi};
+    }
+    __device__ __forceinline__ static void scale(Pair& p, float m) {
+        scaled(p.x0, p.l0, m);
+        scaled(p.x1, p.l1, m);
+    }
+    __device__ void rotate(int k0, int k1, float cm1, float s) const {
+        Pair p = load(k0, k1);
+        rot(p, cm1, s);
+        put(k0, k1, p);
     }
     __device__ void rotate_real(int k0, int k1, float cm1, float s) const {
         const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo[k0], l1 = lo[k1];
@@ -517,11 +564,11 @@ template <> struct Tile<float> {
         lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.re) + e0r, l0.im + (cm1 * l0.im + s * l1.im) + e0i};
         lo[k1] = Cx<float>{l1.re + (cm1 * l1.re - s * l0.re) + e1r, l1.im + (cm1 * l1.im - s * l0.im) + e1i};
     }
-    __device__ void scale(int k, float m) const {  // the product's rounding error goes to lo
-        const Cx<float> h = hi[k], l = lo[k];
-        const float pr = h.re * m, pi = h.im * m;
-        hi[k] = Cx<float>{pr, pi};
-        lo[k] = Cx<float>{fmaf(l.re, m, fmaf(h.re, m, -pr)), fmaf(l.im, m, fmaf(h.im, m, -pi))};
+    __device__ void scale(int k, float m) const {
+        Cx<float> h = hi[k], l = lo[k];
+        scaled(h, l, m);
+        hi[k] = h;
+        lo[k] = l;
     }
     __device__ Cx<float> out(int k) const { return Cx<float>{hi[k].re + lo[k].re, hi[k].im + lo[k].im}; }
     // element k to g[at]: hi + lo folded, or, with a stored residual, hi + lo
@@ -549,6 +596,42 @@ __device__ __forceinline__ void rotate_rows(const Tile<R>& tl, int rows, int nl,
             R cm1, s;
             rot_coeffs(tau * ((tb.cl[l] * rqj) * efield), cm1, s);
             tl.rotate(l * ROT_ROWS + jj, (l + 1) * ROT_ROWS + jj, cm1, s);
+        }
+    }
+    __syncthreads();
+}
+
+// Between two solves with no data stored in between: the even rotation of
+// time index n1, the mask, and the even rotation of n2, applied to each pair
+// in registers (one sweep instead of three; the same arithmetic, operator by
+// operator, as rotate_rows / mask / rotate_rows).  The mask is one factor
+// per r row, so the elements of a row in no even pair (l = 0 when the
+// row's pairs start at 1, the last l when the count left is odd) are
+// scaled on their own.
+template <typename R>
+__device__ __forceinline__ void rotate_mask_rotate_even(const Tile<R>& tl, int rows, int nl, int j0, int jj, int lane,
+                                                        int lanes, const RotTab<R>& tb, R tau1, R ef1, R tau2, R ef2,
+                                                        bool do_mask) {
+    if (jj < rows) {
+        const int j = j0 + jj;
+        const int l0 = int((int64_t(j) * nl) & 1);
+        const R rqj = tb.rq[j];
+        const R m = do_mask ? tb.mask[j] : R(1);
+        for (int l = l0 + 2 * lane; l + 1 < nl; l += 2 * lanes) {
+            const int k0 = l * ROT_ROWS + jj, k1 = (l + 1) * ROT_ROWS + jj;
+            const R c = tb.cl[l] * rqj;
+            typename Tile<R>::Pair p = tl.load(k0, k1);
+            R cm1, s;
+            rot_coeffs(tau1 * (c * ef1), cm1, s);
+            Tile<R>::rot(p, cm1, s);
+            if (do_mask) Tile<R>::scale(p, m);
+            rot_coeffs(tau2 * (c * ef2), cm1, s);
+            Tile<R>::rot(p, cm1, s);
+            tl.put(k0, k1, p);
+        }
+        if (do_mask && lane == 0) {
+            if (l0 == 1) tl.scale(jj, m);
+            if (((nl - l0) & 1) && nl - 1 >= l0) tl.scale((nl - 1) * ROT_ROWS + jj, m);
         }
     }
     __syncthreads();
@@ -609,7 +692,7 @@ __host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
 }
 
 template <typename R>
-__global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf_dist) {
+__global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf_dist) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int si = plan.rot_items[2 * blockIdx.x];
     const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
@@ -686,6 +769,15 @@ __global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf
     const RotTab<R> tb = RotTab<R>::make(S);
     const int jj = threadIdx.x & (ROT_ROWS - 1), lane = threadIdx.x >> 5;
     const int lanes = blockDim.x >> 5;
+    if (post && pre && !reduce) {
+        // odd(n+1); even(n+1), mask, even(n+2) in one sweep; odd(n+2)
+        const R tp = R(S.tau[n_post]), ep = R(S.efield[n_post]);
+        const R tq = R(S.tau[n_pre]), eq = R(S.efield[n_pre]);
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tp, ep);
+        rotate_mask_rotate_even<R>(tl, rows, nl, j0, jj, lane, lanes, tb, tp, ep, tq, eq, do_mask);
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tq, eq);
+        post = pre = do_mask = false;
+    }
     if (post) {
         const R tau = R(S.tau[n_post]), ef = R(S.efield[n_post]);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
@@ -707,7 +799,7 @@ __global__ void __maxnreg__(48) sh_rot_kernel(ion_sh_plan plan, int mode, int pf
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
     }
-    if (post || pre || do_mask) {
+    if (mode != ROT_REDUCE_ONLY) {
 #pragma unroll 4
         for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
             const int l = f >> 5, j2 = f & (ROT_ROWS - 1);
