@@ -32,13 +32,21 @@ __host__ __device__ __forceinline__ int islot(int i, int T) {
     return (i % M) * T + i / M;
 }
 
-// pivots use the correctly rounded reciprocal
-__device__ __forceinline__ float rcp_ieee(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double rcp_ieee(double x) { return __drcp_rn(x); }
+// Reciprocal of a pivot's squared modulus.  FP64: correctly rounded.  FP32:
+// the hardware approximation (PTX rcp.approx.ftz.f32, within 1 ulp; the
+// pivots are of order one, never subnormal): the FP32 elimination's own
+// rounding is of the same order, and the complex64 forms that need more
+// accuracy refine the solve.
+__device__ __forceinline__ float rcp_pivot(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double rcp_pivot(double x) { return __drcp_rn(x); }
 
 template <typename R>
 __device__ __forceinline__ Cx<R> crecip_fast(Cx<R> z) {
-    const R inv = rcp_ieee(z.re * z.re + z.im * z.im);
+    const R inv = rcp_pivot(z.re * z.re + z.im * z.im);
     return {z.re * inv, -z.im * inv};
 }
 
