@@ -98,18 +98,34 @@ struct NoExtra {
 struct LocalHalo {
     __device__ __forceinline__ bool has_left(int t) const { return t > 0; }
     __device__ __forceinline__ bool has_right(int t, int T) const { return t + 1 < T; }
-    template <typename R, int M>
-    __device__ __forceinline__ Cx<R> left(const Cx<R>* psi, int T, int t) const {
+    template <typename R, int M, class P>
+    __device__ __forceinline__ Cx<R> left(const P& psi, int T, int t) const {
         return psi[(M - 1) * T + t - 1];
     }
-    template <typename R>
-    __device__ __forceinline__ Cx<R> right(const Cx<R>* psi, int T, int t) const {
+    template <typename R, class P>
+    __device__ __forceinline__ Cx<R> right(const P& psi, int T, int t) const {
         return psi[t + 1];
     }
 };
 
-template <typename R, int M, class Coef, class Extra, class Halo = LocalHalo>
-__device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const Cx<R>* psi, const Coef& coef,
+// The line a solve reads (``psi`` of the functions below: a pointer to the
+// interleaved shared-memory line, or a view with operator[]): psi + d / 2
+// formed as it is read (``on``), or psi itself.
+template <typename R>
+struct HalfStepView {
+    const Cx<R>* psi;
+    const Cx<R>* d;
+    bool on;
+    __device__ __forceinline__ Cx<R> operator[](int i) const {
+        const Cx<R> p = psi[i];
+        if (!on) return p;
+        const Cx<R> v = d[i];
+        return Cx<R>{p.re + R(0.5) * v.re, p.im + R(0.5) * v.im};
+    }
+};
+
+template <typename R, int M, class Coef, class Extra, class Halo = LocalHalo, class PsiT = const Cx<R>*>
+__device__ __forceinline__ void cn_chunk_eliminate(int T, int t, R w, const PsiT& psi, const Coef& coef,
                                                    const Extra& extra, Cx<R> (&al)[M], Cx<R> (&be)[M],
                                                    Cx<R> (&ga)[M], RedRow<R>& rowS, RedRow<R>& rowE,
                                                    const Halo& halo = Halo{}) {
@@ -289,8 +305,8 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
 
 // All threads of the CTA call this (threads t >= T only meet the barriers).
 // ``out(i, delta)`` is called for the T*M rows of the padded line.
-template <typename R, int M, class Coef, class Extra, class Out>
-__device__ __forceinline__ void block_cn_solve(int T, int t, R w, const Cx<R>* psi, Cx<R>* red, const Coef& coef,
+template <typename R, int M, class Coef, class Extra, class Out, class PsiT = const Cx<R>*>
+__device__ __forceinline__ void block_cn_solve(int T, int t, R w, const PsiT& psi, Cx<R>* red, const Coef& coef,
                                                const Extra& extra, const Out& out) {
     const bool active = t < T;
     Cx<R> al[M], be[M], ga[M];

@@ -385,21 +385,16 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                                                            M == 16 ? 4 : (M == 8 ? 3 : 2));
             Cx<R>* inc = cur;
             if constexpr (REFINE) {
-                // two solves through one call site: delta1 into ext, then
-                // phi = psi + delta1 / 2 in cur and delta1 + delta into ext
+                // two solves through one call site: delta1 into ext, then on
+                // phi = psi + delta1 / 2 (formed as it is read, so cur keeps
+                // psi for the store) delta1 + delta into ext
                 const bool two = glo != nullptr;
                 if (two) inc = ext;
                 for (int pass = 0; pass < (two ? 2 : 1); ++pass) {
-                    block_cn_solve<R, M>(T, threadIdx.x, R(2), cur, red, coef, MinusIExtra<R, M>{ext, T, pass == 1},
+                    block_cn_solve<R, M>(T, threadIdx.x, R(2), HalfStepView<R>{cur, ext, pass == 1}, red, coef,
+                                         MinusIExtra<R, M>{ext, T, pass == 1},
                                          AddOrSetOut<R, M>{inc, T, pass == 1 || !two});
                     __syncthreads();
-                    if (two && pass == 0) {
-                        for (int i = threadIdx.x; i < T * M; i += blockDim.x) {
-                            const int sl = islot<M>(i, T);
-                            cur[sl] = cur[sl] + scale(ext[sl], R(0.5));
-                        }
-                        __syncthreads();
-                    }
                 }
             } else {
                 // plain: psi + delta into cur; with a residual: delta into cur
@@ -413,8 +408,9 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                 for (int k = 0; k < M; ++k) {
                     const int i = threadIdx.x + k * blockDim.x;
                     if (i < nr) {
+                        // refined: cur still holds psi; otherwise the increment
                         Cx<R> lo = refine ? lob[islot<M>(i, T)] : ld(glo + i);
-                        const Cx<R> h = add_exact(ld(g + i), inc[islot<M>(i, T)], lo);
+                        const Cx<R> h = add_exact(refine ? cur[islot<M>(i, T)] : ld(g + i), inc[islot<M>(i, T)], lo);
                         st(g + i, h);
                         st(glo + i, lo);
                     }
