@@ -112,7 +112,17 @@ class ShTables:
 SH_ROT_ROWS = 32
 
 
-SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8), Precision.C64X: (16, 8)}  # default first
+SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8), Precision.C64X: (8, 16)}  # default first
+SH_MAX_LINE_THREADS = 512  # threads of one radial-solve CTA
+
+
+def sh_default_rows(precision, max_n_r: int) -> int:
+    """Rows per thread of the radial solve when none is asked for: the first
+    choice whose CTA holds the longest line of the batch."""
+    for rows in SH_ROWS_CHOICES[Precision(precision)]:
+        if (max_n_r + rows - 1) // rows <= SH_MAX_LINE_THREADS:
+            return rows
+    return max(SH_ROWS_CHOICES[Precision(precision)])
 
 
 def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
@@ -393,7 +403,8 @@ class ShBatch:
         # radial items grouped in buckets of equal CTA size (largest first);
         # each bucket is one launch whose blocks have exactly the threads its
         # lines need
-        need = [_round32(sh_line_threads(s.n_r, self.precision, self.cn_rows)) for s in sims]
+        rows = self.cn_rows or sh_default_rows(self.precision, max([s.n_r for s in sims] + [2]))
+        need = [_round32(sh_line_threads(s.n_r, self.precision, rows)) for s in sims]
         gran = 32
         while len({(n + gran - 1) // gran * gran for n in need}) > 8:
             gran *= 2
@@ -415,11 +426,11 @@ class ShBatch:
             plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)
         plan.cn_items = ptr(d_cn)
         plan.n_cn_items = len(cn)
-        plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, self.cn_rows) for s in sims] + [1]))
+        plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, rows) for s in sims] + [1]))
         plan.rot_items = ptr(d_rot)
         plan.n_rot_items = len(rot)
         plan.rot_rows = self.rot_rows
-        plan.cn_rows = self.cn_rows
+        plan.cn_rows = rows
         ends, threads = [], []
         for k, (i, _) in enumerate(cn):
             if threads and threads[-1] == bsize[i]:
