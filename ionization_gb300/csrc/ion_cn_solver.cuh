@@ -224,7 +224,8 @@ template <> struct PcrTiny<double> {
 // 10 T complex words of ``red`` (pcr_smem_bytes<R>(T) holds 12 T).  On
 // return r[0].d = xs_t and r[1].d = xe_t.
 template <typename R>
-__device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2]) {
+__device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2],
+                                             R tiny = PcrTiny<R>::value) {
     const Cx<R> zero = {R(0), R(0)}, one = {R(1), R(0)};
     Cx<R>* Sa = red;
     Cx<R>* Sc = red + T;
@@ -257,8 +258,9 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
         Cb[t] = e.c;
         Db[t] = e.d;
     }
-    __syncthreads();
-    const int levels = pcr_levels(T);
+    // the rows may already be decoupled below ``tiny`` (see the loop's exit)
+    const bool coupled0 = active && (cabs1(e.a) > tiny || cabs1(e.c) > tiny);
+    const int levels = __syncthreads_or(coupled0) ? pcr_levels(T) : 0;
     int p = 0;
     for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
         if (active) {
@@ -291,7 +293,7 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
         // |tau H_i,i+1| ~ 0.3 (the spherical-harmonic sweeps) by ~0.26 per
         // row, so two or three levels of chunks of 8 rows already reach
         // this; a slowly decaying line runs every level.
-        const bool coupled = active && (cabs1(e.a) > PcrTiny<R>::value || cabs1(e.c) > PcrTiny<R>::value);
+        const bool coupled = active && (cabs1(e.a) > tiny || cabs1(e.c) > tiny);
         if (!__syncthreads_or(coupled)) break;
     }
     if (active) Xe[t] = e.d;
@@ -305,14 +307,16 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
 
 // All threads of the CTA call this (threads t >= T only meet the barriers).
 // ``out(i, delta)`` is called for the T*M rows of the padded line.
+// ``tiny``: the coupling below which the reduced system's rows count as
+// decoupled (PcrTiny: to the working precision).
 template <typename R, int M, class Coef, class Extra, class Out, class PsiT = const Cx<R>*>
 __device__ __forceinline__ void block_cn_solve(int T, int t, R w, const PsiT& psi, Cx<R>* red, const Coef& coef,
-                                               const Extra& extra, const Out& out) {
+                                               const Extra& extra, const Out& out, R tiny = PcrTiny<R>::value) {
     const bool active = t < T;
     Cx<R> al[M], be[M], ga[M];
     RedRow<R> r[2];
     if (active) cn_chunk_eliminate<R, M>(T, t, w, psi, coef, extra, al, be, ga, r[0], r[1]);
-    pcr_solve_cn<R>(T, t, active, red, r);
+    pcr_solve_cn<R>(T, t, active, red, r, tiny);
     if (active) {
         const int s = t * M;
         const Cx<R> xs = r[0].d, xe = r[1].d;

@@ -391,9 +391,14 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                 const bool two = glo != nullptr;
                 if (two) inc = ext;
                 for (int pass = 0; pass < (two ? 2 : 1); ++pass) {
+                    // The correction of the second solve is ~1e-7 of delta1,
+                    // so its reduced system may stop at couplings below
+                    // 2^-13: the error left, ~1e-4 of the correction, is far
+                    // below the FP32 rounding of the coefficients.
                     block_cn_solve<R, M>(T, threadIdx.x, R(2), HalfStepView<R>{cur, ext, pass == 1}, red, coef,
                                          MinusIExtra<R, M>{ext, T, pass == 1},
-                                         AddOrSetOut<R, M>{inc, T, pass == 1 || !two});
+                                         AddOrSetOut<R, M>{inc, T, pass == 1 || !two},
+                                         pass == 1 ? R(1.0 / 8192.0) : PcrTiny<R>::value);
                     __syncthreads();
                 }
             } else {
