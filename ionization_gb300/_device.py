@@ -11,6 +11,7 @@ simulations of different sizes in one batch.
 import concurrent.futures
 import ctypes
 import dataclasses
+import os
 from typing import List, Optional
 
 import numpy as np
@@ -130,18 +131,50 @@ def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
     return (n_r + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
+class _Fill:
+    """A host array written straight into its upload buffer (``fill(dest)``,
+    dest flat, of ``dtype``) instead of being formed and then copied."""
+
+    def __init__(self, shape, dtype, fill):
+        self.shape = tuple(shape)
+        self.dtype = np.dtype(dtype)
+        self.size = int(np.prod(self.shape))
+        self.fill = fill
+
+    def materialize(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        self.fill(out.reshape(-1))
+        return out
+
+
+def _split_hi(g0):
+    def fill(dest):
+        dest[...] = g0.reshape(-1)  # rounded to complex64
+
+    return fill
+
+
+def _split_lo(g0):
+    def fill(dest):
+        flat = g0.reshape(-1)
+        dest[...] = flat - flat.astype(np.complex64)  # the rounding error, in complex64
+
+    return fill
+
+
 def _sh_host_arrays(tab: ShTables, precision) -> dict:
     """The host arrays a spherical-harmonic simulation uploads (None where
-    absent), by attribute name, in their device dtype."""
+    absent), by attribute name, in their device dtype (complex64 psi as
+    ``_Fill``: rounded as it is written to the upload buffer)."""
     precision = Precision(precision)
     f64, f32 = np.float64, np.float32
     g0 = np.asarray(tab.g0, dtype=np.complex128)
     c128 = precision == Precision.C128
     a = {}
-    a["g"] = g0 if c128 else g0.astype(np.complex64)
+    a["g"] = g0 if c128 else _Fill(g0.shape, np.complex64, _split_hi(g0))
     a["g_lo"] = None
     if precision == Precision.C64X:  # psi = g + g_lo
-        a["g_lo"] = (g0 - g0.astype(np.complex64).astype(np.complex128)).astype(np.complex64)
+        a["g_lo"] = _Fill(g0.shape, np.complex64, _split_lo(g0))
     a["d_hd"] = np.asarray(tab.hd, f64) if c128 else None
     a["d_hoff"] = np.asarray(tab.hoff, f64)
     a["d_rq"] = np.asarray(tab.rq, f64)
@@ -202,14 +235,19 @@ class _Arena:
         n = max(self.size, 1)
         host = torch.empty(n, dtype=tdt, pin_memory=self.pin)
         hv = host.numpy()
-        # pack on a few threads: numpy copies of large arrays run outside the GIL
-        chunks = [self.items[k::4] for k in range(4)]
+        # pack on a few threads: numpy copies and casts of large arrays run
+        # outside the GIL
+        nthr = max(1, min(8, os.cpu_count() or 1))
+        chunks = [self.items[k::nthr] for k in range(nthr)]
 
         def pack(items):
             for _, arr, off in items:
-                hv[off:off + arr.size] = arr.reshape(-1)
+                if isinstance(arr, _Fill):
+                    arr.fill(hv[off:off + arr.size])
+                else:
+                    hv[off:off + arr.size] = arr.reshape(-1)
 
-        with concurrent.futures.ThreadPoolExecutor(max_workers=4) as pool:
+        with concurrent.futures.ThreadPoolExecutor(max_workers=nthr) as pool:
             list(pool.map(pack, chunks))
         dev_buf = torch.empty(n, dtype=tdt, device=device())
         dev_buf.copy_(host, non_blocking=self.pin)
@@ -230,7 +268,8 @@ class ShDeviceSim:
         self.store_every = int(tab.store_every)
         self.gauge = int(tab.gauge)
         if arrays is None:
-            arrays = {k: (to_dev(v) if v is not None else None) for k, v in _sh_host_arrays(tab, precision).items()}
+            arrays = {k: (to_dev(v.materialize() if isinstance(v, _Fill) else v) if v is not None else None)
+                      for k, v in _sh_host_arrays(tab, precision).items()}
             self.n_data, n_states, self.n_tiles = _sh_device_sizes(tab)
             arrays["d_norm"] = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
             arrays["d_ip"] = torch.full((self.n_data * max(n_states, 1) * 2,), float("nan"), dtype=torch.float64,
@@ -250,8 +289,13 @@ class ShDeviceSim:
         arenas = {}
         with concurrent.futures.ThreadPoolExecutor(max_workers=8) as pool:  # numpy work outside the GIL
             per = list(pool.map(lambda tab: _sh_host_arrays(tab, precision), tables))
-        for i, host in enumerate(per):
-            for k, v in host.items():
+        # every simulation's g, then every g_lo (same sizes, so the two runs
+        # have the same layout and psi = g + g_lo is formed over both at
+        # once: sh_psi_many), then the tables
+        order = ["g", "g_lo"] + [k for k in (per[0] if per else {}) if k not in ("g", "g_lo")]
+        for k in order:
+            for i, host in enumerate(per):
+                v = host.get(k)
                 if v is not None:
                     arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
         views = {}
@@ -345,9 +389,37 @@ def sh_data_many(sims: List["ShDeviceSim"]):
     return out
 
 
+def _run_of(ts: List[torch.Tensor]):
+    """(base, first offset, end offset) when the tensors are contiguous views
+    of one buffer in increasing order, else None."""
+    if not ts or any(t._base is None or not t.is_contiguous() for t in ts):
+        return None
+    base = ts[0]._base
+    offs = [t.storage_offset() for t in ts]
+    if any(t._base is not base for t in ts) or any(b < a for a, b in zip(offs, offs[1:])):
+        return None
+    return base, offs[0], offs[-1] + ts[-1].numel()
+
+
 def sh_psi_many(sims: List["ShDeviceSim"]) -> List[np.ndarray]:
-    """psi (g + g_lo) of every simulation, complex128: one copy per storage
-    buffer when they share one, else one by one."""
+    """psi (g + g_lo) of every simulation, complex128.  When the g and the
+    g_lo of all simulations are two equal runs of one buffer (the layout of
+    ``ShDeviceSim.bulk``), the sum is formed on the device over both runs at
+    once and read back with one copy; else one copy per storage buffer and
+    the sum on the host."""
+    gs = [s.g for s in sims]
+    los = [s.g_lo for s in sims]
+    rg = _run_of(gs)
+    rl = _run_of(los) if all(t is not None for t in los) else None
+    if rg is not None and rl is not None and rg[0] is rl[0] and rg[2] - rg[1] == rl[2] - rl[1] and \
+            all(b.storage_offset() - a.storage_offset() == rl[1] - rg[1] for a, b in zip(gs, los)):
+        base, g0, g1 = rg
+        flat = base.reshape(-1)
+        psi = flat[g0:g1].to(torch.complex128)
+        psi += flat[rl[1]:rl[2]]
+        host = _host_copy(psi)
+        return [host[g.storage_offset() - g0:g.storage_offset() - g0 + g.numel()].reshape(tuple(g.shape))
+                for g in gs]
     bases = {}
     for s in sims:
         for t in (s.g, s.g_lo):
@@ -408,13 +480,28 @@ class ShBatch:
         gran = 32
         while len({(n + gran - 1) // gran * gran for n in need}) > 8:
             gran *= 2
-        bsize = [(n + gran - 1) // gran * gran for n in need]
-        cn = sorted(((i, l) for i, s in enumerate(sims) for l in range(s.n_l)),
-                    key=lambda it: (-bsize[it[0]], -sims[it[0]].n_r))
-        rot = sorted(((i, k) for i, s in enumerate(sims) for k in range(s.n_tiles)),
-                     key=lambda it: -sims[it[0]].n_l)
-        d_cn = to_dev(np.asarray(cn if cn else [(0, 0)], dtype=np.int32).reshape(-1))
-        d_rot = to_dev(np.asarray(rot if rot else [(0, 0)], dtype=np.int32).reshape(-1))
+        bsize = np.array([(n + gran - 1) // gran * gran for n in need], dtype=np.int64)
+        n_r = np.array([s.n_r for s in sims], dtype=np.int64)
+        n_l = np.array([s.n_l for s in sims], dtype=np.int64)
+        n_t = np.array([s.n_tiles for s in sims], dtype=np.int64)
+
+        def items(counts):
+            # (simulation, index) for every index below each count, in order
+            sim = np.repeat(np.arange(len(counts), dtype=np.int64), counts)
+            first = np.repeat(np.cumsum(counts) - counts, counts)
+            return sim, np.arange(sim.size, dtype=np.int64) - first
+
+        # stable sorts: lines by CTA size, then n_r, descending; tiles by n_l
+        cs, cl = items(n_l)
+        order = np.lexsort((-n_r[cs], -bsize[cs]))
+        cs, cl = cs[order], cl[order]
+        rs, rk = items(n_t)
+        order = np.argsort(-n_l[rs], kind="stable")
+        rs, rk = rs[order], rk[order]
+        cn = np.stack([cs, cl], axis=1).astype(np.int32) if cs.size else np.zeros((1, 2), np.int32)
+        rot = np.stack([rs, rk], axis=1).astype(np.int32) if rs.size else np.zeros((1, 2), np.int32)
+        d_cn = to_dev(cn.reshape(-1))
+        d_rot = to_dev(rot.reshape(-1))
         plan = nat.ShPlan()
         plan.sims = ptr(d_descs)
         plan.n_sims = len(sims)
@@ -425,19 +512,16 @@ class ShBatch:
         if n_vel:
             plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)
         plan.cn_items = ptr(d_cn)
-        plan.n_cn_items = len(cn)
+        plan.n_cn_items = int(cs.size)
         plan.cn_threads = _round32(max([sh_line_threads(s.n_r, self.precision, rows) for s in sims] + [1]))
         plan.rot_items = ptr(d_rot)
-        plan.n_rot_items = len(rot)
+        plan.n_rot_items = int(rs.size)
         plan.rot_rows = self.rot_rows
         plan.cn_rows = rows
-        ends, threads = [], []
-        for k, (i, _) in enumerate(cn):
-            if threads and threads[-1] == bsize[i]:
-                ends[-1] = k + 1
-            else:
-                threads.append(bsize[i])
-                ends.append(k + 1)
+        bs_sorted = bsize[cs]
+        starts = np.concatenate([[0], np.nonzero(np.diff(bs_sorted))[0] + 1]) if cs.size else np.zeros(0, np.int64)
+        threads = [int(bs_sorted[k]) for k in starts]
+        ends = [int(k) for k in starts[1:]] + ([int(cs.size)] if cs.size else [])
         plan.cn_threads = max(threads + [32])
         plan.n_cn_buckets = len(threads)
         for b, (e, th) in enumerate(zip(ends, threads)):

@@ -506,6 +506,8 @@ template <> struct Tile<double> {
         hi[k1] = Cx<double>{x1.re + (cm1 * x1.re - s * x0.re), x1.im + (cm1 * x1.im - s * x0.im)};
     }
     __device__ void scale(int k, double m) const { hi[k] = scaled(hi[k], m); }
+    __device__ __forceinline__ static void renorm(Pair&, bool) {}
+    __device__ void renorm(int, bool) const {}
     __device__ Cx<double> out(int k) const { return hi[k]; }
     __device__ __forceinline__ void store(int k, Cx<double>* g, Cx<double>*, int64_t at) const { st(g + at, hi[k]); }
 };
@@ -571,6 +573,24 @@ template <> struct Tile<float> {
         hi[k] = h;
         lo[k] = l;
     }
+    // what a store and a reload between launches do to (hi, lo): hi + lo
+    // rounded, and with a stored residual (keep) its rounding error as lo
+    // (Fast2Sum), else lo = 0
+    __device__ __forceinline__ static void renorm(Cx<float>& h, Cx<float>& l, bool keep) {
+        const float sr = h.re + l.re, si = h.im + l.im;
+        l = keep ? Cx<float>{l.re - (sr - h.re), l.im - (si - h.im)} : Cx<float>{0.f, 0.f};
+        h = Cx<float>{sr, si};
+    }
+    __device__ __forceinline__ static void renorm(Pair& p, bool keep) {
+        renorm(p.x0, p.l0, keep);
+        renorm(p.x1, p.l1, keep);
+    }
+    __device__ void renorm(int k, bool keep) const {
+        Cx<float> h = hi[k], l = lo[k];
+        renorm(h, l, keep);
+        hi[k] = h;
+        lo[k] = l;
+    }
     __device__ Cx<float> out(int k) const { return Cx<float>{hi[k].re + lo[k].re, hi[k].im + lo[k].im}; }
     // element k to g[at]: hi + lo folded, or, with a stored residual, hi + lo
     // renormalised (Fast2Sum, |hi| >= |lo|) into g[at] and glo[at]
@@ -603,16 +623,18 @@ __device__ __forceinline__ void rotate_rows(const Tile<R>& tl, int rows, int nl,
 }
 
 // Between two solves with no data stored in between: the even rotation of
-// time index n1, the mask, and the even rotation of n2, applied to each pair
-// in registers (one sweep instead of three; the same arithmetic, operator by
-// operator, as rotate_rows / mask / rotate_rows).  The mask is one factor
-// per r row, so the elements of a row in no even pair (l = 0 when the
-// row's pairs start at 1, the last l when the count left is odd) are
-// scaled on their own.
+// time index n1, the mask, the renormalisation of (hi, lo) that a store and
+// reload between the two would make, and the even rotation of n2, applied to
+// each pair in registers (one sweep instead of four; the same arithmetic,
+// operator by operator, as separate sweeps or separate launches, so results
+// do not depend on where a run is cut into launches).  The mask is one
+// factor per r row, so the elements of a row in no even pair (l = 0 when
+// the row's pairs start at 1, the last l when the count left is odd) are
+// scaled and renormalised on their own.
 template <typename R>
 __device__ __forceinline__ void rotate_mask_rotate_even(const Tile<R>& tl, int rows, int nl, int j0, int jj, int lane,
                                                         int lanes, const RotTab<R>& tb, R tau1, R ef1, R tau2, R ef2,
-                                                        bool do_mask) {
+                                                        bool do_mask, bool keep) {
     if (jj < rows) {
         const int j = j0 + jj;
         const int l0 = int((int64_t(j) * nl) & 1);
@@ -626,13 +648,21 @@ __device__ __forceinline__ void rotate_mask_rotate_even(const Tile<R>& tl, int r
             rot_coeffs(tau1 * (c * ef1), cm1, s);
             Tile<R>::rot(p, cm1, s);
             if (do_mask) Tile<R>::scale(p, m);
+            Tile<R>::renorm(p, keep);
             rot_coeffs(tau2 * (c * ef2), cm1, s);
             Tile<R>::rot(p, cm1, s);
             tl.put(k0, k1, p);
         }
-        if (do_mask && lane == 0) {
-            if (l0 == 1) tl.scale(jj, m);
-            if (((nl - l0) & 1) && nl - 1 >= l0) tl.scale((nl - 1) * ROT_ROWS + jj, m);
+        if (lane == 0) {
+            if (l0 == 1) {
+                if (do_mask) tl.scale(jj, m);
+                tl.renorm(jj, keep);
+            }
+            if (((nl - l0) & 1) && nl - 1 >= l0) {
+                const int k = (nl - 1) * ROT_ROWS + jj;
+                if (do_mask) tl.scale(k, m);
+                tl.renorm(k, keep);
+            }
         }
     }
     __syncthreads();
@@ -775,7 +805,7 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
         const R tp = R(S.tau[n_post]), ep = R(S.efield[n_post]);
         const R tq = R(S.tau[n_pre]), eq = R(S.efield[n_pre]);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tp, ep);
-        rotate_mask_rotate_even<R>(tl, rows, nl, j0, jj, lane, lanes, tb, tp, ep, tq, eq, do_mask);
+        rotate_mask_rotate_even<R>(tl, rows, nl, j0, jj, lane, lanes, tb, tp, ep, tq, eq, do_mask, glo != nullptr);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tq, eq);
         post = pre = do_mask = false;
     }
@@ -793,6 +823,11 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
     }
     if (reduce) {
         reduce_tile<R>(S, tl, rows, nl, j0, tile_idx, scratch);
+        __syncthreads();
+    }
+    if (post && pre && Tile<R>::comp) {  // as if stored and reloaded between the two (see above)
+        for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x)
+            if ((f & (ROT_ROWS - 1)) < rows) tl.renorm(f, glo != nullptr);
         __syncthreads();
     }
     if (pre) {

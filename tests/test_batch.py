@@ -1,0 +1,61 @@
+"""Batched form (ionization_gb300.batch): simulations of different sizes,
+pulses, step counts and data cadences advanced together give, each, exactly
+what the same simulation gives on the plain mesh path (spec.to_sim().run()):
+the kernels' arithmetic on a line or a row tile does not depend on its
+batch-mates.  The bulk readback (psi_all, results) equals the per-simulation
+one."""
+
+import numpy as np
+import pytest
+
+from ionization_gb300 import workloads as wl
+
+
+def _specs(precision):
+    # (r_points, l_bound, E0, omega, cycles, cep, steps, store_data_every)
+    shapes = [
+        (300, 12, 0.05, 0.1, 2, 0.0, 40, -1),
+        (170, 7, 0.08, 0.06, 2, 1.0, 55, 5),
+        (520, 21, 0.03, 0.2, 3, 0.3, 33, 4),
+        (96, 3, 0.1, 0.15, 1, 2.0, 17, -1),
+    ]
+    return [wl.sh_spec(f"batch_{k}", *p[:7], precision=precision, store_data_every=p[7],
+                       mask_width=0.4 * wl.DR * p[0])
+            for k, p in enumerate(shapes)]
+
+
+def test_batch_specs_are_uneven():
+    specs = _specs("c128")
+    assert len({s.r_points for s in specs}) == len(specs)
+    assert len({s.time_final for s in specs}) == len(specs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["c128", "c64x", "c64"])
+def test_batch_equals_each_simulation_alone(cuda, precision):
+    from ionization_gb300 import batch as bm
+
+    b = bm.BatchedSphericalHarmonicSimulation(_specs(precision), graph_steps=8)
+    b.run()
+    res = b.results()
+    psis = b.psi_all()
+    for k, spec in enumerate(_specs(precision)):
+        sim = spec.to_sim()
+        sim.run()
+        want = np.asarray(sim.mesh.g)
+        np.testing.assert_array_equal(psis[k], want)
+        np.testing.assert_array_equal(b.psi(k), want)
+        np.testing.assert_array_equal(res[k]["norm"], sim.data.norm)
+        got = list(res[k]["inner_products"].values())  # in test-state order
+        for v, st in zip(got, sim.spec.test_states, strict=True):
+            np.testing.assert_array_equal(v, sim.data.inner_products[st])
+
+
+@pytest.mark.gpu
+def test_autotune_times_every_candidate(cuda):
+    from ionization_gb300 import _device as dev
+    from ionization_gb300 import batch as bm
+
+    best, timings = bm.autotune(_specs("c64x"), precision="c64x", graph_steps=(4,), steps=4)
+    assert set(timings) == {(r, 4) for r in dev.SH_ROWS_CHOICES[dev.Precision.C64X]}
+    assert best in timings and all(v > 0 for v in timings.values())
