@@ -40,8 +40,39 @@ def to_dev(a, dtype=None) -> torch.Tensor:
     return torch.from_numpy(a).to(device(), non_blocking=False)
 
 
-def ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+def ptr(t) -> Optional[int]:
+    """Device address of a tensor or of a ``_DevSlice`` (None: NULL)."""
     return None if t is None else t.data_ptr()
+
+
+class _DevSlice:
+    """Part of a bulk device buffer held as (buffer, element offset, shape):
+    the descriptors need only its address, and a torch view (``tensor``) is
+    made on first use (thousands of small views cost tens of ms to make)."""
+
+    __slots__ = ("buf", "off", "shape", "_t")
+
+    def __init__(self, buf: torch.Tensor, off: int, shape):
+        self.buf, self.off, self.shape, self._t = buf, int(off), tuple(shape), None
+
+    def data_ptr(self) -> int:
+        return self.buf.data_ptr() + self.off * self.buf.element_size()
+
+    def numel(self) -> int:
+        return int(np.prod(self.shape))
+
+    def element_size(self) -> int:
+        return self.buf.element_size()
+
+    @property
+    def tensor(self) -> torch.Tensor:
+        if self._t is None:
+            self._t = self.buf[self.off:self.off + self.numel()].view(self.shape)
+        return self._t
+
+
+def _tensor(t):
+    return t.tensor if isinstance(t, _DevSlice) else t
 
 
 def n_data_slots(t_final: int, store_every: int) -> int:
@@ -228,7 +259,9 @@ class _Arena:
     # copy instead: 0.33 s every time)
     pin = True
 
-    def upload(self) -> dict:
+    def upload(self, tensors=()) -> dict:
+        """Device views by key: torch views for the keys whose name is in
+        ``tensors`` (keys are (index, name)), ``_DevSlice`` for the rest."""
         tdt = {np.dtype(np.float64): torch.float64, np.dtype(np.float32): torch.float32,
                np.dtype(np.int32): torch.int32, np.dtype(np.complex64): torch.complex64,
                np.dtype(np.complex128): torch.complex128}[self.np_dtype]
@@ -237,7 +270,7 @@ class _Arena:
         hv = host.numpy()
         # pack on a few threads: numpy copies and casts of large arrays run
         # outside the GIL
-        nthr = max(1, min(8, os.cpu_count() or 1))
+        nthr = max(1, min(16, os.cpu_count() or 1))
         chunks = [self.items[k::nthr] for k in range(nthr)]
 
         def pack(items):
@@ -251,7 +284,9 @@ class _Arena:
             list(pool.map(pack, chunks))
         dev_buf = torch.empty(n, dtype=tdt, device=device())
         dev_buf.copy_(host, non_blocking=self.pin)
-        return {key: dev_buf[off:off + arr.size].view(arr.shape) for key, arr, off in self.items}
+        return {key: (dev_buf[off:off + arr.size].view(arr.shape) if key[1] in tensors
+                      else _DevSlice(dev_buf, off, arr.shape))
+                for key, arr, off in self.items}
 
 
 class ShDeviceSim:
@@ -300,7 +335,7 @@ class ShDeviceSim:
                     arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
         views = {}
         for ar in arenas.values():
-            views.update(ar.upload())
+            views.update(ar.upload(tensors=("g", "g_lo")))
         torch.cuda.current_stream().synchronize()  # the pinned sources are released below
         sizes = [_sh_device_sizes(tab) for tab in tables]
         n_norm = sum(nd for nd, _, _ in sizes)
@@ -313,9 +348,9 @@ class ShDeviceSim:
         for i, tab in enumerate(tables):
             nd, ns, nt = sizes[i]
             arrays = {k: views.get((i, k)) for k in per[i]}
-            arrays["d_norm"] = d_norm[o_norm:o_norm + nd]
-            arrays["d_ip"] = d_ip[o_ip:o_ip + nd * max(ns, 1) * 2]
-            arrays["d_partials"] = d_part[o_part:o_part + nt * (1 + 2 * ns)]
+            arrays["d_norm"] = _DevSlice(d_norm, o_norm, (nd,))
+            arrays["d_ip"] = _DevSlice(d_ip, o_ip, (nd * max(ns, 1) * 2,))
+            arrays["d_partials"] = _DevSlice(d_part, o_part, (nt * (1 + 2 * ns),))
             sim = cls(tab, precision, arrays=arrays)
             sim._bulk = dict(norm=(d_norm, o_norm, nd), ip=(d_ip, o_ip, nd * max(ns, 1) * 2))
             o_norm += nd
@@ -328,7 +363,7 @@ class ShDeviceSim:
     def nbytes(self) -> int:
         tot = 0
         for v in vars(self).values():
-            if isinstance(v, torch.Tensor):
+            if isinstance(v, (torch.Tensor, _DevSlice)):
                 tot += v.numel() * v.element_size()
         return tot
 
@@ -354,8 +389,8 @@ class ShDeviceSim:
 
     def data(self):
         """(norm[n_data], inner_products[n_states, n_data]) on the host."""
-        norm = self.d_norm.cpu().numpy()
-        ip = self.d_ip.cpu().numpy()[: self.n_data * self.n_states * 2].view(np.complex128)
+        norm = _tensor(self.d_norm).cpu().numpy()
+        ip = _tensor(self.d_ip).cpu().numpy()[: self.n_data * self.n_states * 2].view(np.complex128)
         return norm, ip.reshape(self.n_data, self.n_states).T.copy()
 
     def psi_host(self) -> np.ndarray:
