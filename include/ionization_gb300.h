@@ -126,8 +126,9 @@ int64_t ion_tdma_batched_max_n_c64(void);
  * the (l, r) mesh, exactly as the reference builds its even/odd matrices.
  * Between two solves with no data stored in between, R_even(t+1), the mask
  * and R_even(t+2) are applied to each pair in registers in one sweep, with
- * the same arithmetic as three separate sweeps: results do not depend on
- * how the steps are split into calls (complex128 bit for bit).
+ * the same arithmetic as separate sweeps, and a complex64 state's (hi, lo)
+ * pair is renormalised there as a store and reload between two calls would:
+ * results do not depend on how the steps are split into calls, bit for bit.
  *
  * psi of every simulation is stored (n_l, n_r) in C order (r contiguous),
  * the layout of the reference's ``mesh.g``, at its own device pointer.  A batch
@@ -422,6 +423,11 @@ int ion_reduce_c128(int64_t M, const void *g, int32_t n_states, const void *stat
                     double *out_norm, double *out_ip, void *partials, void *stream);
 int ion_reduce_c64(int64_t M, const void *g, int32_t n_states, const void *states, double weight,
                    double *out_norm, double *out_ip, void *partials, void *stream);
+
+/* psi of a complex64 state read back as complex128 (the g property of a
+ * complex64 mesh, QuantumMesh.g): out[i] = hi[i] + lo[i] in FP64, lo (the
+ * stored residual) may be NULL.  n complex elements, device pointers. */
+int ion_psi_to_c128(int64_t n, const void *hi, const void *lo, void *out, void *stream);
 
 /* ------------------------------------------------------------------------
  * Position expectation values and partial norms (the ZExpectationValue,

@@ -437,21 +437,25 @@ def _run_of(ts: List[torch.Tensor]):
 
 
 def sh_psi_many(sims: List["ShDeviceSim"]) -> List[np.ndarray]:
-    """psi (g + g_lo) of every simulation, complex128.  When the g and the
-    g_lo of all simulations are two equal runs of one buffer (the layout of
-    ``ShDeviceSim.bulk``), the sum is formed on the device over both runs at
-    once and read back with one copy; else one copy per storage buffer and
-    the sum on the host."""
+    """psi (g + g_lo) of every simulation, complex128.  When the g of all
+    simulations are one run of a complex64 buffer, and their g_lo another run
+    with the same layout (``ShDeviceSim.bulk``), psi is formed on the device
+    over the whole run (ion_psi_to_c128) and read back with one copy; else
+    one copy per storage buffer and the sum on the host."""
     gs = [s.g for s in sims]
     los = [s.g_lo for s in sims]
     rg = _run_of(gs)
-    rl = _run_of(los) if all(t is not None for t in los) else None
-    if rg is not None and rl is not None and rg[0] is rl[0] and rg[2] - rg[1] == rl[2] - rl[1] and \
-            all(b.storage_offset() - a.storage_offset() == rl[1] - rg[1] for a, b in zip(gs, los)):
+    has_lo = all(t is not None for t in los)
+    rl = _run_of(los) if has_lo else None
+    if rg is not None and rg[0].dtype == torch.complex64 and (
+            not any(t is not None for t in los) or
+            (rl is not None and rg[0] is rl[0] and rg[2] - rg[1] == rl[2] - rl[1] and
+             all(b.storage_offset() - a.storage_offset() == rl[1] - rg[1] for a, b in zip(gs, los)))):
         base, g0, g1 = rg
         flat = base.reshape(-1)
-        psi = flat[g0:g1].to(torch.complex128)
-        psi += flat[rl[1]:rl[2]]
+        psi = torch.empty(g1 - g0, dtype=torch.complex128, device=base.device)
+        lo = flat[rl[1]:rl[2]] if rl is not None else None
+        nat.call("ion_psi_to_c128", g1 - g0, ptr(flat[g0:g1]), ptr(lo), ptr(psi), stream_ptr())
         host = _host_copy(psi)
         return [host[g.storage_offset() - g0:g.storage_offset() - g0 + g.numel()].reshape(tuple(g.shape))
                 for g in gs]

@@ -203,6 +203,7 @@ _SIGS = {
     "ion_reduce_scratch_bytes": (c_i64, [c_i64, c_i32]),
     "ion_reduce_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
     "ion_reduce_c64": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]),
+    "ion_psi_to_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp]),
     "ion_weighted_norms_scratch_bytes": (c_i64, [c_i64, c_i32]),
     "ion_weighted_norms_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
     "ion_weighted_norms_c64": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),

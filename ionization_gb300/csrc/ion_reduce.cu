@@ -102,6 +102,22 @@ static int reduce_impl(int64_t M, const void* g, int32_t ns, const void* states,
     return check_launch("reduce_stage2");
 }
 
+// psi of a complex64 state as complex128: hi + lo (lo, the stored residual,
+// may be absent), each component one FP64 sum of two floats.  Memory-bound;
+// coalesced 8-byte loads, 16-byte stores.
+__global__ void __launch_bounds__(256) psi_to_c128_kernel(int64_t n, const Cx<float>* hi, const Cx<float>* lo,
+                                                          Cx<double>* out) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const Cx<float> h = hi[i];
+        Cx<double> v = {double(h.re), double(h.im)};
+        if (lo) {
+            const Cx<float> l = lo[i];
+            v = Cx<double>{v.re + double(l.re), v.im + double(l.im)};
+        }
+        out[i] = v;
+    }
+}
+
 }  // namespace ion
 
 using namespace ion;
@@ -118,5 +134,18 @@ int ion_reduce_c128(int64_t M, const void* g, int32_t n_states, const void* stat
 int ion_reduce_c64(int64_t M, const void* g, int32_t n_states, const void* states, double weight,
                    double* out_norm, double* out_ip, void* partials, void* stream) {
     return reduce_impl<float>(M, g, n_states, states, weight, out_norm, out_ip, partials, stream);
+}
+int ion_psi_to_c128(int64_t n, const void* hi, const void* lo, void* out, void* stream) {
+    if (n < 0 || (n > 0 && (!hi || !out))) {
+        set_error("ion_psi_to_c128: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return ION_OK;
+    const int64_t want = (n + 255) / 256;
+    const int blocks = int(want < 8 * 152 ? want : 8 * 152);
+    psi_to_c128_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, static_cast<const Cx<float>*>(hi),
+                                                               static_cast<const Cx<float>*>(lo),
+                                                               static_cast<Cx<double>*>(out));
+    return check_launch("psi_to_c128_kernel");
 }
 }
