@@ -329,18 +329,28 @@ __device__ __forceinline__ void block_cn_solve(int T, int t, R w, const PsiT& ps
 
 // ---------------------------------------------------------------------------
 // Rotation coefficients cos(a) - 1 and sin(a).
-// |a| <= 0.5: Maclaurin series of sin and cos evaluated with Horner's rule in
-// a^2 (truncated where the next term is below 1e-10 of the last kept one in
-// FP32 and below 1e-22 in FP64); otherwise sincos() with
-// cos(a) - 1 = -2 sin^2(a/2).  Returning cos - 1 lets the rotation be
-// applied in increment form.
+// |a| <= 0.5: Maclaurin series of sin and cos, as polynomials in a^2 with
+// the coefficients (-1)^k / n! evaluated by Horner's rule (one fma per
+// term), truncated where the next term is below 1e-10 of the last kept one
+// in FP32 and below 1e-22 in FP64:
+//   sin a = a + (a a^2) P(a^2),   cos a - 1 = a^2 Q(a^2).
+// Otherwise sincos() with cos(a) - 1 = -2 sin^2(a/2).  Returning cos - 1
+// lets the rotation be applied in increment form.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void rot_coeffs(float a, float& cm1, float& s) {
     if (fabsf(a) <= 0.5f) {
         const float a2 = a * a;
-        s = a * (1.f - a2 * (1.f / 6.f) * (1.f - a2 * (1.f / 20.f) * (1.f - a2 * (1.f / 42.f) * (1.f - a2 * (1.f / 72.f)))));
-        cm1 = -0.5f * a2 *
-              (1.f - a2 * (1.f / 12.f) * (1.f - a2 * (1.f / 30.f) * (1.f - a2 * (1.f / 56.f) * (1.f - a2 * (1.f / 90.f)))));
+        float p = 1.f / 362880.f;               // 1/9!
+        p = fmaf(p, a2, -1.f / 5040.f);         // -1/7!
+        p = fmaf(p, a2, 1.f / 120.f);           // 1/5!
+        p = fmaf(p, a2, -1.f / 6.f);            // -1/3!
+        s = fmaf(a * a2, p, a);
+        float q = -1.f / 3628800.f;             // -1/10!
+        q = fmaf(q, a2, 1.f / 40320.f);         // 1/8!
+        q = fmaf(q, a2, -1.f / 720.f);          // -1/6!
+        q = fmaf(q, a2, 1.f / 24.f);            // 1/4!
+        q = fmaf(q, a2, -0.5f);                 // -1/2!
+        cm1 = a2 * q;
     } else {
         float c;
         sincosf(a, &s, &c);
@@ -352,24 +362,28 @@ __device__ __forceinline__ void rot_coeffs(float a, float& cm1, float& s) {
 __device__ __forceinline__ void rot_coeffs(double a, double& cm1, double& s) {
     if (fabs(a) <= 0.5) {
         const double a2 = a * a;
-        double ps = 1.0 - a2 * (1.0 / 272.0);
-        ps = 1.0 - a2 * (1.0 / 210.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 156.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 110.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 72.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 42.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 20.0) * ps;
-        ps = 1.0 - a2 * (1.0 / 6.0) * ps;
-        s = a * ps;
-        double pc = 1.0 - a2 * (1.0 / 306.0);
-        pc = 1.0 - a2 * (1.0 / 240.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 182.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 132.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 90.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 56.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 30.0) * pc;
-        pc = 1.0 - a2 * (1.0 / 12.0) * pc;
-        cm1 = -0.5 * a2 * pc;
+        // 1/n! for odd n = 19 .. 3 and even n = 20 .. 2, alternating in sign
+        double p = -1.0 / 121645100408832000.0;  // -1/19!
+        p = fma(p, a2, 1.0 / 355687428096000.0);  // 1/17!
+        p = fma(p, a2, -1.0 / 1307674368000.0);   // -1/15!
+        p = fma(p, a2, 1.0 / 6227020800.0);       // 1/13!
+        p = fma(p, a2, -1.0 / 39916800.0);        // -1/11!
+        p = fma(p, a2, 1.0 / 362880.0);           // 1/9!
+        p = fma(p, a2, -1.0 / 5040.0);            // -1/7!
+        p = fma(p, a2, 1.0 / 120.0);              // 1/5!
+        p = fma(p, a2, -1.0 / 6.0);               // -1/3!
+        s = fma(a * a2, p, a);
+        double q = 1.0 / 2432902008176640000.0;   // 1/20!
+        q = fma(q, a2, -1.0 / 6402373705728000.0);  // -1/18!
+        q = fma(q, a2, 1.0 / 20922789888000.0);     // 1/16!
+        q = fma(q, a2, -1.0 / 87178291200.0);       // -1/14!
+        q = fma(q, a2, 1.0 / 479001600.0);          // 1/12!
+        q = fma(q, a2, -1.0 / 3628800.0);           // -1/10!
+        q = fma(q, a2, 1.0 / 40320.0);              // 1/8!
+        q = fma(q, a2, -1.0 / 720.0);               // -1/6!
+        q = fma(q, a2, 1.0 / 24.0);                 // 1/4!
+        q = fma(q, a2, -0.5);                       // -1/2!
+        cm1 = a2 * q;
     } else {
         double c;
         sincos(a, &s, &c);
