@@ -331,14 +331,24 @@ __device__ __forceinline__ void block_cn_solve(int T, int t, R w, const PsiT& ps
 // Rotation coefficients cos(a) - 1 and sin(a).
 // |a| <= 0.5: Maclaurin series of sin and cos, as polynomials in a^2 with
 // the coefficients (-1)^k / n! evaluated by Horner's rule (one fma per
-// term), truncated where the next term is below 1e-10 of the last kept one
-// in FP32 and below 1e-22 in FP64:
-//   sin a = a + (a a^2) P(a^2),   cos a - 1 = a^2 Q(a^2).
-// Otherwise sincos() with cos(a) - 1 = -2 sin^2(a/2).  Returning cos - 1
-// lets the rotation be applied in increment form.
+// term):
+//   sin a = a + (a a^2) P(a^2),   cos a - 1 = a^2 Q(a^2),
+// truncated where the next term is below 1e-10 of the result in FP32 and
+// below 1e-19 in FP64: for |a| <= 1/16 (most angles of a step) after
+// a^5 / a^6 in FP32 and a^9 / a^10 in FP64, else after a^9 / a^10 and
+// a^19 / a^20.  Otherwise sincos() with cos(a) - 1 = -2 sin^2(a/2).  The
+// branch depends on a alone, so every launch shape gives the same bits.
+// Returning cos - 1 lets the rotation be applied in increment form.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void rot_coeffs(float a, float& cm1, float& s) {
-    if (fabsf(a) <= 0.5f) {
+    if (fabsf(a) <= 0.0625f) {
+        const float a2 = a * a;
+        const float p = fmaf(1.f / 120.f, a2, -1.f / 6.f);
+        s = fmaf(a * a2, p, a);
+        float q = fmaf(-1.f / 720.f, a2, 1.f / 24.f);
+        q = fmaf(q, a2, -0.5f);
+        cm1 = a2 * q;
+    } else if (fabsf(a) <= 0.5f) {
         const float a2 = a * a;
         float p = 1.f / 362880.f;               // 1/9!
         p = fmaf(p, a2, -1.f / 5040.f);         // -1/7!
@@ -360,7 +370,20 @@ __device__ __forceinline__ void rot_coeffs(float a, float& cm1, float& s) {
 }
 
 __device__ __forceinline__ void rot_coeffs(double a, double& cm1, double& s) {
-    if (fabs(a) <= 0.5) {
+    if (fabs(a) <= 0.0625) {
+        const double a2 = a * a;
+        double p = 1.0 / 362880.0;        // 1/9!
+        p = fma(p, a2, -1.0 / 5040.0);    // -1/7!
+        p = fma(p, a2, 1.0 / 120.0);      // 1/5!
+        p = fma(p, a2, -1.0 / 6.0);       // -1/3!
+        s = fma(a * a2, p, a);
+        double q = -1.0 / 3628800.0;      // -1/10!
+        q = fma(q, a2, 1.0 / 40320.0);    // 1/8!
+        q = fma(q, a2, -1.0 / 720.0);     // -1/6!
+        q = fma(q, a2, 1.0 / 24.0);       // 1/4!
+        q = fma(q, a2, -0.5);             // -1/2!
+        cm1 = a2 * q;
+    } else if (fabs(a) <= 0.5) {
         const double a2 = a * a;
         // 1/n! for odd n = 19 .. 3 and even n = 20 .. 2, alternating in sign
         double p = -1.0 / 121645100408832000.0;  // -1/19!
