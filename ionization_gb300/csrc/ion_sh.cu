@@ -794,6 +794,9 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
     }
     cp_async_commit();
     if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
+    // the step's scalars (FP64 tables, converted to R) while the tile lands
+    const R tp = post ? R(S.tau[n_post]) : R(0), ep = post ? R(S.efield[n_post]) : R(0);
+    const R tq = pre ? R(S.tau[n_pre]) : R(0), eq = pre ? R(S.efield[n_pre]) : R(0);
     cp_async_wait<0>();
     __syncthreads();
 
@@ -802,17 +805,14 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
     const int lanes = blockDim.x >> 5;
     if (post && pre && !reduce) {
         // odd(n+1); even(n+1), mask, even(n+2) in one sweep; odd(n+2)
-        const R tp = R(S.tau[n_post]), ep = R(S.efield[n_post]);
-        const R tq = R(S.tau[n_pre]), eq = R(S.efield[n_pre]);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tp, ep);
         rotate_mask_rotate_even<R>(tl, rows, nl, j0, jj, lane, lanes, tb, tp, ep, tq, eq, do_mask, glo != nullptr);
         rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tq, eq);
         post = pre = do_mask = false;
     }
     if (post) {
-        const R tau = R(S.tau[n_post]), ef = R(S.efield[n_post]);
-        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
-        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tp, ep);  // odd
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tp, ep);  // even
     }
     if (do_mask) {
         for (int f = threadIdx.x; f < nl * ROT_ROWS; f += blockDim.x) {
@@ -831,9 +831,8 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
         __syncthreads();
     }
     if (pre) {
-        const R tau = R(S.tau[n_pre]), ef = R(S.efield[n_pre]);
-        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tau, ef);  // even
-        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tau, ef);  // odd
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 0, tb, tq, eq);  // even
+        rotate_rows<R>(tl, rows, nl, j0, jj, lane, lanes, 1, tb, tq, eq);  // odd
     }
     if (mode != ROT_REDUCE_ONLY) {
 #pragma unroll 4
