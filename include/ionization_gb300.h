@@ -89,9 +89,12 @@ int ion_tdma_c64(int64_t n, const void *sub, const void *diag, const void *sup, 
  * file-scope device array of 5 MiB (5242880 bytes), enough for
  * n <= ion_tdma_noalloc_max_n_c128() = 65536; larger n is rejected with
  * ION_ERR_INVALID_ARGUMENT.  Every GPU that loads this library holds that
- * array until the process exits.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) and caches it; make that first
- * call before any stream capture.  All calls share the one array: calls whose
+ * array until the process exits.  The first call in each CUDA context (on each
+ * device, and again after cudaDeviceReset replaces a device's context) looks
+ * up the array's device address (cudaGetSymbolAddress) whatever n is, and
+ * caches it with the context's id; make that first call before any stream
+ * capture (under capture it returns ION_ERR_INVALID_ARGUMENT instead of doing
+ * the lookup).  All calls share the one array: calls whose
  * work overlaps on the GPU (two streams, or two host threads) race on it and
  * must be serialised by the caller.  The array keeps whatever the last call
  * left in it; nothing in it has to start at zero, because each call writes
@@ -385,6 +388,17 @@ enum { ION_ADI_STRIDED_FIRST = 0, ION_ADI_CONTIG_FIRST = 1 };
  * hz_d and zq may be NULL (no such term). */
 int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t t0,
                          int64_t n_steps, void *stream);
+
+/* One of the two passes of a step, for callers that interleave their own work
+ * between them (and for timing each pass): g_out = (1 + i tau H_a)^-1
+ * (1 - i tau H_b) g_in with a the implicit axis (ION_ADI_PASS_STRIDED: z, whose
+ * lines are strided in memory; ION_ADI_PASS_CONTIG: rho), b the other, tau and
+ * E at time index t_next, then g_out *= mask if apply_mask.  ion_cyl_adi_run
+ * is the pair in the mesh's order with the mask after the second.  g_in and
+ * g_out must not overlap. */
+enum { ION_ADI_PASS_STRIDED = 0, ION_ADI_PASS_CONTIG = 1 };
+int ion_cyl_adi_pass_c128(const ion_cyl_mesh *mesh, const void *g_in, void *g_out, int64_t t_next,
+                          int implicit_axis, int apply_mask, void *stream);
 int64_t ion_cyl_max_points_c128(void);
 
 /* ------------------------------------------------------------------------

@@ -29,6 +29,8 @@ ION_SH_ONLY_VELOCITY = 4
 ION_GAUGE_LENGTH = 0
 ION_ADI_STRIDED_FIRST = 0
 ION_ADI_CONTIG_FIRST = 1
+ION_ADI_PASS_STRIDED = 0
+ION_ADI_PASS_CONTIG = 1
 ION_GAUGE_VELOCITY = 1
 ION_LINE_RESIDUAL = 1
 
@@ -195,6 +197,7 @@ _SIGS = {
     "ion_line_max_n_c64": (c_i64, []),
     "ion_line_max_n_c64x": (c_i64, []),
     "ion_cyl_adi_run_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
+    "ion_cyl_adi_pass_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "ion_cyl_max_points_c128": (c_i64, []),
     "ion_tridiag_eig_scratch_doubles": (c_i64, [c_i32, c_i32]),
     "ion_tridiag_count_below": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -63,7 +63,13 @@ __device__ __forceinline__ void st(Cx<R>* p, Cx<R> a) {
 // host-side status plumbing
 // ---------------------------------------------------------------------------
 void set_error(const char* fmt, ...);
+const char* last_error();
 int check_launch(const char* what);
+// the current device and the id of its current context (ion_runtime.cu)
+int current_context(int* dev, unsigned long long* ctx_id);
+// raise `kernel`'s dynamic shared-memory limit to `bytes` in the current
+// context, once per (kernel, device, context); ION_OK or ION_ERR_CUDA
+int ensure_smem_limit(const void* kernel, int bytes, const char* name);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

@@ -206,9 +206,9 @@ static size_t rhopass_smem(int nr, int threads) {
     return 2 * size_t(nr) * 16 + size_t(threads) * CYL_M * 16 + pcr_smem_bytes<double>(threads);
 }
 
-static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int64_t n_steps, void* stream) {
-    if (!m || !g || !g_tmp || m->n_z < 2 || m->n_rho < 2 || n_steps < 0 || t0 < 0 || !m->hz_off || !m->hr_d ||
-        !m->hr_off || !m->tau || !m->efield || (m->order != ION_ADI_STRIDED_FIRST && m->order != ION_ADI_CONTIG_FIRST)) {
+static int cyl_validate(const ion_cyl_mesh* m) {
+    if (!m || m->n_z < 2 || m->n_rho < 2 || !m->hz_off || !m->hr_d || !m->hr_off || !m->tau || !m->efield ||
+        (m->order != ION_ADI_STRIDED_FIRST && m->order != ION_ADI_CONTIG_FIRST)) {
         set_error("ion_cyl: invalid argument");
         return ION_ERR_INVALID_ARGUMENT;
     }
@@ -218,31 +218,55 @@ static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int6
         set_error("ion_cyl: mesh %d x %d too large for one CTA per line", m->n_z, m->n_rho);
         return ION_ERR_UNSUPPORTED;
     }
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(cyl_zpass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(cyl_rhopass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
+    if (int e = ensure_smem_limit((const void*)cyl_zpass_kernel, 200 * 1024, "cyl_zpass_kernel")) return e;
+    if (int e = ensure_smem_limit((const void*)cyl_rhopass_kernel, 200 * 1024, "cyl_rhopass_kernel")) return e;
+    return ION_OK;
+}
+
+// one pass: implicit along the strided axis (z) or along the contiguous one (rho)
+static int cyl_pass(const ion_cyl_mesh* m, const Cx<double>* gin, Cx<double>* gout, int64_t tn, int implicit_axis,
+                    int do_mask, cudaStream_t s) {
+    if (implicit_axis == ION_ADI_PASS_STRIDED) {
+        const int bz = (cyl_threads(m->n_z) + 31) / 32 * 32;
+        cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gin, gout, tn, bz, do_mask);
+        return check_launch("cyl_zpass_kernel");
     }
+    const int br = (cyl_threads(m->n_rho) + 31) / 32 * 32;
+    cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gin, gout, tn, br, do_mask);
+    return check_launch("cyl_rhopass_kernel");
+}
+
+static int cyl_run(const ion_cyl_mesh* m, void* g, void* g_tmp, int64_t t0, int64_t n_steps, void* stream) {
+    if (!g || !g_tmp || n_steps < 0 || t0 < 0) {
+        set_error("ion_cyl: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (int e = cyl_validate(m)) return e;
     cudaStream_t s = as_stream(stream);
     auto* gg = static_cast<Cx<double>*>(g);
     auto* gt = static_cast<Cx<double>*>(g_tmp);
-    const bool contig_first = m->order == ION_ADI_CONTIG_FIRST;
+    // ION_ADI_CONTIG_FIRST: E(H_z) I(H_rho), then E(H_rho) I(H_z) and the mask;
+    // ION_ADI_STRIDED_FIRST: E(H_rho) I(H_z), then E(H_z) I(H_rho) and the mask
+    const int first = m->order == ION_ADI_CONTIG_FIRST ? ION_ADI_PASS_CONTIG : ION_ADI_PASS_STRIDED;
+    const int second = first == ION_ADI_PASS_CONTIG ? ION_ADI_PASS_STRIDED : ION_ADI_PASS_CONTIG;
     for (int64_t k = 0; k < n_steps; ++k) {
         const int64_t tn = t0 + k + 1;
-        if (contig_first) {  // E(H_z) I(H_rho), then E(H_rho) I(H_z) and the mask
-            cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gg, gt, tn, br, 0);
-            if (int e = check_launch("cyl_rhopass_kernel")) return e;
-            cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gt, gg, tn, bz, 1);
-            if (int e = check_launch("cyl_zpass_kernel")) return e;
-        } else {  // E(H_rho) I(H_z), then E(H_z) I(H_rho) and the mask
-            cyl_zpass_kernel<<<m->n_rho, bz, zpass_smem(bz), s>>>(*m, gg, gt, tn, bz, 0);
-            if (int e = check_launch("cyl_zpass_kernel")) return e;
-            cyl_rhopass_kernel<<<m->n_z, br, rhopass_smem(m->n_rho, br), s>>>(*m, gt, gg, tn, br, 1);
-            if (int e = check_launch("cyl_rhopass_kernel")) return e;
-        }
+        if (int e = cyl_pass(m, gg, gt, tn, first, 0, s)) return e;
+        if (int e = cyl_pass(m, gt, gg, tn, second, 1, s)) return e;
     }
     return ION_OK;
+}
+
+static int cyl_pass_entry(const ion_cyl_mesh* m, const void* g_in, void* g_out, int64_t t_next, int implicit_axis,
+                          int apply_mask, void* stream) {
+    if (!g_in || !g_out || g_in == g_out || t_next < 1 ||
+        (implicit_axis != ION_ADI_PASS_STRIDED && implicit_axis != ION_ADI_PASS_CONTIG)) {
+        set_error("ion_cyl_adi_pass: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (int e = cyl_validate(m)) return e;
+    return cyl_pass(m, static_cast<const Cx<double>*>(g_in), static_cast<Cx<double>*>(g_out), t_next, implicit_axis,
+                    apply_mask ? 1 : 0, as_stream(stream));
 }
 
 }  // namespace ion
@@ -253,6 +277,10 @@ extern "C" {
 int ion_cyl_adi_run_c128(const ion_cyl_mesh* mesh, void* g, void* g_tmp, int64_t t0, int64_t n_steps,
                          void* stream) {
     return cyl_run(mesh, g, g_tmp, t0, n_steps, stream);
+}
+int ion_cyl_adi_pass_c128(const ion_cyl_mesh* mesh, const void* g_in, void* g_out, int64_t t_next,
+                          int implicit_axis, int apply_mask, void* stream) {
+    return cyl_pass_entry(mesh, g_in, g_out, t_next, implicit_axis, apply_mask, stream);
 }
 int64_t ion_cyl_max_points_c128(void) { return int64_t(CYL_M) * CYL_MAX_T; }
 }

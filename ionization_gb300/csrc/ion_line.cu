@@ -987,11 +987,7 @@ static int line_res_validate(const ion_line_plan* p) {
 }
 
 static int line_res_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(line_res_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
-        attr = true;
-    }
+    if (int e = ensure_smem_limit((const void*)line_res_kernel, int(LINE_SMEM_LIMIT), "line_res_kernel")) return e;
     const unsigned C = unsigned(p->cluster > 1 ? p->cluster : 1);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(p->n_sims) * C);
@@ -1042,11 +1038,7 @@ static int line_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream
     if (line_residual<R>(p)) return line_res_launch(p, mode, n_steps, s);
     if (p->cluster > 1) {
         auto k = line_cluster_kernel<R, M>;
-        static bool cattr = false;
-        if (!cattr) {
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
-            cattr = true;
-        }
+        if (int e = ensure_smem_limit((const void*)k, int(LINE_SMEM_LIMIT), "line_cluster_kernel")) return e;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(unsigned(p->n_sims) * unsigned(p->cluster));
         cfg.blockDim = dim3(unsigned(p->threads));
@@ -1069,11 +1061,8 @@ static int line_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream
         cudaLaunchKernelEx(&cfg, k, *p, mode, n_steps);
         return check_launch("line_cluster_kernel");
     }
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(line_step_kernel<R, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(LINE_SMEM_LIMIT));
-        attr = true;
-    }
+    if (int e = ensure_smem_limit((const void*)line_step_kernel<R, M>, int(LINE_SMEM_LIMIT), "line_step_kernel"))
+        return e;
     line_step_kernel<R, M><<<p->n_sims, p->threads, line_smem<R>(p->threads, M), s>>>(*p, mode, n_steps);
     return check_launch("line_step_kernel");
 }

@@ -1133,11 +1133,7 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     if (p->n_rot_items == 0) return ION_OK;
     if (!(p->flags & ION_SH_ONLY_VELOCITY)) {
         const size_t smem = rot_smem<R>(p);
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(sh_rot_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            attr = true;
-        }
+        if (int e = ensure_smem_limit((const void*)sh_rot_kernel<R>, 200 * 1024, "sh_rot_kernel")) return e;
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
         sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
@@ -1145,11 +1141,7 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     }
     if (p->flags & (ION_SH_VELOCITY | ION_SH_ONLY_VELOCITY)) {
         const size_t smem = rot_smem_bytes<R>(p->max_n_l, VEL_ROWS);
-        static bool vattr = false;
-        if (!vattr) {
-            cudaFuncSetAttribute(sh_rot_vel_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            vattr = true;
-        }
+        if (int e = ensure_smem_limit((const void*)sh_rot_vel_kernel<R>, 200 * 1024, "sh_rot_vel_kernel")) return e;
         sh_rot_vel_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode);
         if (int e = check_launch("sh_rot_vel_kernel")) return e;
     }
@@ -1158,14 +1150,10 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
 
 template <typename R, int MAXM>
 static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        cudaFuncSetAttribute(sh_cn_pipelined<R, MAXM, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        attr = true;
-    }
+    if (int e = ensure_smem_limit((const void*)sh_cn_pipelined<R, MAXM, false>, 200 * 1024, "sh_cn_pipelined"))
+        return e;
+    if (int e = ensure_smem_limit((const void*)sh_cn_pipelined<R, MAXM, true>, 200 * 1024, "sh_cn_pipelined"))
+        return e;
     const int nb = p->n_cn_buckets;
     int begin = 0;
     for (int b = 0; b < (nb > 0 ? nb : 1); ++b) {

@@ -20,24 +20,6 @@
 
 namespace ion {
 
-static thread_local char g_err[512] = "";
-
-void set_error(const char* fmt, ...) {
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(g_err, sizeof(g_err), fmt, ap);
-    va_end(ap);
-}
-
-int check_launch(const char* what) {
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        set_error("%s: %s", what, cudaGetErrorString(e));
-        return ION_ERR_CUDA;
-    }
-    return ION_OK;
-}
-
 // per-precision tuning: rows per thread and largest CTA
 template <typename R> struct TdmaCfg;
 template <> struct TdmaCfg<double> {
@@ -234,17 +216,8 @@ static size_t block_smem(int T) {
 
 template <typename R, int MAXM, class K>
 static int set_smem_attr(K kernel, size_t bytes) {
-    static bool done = false;
-    if (!done) {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if (e != cudaSuccess) {
-            set_error("cudaFuncSetAttribute: %s", cudaGetErrorString(e));
-            return ION_ERR_CUDA;
-        }
-        done = true;
-    }
     (void)bytes;
-    return ION_OK;
+    return ensure_smem_limit(reinterpret_cast<const void*>(kernel), 200 * 1024, "ion_tdma");
 }
 
 template <typename R>
@@ -373,29 +346,53 @@ constexpr int64_t NOALLOC_SCRATCH_BYTES = 5242880;
 // Held by every GPU that loads this library, until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
-// The array's name is only a host-side stand-in; its device address is
-// looked up once per device, with that device current, and cached.
-static void* g_noalloc_addr[64] = {nullptr};
+// The array's name is only a host-side stand-in; its device address belongs
+// to the CUDA context that loaded this module.  It is looked up with the
+// device current and cached per device together with that context's id, so a
+// new context on the same device (after cudaDeviceReset, say) looks it up
+// again instead of reusing a stale address.
+struct NoallocSlot {
+    unsigned long long ctx;
+    void* addr;
+};
+static NoallocSlot g_noalloc_slot[64] = {};
 static std::mutex g_noalloc_mu;
 
-static int noalloc_scratch_address(void** out) {
+static int noalloc_scratch_address(cudaStream_t stream, void** out) {
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 64) {
-        set_error("ion_tdma_noalloc_c128: no usable current device (%s)", cudaGetErrorString(e));
+    unsigned long long ctx = 0;
+    if (current_context(&dev, &ctx)) {
+        set_error("ion_tdma_noalloc_c128: %s", last_error());
         return ION_ERR_CUDA;
     }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (g_noalloc_addr[dev] == nullptr) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            set_error("ion_tdma_noalloc_c128: cudaGetSymbolAddress failed (%s)", cudaGetErrorString(e));
-            return ION_ERR_CUDA;
-        }
-        g_noalloc_addr[dev] = p;
+    if (dev < 0 || dev >= 64) {
+        set_error("ion_tdma_noalloc_c128: device ordinal %d is beyond the 64 this library tracks", dev);
+        return ION_ERR_UNSUPPORTED;
     }
-    *out = g_noalloc_addr[dev];
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoallocSlot& slot = g_noalloc_slot[dev];
+    if (slot.addr != nullptr && slot.ctx == ctx) {
+        *out = slot.addr;
+        return ION_OK;
+    }
+    // the lookup may load the module, which a stream capture does not allow
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        set_error("ion_tdma_noalloc_c128: the first call in this CUDA context on device %d is under stream "
+                  "capture; call it once before capturing", dev);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        set_error("ion_tdma_noalloc_c128: cudaGetSymbolAddress failed (%s)", cudaGetErrorString(e));
+        return ION_ERR_CUDA;
+    }
+    slot.ctx = ctx;
+    slot.addr = p;
+    *out = p;
     return ION_OK;
 }
 
@@ -412,12 +409,13 @@ static int tdma_noalloc_c128(int64_t n, const void* sub, const void* diag, const
                   (long long)n, (long long)need, (long long)NOALLOC_SCRATCH_BYTES);
         return ION_ERR_INVALID_ARGUMENT;
     }
+    // looked up on every call, whatever n is, so that the first call in a
+    // context does the set-up even when it is a small system
     void* scratch = nullptr;
-    if (need > 0)
-        if (int e = noalloc_scratch_address(&scratch)) return e;
+    if (int e = noalloc_scratch_address(as_stream(stream), &scratch)) return e;
     // every scratch word the partition reads is written earlier in the same
     // call, so nothing has to be cleared between calls
-    return tdma_impl<double>(n, sub, diag, sup, d, x, scratch, NOALLOC_SCRATCH_BYTES, stream);
+    return tdma_impl<double>(n, sub, diag, sup, d, x, need > 0 ? scratch : nullptr, NOALLOC_SCRATCH_BYTES, stream);
 }
 
 }  // namespace ion
@@ -432,8 +430,6 @@ int ion_tdma_noalloc_c128(int64_t n, const void* sub, const void* diag, const vo
 }
 int64_t ion_tdma_noalloc_max_n_c128(void) { return NOALLOC_MAX_N; }
 
-const char* ion_last_error(void) { return g_err; }
-int ion_version(void) { return 100; }
 
 int64_t ion_tdma_scratch_bytes_c128(int64_t n) {
     return n < 1 ? 0 : scratch_elems<double>(n) * int64_t(sizeof(Cx<double>));

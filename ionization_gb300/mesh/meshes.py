@@ -81,6 +81,18 @@ class QuantumMesh:
             hi = v.astype(np.complex64).astype(np.complex128)
             lo.copy_(torch.from_numpy((v - hi).astype(np.complex64)).to(lo.device))
 
+    def _native_state(self):
+        """Host copies of the device arrays that hold psi (the state itself and,
+        in the c64x form, its residual), for an exact save and restore."""
+        lo = self._psi_residual()
+        return (self._psi_device().cpu().numpy().copy(), None if lo is None else lo.cpu().numpy().copy())
+
+    def _set_native_state(self, state):
+        hi, lo = state
+        self._psi_device().copy_(torch.from_numpy(np.ascontiguousarray(hi)).to(self._psi_device().device))
+        if lo is not None and self._psi_residual() is not None:
+            self._psi_residual().copy_(torch.from_numpy(np.ascontiguousarray(lo)).to(self._psi_residual().device))
+
     @property
     def psi(self):
         return self.g / self.g_factor

@@ -165,8 +165,13 @@ class MeshSimulation:
     def save(self, target_dir=None, save_mesh: bool = True):
         target_dir = target_dir or os.getcwd()
         path = os.path.join(target_dir, f"{self.name}.sim")
-        self._pull_data()
-        state = dict(spec=self.spec, time_index=self.time_index, g=self.mesh.g if save_mesh else None,
+        if self.mesh is not None:  # a simulation whose mesh was dropped keeps its data as they are
+            self._pull_data()
+        keep = save_mesh and self.mesh is not None
+        # ``native``: the device arrays as they are, so a reload continues the
+        # run bit for bit whatever transform lies between them and ``g``
+        state = dict(spec=self.spec, time_index=self.time_index, g=self.mesh.g if keep else None,
+                     native=self.mesh._native_state() if keep else None,
                      initial_data_done=self._initial_data_done,
                      data={type(ds): vars(ds).copy() for ds in self.datastores_by_type.values()})
         for d in state["data"].values():
@@ -185,7 +190,10 @@ class MeshSimulation:
             state = pickle.load(f)
         sim = state["spec"].to_sim()
         if state["g"] is not None:
-            sim.mesh.g = state["g"]
+            if state.get("native") is not None:
+                sim.mesh._set_native_state(state["native"])
+            else:
+                sim.mesh.g = state["g"]
             sim._restore_index(state["time_index"])
         else:
             sim.mesh = None

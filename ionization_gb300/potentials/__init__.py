@@ -7,7 +7,7 @@ uploaded once per run) and the mask m(r) (tabulated once).  Formulas and
 operation order follow the reference so that tables are bit-identical.
 """
 
-import functools
+import operator
 
 import numpy as np
 import scipy.integrate as integ
@@ -30,10 +30,10 @@ class PotentialEnergySum(summables.Sum, PotentialEnergy):
     container_name = "potentials"
 
     def get_electric_field_amplitude(self, t):
-        return sum(x.get_electric_field_amplitude(t) for x in self._container)
+        return sum(x.get_electric_field_amplitude(t) for x in self.members())
 
     def get_vector_potential_amplitude_numeric(self, times, rule="simps"):
-        return sum(x.get_vector_potential_amplitude_numeric(times, rule=rule) for x in self._container)
+        return sum(x.get_vector_potential_amplitude_numeric(times, rule=rule) for x in self.members())
 
 
 class NoPotentialEnergy(PotentialEnergy):
@@ -88,9 +88,7 @@ class TimeWindow(summables.Summand):
 
 class TimeWindowSum(summables.Sum, TimeWindow):
     container_name = "windows"
-
-    def __call__(self, *args, **kwargs):
-        return functools.reduce(lambda a, b: a * b, (x(*args, **kwargs) for x in self._container))
+    fold = staticmethod(operator.mul)  # windows multiply
 
 
 class NoTimeWindow(TimeWindow):
@@ -148,6 +146,11 @@ DEFAULT_PHASE = 0
 DEFAULT_PULSE_CENTER = 0
 
 
+def _carrier_wavelength(omega):
+    """Wavelength of angular frequency ``omega``: c / (omega / 2 pi)."""
+    return u.c / (omega / u.twopi)
+
+
 class CosSquaredPulse(UniformLinearlyPolarizedElectricPotential):
     """cos^2-envelope pulse parameterised by number of cycles
     (pulses.py:1696-1814).  Like the reference it stores the carrier as a
@@ -170,24 +173,12 @@ class CosSquaredPulse(UniformLinearlyPolarizedElectricPotential):
         self.pulse_center = pulse_center
 
     @classmethod
-    def from_omega_carrier(
-        cls,
-        amplitude=0.1 * u.atomic_electric_field,
-        omega_carrier=u.twopi * u.c / (800 * u.nm),
-        number_of_cycles=4,
-        phase=DEFAULT_PHASE,
-        pulse_center=DEFAULT_PULSE_CENTER,
-        **kwargs,
-    ):
-        wavelength = u.c / (omega_carrier / u.twopi)
-        return cls(
-            amplitude=amplitude,
-            wavelength=wavelength,
-            number_of_cycles=number_of_cycles,
-            phase=phase,
-            pulse_center=pulse_center,
-            **kwargs,
-        )
+    def from_omega_carrier(cls, amplitude=0.1 * u.atomic_electric_field, omega_carrier=u.twopi * u.c / (800 * u.nm),
+                           number_of_cycles=4, phase=DEFAULT_PHASE, pulse_center=DEFAULT_PULSE_CENTER, **kwargs):
+        """The pulse with angular carrier frequency ``omega_carrier``.  The
+        carrier is kept as the wavelength c / (omega / 2 pi), and omega is
+        recomputed from it, so E(t) matches the reference's to the last bit."""
+        return cls(amplitude, _carrier_wavelength(omega_carrier), number_of_cycles, phase, pulse_center, **kwargs)
 
     @classmethod
     def from_sin2_envelope(cls, amplitude, omega, number_of_cycles, cep=0.0, t_start=0.0):
@@ -312,9 +303,7 @@ class Mask(summables.Summand):
 
 class MaskSum(summables.Sum, Mask):
     container_name = "masks"
-
-    def __call__(self, *args, **kwargs):
-        return functools.reduce(lambda a, b: a * b, (x(*args, **kwargs) for x in self._container))
+    fold = staticmethod(operator.mul)  # masks multiply
 
 
 class NoMask(Mask):
@@ -328,12 +317,14 @@ class RadialCosineMask(Mask):
     absorbs at +z, as in the reference."""
 
     def __init__(self, inner_radius=50 * u.bohr_radius, outer_radius=100 * u.bohr_radius, smoothness=8):
-        if inner_radius < 0 or outer_radius < 0:
-            raise exceptions.InvalidMaskParameter("inner and outer radius must be non-negative")
-        if inner_radius >= outer_radius:
-            raise exceptions.InvalidMaskParameter("outer radius must be larger than inner radius")
+        if min(inner_radius, outer_radius) < 0:
+            raise exceptions.InvalidMaskParameter(
+                f"mask radii cannot be negative (inner {inner_radius}, outer {outer_radius})")
+        if not inner_radius < outer_radius:
+            raise exceptions.InvalidMaskParameter(
+                f"the mask's inner radius {inner_radius} is not below its outer radius {outer_radius}")
         if smoothness < 1:
-            raise exceptions.InvalidMaskParameter("smoothness must be greater than 1")
+            raise exceptions.InvalidMaskParameter(f"mask smoothness {smoothness} is below 1")
         super().__init__()
         self.inner_radius = inner_radius
         self.outer_radius = outer_radius

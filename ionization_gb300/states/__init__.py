@@ -142,14 +142,15 @@ class HydrogenBoundState(SphericalHarmonicState):
     derivation = Derivation.ANALYTIC
 
     def __init__(self, n=1, l=0, m=0, amplitude=1):
+        bad = None
         if int(n) != n or n < 1:
-            raise exceptions.IllegalQuantumState(f"n ({n}) must be an integer greater than zero")
-        if int(l) != l or not 0 <= l < n:
-            raise exceptions.IllegalQuantumState(
-                f"l ({l}) must be an integer greater than or equal to zero and less than n ({n})"
-            )
-        if int(m) != m or not -l <= m <= l:
-            raise exceptions.IllegalQuantumState(f"|m| (|{m}|) must be an integer less than or equal to l ({l})")
+            bad = f"principal quantum number n = {n} is not a positive integer"
+        elif int(l) != l or not 0 <= l < n:
+            bad = f"angular momentum l = {l} is not an integer in [0, {n}) for n = {n}"
+        elif int(m) != m or abs(m) > l:
+            bad = f"magnetic quantum number m = {m} is not an integer in [-{l}, {l}]"
+        if bad:
+            raise exceptions.IllegalQuantumState(bad)
         self.n = int(n)
         super().__init__(l=int(l), m=int(m), amplitude=amplitude)
 
@@ -195,7 +196,7 @@ class HydrogenCoulombState(SphericalHarmonicState):
 
     def __init__(self, energy=1 * u.eV, l=0, m=0, amplitude=1.0):
         if energy < 0:
-            raise exceptions.IllegalQuantumState("energy must be greater than zero")
+            raise exceptions.IllegalQuantumState(f"a free state's energy cannot be negative (got {energy})")
         self.energy = energy
         super().__init__(l=l, m=m, amplitude=amplitude)
 

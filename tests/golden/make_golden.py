@@ -1,8 +1,8 @@
 #!/usr/bin/env python
 """Generate golden fixtures by running the REFERENCE ionization library.
 
-This script needs a checkout of the reference (default ``/root/reference``,
-override with ``--ref``); it imports it read-only through ``refstub/loader.py``
+This script needs a checkout of the reference, given with ``--ref`` or the
+``IONIZATION_REFERENCE`` environment variable; it imports it read-only through ``refstub/loader.py``
 (atomic-unit ``simulacra`` stub) and writes ``tests/golden/*.npz``.  The
 fixtures are committed; tests only read them.
 
@@ -484,6 +484,9 @@ def _observable_arrays(sim, kind):
     out = dict(
         radii=np.asarray(OBS_RADII[kind]),
         norm_within_radius=np.array([sim.data.norm_within_radius[r] for r in OBS_RADII[kind]]),
+        # the Fields datastore (data.py:152-181): E(t) and A(t) at the data times
+        electric_field_amplitude=np.asarray(sim.data.electric_field_amplitude),
+        vector_potential_amplitude=np.asarray(sim.data.vector_potential_amplitude),
     )
     if kind != "line":
         out["z_expectation_value"] = np.asarray(sim.data.z_expectation_value)
@@ -523,12 +526,15 @@ def gen_observables(ion):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("IONIZATION_REFERENCE"),
+                    help="path of the reference checkout (or set IONIZATION_REFERENCE)")
     ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the reference checkout with --ref or IONIZATION_REFERENCE")
 
     from loader import import_reference
 

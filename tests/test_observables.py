@@ -41,6 +41,26 @@ def test_oracle_observables_match_reference(kind, name):
         np.testing.assert_allclose(obs[-1]["by_l"], z["norm_by_l_final"], rtol=0, atol=1e-13)
 
 
+@pytest.mark.parametrize("kind,name", [("line", "line_observables_small"), ("sh", "sh_observables_small"),
+                                       ("cyl", "cyl_observables_small")])
+def test_fields_tables_match_reference(kind, name):
+    """The Fields datastore's host tables: E at the data times and A from the
+    one-pass prefix integrals, against the reference's per-data-time Simpson
+    integrals (data.py:152-181)."""
+    from ionization_gb300 import potentials
+
+    from .specs import pulse
+
+    params, z = load_golden(name)
+    times = z["times"]
+    idx = np.searchsorted(times, z["data_times"])
+    ep = pulse(params["pulse"])
+    a = potentials.vector_potential_table(ep, times)[idx]
+    e = np.array([ep.get_electric_field_amplitude(t) for t in times[idx]])
+    np.testing.assert_array_equal(e, z["electric_field_amplitude"])
+    np.testing.assert_allclose(a, z["vector_potential_amplitude"], rtol=0, atol=1e-15)
+
+
 def _product_datastores(kind, radii):
     from ionization_gb300.mesh import data
 
@@ -60,6 +80,9 @@ def test_device_observables_c128(cuda, kind, name):
     sim.run()
     within = np.array([sim.data.norm_within_radius[r] for r in sorted(radii)])
     np.testing.assert_allclose(within, z["norm_within_radius"], rtol=0, atol=TOL)
+    np.testing.assert_array_equal(sim.data.electric_field_amplitude, z["electric_field_amplitude"])
+    np.testing.assert_allclose(sim.data.vector_potential_amplitude, z["vector_potential_amplitude"], rtol=0,
+                               atol=1e-15)
     obs = out["observed"]
     np.testing.assert_allclose(sim.data.z_expectation_value, [o["z"] for o in obs], rtol=0, atol=TOL)
     np.testing.assert_allclose(sim.data.r_expectation_value, [o["r"] for o in obs], rtol=0, atol=TOL)
