@@ -452,8 +452,8 @@ def run_e2e(args, specs, tables, rows, gs, points, precision):
     psis = b.psi_all()  # g (+ its residual) to the host
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    h2d = sum(s.nbytes() for s in b.sims) - sum(int(s.d_partials.numel()) * 8 for s in b.sims)
-    d2h = sum(s.g.numel() * s.g.element_size() * (1 if s.g_lo is None else 2) for s in b.sims)
+    h2d = sum(s.h2d_bytes for s in b.sims)  # psi (complex128, split on the device) and the tables
+    d2h = sum(s.g.numel() * 16 for s in b.sims)  # psi read back as complex128 (ion_psi_to_c128)
     d2h += sum(r["norm"].nbytes + 16 * len(r["inner_products"]) * len(r["norm"]) for r in res)
     del b, psis
     return {"value": points * K / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / K),

@@ -174,15 +174,17 @@ typedef struct ion_sh_sim {
     double *partials;       /* [n_tiles * (1 + 2*n_states)] device scratch for reductions */
     int32_t n_tiles;        /* number of row tiles of this simulation */
     int32_t gauge;          /* ION_GAUGE_LENGTH (0) or ION_GAUGE_VELOCITY, see below */
-    /* _c64 entry points only, or NULL: the rounding residual of psi,
-     * complex64 (n_l, n_r) like g.  With it psi = g + g_lo carries about 48
-     * significant bits: the arithmetic stays FP32, each step's increment is
-     * added to (g, g_lo) with an exact two-sum and the pair is renormalised
-     * when stored, so storing psi no longer rounds it to FP32 precision; the
-     * explicit half of the radial step is then formed from neighbour
-     * differences and an exact row sum of the same FP32 coefficients, which
-     * removes the cancellation of the kinetic terms and keeps the step
-     * unitary. */
+    /* _c64 entry points only, or NULL: the rounding residual of psi, (n_l, n_r)
+     * like g, one 32-bit word a point holding its real and imaginary parts as
+     * bf16 (real in the low 16 bits, each rounded to nearest even): the
+     * ION_LO_BF16X2 format.  psi = g + g_lo carries about 33 significant bits
+     * in 12 bytes a point: the arithmetic stays FP32, each step's increment
+     * is added to (g, g_lo) with an exact two-sum and the pair is
+     * renormalised (|g_lo| <= ulp(g) / 2) when stored, so storing psi no
+     * longer rounds it to FP32 precision; the explicit half of the radial
+     * step is then formed from neighbour differences and an exact row sum of
+     * the same FP32 coefficients, which removes the cancellation of the
+     * kinetic terms and keeps the step unitary. */
     void *g_lo;
     /* ION_GAUGE_VELOCITY (SphericalHarmonicVelocityGaugeOperators,
      * mesh_operators.py:1130-1408): the split operators are h1, rotations of
@@ -195,6 +197,24 @@ typedef struct ion_sh_sim {
      * cl the plain c_l. */
     const double *h2r;      /* [n_r-1] hbar (q/m) / (2 dr) alpha(j), or NULL */
     const float *h2r32;
+    /* _c64 entry points with g_lo and ION_SH_REFINE only, or NULL: [n_l*n_r]
+     * bf16 (C order like g), the row-sum remainder of the radial step per
+     * point: tau * (H_ii + H_i,i-1 + H_i,i+1) with the FP64 tables and tau,
+     * minus the same sum of the FP32 coefficients the solve forms
+     * (tau32 * fma(l(l+1), cent32, kinv32) (+ corr0 at the first point),
+     * tau32 * hoff32).  The refinement adds it to the explicit half's exact
+     * row sum, so the refined solve converges to the FP64 system instead of
+     * to the one the FP32 tables round it to.  That rounding acts as a random
+     * potential of ~1e-7 of the kinetic diagonal; in strongly driven runs it
+     * moves the final populations by up to ~5e-6.  Filled on the device by
+     * ion_sh_row_lo_c64. */
+    uint16_t *row_lo;
+    /* FP64 per-r tables of the radial diagonal, kinv + l(l+1) cent (+ corr0 at
+     * the first point of l = 0): what ion_sh_row_lo_c64 forms row_lo from
+     * (NULL when row_lo is) */
+    const double *kinv;
+    const double *cent;
+    double corr0;
 } ion_sh_sim;
 
 enum { ION_GAUGE_LENGTH = 0, ION_GAUGE_VELOCITY = 1 };
@@ -252,6 +272,14 @@ int ion_sh_split_phase_c64(const ion_sh_plan *plan, int phase, void *stream);
 /* Reduce the data of the current time index (used for t = 0 before the run). */
 int ion_sh_reduce_c128(const ion_sh_plan *plan, void *stream);
 int ion_sh_reduce_c64(const ion_sh_plan *plan, void *stream);
+
+/* Fill row_lo of every simulation of the plan that carries one (c64x set-up,
+ * once per simulation before its first step): per point, tau * (the FP64
+ * row sum kinv + l(l+1) cent [+ corr0] + hoff[i-1] + hoff[i]) minus the sum
+ * of the FP32 coefficients the radial solve forms for that row, with the
+ * solve's own FP32 arithmetic, rounded to bf16; tau = tau[t+1] at the
+ * simulation's current time index t (the time step is uniform). */
+int ion_sh_row_lo_c64(const ion_sh_plan *plan, void *stream);
 /* Largest n_r the radial solve supports in one CTA. */
 int64_t ion_sh_max_n_r_c128(void);
 int64_t ion_sh_max_n_r_c64(void);
@@ -301,7 +329,8 @@ typedef struct ion_line_sim {
     const void *twiddle;   /* [n] exp(-2 pi i m / n), complex128 for _c128, complex64 for _c64 */
     const float *vstat32;
     /* _c64 entry points with ION_LINE_RESIDUAL: the rounding residual of psi
-     * (complex64 [n], psi = g + g_lo), or NULL */
+     * ([n] words in the ION_LO_BF16X2 format of ion_sh_sim.g_lo,
+     * psi = g + g_lo), or NULL */
     void *g_lo;
     /* ION_GAUGE_VELOCITY (LineVelocityGaugeOperators, mesh_operators.py:352-427):
      * the split operators are rotations [[cos, sin], [-sin, cos]] of the pairs
@@ -310,6 +339,12 @@ typedef struct ion_line_sim {
      * even.  vcoef = hbar (q/m) / (2 dz).  Runs in one CTA (cluster and
      * residual plans leave such a line untouched). */
     double vcoef;
+    /* ION_LINE_RESIDUAL only, or NULL: the low parts of the FP32 tables,
+     * x_lo = float(x - double(x32)).  The residual form's explicit half adds
+     * them (and the low parts of tau and of the field term) to the FP32 row
+     * sums, so its refinement solves the FP64 system. */
+    const float *hd_lo32;   /* [n] */
+    const float *hoff_lo32; /* [n-1] */
 } ion_line_sim;
 
 typedef struct ion_line_plan {
@@ -440,14 +475,21 @@ int ion_reduce_c64(int64_t M, const void *g, int32_t n_states, const void *state
 
 /* psi of a complex64 state read back as complex128 (the g property of a
  * complex64 mesh, QuantumMesh.g): out[i] = hi[i] + lo[i] in FP64, lo (the
- * stored residual) may be NULL.  n complex elements, device pointers. */
+ * stored residual, ION_LO_BF16X2 words) may be NULL.  n complex elements,
+ * device pointers. */
 int ion_psi_to_c128(int64_t n, const void *hi, const void *lo, void *out, void *stream);
+/* The inverse, for uploads: a complex128 psi split into the complex64 hi
+ * (rounded to nearest) and, when lo is not NULL, the packed residual
+ * (ION_LO_BF16X2) of psi - hi.  n complex elements, device pointers; in may
+ * not alias hi or lo. */
+int ion_psi_split_c128(int64_t n, const void *in, void *hi, void *lo, void *stream);
 
 /* ------------------------------------------------------------------------
  * Position expectation values and partial norms (the ZExpectationValue,
  * RExpectationValue, NormWithinRadius and NormBySphericalHarmonic datastores,
  * ionization/mesh/data.py:344-464).  FP64 two-stage sums with a compensated
- * second stage; the complex64 forms accept the stored residual g_lo (or NULL).
+ * second stage; the complex64 forms accept the stored residual g_lo
+ * (ION_LO_BF16X2 words, or NULL).
  *
  * ion_weighted_norms_*: out[k] = weight * sum_i w[k * n + i] |g_i|^2 for
  *   1 <= n_w <= 8 weight vectors (element-wise operators on line and

@@ -144,15 +144,21 @@ class ShTables:
 SH_ROT_ROWS = 32
 
 
-SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8), Precision.C64X: (8, 16)}  # default first
+SH_ROWS_CHOICES = {Precision.C128: (8, 4), Precision.C64: (16, 8), Precision.C64X: (8, 4, 16)}  # default first
 SH_MAX_LINE_THREADS = 512  # threads of one radial-solve CTA
+
+
+def sh_max_line_threads(precision, rows: int) -> int:
+    """Largest radial-solve CTA at ``rows`` rows per thread: the complex64
+    4-row variant runs in 64 registers and so takes up to 1024 threads."""
+    return 1024 if Precision(precision) != Precision.C128 and rows == 4 else SH_MAX_LINE_THREADS
 
 
 def sh_default_rows(precision, max_n_r: int) -> int:
     """Rows per thread of the radial solve when none is asked for: the first
     choice whose CTA holds the longest line of the batch."""
     for rows in SH_ROWS_CHOICES[Precision(precision)]:
-        if (max_n_r + rows - 1) // rows <= SH_MAX_LINE_THREADS:
+        if (max_n_r + rows - 1) // rows <= sh_max_line_threads(precision, rows):
             return rows
     return max(SH_ROWS_CHOICES[Precision(precision)])
 
@@ -178,35 +184,81 @@ class _Fill:
         return out
 
 
-def _split_hi(g0):
-    def fill(dest):
-        dest[...] = g0.reshape(-1)  # rounded to complex64
+def lo_pack(lo) -> np.ndarray:
+    """The stored residual of a complex64 state from its complex value: one
+    32-bit word a point (int32 holding the bits), the real part's bf16 in the
+    low half and the imaginary part's in the high half, each rounded to
+    nearest even as the device's cvt.rn.bf16x2.f32 does."""
+    c = np.ascontiguousarray(np.asarray(lo, dtype=np.complex64))
+    u = c.view(np.uint32).reshape(c.shape + (2,)).astype(np.uint64)
+    r = ((u + np.uint64(0x7FFF) + ((u >> np.uint64(16)) & np.uint64(1))) >> np.uint64(16)) & np.uint64(0xFFFF)
+    return (r[..., 0] | (r[..., 1] << np.uint64(16))).astype(np.uint32).view(np.int32)
 
-    return fill
+
+def lo_unpack(w) -> np.ndarray:
+    """The complex128 value of packed residual words (``lo_pack``)."""
+    u = np.ascontiguousarray(np.asarray(w)).view(np.uint32)
+    re = (u << np.uint32(16)).view(np.float32).astype(np.float64)
+    im = (u & np.uint32(0xFFFF0000)).view(np.float32).astype(np.float64)
+    return re + 1j * im
 
 
-def _split_lo(g0):
-    def fill(dest):
-        flat = g0.reshape(-1)
-        dest[...] = flat - flat.astype(np.complex64)  # the rounding error, in complex64
+def _lo32(a) -> np.ndarray:
+    """The FP32 low part of FP64 values: float32(a - float32(a))."""
+    a = np.asarray(a, dtype=np.float64)
+    return (a - a.astype(np.float32).astype(np.float64)).astype(np.float32)
 
-    return fill
+
+def bf16_bits(x) -> np.ndarray:
+    """FP64 values rounded to FP32 and then to bf16 (nearest even), as int16 bits."""
+    u = np.ascontiguousarray(np.asarray(x, dtype=np.float64).astype(np.float32)).view(np.uint32).astype(np.uint64)
+    r = ((u + np.uint64(0x7FFF) + ((u >> np.uint64(16)) & np.uint64(1))) >> np.uint64(16)) & np.uint64(0xFFFF)
+    return r.astype(np.uint16).view(np.int16)
+
+
+def sh_row_remainder(tab: "ShTables") -> np.ndarray:
+    """[n_l, n_r] FP64, a host restatement of ion_sh_row_lo_c64: the exact row
+    sum of the radial step's coefficients, tau (H_ii + H_i,i-1 + H_i,i+1) from
+    the FP64 tables, minus the sum of the FP32 coefficients the complex64
+    radial solve forms for that row: bd = fl(tau32 fl(fma(l(l+1), cent32,
+    kinv32)) [+ corr0 at (0, 0)]), bo = fl(tau32 hoff32).  Every FP32
+    operation is reproduced in FP64 and rounded once (the products and sums
+    of FP32 values it rounds are exact in FP64)."""
+    f32 = lambda v: np.asarray(v, np.float64).astype(np.float32).astype(np.float64)  # noqa: E731
+    nl, nr = int(tab.n_l), int(tab.n_r)
+    tau64 = float(tab.tau[1]) if len(tab.tau) > 1 else 0.0
+    tau32 = float(np.float32(tau64))
+    ll1 = (np.arange(nl, dtype=np.float64) * (np.arange(nl, dtype=np.float64) + 1))[:, None]
+    h32 = f32(f32(tab.kinv)[None, :] + ll1 * f32(tab.cent)[None, :])
+    h32[0, 0] = f32(h32[0, 0] + f32(tab.corr0))
+    bd32 = f32(tau32 * h32)
+    bo32 = np.zeros(nr + 1)
+    bo32[1:nr] = f32(tau32 * f32(tab.hoff))  # bo32[i + 1] couples rows i and i + 1
+    ho = np.zeros(nr + 1)
+    ho[1:nr] = np.asarray(tab.hoff, np.float64)
+    hd = np.asarray(tab.hd, np.float64).reshape(nl, nr)
+    exact = tau64 * (hd + (ho[:-1] + ho[1:])[None, :])
+    return exact - (bd32 + (bo32[:-1] + bo32[1:])[None, :])
 
 
 def _sh_host_arrays(tab: ShTables, precision) -> dict:
     """The host arrays a spherical-harmonic simulation uploads (None where
-    absent), by attribute name, in their device dtype (complex64 psi as
-    ``_Fill``: rounded as it is written to the upload buffer)."""
+    absent), by attribute name, in their device dtype."""
     precision = Precision(precision)
     f64, f32 = np.float64, np.float32
     g0 = np.asarray(tab.g0, dtype=np.complex128)
     c128 = precision == Precision.C128
+    x = precision == Precision.C64X
     a = {}
-    a["g"] = g0 if c128 else _Fill(g0.shape, np.complex64, _split_hi(g0))
-    a["g_lo"] = None
-    if precision == Precision.C64X:  # psi = g + g_lo
-        a["g_lo"] = _Fill(g0.shape, np.complex64, _split_lo(g0))
+    # complex64 forms: psi goes up as complex128 and is split on the device
+    # into g and (c64x) its packed residual g_lo (ion_psi_split_c128)
+    a["g"] = g0 if c128 else None
+    a["g_in"] = None if c128 else g0
     a["d_hd"] = np.asarray(tab.hd, f64) if c128 else None
+    # c64x: the FP64 per-r diagonal tables the device forms the row-sum
+    # remainders from (ion_sh_row_lo_c64)
+    a["d_kinv64"] = np.asarray(tab.kinv, f64) if x else None
+    a["d_cent64"] = np.asarray(tab.cent, f64) if x else None
     a["d_hoff"] = np.asarray(tab.hoff, f64)
     a["d_rq"] = np.asarray(tab.rq, f64)
     a["d_cl"] = np.asarray(tab.cl, f64)
@@ -289,6 +341,49 @@ class _Arena:
                 for key, arr, off in self.items}
 
 
+def _sh_state_buffers(total: int, precision, counts) -> List[dict]:
+    """Device-only state of complex64 simulations, one dense buffer per kind
+    sliced in order: g (complex64), and for c64x g_lo (packed residual words)
+    and d_row_lo (bf16 row-sum remainders).  Per simulation, by attribute."""
+    precision = Precision(precision)
+    out = [dict(g_lo=None, d_row_lo=None) for _ in counts]
+    if precision == Precision.C128:
+        return out
+    g = torch.empty(max(total, 1), dtype=torch.complex64, device=device())
+    lo = rl = None
+    if precision == Precision.C64X:
+        lo = torch.empty(max(total, 1), dtype=torch.int32, device=device())
+        rl = torch.empty(max(total, 1), dtype=torch.int16, device=device())
+    off = 0
+    for i, n in enumerate(counts):
+        out[i]["g"] = g[off:off + n]
+        if lo is not None:
+            out[i]["g_lo"] = lo[off:off + n]
+            out[i]["d_row_lo"] = rl[off:off + n]
+        off += n
+    return out
+
+
+def _sh_prepare(sims: List["ShDeviceSim"]):
+    """Finish the upload of complex64 simulations on the device: psi split
+    into g and g_lo, then (c64x) the row-sum remainders of the radial step.
+    The uploaded complex128 psi is released."""
+    todo = [s for s in sims if getattr(s, "g_in", None) is not None]
+    for s in todo:
+        n = s.n_l * s.n_r
+        s.g = s.g.reshape(s.n_l, s.n_r)
+        if s.g_lo is not None:
+            s.g_lo = s.g_lo.reshape(s.n_l, s.n_r)
+        nat.call("ion_psi_split_c128", n, ptr(s.g_in), ptr(s.g), ptr(s.g_lo), stream_ptr())
+    rows = [s for s in todo if getattr(s, "d_row_lo", None) is not None]
+    if rows:
+        nat.call("ion_sh_row_lo_c64", ctypes.byref(ShBatch(rows[0].precision, rows).plan), stream_ptr())
+    if todo:
+        torch.cuda.current_stream().synchronize()  # before the uploaded psi is released
+    for s in todo:
+        s.g_in = None
+
+
 class ShDeviceSim:
     """Device buffers of one spherical-harmonic simulation.  ``arrays``: the
     device tensors by attribute name, when built together with others
@@ -303,8 +398,11 @@ class ShDeviceSim:
         self.store_every = int(tab.store_every)
         self.gauge = int(tab.gauge)
         if arrays is None:
+            host = _sh_host_arrays(tab, precision)
+            self.h2d_bytes = sum(int(v.size) * np.dtype(v.dtype).itemsize for v in host.values() if v is not None)
             arrays = {k: (to_dev(v.materialize() if isinstance(v, _Fill) else v) if v is not None else None)
-                      for k, v in _sh_host_arrays(tab, precision).items()}
+                      for k, v in host.items()}
+            arrays.update(_sh_state_buffers(tab.n_l * tab.n_r, self.precision, [tab.n_l * tab.n_r])[0])
             self.n_data, n_states, self.n_tiles = _sh_device_sizes(tab)
             arrays["d_norm"] = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
             arrays["d_ip"] = torch.full((self.n_data * max(n_states, 1) * 2,), float("nan"), dtype=torch.float64,
@@ -316,6 +414,8 @@ class ShDeviceSim:
         for k, v in arrays.items():
             setattr(self, k, v)
         self.n_states = n_states
+        if self.g_in is not None and not getattr(self, "_deferred", False):
+            _sh_prepare([self])
 
     @classmethod
     def bulk(cls, tables: List[ShTables], precision) -> List["ShDeviceSim"]:
@@ -324,10 +424,8 @@ class ShDeviceSim:
         arenas = {}
         with concurrent.futures.ThreadPoolExecutor(max_workers=8) as pool:  # numpy work outside the GIL
             per = list(pool.map(lambda tab: _sh_host_arrays(tab, precision), tables))
-        # every simulation's g, then every g_lo (same sizes, so the two runs
-        # have the same layout and psi = g + g_lo is formed over both at
-        # once: sh_psi_many), then the tables
-        order = ["g", "g_lo"] + [k for k in (per[0] if per else {}) if k not in ("g", "g_lo")]
+        # every simulation's g (complex128) or uploaded psi first, then the tables
+        order = ["g", "g_in"] + [k for k in (per[0] if per else {}) if k not in ("g", "g_in")]
         for k in order:
             for i, host in enumerate(per):
                 v = host.get(k)
@@ -335,7 +433,12 @@ class ShDeviceSim:
                     arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
         views = {}
         for ar in arenas.values():
-            views.update(ar.upload(tensors=("g", "g_lo")))
+            views.update(ar.upload(tensors=("g", "g_in")))
+        # complex64 forms: g, g_lo and the row remainders, each one dense run
+        # over the simulations (psi = g + g_lo is formed over the whole run at
+        # once by sh_psi_many)
+        counts = [tab.n_l * tab.n_r for tab in tables]
+        state = _sh_state_buffers(sum(counts), Precision(precision), counts)
         torch.cuda.current_stream().synchronize()  # the pinned sources are released below
         sizes = [_sh_device_sizes(tab) for tab in tables]
         n_norm = sum(nd for nd, _, _ in sizes)
@@ -348,15 +451,20 @@ class ShDeviceSim:
         for i, tab in enumerate(tables):
             nd, ns, nt = sizes[i]
             arrays = {k: views.get((i, k)) for k in per[i]}
+            arrays.update(state[i])
             arrays["d_norm"] = _DevSlice(d_norm, o_norm, (nd,))
             arrays["d_ip"] = _DevSlice(d_ip, o_ip, (nd * max(ns, 1) * 2,))
             arrays["d_partials"] = _DevSlice(d_part, o_part, (nt * (1 + 2 * ns),))
-            sim = cls(tab, precision, arrays=arrays)
+            sim = cls.__new__(cls)
+            sim._deferred = True  # prepared together below
+            sim.__init__(tab, precision, arrays=arrays)
+            sim.h2d_bytes = sum(int(v.size) * np.dtype(v.dtype).itemsize for v in per[i].values() if v is not None)
             sim._bulk = dict(norm=(d_norm, o_norm, nd), ip=(d_ip, o_ip, nd * max(ns, 1) * 2))
             o_norm += nd
             o_ip += nd * max(ns, 1) * 2
             o_part += nt * (1 + 2 * ns)
             sims.append(sim)
+        _sh_prepare(sims)
         return sims
 
 
@@ -385,6 +493,8 @@ class ShDeviceSim:
         d.g_lo = ptr(self.g_lo)
         d.gauge = self.gauge
         d.h2r, d.h2r32 = ptr(self.d_h2r), ptr(self.d_h2r32)
+        d.row_lo = ptr(self.d_row_lo)
+        d.kinv, d.cent, d.corr0 = ptr(self.d_kinv64), ptr(self.d_cent64), float(self.tab.corr0)
         return d
 
     def data(self):
@@ -396,7 +506,7 @@ class ShDeviceSim:
     def psi_host(self) -> np.ndarray:
         g = self.g.cpu().numpy().astype(np.complex128)
         if self.g_lo is not None:
-            g = g + self.g_lo.cpu().numpy().astype(np.complex128)
+            g = g + lo_unpack(self.g_lo.cpu().numpy())
         return g
 
 
@@ -447,14 +557,15 @@ def sh_psi_many(sims: List["ShDeviceSim"]) -> List[np.ndarray]:
     rg = _run_of(gs)
     has_lo = all(t is not None for t in los)
     rl = _run_of(los) if has_lo else None
+    # the residual words of the run laid out point for point like g
     if rg is not None and rg[0].dtype == torch.complex64 and (
             not any(t is not None for t in los) or
-            (rl is not None and rg[0] is rl[0] and rg[2] - rg[1] == rl[2] - rl[1] and
-             all(b.storage_offset() - a.storage_offset() == rl[1] - rg[1] for a, b in zip(gs, los)))):
+            (rl is not None and rg[2] - rg[1] == rl[2] - rl[1] and
+             all(b.storage_offset() - rl[1] == a.storage_offset() - rg[1] for a, b in zip(gs, los)))):
         base, g0, g1 = rg
         flat = base.reshape(-1)
         psi = torch.empty(g1 - g0, dtype=torch.complex128, device=base.device)
-        lo = flat[rl[1]:rl[2]] if rl is not None else None
+        lo = rl[0].reshape(-1)[rl[1]:rl[2]] if rl is not None else None
         nat.call("ion_psi_to_c128", g1 - g0, ptr(flat[g0:g1]), ptr(lo), ptr(psi), stream_ptr())
         host = _host_copy(psi)
         return [host[g.storage_offset() - g0:g.storage_offset() - g0 + g.numel()].reshape(tuple(g.shape))
@@ -475,7 +586,7 @@ def sh_psi_many(sims: List["ShDeviceSim"]) -> List[np.ndarray]:
     def one(s):
         g = view(s.g).astype(np.complex128)
         if s.g_lo is not None:
-            g += view(s.g_lo)
+            g += lo_unpack(view(s.g_lo))
         return g
 
     with concurrent.futures.ThreadPoolExecutor(max_workers=8) as pool:  # numpy work outside the GIL
@@ -682,14 +793,17 @@ class LineDeviceSim:
         g0 = np.asarray(tab.g0, dtype=np.complex128)
         self.g = to_dev(g0).to(complex_dtype(precision))
         self.g_lo = None
-        if self.precision == Precision.C64X:  # psi = g + g_lo
+        if self.precision == Precision.C64X:  # psi = g + g_lo (packed)
             hi = g0.astype(np.complex64)
-            self.g_lo = to_dev((g0 - hi.astype(np.complex128)).astype(np.complex64))
+            self.g_lo = to_dev(lo_pack(g0 - hi.astype(np.complex128)))
         self.d_hd, self.d_hoff, self.d_zq = to_dev(tab.hd, f64), to_dev(tab.hoff, f64), to_dev(tab.zq, f64)
         self.d_mask = to_dev(tab.mask, f64) if tab.mask is not None else None
         self.d_tau, self.d_ef = to_dev(tab.tau, f64), to_dev(tab.efield, f64)
         self.d_hd32, self.d_hoff32, self.d_zq32 = to_dev(tab.hd, f32), to_dev(tab.hoff, f32), to_dev(tab.zq, f32)
         self.d_mask32 = to_dev(tab.mask, f32) if tab.mask is not None else None
+        self.d_hd_lo32 = self.d_hoff_lo32 = None
+        if self.precision == Precision.C64X:
+            self.d_hd_lo32, self.d_hoff_lo32 = to_dev(_lo32(tab.hd)), to_dev(_lo32(tab.hoff))
         self.d_vstat = self.d_vstat32 = self.d_kin = self.d_twiddle = None
         if tab.method == nat.ION_LINE_FFT:
             self.d_vstat, self.d_vstat32 = to_dev(tab.vstat, f64), to_dev(tab.vstat, f32)
@@ -721,6 +835,7 @@ class LineDeviceSim:
         d.vstat, d.kin, d.twiddle, d.vstat32 = ptr(self.d_vstat), ptr(self.d_kin), ptr(self.d_twiddle), ptr(self.d_vstat32)
         d.g_lo = ptr(self.g_lo)
         d.gauge, d.vcoef = int(self.tab.gauge), float(self.tab.vcoef)
+        d.hd_lo32, d.hoff_lo32 = ptr(self.d_hd_lo32), ptr(self.d_hoff_lo32)
         return d
 
     def data(self):
@@ -731,7 +846,7 @@ class LineDeviceSim:
     def psi_host(self) -> np.ndarray:
         g = self.g.cpu().numpy().astype(np.complex128)
         if self.g_lo is not None:
-            g = g + self.g_lo.cpu().numpy().astype(np.complex128)
+            g = g + lo_unpack(self.g_lo.cpu().numpy())
         return g
 
 

@@ -79,6 +79,10 @@ class ShSim(ctypes.Structure):
         ("g_lo", c_vp),
         ("h2r", c_vp),
         ("h2r32", c_vp),
+        ("row_lo", c_vp),
+        ("kinv", c_vp),
+        ("cent", c_vp),
+        ("corr0", c_f64),
     ]
 
 
@@ -132,6 +136,8 @@ class LineSim(ctypes.Structure):
         ("vstat32", c_vp),
         ("g_lo", c_vp),
         ("vcoef", c_f64),
+        ("hd_lo32", c_vp),
+        ("hoff_lo32", c_vp),
     ]
 
 
@@ -197,6 +203,8 @@ _SIGS = {
     "ion_line_max_n_c64": (c_i64, []),
     "ion_line_max_n_c64x": (c_i64, []),
     "ion_cyl_adi_run_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
+    "ion_sh_row_lo_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
+    "ion_psi_split_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp]),
     "ion_cyl_adi_pass_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "ion_cyl_max_points_c128": (c_i64, []),
     "ion_tridiag_eig_scratch_doubles": (c_i64, [c_i32, c_i32]),

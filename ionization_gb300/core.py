@@ -26,9 +26,11 @@ class Precision(StrEnum):
     C128: complex128 state and FP64 arithmetic (matches the reference).
     C64: complex64 state, FP32 sweeps, FP64 fields, coefficients and
     reductions.
-    C64X: as C64, with the rounding residual of the state kept in a second
-    complex64 array (spherical-harmonic meshes): storing the state no longer
-    rounds it to FP32, which removes the dominant error of C64."""
+    C64X: as C64, with the rounding residual of the state kept beside it
+    (two bf16 a point, 12 bytes a point in all) and refined radial solves
+    whose residual is formed with the FP64 Hamiltonian: storing the state no
+    longer rounds it to FP32 and the FP32 coefficient tables no longer
+    perturb the dynamics, which removes the dominant errors of C64."""
 
     C128 = "c128"
     C64 = "c64"

@@ -60,6 +60,25 @@ __device__ __forceinline__ void st(Cx<R>* p, Cx<R> a) {
 }
 
 // ---------------------------------------------------------------------------
+// The stored residual of a complex64 state with residual (c64x): psi = g + lo
+// with g complex64 and lo two bf16 in one 32-bit word (re in the low half,
+// im in the high half), 12 bytes per point.  |lo| <= ulp(g) / 2 after every
+// renormalisation, so its 8 significant bits carry psi to ~33 bits; bf16
+// keeps FP32's exponent range, so lo needs no scaling.  Packing rounds each
+// component to nearest even (cvt.rn.bf16x2.f32); unpacking is exact.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lo_pack(Cx<float> v) {
+    uint32_t w;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(w) : "f"(v.im), "f"(v.re));
+    return w;
+}
+__device__ __forceinline__ Cx<float> lo_unpack(uint32_t w) {
+    return Cx<float>{__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u)};
+}
+// lo as a later unpack of its packed form sees it
+__device__ __forceinline__ Cx<float> lo_round(Cx<float> v) { return lo_unpack(lo_pack(v)); }
+
+// ---------------------------------------------------------------------------
 // host-side status plumbing
 // ---------------------------------------------------------------------------
 void set_error(const char* fmt, ...);

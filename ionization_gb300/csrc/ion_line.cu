@@ -724,21 +724,23 @@ struct LineResCoef {
     const Cx<float>* lob;
     const Cx<float>* prev;  // previous CTA's residual buffer (DSMEM) or nullptr
     const Cx<float>* next;
-    const double* hd64;  // the FP64 diagonal of H0 that hd32 rounds
+    const float* hd_lo;    // hd64 - hd32, the low part of the FP64 diagonal of H0, or NULL
+    const float* hoff_lo;  // hoff64 - hoff32, or NULL
+    float tau_lo;          // tau64 - tau32
     int T, L;
     __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const { c(i, bo, bd); }
     // bd_exact - bd for the diagonal bd = tau * fma(zq, E, hd32) of local row
     // i: the rounding of hd32 from the FP64 diagonal (hd = -2p + V loses the
     // low bits of V beside the kinetic term, a random potential of ~1e-8 of
-    // the kinetic diagonal) plus the rounding of the field term and of the
-    // product with tau, formed with error-free transforms.  The explicit half
-    // uses the exact diagonal; the refinement then solves with it.
+    // the kinetic diagonal) plus the rounding of the field term, of tau and
+    // of the product with tau, formed with error-free transforms.  The
+    // explicit half uses the exact diagonal; the refinement then solves with it.
     __device__ __forceinline__ float bd_lo(int i) const {
         const int gi = c.off + i;
         const LineCnCoef<float>& k = c.c;
         if (gi >= k.n) return 0.f;
         const float hd = k.tb.hd[gi];
-        float h = hd, herr = float(hd64[gi] - double(hd));
+        float h = hd, herr = hd_lo ? hd_lo[gi] : 0.f;
         if (k.with_field) {
             const float zq = k.tb.zq[gi];
             h = fmaf(zq, k.efield, hd);
@@ -749,7 +751,16 @@ struct LineResCoef {
             herr += ((sm - h) + se) + pe;
         }
         const float b = k.tau * h;
-        return fmaf(k.tau, h, -b) + k.tau * herr;
+        return fmaf(k.tau, h, -b) + fmaf(k.tau, herr, tau_lo * h);
+    }
+    // bo_exact - bo for the coupling of local rows i and i + 1 (0 outside
+    // the line): the low parts of hoff and of tau, and the product's rounding
+    __device__ __forceinline__ float bo_lo(int i) const {
+        const int gi = c.off + i;
+        const LineCnCoef<float>& k = c.c;
+        if (gi < 0 || gi >= k.n - 1) return 0.f;
+        const float o = k.tb.hoff[gi];
+        return fmaf(k.tau, o, -(k.tau * o)) + fmaf(k.tau, hoff_lo ? hoff_lo[gi] : 0.f, tau_lo * o);
     }
     __device__ __forceinline__ Cx<float> lo_at(int i) const {
         if (i < 0) return prev ? prev[islot<M>(L - 1, T)] : Cx<float>{0.f, 0.f};
@@ -764,7 +775,10 @@ __device__ __forceinline__ Cx<float> stencil_row(const LineResCoef<M>& c, int i,
     float e1, e2;
     const float s1 = two_sum_full(bd, a0, e1);
     const float rs = two_sum_full(s1, bo, e2);
-    const float rl = (e1 + e2) + c.bd_lo(i);
+    // the remainders of the FP64 diagonal and couplings enter the row sum;
+    // the couplings' own roundings act on neighbour differences only, which
+    // matters far less (a relative error of ~1e-7 in the kinetic energy)
+    const float rl = ((e1 + e2) + c.bd_lo(i)) + (c.bo_lo(i - 1) + c.bo_lo(i));
     const Cx<float> dm = p0 - p1, dp = p2 - p1;
     const Cx<float> l0 = c.lo_at(i - 1), l1 = c.lo_at(i), l2 = c.lo_at(i + 1);
     return Cx<float>{a0 * dm.re + bo * dp.re + (rs * p1.re + rl * p1.re) + (a0 * l0.re + bd * l1.re + bo * l2.re),
@@ -864,7 +878,7 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     double* scratch = reinterpret_cast<double*>(red + 12 * plan.threads);
     double* part = scratch + 32;
     Cx<float>* g = static_cast<Cx<float>*>(S.g);
-    Cx<float>* glo = static_cast<Cx<float>*>(S.g_lo);
+    uint32_t* glo = static_cast<uint32_t*>(S.g_lo);  // packed bf16x2
     const Cx<float> zero = {0.f, 0.f};
 
     if (mode == 1) {
@@ -872,7 +886,7 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
         for (int i = threadIdx.x; i < L; i += blockDim.x) {
             const bool in = off + i < n;
             line[islot<M>(i, T)] = in ? ld(g + off + i) : zero;
-            lob[islot<M>(i, T)] = in ? ld(glo + off + i) : zero;
+            lob[islot<M>(i, T)] = in ? lo_unpack(glo[off + i]) : zero;
         }
         __syncthreads();
         line_reduce_res<M>(S, line, lob, T, off, t0, scratch, part, rank, C);
@@ -890,7 +904,7 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     // the pair at global row gi as staged: (g, g_lo) with the first phase
     auto staged = [&](int gi, Cx<float>& h, Cx<float>& lw) {
         h = ld(g + gi);
-        lw = ld(glo + gi);
+        lw = lo_unpack(glo[gi]);
         if (split) phase_res(h, lw, (tb.zq[gi] * ef) * tau);
     };
     for (int i = threadIdx.x; i < L; i += blockDim.x) {
@@ -902,7 +916,8 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
     cl.sync();  // the neighbours' halo rows are staged
     const LineResCoef<M> coef{OffsetCoef<float>{LineCnCoef<float>{tb, tau, ef, !split, n}, off}, lob,
                               rank > 0 ? cl.map_shared_rank(lob, rank - 1) : nullptr,
-                              rank + 1 < C ? cl.map_shared_rank(lob, rank + 1) : nullptr, S.hd, T, L};
+                              rank + 1 < C ? cl.map_shared_rank(lob, rank + 1) : nullptr, S.hd_lo32, S.hoff_lo32,
+                              float(S.tau[t + 1] - double(tau)), T, L};
     const ClusterHalo<float> halo{rank > 0 ? cl.map_shared_rank(line, rank - 1) : nullptr,
                                   rank + 1 < C ? cl.map_shared_rank(line, rank + 1) : nullptr};
     const int tid = threadIdx.x;
@@ -948,10 +963,13 @@ __global__ void __launch_bounds__(512) line_res_kernel(ion_line_plan plan, int m
         h = add_exact_f(h, ext[sl], lw);
         if (split) phase_res(h, lw, (tb.zq[gi] * ef) * tau);
         if (tb.mask) scale_res(h, lw, tb.mask[gi]);
+        // the residual as stored (packed): the data reductions below see what
+        // the next step reloads
+        const uint32_t w = lo_pack(lw);
         line[sl] = h;
-        lob[sl] = lw;
+        lob[sl] = lo_unpack(w);
         st(g + gi, h);
-        st(glo + gi, lw);
+        glo[gi] = w;
     }
     __syncthreads();
     if (line_is_data(t + 1, tf, S.store_every)) line_reduce_res<M>(S, line, lob, T, off, t + 1, scratch, part, rank, C);

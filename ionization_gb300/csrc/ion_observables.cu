@@ -50,24 +50,13 @@ __device__ __forceinline__ double obs_block_sum(double v, double* sh) {
     return r;
 }
 
+// glo: the stored residual of a complex64 state (packed bf16x2), or NULL
 template <typename R>
-__device__ __forceinline__ double abs2_at(const Cx<R>* g, const Cx<R>* glo, int64_t k) {
-    const Cx<R> x = ld(g + k);
-    double re = double(x.re), im = double(x.im);
-    if (glo) {
-        const Cx<R> e = ld(glo + k);
-        re += double(e.re);
-        im += double(e.im);
-    }
-    return re * re + im * im;
-}
-
-template <typename R>
-__device__ __forceinline__ Cx<double> value_at(const Cx<R>* g, const Cx<R>* glo, int64_t k) {
+__device__ __forceinline__ Cx<double> value_at(const Cx<R>* g, const uint32_t* glo, int64_t k) {
     const Cx<R> x = ld(g + k);
     Cx<double> v = {double(x.re), double(x.im)};
     if (glo) {
-        const Cx<R> e = ld(glo + k);
+        const Cx<float> e = lo_unpack(glo[k]);
         v.re += double(e.re);
         v.im += double(e.im);
     }
@@ -75,7 +64,13 @@ __device__ __forceinline__ Cx<double> value_at(const Cx<R>* g, const Cx<R>* glo,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(OBS_THREADS) weighted_stage1(int64_t n, const Cx<R>* g, const Cx<R>* glo, int nw,
+__device__ __forceinline__ double abs2_at(const Cx<R>* g, const uint32_t* glo, int64_t k) {
+    const Cx<double> v = value_at(g, glo, k);
+    return v.re * v.re + v.im * v.im;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(OBS_THREADS) weighted_stage1(int64_t n, const Cx<R>* g, const uint32_t* glo, int nw,
                                                                const double* w, double* part) {
     __shared__ double sh[32];
     double acc[OBS_MAX_W];
@@ -111,7 +106,7 @@ __global__ void obs_stage2(int nparts, int nq, const double* part, double weight
 // one CTA per tile of OBS_ROWS rows x all l; warp w takes l = w, w + 8, ...
 // and lane jj the row j0 + jj, so a warp's loads are one contiguous segment
 template <typename R>
-__global__ void __launch_bounds__(OBS_THREADS) sh_obs_stage1(const Cx<R>* g, const Cx<R>* glo, int nr, int nl,
+__global__ void __launch_bounds__(OBS_THREADS) sh_obs_stage1(const Cx<R>* g, const uint32_t* glo, int nr, int nl,
                                                              const double* r, const double* cl, int nrad,
                                                              const double* radii, double* part) {
     __shared__ double sh[32];
@@ -173,7 +168,7 @@ static int weighted_impl(int64_t n, const void* g, const void* g_lo, int32_t nw,
     cudaStream_t s = as_stream(stream);
     double* part = static_cast<double*>(scratch);
     weighted_stage1<R><<<blocks, OBS_THREADS, 0, s>>>(n, static_cast<const Cx<R>*>(g),
-                                                      static_cast<const Cx<R>*>(g_lo), nw, w, part);
+                                                      static_cast<const uint32_t*>(g_lo), nw, w, part);
     if (int e = check_launch("weighted_stage1")) return e;
     obs_stage2<<<1, 32, 0, s>>>(blocks, nw, part, weight, out);
     return check_launch("obs_stage2");
@@ -197,7 +192,7 @@ static int sh_obs_impl(const void* g, const void* g_lo, int32_t nr, int32_t nl, 
     }
     cudaStream_t s = as_stream(stream);
     double* part = static_cast<double*>(scratch);
-    sh_obs_stage1<R><<<tiles, OBS_THREADS, 0, s>>>(static_cast<const Cx<R>*>(g), static_cast<const Cx<R>*>(g_lo),
+    sh_obs_stage1<R><<<tiles, OBS_THREADS, 0, s>>>(static_cast<const Cx<R>*>(g), static_cast<const uint32_t*>(g_lo),
                                                    nr, nl, r, cl, nrad, radii, part);
     if (int e = check_launch("sh_obs_stage1")) return e;
     obs_stage2<<<1, 128, 0, s>>>(tiles, nq, part, weight, out);

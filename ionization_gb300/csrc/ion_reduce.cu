@@ -102,19 +102,32 @@ static int reduce_impl(int64_t M, const void* g, int32_t ns, const void* states,
     return check_launch("reduce_stage2");
 }
 
-// psi of a complex64 state as complex128: hi + lo (lo, the stored residual,
-// may be absent), each component one FP64 sum of two floats.  Memory-bound;
-// coalesced 8-byte loads, 16-byte stores.
-__global__ void __launch_bounds__(256) psi_to_c128_kernel(int64_t n, const Cx<float>* hi, const Cx<float>* lo,
+// psi of a complex64 state as complex128: hi + lo (lo, the stored residual
+// packed as bf16x2, may be absent), each component one FP64 sum of two
+// floats.  Memory-bound; coalesced 8- and 4-byte loads, 16-byte stores.
+__global__ void __launch_bounds__(256) psi_to_c128_kernel(int64_t n, const Cx<float>* hi, const uint32_t* lo,
                                                           Cx<double>* out) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
         const Cx<float> h = hi[i];
         Cx<double> v = {double(h.re), double(h.im)};
         if (lo) {
-            const Cx<float> l = lo[i];
+            const Cx<float> l = lo_unpack(lo[i]);
             v = Cx<double>{v.re + double(l.re), v.im + double(l.im)};
         }
         out[i] = v;
+    }
+}
+
+// complex128 psi into the complex64 hi (nearest) and, if lo, the packed
+// residual of psi - hi (each component's difference is exact in FP64 and
+// rounded to FP32, then to bf16)
+__global__ void __launch_bounds__(256) psi_split_kernel(int64_t n, const Cx<double>* in, Cx<float>* hi,
+                                                        uint32_t* lo) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const Cx<double> v = in[i];
+        const Cx<float> h = {float(v.re), float(v.im)};
+        hi[i] = h;
+        if (lo) lo[i] = lo_pack(Cx<float>{float(v.re - double(h.re)), float(v.im - double(h.im))});
     }
 }
 
@@ -123,6 +136,18 @@ __global__ void __launch_bounds__(256) psi_to_c128_kernel(int64_t n, const Cx<fl
 using namespace ion;
 
 extern "C" {
+int ion_psi_split_c128(int64_t n, const void* in, void* hi, void* lo, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !hi))) {
+        set_error("ion_psi_split_c128: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return ION_OK;
+    const int64_t want = (n + 255) / 256;
+    const int blocks = int(want < 8 * 152 ? want : 8 * 152);
+    psi_split_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, static_cast<const Cx<double>*>(in),
+                                                             static_cast<Cx<float>*>(hi), static_cast<uint32_t*>(lo));
+    return check_launch("psi_split_kernel");
+}
 int64_t ion_reduce_scratch_bytes(int64_t M, int32_t n_states) {
     (void)M;
     return int64_t(RED_BLOCKS) * (1 + 2 * int64_t(n_states < 0 ? 0 : n_states)) * int64_t(sizeof(double));
@@ -144,7 +169,7 @@ int ion_psi_to_c128(int64_t n, const void* hi, const void* lo, void* out, void* 
     const int64_t want = (n + 255) / 256;
     const int blocks = int(want < 8 * 152 ? want : 8 * 152);
     psi_to_c128_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, static_cast<const Cx<float>*>(hi),
-                                                               static_cast<const Cx<float>*>(lo),
+                                                               static_cast<const uint32_t*>(lo),
                                                                static_cast<Cx<double>*>(out));
     return check_launch("psi_to_c128_kernel");
 }

@@ -187,20 +187,26 @@ struct ShCnCoef32 {
     const float* hoff;
     float ll1, corr0, tau;
     int n;
-    // the line's stored residual (c64x) staged in shared memory in the
-    // line's interleaved layout (slot (i mod 2^mshift) T + i >> mshift), or NULL
-    const Cx<float>* lob;
+    // the line's stored residual (c64x, packed bf16x2) staged in shared memory
+    // in the line's interleaved layout (slot (i mod 2^mshift) T + i >> mshift),
+    // or NULL
+    const uint32_t* lob;
     int T, mshift;
+    // the line's row-sum remainders (ion_sh_sim.row_lo, bf16), or NULL: with
+    // them the explicit half applies the FP64 Hamiltonian (the refinement)
+    const uint16_t* rlo;
     __device__ __forceinline__ Cx<float> lo_at(int i) const {
-        return lob[(i & ((1 << mshift) - 1)) * T + (i >> mshift)];
+        return lo_unpack(lob[(i & ((1 << mshift) - 1)) * T + (i >> mshift)]);
     }
+    __device__ __forceinline__ float row_rem(int i) const { return __uint_as_float(uint32_t(rlo[i]) << 16); }
+    // the FP32 diagonal before tau, as every solve forms it (load_chunk too)
     __device__ __forceinline__ void operator()(int i, float& bo, float& bd) const {
         if (i < 0 || i >= n) {
             bo = 0.f;
             bd = 0.f;
             return;
         }
-        float h = kinv[i] + ll1 * cent[i];
+        float h = fmaf(ll1, cent[i], kinv[i]);
         if (i == 0) h = h + corr0;
         bd = tau * h;
         bo = (i < n - 1) ? tau * hoff[i] : 0.f;
@@ -220,7 +226,7 @@ __device__ __forceinline__ void load_chunk(const ShCnCoef32<RES>& c, int s, floa
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             const int k = 4 * q + e, i = s + k;
-            float h = kk[e] + c.ll1 * cc[e];
+            float h = fmaf(c.ll1, cc[e], kk[e]);  // as ShCnCoef32::operator()
             if (i == 0) h = h + c.corr0;
             bd[k] = i < c.n ? c.tau * h : 0.f;
             bo[k] = i < c.n - 1 ? c.tau * hh[e] : 0.f;
@@ -256,7 +262,11 @@ __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i
     float e1, e2;
     const float s1 = two_sum_err(bd, a0, e1);
     const float rs = two_sum_err(s1, bo, e2);
-    const float rl = e1 + e2;  // rs + rl = a0 + bd + bo to ~2^-48
+    float rl = e1 + e2;  // rs + rl = a0 + bd + bo to ~2^-48
+    // with the remainders, rs + rl is the FP64 Hamiltonian's row sum; the
+    // couplings' own roundings act on neighbour differences only, which
+    // matters far less (a relative error of ~1e-7 in the kinetic energy)
+    if (c.rlo != nullptr && i < c.n) rl += c.row_rem(i);
     const Cx<float> dm = p0 - p1, dp = p2 - p1;
     Cx<float> v = {a0 * dm.re + bo * dp.re + (rs * p1.re + rl * p1.re),
                    a0 * dm.im + bo * dp.im + (rs * p1.im + rl * p1.im)};
@@ -273,25 +283,28 @@ __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i
 template <typename R, bool RES> struct ShCnCoefFor;
 template <bool RES> struct ShCnCoefFor<double, RES> {
     using type = ShCnCoef<double>;
-    __device__ static type make(const ion_sh_sim& S, int l, double tau, const void*, int, int) {
+    __device__ static type make(const ion_sh_sim& S, int l, double tau, const void*, int, int, bool = false) {
         return type{ShH<double>::make(S, l), tau, S.n_r};
     }
 };
 template <bool RES> struct ShCnCoefFor<float, RES> {
     using type = ShCnCoef32<RES>;
-    // lob: the line's residual staged in shared memory, or NULL
-    __device__ static type make(const ion_sh_sim& S, int l, float tau, const void* lob, int T, int mshift) {
+    // lob: the line's residual staged in shared memory, or NULL; exact: with
+    // the row-sum remainders (when the simulation carries them)
+    __device__ static type make(const ion_sh_sim& S, int l, float tau, const void* lob, int T, int mshift,
+                                bool exact = false) {
         return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r,
-                    static_cast<const Cx<float>*>(lob), T, mshift};
+                    static_cast<const uint32_t*>(lob), T, mshift,
+                    (exact && S.row_lo) ? S.row_lo + int64_t(l) * S.n_r : nullptr};
     }
 };
 
 // psi of item ``item`` into ``dst`` (interleaved, zero padding), and its
-// stored residual into ``lodst`` when given (complex64 with g_lo),
-// asynchronously
+// stored residual (packed bf16x2) into ``lodst`` when given (complex64 with
+// g_lo), asynchronously
 template <typename R, int M>
 __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int item, Cx<R>* dst,
-                                                  Cx<R>* lodst = nullptr) {
+                                                  uint32_t* lodst = nullptr) {
     const int si = plan.cn_items[2 * item];
     const int l = plan.cn_items[2 * item + 1];
     const ion_sh_sim& S = plan.sims[si];
@@ -300,7 +313,7 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
     const int T = (nr + M - 1) / M;
     const int npad = T * M;
     const Cx<R>* g = static_cast<const Cx<R>*>(S.g) + int64_t(l) * nr;
-    const Cx<R>* glo = (lodst && S.g_lo) ? static_cast<const Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
+    const uint32_t* glo = (lodst && S.g_lo) ? static_cast<const uint32_t*>(S.g_lo) + int64_t(l) * nr : nullptr;
     for (int i = threadIdx.x; i < npad; i += blockDim.x) {
         Cx<R>* d = dst + islot<M>(i, T);
         if (i < nr) {
@@ -308,10 +321,10 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
                 cp_async16(d, g + i);
             else
                 cp_async8(d, g + i);
-            if (glo) cp_async8(lodst + islot<M>(i, T), glo + i);
+            if (glo) cp_async4(lodst + islot<M>(i, T), glo + i);
         } else {
             *d = Cx<R>{R(0), R(0)};
-            if (glo) lodst[islot<M>(i, T)] = Cx<R>{R(0), R(0)};
+            if (glo) lodst[islot<M>(i, T)] = 0u;
         }
     }
 }
@@ -337,19 +350,26 @@ struct MinusIExtra {
 //   A delta = Y - A Delta1 = -i B (2 psi + Delta1) - Delta1,
 // i.e. the same solver on phi = psi + Delta1 / 2 with X = -i Delta1, so the
 // fixed rounding of the elimination of A acts only on the small residual.
+// 4 rows per thread (complex64) fits in 64 registers, so those CTAs may
+// hold up to 1024 threads (lines of up to 4096 points at 32 warps an SM)
+template <typename R, int M>
+__host__ __device__ constexpr int sh_cn_max_threads() {
+    return (M == 4 && sizeof(R) == 4) ? 1024 : 512;
+}
+
 template <typename R, int M, bool REFINE>
-__global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int item0, int item_end, int dbuf) {
+__global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion_sh_plan plan, int item0, int item_end, int dbuf) {
     constexpr int refine = REFINE ? 1 : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cap = blockDim.x * M;
     // psi (double-buffered), with refinement the increment and the staged
-    // residual (double-buffered like psi), then the PCR scratch
+    // residual (packed, double-buffered like psi), then the PCR scratch
     Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* buf1 = buf0 + cap;
     Cx<R>* ext = buf0 + (dbuf ? 2 : 1) * cap;
-    Cx<R>* lob0 = ext + (refine ? cap : 0);
-    Cx<R>* lob1 = lob0 + (dbuf ? cap : 0);
-    Cx<R>* red = lob0 + (refine ? (dbuf ? 2 : 1) * cap : 0);
+    uint32_t* lob0 = reinterpret_cast<uint32_t*>(ext + (refine ? cap : 0));
+    uint32_t* lob1 = lob0 + (dbuf ? cap : 0);
+    Cx<R>* red = reinterpret_cast<Cx<R>*>(lob0 + (refine ? (dbuf ? 2 : 1) * cap : 0));
     int item = item0 + blockIdx.x;
     if (item >= item_end) return;
     if (dbuf) {
@@ -358,7 +378,7 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
     }
     for (int j = 0; item < item_end; item += gridDim.x, ++j) {
         Cx<R>* cur = (dbuf && (j & 1)) ? buf1 : buf0;
-        Cx<R>* lob = (dbuf && (j & 1)) ? lob1 : lob0;
+        uint32_t* lob = (dbuf && (j & 1)) ? lob1 : lob0;
         if (dbuf) {
             const int next = item + gridDim.x;
             if (next < item_end)
@@ -380,22 +400,28 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
             const int T = (nr + M - 1) / M;
             const R tau = R(S.tau[t + 1]);
             // with a stored residual the solve leaves the increment in ``inc``
-            Cx<R>* glo = sizeof(R) == 4 && S.g_lo ? static_cast<Cx<R>*>(S.g_lo) + int64_t(l) * nr : nullptr;
-            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T,
-                                                           M == 16 ? 4 : (M == 8 ? 3 : 2));
+            uint32_t* glo = sizeof(R) == 4 && S.g_lo ? static_cast<uint32_t*>(S.g_lo) + int64_t(l) * nr : nullptr;
+            const int mshift = M == 16 ? 4 : (M == 8 ? 3 : 2);
+            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T, mshift);
             Cx<R>* inc = cur;
             if constexpr (REFINE) {
                 // two solves through one call site: delta1 into ext, then on
                 // phi = psi + delta1 / 2 (formed as it is read, so cur keeps
-                // psi for the store) delta1 + delta into ext
+                // psi for the store) delta1 + delta into ext.  The second
+                // forms its residual with the FP64 Hamiltonian's row sums
+                // (ion_sh_sim.row_lo), so the refined solve converges to the
+                // FP64 system.
                 const bool two = glo != nullptr;
                 if (two) inc = ext;
+                const auto coef2 = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T,
+                                                                mshift, true);
                 for (int pass = 0; pass < (two ? 2 : 1); ++pass) {
                     // The correction of the second solve is ~1e-7 of delta1,
                     // so its reduced system may stop at couplings below
                     // 2^-13: the error left, ~1e-4 of the correction, is far
                     // below the FP32 rounding of the coefficients.
-                    block_cn_solve<R, M>(T, threadIdx.x, R(2), HalfStepView<R>{cur, ext, pass == 1}, red, coef,
+                    block_cn_solve<R, M>(T, threadIdx.x, R(2), HalfStepView<R>{cur, ext, pass == 1}, red,
+                                         pass == 1 ? coef2 : coef,
                                          MinusIExtra<R, M>{ext, T, pass == 1},
                                          AddOrSetOut<R, M>{inc, T, pass == 1 || !two},
                                          pass == 1 ? R(1.0 / 8192.0) : PcrTiny<R>::value);
@@ -414,10 +440,11 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
                     const int i = threadIdx.x + k * blockDim.x;
                     if (i < nr) {
                         // refined: cur still holds psi; otherwise the increment
-                        Cx<R> lo = refine ? lob[islot<M>(i, T)] : ld(glo + i);
+                        const Cx<float> lo0 = lo_unpack(refine ? lob[islot<M>(i, T)] : glo[i]);
+                        Cx<R> lo = Cx<R>{R(lo0.re), R(lo0.im)};
                         const Cx<R> h = add_exact(refine ? cur[islot<M>(i, T)] : ld(g + i), inc[islot<M>(i, T)], lo);
                         st(g + i, h);
-                        st(glo + i, lo);
+                        glo[i] = lo_pack(Cx<float>{float(lo.re), float(lo.im)});
                     }
                 }
             } else {
@@ -433,9 +460,13 @@ __global__ void __launch_bounds__(512) sh_cn_pipelined(ion_sh_plan plan, int ite
     cp_async_wait<0>();
 }
 
+// psi (x2 when double-buffered); with refinement the increment and the
+// packed residual (4 bytes a row, x2 when double-buffered); the PCR scratch
 template <typename R>
-__host__ __device__ inline size_t sh_cn_pipelined_smem(int threads, int M, int buffers) {
-    return size_t(buffers) * threads * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads);
+__host__ __device__ inline size_t sh_cn_pipelined_smem(int threads, int M, int refine, int dbuf) {
+    const size_t cap = size_t(threads) * M;
+    const size_t nb = dbuf ? 2 : 1;
+    return nb * cap * sizeof(Cx<R>) + (refine ? cap * sizeof(Cx<R>) + nb * cap * 4 : 0) + pcr_smem_bytes<R>(threads);
 }
 
 // ---------------------------------------------------------------------------
@@ -508,25 +539,40 @@ template <> struct Tile<double> {
     __device__ void scale(int k, double m) const { hi[k] = scaled(hi[k], m); }
     __device__ __forceinline__ static void renorm(Pair&, bool) {}
     __device__ void renorm(int, bool) const {}
+    __device__ __forceinline__ static void quant(Pair&) {}
     __device__ Cx<double> out(int k) const { return hi[k]; }
-    __device__ __forceinline__ void store(int k, Cx<double>* g, Cx<double>*, int64_t at) const { st(g + at, hi[k]); }
+    __device__ __forceinline__ void store(int k, Cx<double>* g, uint32_t*, int64_t at) const { st(g + at, hi[k]); }
 };
+// The complex64 tile keeps its compensation word lo packed as bf16x2, the
+// format of the stored residual: every operator unpacks it, works in FP32 and
+// packs it again, which is exactly what a store and a reload between two
+// launches do to it, so results do not depend on where a run is cut into
+// launches; the register sweeps that chain operators round lo the same way
+// between them (``quant``).
 template <> struct Tile<float> {
     Cx<float>* hi;
-    Cx<float>* lo;
+    uint32_t* lo;
     static constexpr bool comp = true;
     struct Pair {
         Cx<float> x0, x1, l0, l1;
     };
     __device__ Cx<double> value(int k) const {
-        return Cx<double>{double(hi[k].re) + double(lo[k].re), double(hi[k].im) + double(lo[k].im)};
+        const Cx<float> l = lo_unpack(lo[k]);
+        return Cx<double>{double(hi[k].re) + double(l.re), double(hi[k].im) + double(l.im)};
     }
-    __device__ __forceinline__ Pair load(int k0, int k1) const { return Pair{hi[k0], hi[k1], lo[k0], lo[k1]}; }
+    __device__ __forceinline__ Pair load(int k0, int k1) const {
+        return Pair{hi[k0], hi[k1], lo_unpack(lo[k0]), lo_unpack(lo[k1])};
+    }
     __device__ __forceinline__ void put(int k0, int k1, const Pair& p) const {
         hi[k0] = p.x0;
         hi[k1] = p.x1;
-        lo[k0] = p.l0;
-        lo[k1] = p.l1;
+        lo[k0] = lo_pack(p.l0);
+        lo[k1] = lo_pack(p.l1);
+    }
+    // lo as a put and a load between two operators leave it
+    __device__ __forceinline__ static void quant(Pair& p) {
+        p.l0 = lo_round(p.l0);
+        p.l1 = lo_round(p.l1);
     }
     __device__ __forceinline__ static void rot(Pair& p, float cm1, float s) {
         const Cx<float> x0 = p.x0, x1 = p.x1, l0 = p.l0, l1 = p.l1;
@@ -556,7 +602,7 @@ template <> struct Tile<float> {
         put(k0, k1, p);
     }
     __device__ void rotate_real(int k0, int k1, float cm1, float s) const {
-        const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo[k0], l1 = lo[k1];
+        const Cx<float> x0 = hi[k0], x1 = hi[k1], l0 = lo_unpack(lo[k0]), l1 = lo_unpack(lo[k1]);
         float e0r, e0i, e1r, e1i;
         const float h0r = two_sum(x0.re, cm1 * x0.re + s * x1.re, e0r);
         const float h0i = two_sum(x0.im, cm1 * x0.im + s * x1.im, e0i);
@@ -564,14 +610,14 @@ template <> struct Tile<float> {
         const float h1i = two_sum(x1.im, cm1 * x1.im - s * x0.im, e1i);
         hi[k0] = Cx<float>{h0r, h0i};
         hi[k1] = Cx<float>{h1r, h1i};
-        lo[k0] = Cx<float>{l0.re + (cm1 * l0.re + s * l1.re) + e0r, l0.im + (cm1 * l0.im + s * l1.im) + e0i};
-        lo[k1] = Cx<float>{l1.re + (cm1 * l1.re - s * l0.re) + e1r, l1.im + (cm1 * l1.im - s * l0.im) + e1i};
+        lo[k0] = lo_pack(Cx<float>{l0.re + (cm1 * l0.re + s * l1.re) + e0r, l0.im + (cm1 * l0.im + s * l1.im) + e0i});
+        lo[k1] = lo_pack(Cx<float>{l1.re + (cm1 * l1.re - s * l0.re) + e1r, l1.im + (cm1 * l1.im - s * l0.im) + e1i});
     }
     __device__ void scale(int k, float m) const {
-        Cx<float> h = hi[k], l = lo[k];
+        Cx<float> h = hi[k], l = lo_unpack(lo[k]);
         scaled(h, l, m);
         hi[k] = h;
-        lo[k] = l;
+        lo[k] = lo_pack(l);
     }
     // what a store and a reload between launches do to (hi, lo): hi + lo
     // rounded, and with a stored residual (keep) its rounding error as lo
@@ -586,19 +632,22 @@ template <> struct Tile<float> {
         renorm(p.x1, p.l1, keep);
     }
     __device__ void renorm(int k, bool keep) const {
-        Cx<float> h = hi[k], l = lo[k];
+        Cx<float> h = hi[k], l = lo_unpack(lo[k]);
         renorm(h, l, keep);
         hi[k] = h;
-        lo[k] = l;
+        lo[k] = lo_pack(l);
     }
-    __device__ Cx<float> out(int k) const { return Cx<float>{hi[k].re + lo[k].re, hi[k].im + lo[k].im}; }
+    __device__ Cx<float> out(int k) const {
+        const Cx<float> l = lo_unpack(lo[k]);
+        return Cx<float>{hi[k].re + l.re, hi[k].im + l.im};
+    }
     // element k to g[at]: hi + lo folded, or, with a stored residual, hi + lo
-    // renormalised (Fast2Sum, |hi| >= |lo|) into g[at] and glo[at]
-    __device__ __forceinline__ void store(int k, Cx<float>* g, Cx<float>* glo, int64_t at) const {
-        const Cx<float> h = hi[k], l = lo[k];
+    // renormalised (Fast2Sum, |hi| >= |lo|) into g[at] and glo[at] (packed)
+    __device__ __forceinline__ void store(int k, Cx<float>* g, uint32_t* glo, int64_t at) const {
+        const Cx<float> h = hi[k], l = lo_unpack(lo[k]);
         const float sr = h.re + l.re, si = h.im + l.im;
         st(g + at, Cx<float>{sr, si});
-        if (glo) st(glo + at, Cx<float>{l.re - (sr - h.re), l.im - (si - h.im)});
+        if (glo) glo[at] = lo_pack(Cx<float>{l.re - (sr - h.re), l.im - (si - h.im)});
     }
 };
 
@@ -647,8 +696,13 @@ __device__ __forceinline__ void rotate_mask_rotate_even(const Tile<R>& tl, int r
             R cm1, s;
             rot_coeffs(tau1 * (c * ef1), cm1, s);
             Tile<R>::rot(p, cm1, s);
-            if (do_mask) Tile<R>::scale(p, m);
+            Tile<R>::quant(p);
+            if (do_mask) {
+                Tile<R>::scale(p, m);
+                Tile<R>::quant(p);
+            }
             Tile<R>::renorm(p, keep);
+            Tile<R>::quant(p);
             rot_coeffs(tau2 * (c * ef2), cm1, s);
             Tile<R>::rot(p, cm1, s);
             tl.put(k0, k1, p);
@@ -717,9 +771,11 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, in
     }
 }
 
+// the tile (complex64: hi and the packed lo, 12 bytes an element) and the
+// block-sum scratch
 template <typename R>
 __host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
-    return size_t(max_nl) * rows * sizeof(Cx<R>) * (std::is_same<R, float>::value ? 2 : 1) + 32 * sizeof(double);
+    return size_t(max_nl) * rows * (sizeof(Cx<R>) + (std::is_same<R, float>::value ? 4 : 0)) + 32 * sizeof(double);
 }
 
 template <typename R>
@@ -764,15 +820,15 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
     tl.hi = hi;
     double* scratch;
     if constexpr (Tile<R>::comp) {
-        tl.lo = hi + tile_elems;
-        scratch = reinterpret_cast<double*>(hi + 2 * tile_elems);
+        tl.lo = reinterpret_cast<uint32_t*>(hi + tile_elems);
+        scratch = reinterpret_cast<double*>(tl.lo + tile_elems);
     } else {
         scratch = reinterpret_cast<double*>(hi + tile_elems);
     }
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
     // complex64 with a stored residual: the tile's compensation word starts
     // from it and is stored back renormalised instead of folded into g
-    Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
+    uint32_t* glo = Tile<R>::comp ? static_cast<uint32_t*>(S.g_lo) : nullptr;
     // the tile by asynchronous copies: every thread's loads are in flight
     // together without holding registers (register loads left the pass
     // waiting on global memory at a third of the DRAM bandwidth)
@@ -786,9 +842,9 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
                 cp_async8(hi + f, g + at);
             if constexpr (Tile<R>::comp) {
                 if (glo)
-                    cp_async8(tl.lo + f, glo + at);
+                    cp_async4(tl.lo + f, glo + at);
                 else
-                    tl.lo[f] = Cx<R>{R(0), R(0)};
+                    tl.lo[f] = 0u;
             }
         }
     }
@@ -940,13 +996,13 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
     tl.hi = hi;
     double* scratch;
     if constexpr (Tile<R>::comp) {
-        tl.lo = hi + tile_elems;
-        scratch = reinterpret_cast<double*>(hi + 2 * tile_elems);
+        tl.lo = reinterpret_cast<uint32_t*>(hi + tile_elems);
+        scratch = reinterpret_cast<double*>(tl.lo + tile_elems);
     } else {
         scratch = reinterpret_cast<double*>(hi + tile_elems);
     }
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
-    Cx<R>* glo = Tile<R>::comp ? static_cast<Cx<R>*>(S.g_lo) : nullptr;
+    uint32_t* glo = Tile<R>::comp ? static_cast<uint32_t*>(S.g_lo) : nullptr;
     const int span = jhi - jlo;
     for (int f = threadIdx.x; f < nl * span; f += blockDim.x) {  // asynchronous, as in sh_rot_kernel
         const int l = f / span, jj = jlo + f % span;
@@ -957,9 +1013,9 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
             cp_async8(hi + l * VEL_ROWS + jj, g + at);
         if constexpr (Tile<R>::comp) {
             if (glo)
-                cp_async8(tl.lo + l * VEL_ROWS + jj, glo + at);
+                cp_async4(tl.lo + l * VEL_ROWS + jj, glo + at);
             else
-                tl.lo[l * VEL_ROWS + jj] = Cx<R>{R(0), R(0)};
+                tl.lo[l * VEL_ROWS + jj] = 0u;
         }
     }
     cp_async_commit();
@@ -1075,8 +1131,14 @@ template <> struct ShRows<double> {
     static bool ok(int r) { return r == 4 || r == 8; }
 };
 template <> struct ShRows<float> {
-    static bool ok(int r) { return r == 8 || r == 16; }
+    static bool ok(int r) { return r == 4 || r == 8 || r == 16; }
 };
+
+// the largest CTA of the radial solve at ``rows`` rows per thread
+template <typename R>
+static int sh_max_threads(int rows) {
+    return rows == 4 ? sh_cn_max_threads<R, 4>() : 512;
+}
 
 template <typename R>
 static int sh_rows(const ion_sh_plan* p) {
@@ -1087,7 +1149,7 @@ template <typename R>
 static int sh_validate(const ion_sh_plan* p) {
     if (!p || !p->sims || p->n_sims < 0 || p->n_cn_items < 0 || p->n_rot_items < 0 ||
         p->rot_rows <= 0 || p->rot_rows > 32 || p->max_n_l <= 0 || p->max_n_r < 2 ||
-        p->cn_threads <= 0 || p->cn_threads > ShCfg<R>::MAX_T || (p->cn_threads & 31) ||
+        p->cn_threads <= 0 || p->cn_threads > sh_max_threads<R>(sh_rows<R>(p)) || (p->cn_threads & 31) ||
         (p->cn_rows != 0 && !ShRows<R>::ok(p->cn_rows))) {
         set_error("ion_sh: invalid plan");
         return ION_ERR_INVALID_ARGUMENT;
@@ -1099,7 +1161,7 @@ static int sh_validate(const ion_sh_plan* p) {
     for (int b = 0, prev = 0; b < p->n_cn_buckets; ++b) {
         const int th = p->cn_bucket_threads[b];
         if (p->cn_bucket_end[b] < prev || p->cn_bucket_end[b] > p->n_cn_items || th <= 0 ||
-            th > ShCfg<R>::MAX_T || (th & 31) || th > p->cn_threads) {
+            th > sh_max_threads<R>(sh_rows<R>(p)) || (th & 31) || th > p->cn_threads) {
             set_error("ion_sh: invalid bucket %d", b);
             return ION_ERR_INVALID_ARGUMENT;
         }
@@ -1115,7 +1177,7 @@ static int sh_validate(const ion_sh_plan* p) {
         return ION_ERR_UNSUPPORTED;
     }
     const int rows = sh_rows<R>(p);
-    if (int64_t(p->max_n_r) > int64_t(rows) * ShCfg<R>::MAX_T ||
+    if (int64_t(p->max_n_r) > int64_t(rows) * sh_max_threads<R>(rows) ||
         sh_line_threads(p->max_n_r, rows) > p->cn_threads) {
         set_error("ion_sh: cn_threads %d / rows %d too small for n_r %d", p->cn_threads, rows, p->max_n_r);
         return ION_ERR_INVALID_ARGUMENT;
@@ -1161,12 +1223,11 @@ static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
         if (end > begin) {
             const int refine = (p->flags & ION_SH_REFINE) && sizeof(R) == 4 ? 1 : 0;
-            // psi x2, with refinement the increment and the staged residual x2
             int dbuf = 1;
-            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, 2 + 3 * refine);
+            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, refine, 1);
             if (smem > 200 * 1024) {
                 dbuf = 0;
-                smem = sh_cn_pipelined_smem<R>(threads, MAXM, 1 + 2 * refine);
+                smem = sh_cn_pipelined_smem<R>(threads, MAXM, refine, 0);
             }
             if (smem > 200 * 1024) {
                 set_error("ion_sh: radial line too long for shared memory");
@@ -1196,7 +1257,11 @@ int sh_launch_cn<double>(const ion_sh_plan* p, cudaStream_t s) {
 template <>
 int sh_launch_cn<float>(const ion_sh_plan* p, cudaStream_t s) {
     if (p->n_cn_items == 0) return ION_OK;
-    return sh_rows<float>(p) == 8 ? sh_launch_cn_pipelined<float, 8>(p, s) : sh_launch_cn_pipelined<float, 16>(p, s);
+    switch (sh_rows<float>(p)) {
+        case 4: return sh_launch_cn_pipelined<float, 4>(p, s);
+        case 8: return sh_launch_cn_pipelined<float, 8>(p, s);
+        default: return sh_launch_cn_pipelined<float, 16>(p, s);
+    }
 }
 
 template <typename R>
@@ -1238,6 +1303,45 @@ static int sh_phase(const ion_sh_plan* p, int phase, void* stream) {
     }
 }
 
+// The row-sum remainders of the c64x radial step (ion_sh_sim.row_lo): one
+// CTA per (simulation, l) line.  The FP32 coefficients are formed exactly as
+// the solve forms them (ShCnCoef32 and load_chunk), so the remainder is of
+// exactly the values the solve uses; their sum is exact in FP64.
+__global__ void __launch_bounds__(256) sh_row_lo_kernel(ion_sh_plan plan) {
+    const int si = plan.cn_items[2 * blockIdx.x];
+    const int l = plan.cn_items[2 * blockIdx.x + 1];
+    const ion_sh_sim& S = plan.sims[si];
+    if (!S.row_lo || !S.kinv || !S.cent || !S.hoff || !S.kinv32 || !S.cent32 || !S.hoff32) return;
+    const int n = S.n_r;
+    const int64_t tn = S.t < S.t_final ? S.t + 1 : S.t_final;
+    const double tau = S.tau[tn > 0 ? tn : 1];
+    const float tau32 = float(tau);
+    const float ll1 = float(l) * float(l + 1);
+    const float c032 = l == 0 ? S.corr0_32 : 0.f;
+    const double ll1d = double(l) * double(l + 1);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float h = fmaf(ll1, S.cent32[i], S.kinv32[i]);
+        if (i == 0) h = h + c032;
+        const float bd = tau32 * h;
+        const float bo = i < n - 1 ? tau32 * S.hoff32[i] : 0.f;
+        const float a0 = i > 0 ? tau32 * S.hoff32[i - 1] : 0.f;
+        const double sum32 = (double(bd) + double(a0)) + double(bo);
+        double row = S.kinv[i] + ll1d * S.cent[i];
+        if (i == 0 && l == 0) row += S.corr0;
+        if (i > 0) row += S.hoff[i - 1];
+        if (i < n - 1) row += S.hoff[i];
+        const uint32_t w = lo_pack(Cx<float>{float(tau * row - sum32), 0.f});
+        S.row_lo[int64_t(l) * n + i] = uint16_t(w & 0xffffu);
+    }
+}
+
+static int sh_row_lo(const ion_sh_plan* p, void* stream) {
+    if (int e = sh_validate<float>(p)) return e;
+    if (p->n_cn_items == 0) return ION_OK;
+    sh_row_lo_kernel<<<p->n_cn_items, 256, 0, as_stream(stream)>>>(*p);
+    return check_launch("sh_row_lo_kernel");
+}
+
 template <typename R>
 static int sh_reduce(const ion_sh_plan* p, void* stream) {
     if (int e = sh_validate<R>(p)) return e;
@@ -1268,6 +1372,7 @@ int ion_sh_split_phase_c64(const ion_sh_plan* plan, int phase, void* stream) {
 }
 int ion_sh_reduce_c128(const ion_sh_plan* plan, void* stream) { return sh_reduce<double>(plan, stream); }
 int ion_sh_reduce_c64(const ion_sh_plan* plan, void* stream) { return sh_reduce<float>(plan, stream); }
+int ion_sh_row_lo_c64(const ion_sh_plan* plan, void* stream) { return sh_row_lo(plan, stream); }
 int64_t ion_sh_max_n_r_c128(void) { return int64_t(ShCfg<double>::MAXM) * ShCfg<double>::MAX_T; }
 int64_t ion_sh_max_n_r_c64(void) { return int64_t(ShCfg<float>::MAXM) * ShCfg<float>::MAX_T; }
 

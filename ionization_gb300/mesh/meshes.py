@@ -68,7 +68,7 @@ class QuantumMesh:
         g = self._psi_device().cpu().numpy().astype(np.complex128)
         lo = self._psi_residual()
         if lo is not None:
-            g = g + lo.cpu().numpy().astype(np.complex128)
+            g = g + dev.lo_unpack(lo.cpu().numpy()).reshape(g.shape)
         return g.reshape(self.mesh_shape)
 
     @g.setter
@@ -79,7 +79,7 @@ class QuantumMesh:
         lo = self._psi_residual()
         if lo is not None:
             hi = v.astype(np.complex64).astype(np.complex128)
-            lo.copy_(torch.from_numpy((v - hi).astype(np.complex64)).to(lo.device))
+            lo.copy_(torch.from_numpy(dev.lo_pack(v - hi)).to(lo.device))
 
     def _native_state(self):
         """Host copies of the device arrays that hold psi (the state itself and,

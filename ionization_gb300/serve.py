@@ -112,14 +112,16 @@ def device_bytes(req: Request, precision: Optional[str] = None) -> int:
     """Device memory a request holds while it runs (psi, coefficient and field
     tables, test states, data buffers)."""
     prec = Precision(precision or req.precision)
-    c = 8 if prec == Precision.C64 else 16  # complex64 + residual counts twice
+    c = {Precision.C64: 8, Precision.C64X: 12}.get(prec, 16)  # c64x: complex64 + packed residual
     n_t = req.steps + 1
     if req.kind == "sh":
         nr, nl, ns = req.points, req.l_bound, 15
-        return (nr * nl * c + (nr * nl * 8 if prec == Precision.C128 else 0) + nr * (5 * 8 + 6 * 4)
+        # FP64 and FP32 per-r tables; c64x adds the bf16 row-sum remainders
+        return (nr * nl * c + (nr * nl * 8 if prec == Precision.C128 else 0)
+                + (nr * nl * 2 if prec == Precision.C64X else 0) + nr * (7 * 8 + 6 * 4)
                 + nl * 12 + 2 * 8 * n_t + ns * nr * 16 + (nr // 32 + 1) * (1 + 2 * ns) * 8 + 4096)
     n = req.points
-    return n * c + n * (4 * 8 + 4 * 4) + 2 * 8 * n_t + n * 16 + 4096
+    return n * c + n * (4 * 8 + 6 * 4) + 2 * 8 * n_t + n * 16 + 4096
 
 
 class _Group:

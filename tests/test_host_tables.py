@@ -87,3 +87,29 @@ def test_data_slots_match_reference_mask():
                 assert dev.is_data_time(t, tf, every) == bool(mask[t])
                 if mask[t]:
                     assert dev.data_slot(t, tf, every) == slots[t]
+
+
+def test_residual_packing_rounds_like_bf16():
+    """The stored residual of a complex64 state (two bf16 in one word) is
+    packed on the host with round-to-nearest-even, as the device packs it:
+    torch's float32 -> bfloat16 conversion gives the same values, over
+    magnitudes from subnormal to large, zeros and ties included."""
+    import torch
+
+    from ionization_gb300 import _device as dev
+
+    rng = np.random.default_rng(1)
+    n = 100_000
+    x = (rng.normal(size=n) * np.exp(rng.uniform(-90, 5, n))
+         + 1j * rng.normal(size=n) * np.exp(rng.uniform(-90, 5, n))).astype(np.complex64)
+    x[:8] = 0
+    x[8:16] = np.float32(1e-40) - 1j * np.float32(3e-42)
+    x[16:18] = np.float32(1 + 2 ** -8) + 1j * np.float32(1 + 3 * 2 ** -8)  # ties: to even
+    w = dev.lo_pack(x)
+    assert w.dtype == np.int32 and w.shape == x.shape
+    u = dev.lo_unpack(w)
+    want_re = torch.from_numpy(x.real.copy()).to(torch.bfloat16).float().numpy()
+    want_im = torch.from_numpy(x.imag.copy()).to(torch.bfloat16).float().numpy()
+    assert np.array_equal(u.real.astype(np.float32), want_re)
+    assert np.array_equal(u.imag.astype(np.float32), want_im)
+    assert u[16] == 1 + 1j * (1 + 2 ** -6)
