@@ -668,7 +668,10 @@ def run_per_config(args, peak):
     from ionization_gb300 import mesh
     from ionization_gb300 import workloads as wl
 
-    cpu_jobs = {"line_cn_4096": 200, "line_fft_4096": 200, "sh_2000x41": 6, "cyl_2000x1000": 2}
+    want = set(args.configs.split(",")) if args.configs else {"line_cn_4096", "line_fft_4096", "sh_2000x41",
+                                                               "cyl_2000x1000"}
+    cpu_jobs = {k: n for k, n in {"line_cn_4096": 200, "line_fft_4096": 200, "sh_2000x41": 6,
+                                  "cyl_2000x1000": 2}.items() if k in want}
     cpu = {}
     pool = None
     if not args.no_cpu:  # the CPU legs run in spawned processes while the GPU legs run
@@ -691,7 +694,7 @@ def run_per_config(args, peak):
 
     # cfg 1: the 4096-point soft-core line, Crank-Nicolson (ADI), 4000 steps; one
     # launch runs all its steps, so the kernel time is the run's time
-    for prec in ("c128", "c64x"):
+    for prec in ("c128", "c64x") if "line_cn_4096" in want else ():
         K = 4000
         spec = wl.line_softcore_4096(steps=K + 20, precision=prec)
         sim, ms = timed_run(spec, K)
@@ -702,7 +705,7 @@ def run_per_config(args, peak):
             resident="psi (64 KB) stays in shared memory through the launch: not an HBM-bound run")
         del sim
     # the Fourier split-step on the same line
-    for prec in ("c128", "c64"):
+    for prec in ("c128", "c64") if "line_fft_4096" in want else ():
         K = 4000
         spec = wl.line_softcore("line_fft_4096", 4096, 0.05, 0.057, 4, 0.0, K + 20, precision=prec,
                                 evolution_method=mesh.FourierSplitOperator())
@@ -712,48 +715,50 @@ def run_per_config(args, peak):
             dtype=prec, kind="line", points=4096, K=K, total_ms=ms, kernels={"line_step_kernel": ms / K},
             resident="psi stays in shared memory through the launch: not an HBM-bound run")
         del sim
-    # cfg 2: Nr 2000 x l < 41, split operator, complex128 (the plain drop-in)
-    K = 400
-    spec = wl.sh_hydrogen_2000x41(steps=K + 40, precision="c128")
-    sim = spec.to_sim()
-    sim.run(max_steps=20)
-    torch.cuda.synchronize()
-    plan = sim.mesh._batch.plan
-    t = time_phases(plan, "c128", K, stream)
-    out["sh_2000x41_c128"] = dict(
-        name="sh_2000x41", workload="sh_hydrogen_2000x41: Nr 2000, l < 41, split operator, complex128",
-        dtype="c128", kind="sh", points=82000, K=K, total_ms=t["elapsed_ms"],
-        kernels={"sh_cn_pipelined": t["cn_ms"], "sh_rot_kernel": t["rot_ms"]},
-        resident="psi (1.3 MB) is L2-resident: not an HBM-bound run")
-    del sim
-    # cfg 3: cylindrical slice 2000 x 1000, ADI, complex128; each pass timed
-    K = 50
-    spec = wl.cyl_hydrogen_2000x1000(steps=K + 10)
-    sim = spec.to_sim()
-    sim.run(max_steps=5)
-    torch.cuda.synchronize()
-    m = sim.mesh
-    t0 = m._t
-    ev = _events(3 * K)
-    for k in range(K):
-        tn = t0 + k + 1
-        ev[3 * k].record(stream)
-        nat.call("ion_cyl_adi_pass_c128", m._cm, m._g.data_ptr(), m._gtmp.data_ptr(), tn, nat.ION_ADI_PASS_STRIDED,
-                 0, stream.cuda_stream)
-        ev[3 * k + 1].record(stream)
-        nat.call("ion_cyl_adi_pass_c128", m._cm, m._gtmp.data_ptr(), m._g.data_ptr(), tn, nat.ION_ADI_PASS_CONTIG,
-                 1, stream.cuda_stream)
-        ev[3 * k + 2].record(stream)
-    torch.cuda.synchronize()
-    zp = float(np.mean([ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(K)]))
-    rp = float(np.mean([ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(K)]))
-    total = ev[0].elapsed_time(ev[-1])
-    out["cyl_2000x1000_c128"] = dict(
-        name="cyl_2000x1000", workload="cyl_hydrogen_2000x1000: 2000 (z) x 1000 (rho), ADI, complex128",
-        dtype="c128", kind="cyl", points=2_000_000, K=K, total_ms=total,
-        kernels={"cyl_zpass_kernel": zp, "cyl_rhopass_kernel": rp},
-        resident="psi 32 MB: within L2 (129 MB) between the passes")
-    del sim, m
+    if "sh_2000x41" in want:
+        # cfg 2: Nr 2000 x l < 41, split operator, complex128 (the plain drop-in)
+        K = 400
+        spec = wl.sh_hydrogen_2000x41(steps=K + 40, precision="c128")
+        sim = spec.to_sim()
+        sim.run(max_steps=20)
+        torch.cuda.synchronize()
+        plan = sim.mesh._batch.plan
+        t = time_phases(plan, "c128", K, stream)
+        out["sh_2000x41_c128"] = dict(
+            name="sh_2000x41", workload="sh_hydrogen_2000x41: Nr 2000, l < 41, split operator, complex128",
+            dtype="c128", kind="sh", points=82000, K=K, total_ms=t["elapsed_ms"],
+            kernels={"sh_cn_pipelined": t["cn_ms"], "sh_rot_kernel": t["rot_ms"]},
+            resident="psi (1.3 MB) is L2-resident: not an HBM-bound run")
+        del sim
+    if "cyl_2000x1000" in want:
+        # cfg 3: cylindrical slice 2000 x 1000, ADI, complex128; each pass timed
+        K = 50
+        spec = wl.cyl_hydrogen_2000x1000(steps=K + 10)
+        sim = spec.to_sim()
+        sim.run(max_steps=5)
+        torch.cuda.synchronize()
+        m = sim.mesh
+        t0 = m._t
+        ev = _events(3 * K)
+        for k in range(K):
+            tn = t0 + k + 1
+            ev[3 * k].record(stream)
+            nat.call("ion_cyl_adi_pass_c128", m._cm, m._g.data_ptr(), m._gtmp.data_ptr(), tn, nat.ION_ADI_PASS_STRIDED,
+                     0, stream.cuda_stream)
+            ev[3 * k + 1].record(stream)
+            nat.call("ion_cyl_adi_pass_c128", m._cm, m._gtmp.data_ptr(), m._g.data_ptr(), tn, nat.ION_ADI_PASS_CONTIG,
+                     1, stream.cuda_stream)
+            ev[3 * k + 2].record(stream)
+        torch.cuda.synchronize()
+        zp = float(np.mean([ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(K)]))
+        rp = float(np.mean([ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(K)]))
+        total = ev[0].elapsed_time(ev[-1])
+        out["cyl_2000x1000_c128"] = dict(
+            name="cyl_2000x1000", workload="cyl_hydrogen_2000x1000: 2000 (z) x 1000 (rho), ADI, complex128",
+            dtype="c128", kind="cyl", points=2_000_000, K=K, total_ms=total,
+            kernels={"cyl_zpass_kernel": zp, "cyl_rhopass_kernel": rp},
+            resident="psi 32 MB: within L2 (129 MB) between the passes")
+        del sim, m
     torch.cuda.synchronize()
     if pool is not None:
         for k, r in cpu_async.items():
@@ -854,13 +859,26 @@ def main():
     ap.add_argument("--accuracy", default="full", choices=["full", "subset"],
                     help="accuracy over all 512 simulations (default) or a seeded subset of 8")
     ap.add_argument("--no-per-config", action="store_true", help="skip the per-configuration lines")
-    ap.add_argument("--rows", type=int, default=0, choices=[0, 8, 16],
+    ap.add_argument("--configs", default="", help="comma list of per-configuration workloads to run "
+                    "(line_cn_4096, line_fft_4096, sh_2000x41, cyl_2000x1000; default all)")
+    ap.add_argument("--only-per-config", action="store_true",
+                    help="run only the per-configuration lines and print them (a profiling case)")
+    ap.add_argument("--rows", type=int, default=0, choices=[0, 4, 8, 16],
                     help="rows per thread of the radial solve; 0 = autotune")
     args = ap.parse_args()
 
     from ionization_gb300 import replicas
 
     rank, world, local_rank = replicas.rank_world()
+    if args.only_per_config:
+        import torch
+
+        import ionization_gb300 as ig
+
+        torch.cuda.set_device(local_rank)
+        ig.build()
+        print(json.dumps(run_per_config(args, measured_peaks()[0])), flush=True)
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
