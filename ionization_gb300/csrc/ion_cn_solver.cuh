@@ -220,33 +220,36 @@ template <> struct PcrTiny<double> {
 // a xs_t + xe_t + c xs_{t+1} = d.  Substituting the first-row equations of
 // threads t and t+1 into r[1] leaves one tridiagonal row in xe per thread
 // (one step of odd-even reduction); PCR solves those T rows (ceil(log2 T)
-// levels of one row per thread), and xs_t follows from r[0].  Uses
-// 10 T complex words of ``red`` (pcr_smem_bytes<R>(T) holds 12 T).  On
-// return r[0].d = xs_t and r[1].d = xe_t.
+// levels of one row per thread), and xs_t follows from r[0].  One region of
+// 3 T complex words of ``red`` (pcr_cn_smem_bytes<R>(T)) holds, in turn, the
+// first rows, each level's rows and the solved xe: every exchange reads its
+// neighbours, meets a barrier, then writes.  On return r[0].d = xs_t and
+// r[1].d = xe_t.
+template <typename R>
+__host__ __device__ constexpr size_t pcr_cn_smem_bytes(int T) {
+    return 3 * size_t(T) * sizeof(Cx<R>);
+}
+
 template <typename R>
 __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* red, RedRow<R> (&r)[2],
                                              R tiny = PcrTiny<R>::value) {
     const Cx<R> zero = {R(0), R(0)}, one = {R(1), R(0)};
-    Cx<R>* Sa = red;
-    Cx<R>* Sc = red + T;
-    Cx<R>* Sd = red + 2 * T;
-    Cx<R>* Ab = red + 3 * T;  // double-buffered [2][T]
-    Cx<R>* Cb = red + 5 * T;
-    Cx<R>* Db = red + 7 * T;
-    Cx<R>* Xe = red + 9 * T;
+    Cx<R>* A = red;
+    Cx<R>* C = red + T;
+    Cx<R>* D = red + 2 * T;
     if (active) {
-        Sa[t] = r[0].a;
-        Sc[t] = r[0].c;
-        Sd[t] = r[0].d;
+        A[t] = r[0].a;
+        C[t] = r[0].c;
+        D[t] = r[0].d;
     }
     __syncthreads();
     RedRow<R> e = {zero, zero, zero};
     if (active) {
         Cx<R> an = zero, cn = zero, dn = zero;  // the next thread's first row
         if (t + 1 < T) {
-            an = Sa[t + 1];
-            cn = Sc[t + 1];
-            dn = Sd[t + 1];
+            an = A[t + 1];
+            cn = C[t + 1];
+            dn = D[t + 1];
         }
         const RedRow<R>& S = r[0];
         const RedRow<R>& E = r[1];
@@ -254,39 +257,41 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
         e.a = -(E.a * S.a) * inv;
         e.c = -(E.c * cn) * inv;
         e.d = (E.d - E.a * S.d - E.c * dn) * inv;
-        Ab[t] = e.a;
-        Cb[t] = e.c;
-        Db[t] = e.d;
+    }
+    __syncthreads();  // every first row is read
+    if (active) {
+        A[t] = e.a;
+        C[t] = e.c;
+        D[t] = e.d;
     }
     // the rows may already be decoupled below ``tiny`` (see the loop's exit)
     const bool coupled0 = active && (cabs1(e.a) > tiny || cabs1(e.c) > tiny);
     const int levels = __syncthreads_or(coupled0) ? pcr_levels(T) : 0;
-    int p = 0;
     for (int lev = 0, sig = 1; lev < levels; ++lev, sig <<= 1) {
+        Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
         if (active) {
-            const int base = p * T;
-            Cx<R> am = zero, cm = zero, dm = zero, ap = zero, cpp = zero, dp = zero;
             if (t - sig >= 0) {
-                am = Ab[base + t - sig];
-                cm = Cb[base + t - sig];
-                dm = Db[base + t - sig];
+                am = A[t - sig];
+                cm = C[t - sig];
+                dm = D[t - sig];
             }
             if (t + sig < T) {
-                ap = Ab[base + t + sig];
-                cpp = Cb[base + t + sig];
-                dp = Db[base + t + sig];
+                ap = A[t + sig];
+                cpp = C[t + sig];
+                dp = D[t + sig];
             }
+        }
+        __syncthreads();  // every neighbour row of this level is read
+        if (active) {
             const Cx<R> a = e.a, c = e.c, d = e.d;
             const Cx<R> inv = crecip_fast(one - cm * a - ap * c);
             e.a = -(am * a) * inv;
             e.c = -(cpp * c) * inv;
             e.d = (d - dm * a - dp * c) * inv;
-            const int wb = (p ^ 1) * T;
-            Ab[wb + t] = e.a;
-            Cb[wb + t] = e.c;
-            Db[wb + t] = e.d;
+            A[t] = e.a;
+            C[t] = e.c;
+            D[t] = e.d;
         }
-        p ^= 1;
         // Early exit: once every row's couplings are below PcrTiny the
         // rows are decoupled to the working precision and x = d.  The
         // inverse of 1 + i tau H decays geometrically along a line: with
@@ -296,10 +301,9 @@ __device__ __forceinline__ void pcr_solve_cn(int T, int t, bool active, Cx<R>* r
         const bool coupled = active && (cabs1(e.a) > tiny || cabs1(e.c) > tiny);
         if (!__syncthreads_or(coupled)) break;
     }
-    if (active) Xe[t] = e.d;
-    __syncthreads();
+    // D holds every xe (the barrier above ends the last write)
     if (active) {
-        const Cx<R> xem1 = t > 0 ? Xe[t - 1] : zero;
+        const Cx<R> xem1 = t > 0 ? D[t - 1] : zero;
         r[0].d = r[0].d - r[0].a * xem1 - r[0].c * e.d;
         r[1].d = e.d;
     }

@@ -402,7 +402,13 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
             // with a stored residual the solve leaves the increment in ``inc``
             uint32_t* glo = sizeof(R) == 4 && S.g_lo ? static_cast<uint32_t*>(S.g_lo) + int64_t(l) * nr : nullptr;
             const int mshift = M == 16 ? 4 : (M == 8 ? 3 : 2);
-            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T, mshift);
+            // With refinement the first solve needs only an approximation of
+            // delta1: the second forms the exact residual of whatever delta1
+            // is and leaves (I - A'^-1 A) times its error, ~1e-4 of it (the
+            // second solve's own PCR stops at 2^-13), so the first uses the
+            // plain FP32 stencil, without the exact row sums and the residual
+            // terms (an error of ~1e-5 of delta1, ~1e-9 after the correction).
+            const auto coef = ShCnCoefFor<R, REFINE>::make(S, l, tau, nullptr, T, mshift);
             Cx<R>* inc = cur;
             if constexpr (REFINE) {
                 // two solves through one call site: delta1 into ext, then on
@@ -466,7 +472,7 @@ template <typename R>
 __host__ __device__ inline size_t sh_cn_pipelined_smem(int threads, int M, int refine, int dbuf) {
     const size_t cap = size_t(threads) * M;
     const size_t nb = dbuf ? 2 : 1;
-    return nb * cap * sizeof(Cx<R>) + (refine ? cap * sizeof(Cx<R>) + nb * cap * 4 : 0) + pcr_smem_bytes<R>(threads);
+    return nb * cap * sizeof(Cx<R>) + (refine ? cap * sizeof(Cx<R>) + nb * cap * 4 : 0) + pcr_cn_smem_bytes<R>(threads);
 }
 
 // ---------------------------------------------------------------------------
