@@ -447,17 +447,22 @@ def run_e2e(args, specs, tables, rows, gs, points, precision):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
     b.step(K)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
     res = b.results()
     psis = b.psi_all()  # g (+ its residual) to the host
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    split = {"upload_s": round(t1 - t0, 3), "steps_s": round(t2 - t1, 3), "readback_s": round(wall - (t2 - t0), 3)}
     h2d = sum(s.h2d_bytes for s in b.sims)  # psi (complex128, split on the device) and the tables
     d2h = sum(s.g.numel() * 16 for s in b.sims)  # psi read back as complex128 (ion_psi_to_c128)
     d2h += sum(r["norm"].nbytes + 16 * len(r["inner_products"]) * len(r["norm"]) for r in res)
     del b, psis
     return {"value": points * K / wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d / K),
-            "d2h_bytes_per_step": int(d2h / K), "steps": K, "wall_s": round(wall, 3)}
+            "d2h_bytes_per_step": int(d2h / K), "steps": K, "wall_s": round(wall, 3), **split}
 
 
 def run_serving(args):

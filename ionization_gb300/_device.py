@@ -139,6 +139,9 @@ class ShTables:
     # A(times[t]) and h2r [n_r - 1] the r factor of the h2 blocks
     gauge: int = 0
     h2r: Optional[np.ndarray] = None
+    # the l rows of g0 that are not zero (None: find them); only those rows
+    # are uploaded, the rest are zeroed on the device
+    g0_rows: Optional[np.ndarray] = None
 
 
 SH_ROT_ROWS = 32
@@ -250,10 +253,12 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     c128 = precision == Precision.C128
     x = precision == Precision.C64X
     a = {}
-    # complex64 forms: psi goes up as complex128 and is split on the device
-    # into g and (c64x) its packed residual g_lo (ion_psi_split_c128)
-    a["g"] = g0 if c128 else None
-    a["g_in"] = None if c128 else g0
+    # psi goes up as its nonzero l rows only (an initial state is usually a few
+    # l components: hydrogen 1s has one), complex128; the device zeroes the
+    # other rows and, for the complex64 forms, splits these into g and (c64x)
+    # its packed residual g_lo (ion_psi_split_c128)
+    rows = sh_nonzero_rows(tab)
+    a["g_in"] = np.ascontiguousarray(g0[rows]) if rows.size else np.zeros((1, tab.n_r), np.complex128)
     a["d_hd"] = np.asarray(tab.hd, f64) if c128 else None
     # c64x: the FP64 per-r diagonal tables the device forms the row-sum
     # remainders from (ion_sh_row_lo_c64)
@@ -341,15 +346,22 @@ class _Arena:
                 for key, arr, off in self.items}
 
 
+def sh_nonzero_rows(tab: "ShTables") -> np.ndarray:
+    """The l rows of a simulation's initial psi that are not all zero."""
+    if tab.g0_rows is not None:
+        return np.asarray(tab.g0_rows, dtype=np.int64)
+    g0 = np.asarray(tab.g0).reshape(tab.n_l, tab.n_r)
+    return np.flatnonzero(np.any(g0 != 0, axis=1)).astype(np.int64)
+
+
 def _sh_state_buffers(total: int, precision, counts) -> List[dict]:
-    """Device-only state of complex64 simulations, one dense buffer per kind
-    sliced in order: g (complex64), and for c64x g_lo (packed residual words)
-    and d_row_lo (bf16 row-sum remainders).  Per simulation, by attribute."""
+    """Device-only state of simulations, one dense buffer per kind sliced in
+    order: g (complex128 or complex64), and for c64x g_lo (packed residual
+    words) and d_row_lo (bf16 row-sum remainders).  Per simulation, by
+    attribute."""
     precision = Precision(precision)
     out = [dict(g_lo=None, d_row_lo=None) for _ in counts]
-    if precision == Precision.C128:
-        return out
-    g = torch.empty(max(total, 1), dtype=torch.complex64, device=device())
+    g = torch.empty(max(total, 1), dtype=complex_dtype(precision), device=device())
     lo = rl = None
     if precision == Precision.C64X:
         lo = torch.empty(max(total, 1), dtype=torch.int32, device=device())
@@ -365,16 +377,30 @@ def _sh_state_buffers(total: int, precision, counts) -> List[dict]:
 
 
 def _sh_prepare(sims: List["ShDeviceSim"]):
-    """Finish the upload of complex64 simulations on the device: psi split
-    into g and g_lo, then (c64x) the row-sum remainders of the radial step.
-    The uploaded complex128 psi is released."""
+    """Finish the upload of simulations on the device: psi zeroed and its
+    uploaded rows put in place (complex64 forms: split into g and g_lo), then
+    (c64x) the row-sum remainders of the radial step.  The uploaded rows are
+    released."""
     todo = [s for s in sims if getattr(s, "g_in", None) is not None]
+    bases = {}
     for s in todo:
-        n = s.n_l * s.n_r
         s.g = s.g.reshape(s.n_l, s.n_r)
         if s.g_lo is not None:
             s.g_lo = s.g_lo.reshape(s.n_l, s.n_r)
-        nat.call("ion_psi_split_c128", n, ptr(s.g_in), ptr(s.g), ptr(s.g_lo), stream_ptr())
+        for t in (s.g, s.g_lo):
+            if t is not None:
+                b = t._base if t._base is not None else t
+                bases.setdefault(id(b), b)
+    for b in bases.values():  # the state buffers are dense runs: one fill each
+        b.zero_()
+    for s in todo:
+        n = s.n_r
+        for k, l in enumerate(s.g_rows):
+            if s.g.dtype == torch.complex128:
+                s.g[l].copy_(s.g_in[k])
+            else:
+                nat.call("ion_psi_split_c128", n, ptr(s.g_in[k]), ptr(s.g[l]),
+                         None if s.g_lo is None else ptr(s.g_lo[l]), stream_ptr())
     rows = [s for s in todo if getattr(s, "d_row_lo", None) is not None]
     if rows:
         nat.call("ion_sh_row_lo_c64", ctypes.byref(ShBatch(rows[0].precision, rows).plan), stream_ptr())
@@ -414,6 +440,7 @@ class ShDeviceSim:
         for k, v in arrays.items():
             setattr(self, k, v)
         self.n_states = n_states
+        self.g_rows = [int(l) for l in sh_nonzero_rows(tab)]
         if self.g_in is not None and not getattr(self, "_deferred", False):
             _sh_prepare([self])
 
@@ -424,8 +451,8 @@ class ShDeviceSim:
         arenas = {}
         with concurrent.futures.ThreadPoolExecutor(max_workers=8) as pool:  # numpy work outside the GIL
             per = list(pool.map(lambda tab: _sh_host_arrays(tab, precision), tables))
-        # every simulation's g (complex128) or uploaded psi first, then the tables
-        order = ["g", "g_in"] + [k for k in (per[0] if per else {}) if k not in ("g", "g_in")]
+        # every simulation's uploaded psi rows first, then the tables
+        order = ["g_in"] + [k for k in (per[0] if per else {}) if k != "g_in"]
         for k in order:
             for i, host in enumerate(per):
                 v = host.get(k)
@@ -433,10 +460,10 @@ class ShDeviceSim:
                     arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
         views = {}
         for ar in arenas.values():
-            views.update(ar.upload(tensors=("g", "g_in")))
-        # complex64 forms: g, g_lo and the row remainders, each one dense run
-        # over the simulations (psi = g + g_lo is formed over the whole run at
-        # once by sh_psi_many)
+            views.update(ar.upload(tensors=("g_in",)))
+        # g, g_lo and the row remainders, each one dense run over the
+        # simulations (psi = g + g_lo is formed over the whole run at once by
+        # sh_psi_many)
         counts = [tab.n_l * tab.n_r for tab in tables]
         state = _sh_state_buffers(sum(counts), Precision(precision), counts)
         torch.cuda.current_stream().synchronize()  # the pinned sources are released below

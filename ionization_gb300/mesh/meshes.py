@@ -510,6 +510,7 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
             tau=self._tau_host.copy(), efield=efield, kinv=tb["kinv"], cent=tb["cent"], corr0=tb["corr0"],
             state_l=sl, state_g=np.array(sg, dtype=np.complex128).reshape(len(sl), spec.r_points),
             weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
+            g0_rows=np.flatnonzero(np.any(np.asarray(g0).reshape(spec.l_bound, spec.r_points) != 0, axis=1)),
             store_every=spec.store_data_every, gauge=gauge, h2r=h2r,
         )
         if getattr(spec, "host_only", False):
