@@ -230,6 +230,10 @@ enum { ION_SH_REFINE = 1 };
 /* ion_sh_plan.flags: some simulations are in the velocity gauge (their
  * rotation pass runs in its own kernel), or all of them are. */
 enum { ION_SH_VELOCITY = 2, ION_SH_ONLY_VELOCITY = 4 };
+/* ion_sh_plan.flags: run the length gauge's rotation pass with its tile in
+ * shared memory (the form used beyond l_bound 256) instead of in registers;
+ * the two give the same results bit for bit. */
+enum { ION_SH_ROT_TILE = 8 };
 
 typedef struct ion_sh_plan {
     ion_sh_sim *sims;         /* device array [n_sims] */
@@ -364,7 +368,10 @@ typedef struct ion_line_plan {
     int32_t pad2_;
 } ion_line_plan;
 
-enum { ION_LINE_RESIDUAL = 1 };
+/* ION_LINE_HAS_FFT: the plan holds ION_LINE_FFT simulations; their CTAs take
+ * the shared memory that caches a step's phase factors (a Fourier line in a
+ * plan without the flag is left untouched). */
+enum { ION_LINE_RESIDUAL = 1, ION_LINE_HAS_FFT = 2 };
 
 int ion_line_run_c128(const ion_line_plan *plan, int64_t n_steps, void *stream);
 int ion_line_run_c64(const ion_line_plan *plan, int64_t n_steps, void *stream);

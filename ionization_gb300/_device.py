@@ -624,10 +624,13 @@ class ShBatch:
     """Many spherical-harmonic simulations advanced together."""
 
     def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None, cn_rows: int = 0,
-                 rot_rows: int = SH_ROT_ROWS):
+                 rot_rows: int = SH_ROT_ROWS, rot_kernel: str = "registers"):
         self.precision = Precision(precision)
         self.sims: List[ShDeviceSim] = list(sims or [])
         self.cn_rows = int(cn_rows)
+        if rot_kernel not in ("registers", "tile"):
+            raise ValueError("rot_kernel is 'registers' or 'tile'")
+        self.rot_kernel = rot_kernel  # the length gauge's rotation pass: tile in registers or in shared memory
         self.rot_rows = int(rot_rows)
         if self.rot_rows != SH_ROT_ROWS:
             raise ValueError("row tiles of the rotation pass are fixed by the partial-sum layout")
@@ -685,6 +688,8 @@ class ShBatch:
         plan.max_n_l = max([s.n_l for s in sims] + [1])
         plan.max_n_r = max([s.n_r for s in sims] + [2])
         plan.flags = nat.ION_SH_REFINE if any(s.g_lo is not None for s in sims) else 0
+        if self.rot_kernel == "tile":
+            plan.flags |= nat.ION_SH_ROT_TILE
         n_vel = sum(1 for s in sims if s.gauge == nat.ION_GAUGE_VELOCITY)
         if n_vel:
             plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)
@@ -931,6 +936,8 @@ class LineBatch:
                 p.threads = _round32(max(-(-s.n // (c * maxm)) for s in sims))
                 p.cluster = c
                 p.flags = nat.ION_LINE_RESIDUAL if self.precision == Precision.C64X else 0
+                if any(s.tab.method == nat.ION_LINE_FFT for s in sims):
+                    p.flags |= nat.ION_LINE_HAS_FFT
                 plans.append(p)
                 keep.append(d)
             self._plans = plans

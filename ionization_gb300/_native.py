@@ -26,6 +26,7 @@ ION_LINE_FFT = 2
 ION_SH_REFINE = 1
 ION_SH_VELOCITY = 2
 ION_SH_ONLY_VELOCITY = 4
+ION_SH_ROT_TILE = 8
 ION_GAUGE_LENGTH = 0
 ION_ADI_STRIDED_FIRST = 0
 ION_ADI_CONTIG_FIRST = 1
@@ -33,6 +34,7 @@ ION_ADI_PASS_STRIDED = 0
 ION_ADI_PASS_CONTIG = 1
 ION_GAUGE_VELOCITY = 1
 ION_LINE_RESIDUAL = 1
+ION_LINE_HAS_FFT = 2
 
 
 class NativeLibraryError(RuntimeError):

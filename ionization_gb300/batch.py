@@ -41,7 +41,7 @@ class BatchedSphericalHarmonicSimulation:
     in complex64 with FP64 fields, coefficient tables and reductions)."""
 
     def __init__(self, specs, precision: Optional[str] = None, graph_steps: int = 64, use_graphs: bool = True,
-                 cn_rows: int = 0, tables=None):
+                 cn_rows: int = 0, tables=None, rot_kernel: str = "registers"):
         self.specs = list(specs)
         self.precision = Precision(precision or self.specs[0].precision)
         if tables is None:
@@ -49,7 +49,7 @@ class BatchedSphericalHarmonicSimulation:
         self.tables = tables
         dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
         self.sims = dsims
-        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows)
+        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows, rot_kernel=rot_kernel)
         self.graph_steps = int(graph_steps)
         self.use_graphs = use_graphs
         self._graphs = {}

@@ -138,9 +138,18 @@ __device__ void line_reduce(const ion_line_sim& S, const Cx<R>* line, int T, int
     }
 }
 
+// words of the region after the line: the reduced system of a
+// Crank-Nicolson line, or (a plan with Fourier split-step lines, ION_LINE_HAS_FFT)
+// the cached phase factors of a Fourier line, whichever is larger
 template <typename R>
-__host__ __device__ inline size_t line_smem(int threads, int M) {
-    return size_t(threads) * M * sizeof(Cx<R>) + pcr_smem_bytes<R>(threads) + 32 * sizeof(double);
+__host__ __device__ inline size_t line_red_words(int threads, int M, bool fft) {
+    const size_t cn = pcr_smem_bytes<R>(threads) / sizeof(Cx<R>);
+    const size_t ft = fft ? 2 * size_t(threads) * M : 0;
+    return cn > ft ? cn : ft;
+}
+template <typename R>
+__host__ __device__ inline size_t line_smem(int threads, int M, bool fft = false) {
+    return (size_t(threads) * M + line_red_words<R>(threads, M, fft)) * sizeof(Cx<R>) + 32 * sizeof(double);
 }
 
 // ---------------------------------------------------------------------------
@@ -236,8 +245,22 @@ template <> __device__ __forceinline__ float kinetic_angle<float>(double a) {
     return float(fma(-turns, 6.283185307179586, a));
 }
 
+// x * exp(-i theta) from theta's rotation coefficients c = (cos - 1, sin),
+// as phase() forms it
 template <typename R>
-__device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, double* scratch) {
+__device__ __forceinline__ Cx<R> apply_phase(Cx<R> x, Cx<R> c) {
+    return Cx<R>{x.re + (c.re * x.re + c.im * x.im), x.im + (c.re * x.im - c.im * x.re)};
+}
+
+// One step of a Fourier line held in x.  pc[n], kc[n]: the step's potential
+// phase and the kinetic phase (cos - 1, sin) per point, cached in shared
+// memory: the potential phase is applied twice per step from one evaluation,
+// and the kinetic phase, which depends on tau alone, is evaluated again only
+// when tau changes (ktau: the tau kc holds, the same in every thread).  The
+// arithmetic is that of evaluating every phase where it is applied.
+template <typename R>
+__device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, double* scratch, Cx<R>* pc,
+                              Cx<R>* kc, double& ktau) {
     const int n = S.n;
     const int lg = 31 - __clz(n);
     const FftTab<R> tb = FftTab<R>::make(S);
@@ -246,7 +269,12 @@ __device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, 
     const double tau = S.tau[t + 1];
     const R taur = R(tau), ef = R(S.efield[t + 1]);
 
-    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = phase(ld(g + i), taur * (tb.v[i] + tb.zq[i] * ef));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        Cx<R> c;
+        rot_coeffs(taur * (tb.v[i] + tb.zq[i] * ef), c.re, c.im);
+        pc[i] = c;
+        x[i] = apply_phase(ld(g + i), c);
+    }
     __syncthreads();
     for (int lq = lg - 2; lq >= 0; lq -= 2) {
         fft_dif4(x, n, lq, tw);
@@ -257,8 +285,16 @@ __device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, 
         __syncthreads();
     }
     const R inv_n = R(1) / R(n);  // exact: n is a power of two
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        x[i] = scale(phase(x[i], kinetic_angle<R>(2.0 * tau * S.kin[i])), inv_n);
+    const bool fresh = tau != ktau;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        if (fresh) {
+            Cx<R> c;
+            rot_coeffs(kinetic_angle<R>(2.0 * tau * S.kin[i]), c.re, c.im);
+            kc[i] = c;
+        }
+        x[i] = scale(apply_phase(x[i], kc[i]), inv_n);
+    }
+    ktau = tau;
     __syncthreads();
     if (lg & 1) {
         fft_pairs(x, n);
@@ -269,7 +305,7 @@ __device__ void line_fft_step(ion_line_sim& S, int64_t t, Cx<R>* x, int stride, 
         __syncthreads();
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        Cx<R> y = phase(x[i], taur * (tb.v[i] + tb.zq[i] * ef));
+        Cx<R> y = apply_phase(x[i], pc[i]);
         if (tb.mask) y = Cx<R>{y.re * tb.mask[i], y.im * tb.mask[i]};
         x[i] = y;
         st(g + i, y);
@@ -306,10 +342,15 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     const int npad = T * M;
     Cx<R>* line = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* red = line + plan.threads * M;
-    double* scratch = reinterpret_cast<double*>(red + 12 * plan.threads);
+    const bool fft_plan = (plan.flags & ION_LINE_HAS_FFT) != 0;
+    double* scratch = reinterpret_cast<double*>(red + line_red_words<R>(plan.threads, M, fft_plan));
     Cx<R>* g = static_cast<Cx<R>*>(S.g);
     const Cx<R> zero = {R(0), R(0)};
     if (n < 2 || n > plan.max_n) return;  // the plan's shared memory is sized for max_n
+    // a Fourier line needs the phase caches (ION_LINE_HAS_FFT): without them
+    // it is left untouched, like a line of another plan
+    if (S.method == ION_LINE_FFT && !fft_plan) return;
+    double ktau = -1.0;  // no kinetic phase cached yet (tau > 0)
 
     if (mode == 1) {
         if (!line_is_data(t0, tf, S.store_every)) return;
@@ -322,7 +363,7 @@ __global__ void __launch_bounds__(512) line_step_kernel(ion_line_plan plan, int 
     if (t0 >= tend) return;
     for (int64_t t = t0; t < tend; ++t) {  // each step ends with a CTA barrier
     if (S.method == ION_LINE_FFT) {
-        line_fft_step<R>(S, t, line, T, scratch);
+        line_fft_step<R>(S, t, line, T, scratch, red, red + plan.threads * M, ktau);
         continue;
     }
     const LineTab<R> tb = LineTab<R>::make(S);
@@ -1043,7 +1084,8 @@ static int line_validate(const ion_line_plan* p) {
         set_error("ion_line: max_n = %d needs more than %d threads x %d CTAs", p->max_n, p->threads, C);
         return ION_ERR_INVALID_ARGUMENT;
     }
-    if (line_cluster_smem<R>(p->threads, M) > LINE_SMEM_LIMIT) {
+    if (line_cluster_smem<R>(p->threads, M) > LINE_SMEM_LIMIT ||
+        line_smem<R>(p->threads, M, (p->flags & ION_LINE_HAS_FFT) != 0) > LINE_SMEM_LIMIT) {
         set_error("ion_line: line too long for shared memory");
         return ION_ERR_UNSUPPORTED;
     }
@@ -1081,7 +1123,8 @@ static int line_launch(const ion_line_plan* p, int mode, int n_steps, cudaStream
     }
     if (int e = ensure_smem_limit((const void*)line_step_kernel<R, M>, int(LINE_SMEM_LIMIT), "line_step_kernel"))
         return e;
-    line_step_kernel<R, M><<<p->n_sims, p->threads, line_smem<R>(p->threads, M), s>>>(*p, mode, n_steps);
+    line_step_kernel<R, M><<<p->n_sims, p->threads,
+                             line_smem<R>(p->threads, M, (p->flags & ION_LINE_HAS_FFT) != 0), s>>>(*p, mode, n_steps);
     return check_launch("line_step_kernel");
 }
 
