@@ -229,26 +229,39 @@ HEADLINE = "c64x"  # complex64 arithmetic, residual-compensated state: meets the
 
 
 def time_batch(specs, tables, precision, K, warmup, rows, gs, local_rank, barrier):
-    """K steps of the whole batch with per-kernel CUDA events on the launching
-    stream (ion_sh_split_phase: rotations before the first solve, then per step
-    radial solve / rotation pass / advance) and the clocks sampled meanwhile."""
+    """K steps of the whole batch through the API's own path (CUDA-graph
+    replays of ``gs`` steps, the remainder launched directly), timed with CUDA
+    events on the launching stream and the clocks sampled meanwhile; then,
+    outside the timed region, min(K, 20) steps phase by phase with events
+    around each radial solve and rotation pass for the per-kernel times."""
     import torch
 
-    from ionization_gb300 import _native as nat
     from ionization_gb300 import batch as bm
 
     b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows,
                                               tables=tables)
-    b.step(max(warmup, 3))
+    b.step(gs + max(warmup, 3))  # captures the graph
     torch.cuda.synchronize()
     plan = b.batch.plan
     stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier()
     torch.cuda.synchronize()
     with Clocks(local_rank) as clk:
-        out = time_phases(plan, precision, K, stream)
+        e0.record(stream)
+        b.step(K)
+        e1.record(stream)
+        torch.cuda.synchronize()
     barrier()
-    out["clocks"] = clk.summary()
+    elapsed = e0.elapsed_time(e1)
+    # launches of the timed steps: per run of n steps one rotation pass before
+    # the first solve, then per step the radial buckets, the rotation pass and
+    # the advance
+    per_step = max(int(plan.n_cn_buckets), 1) + 2
+    runs = [gs] * (K // gs) + ([K % gs] if K % gs else [])
+    launches = sum(1 + per_step * n for n in runs)
+    out = time_phases(plan, precision, min(K, 20), stream)
+    out.update(elapsed_ms=elapsed, launches=launches, clocks=clk.summary(), shape=bm.plan_shape(b))
     del b
     torch.cuda.synchronize()
     return out
@@ -310,9 +323,10 @@ def run_ours(args, rank, world, local_rank):
     points = int(sum(t.n_r * t.n_l for t in tables))
 
     if args.rows:  # a fixed launch shape (e.g. for a profiler run, whose timings would mislead the autotuner)
-        (best_rows, best_gs), tune = (args.rows, 32), {}
+        best, tune = dict(rows=args.rows, graph_steps=32), {}
     else:
-        (best_rows, best_gs), tune = bm.autotune(specs, HEADLINE, graph_steps=(32,), steps=16, tables=tables)
+        best, tune = bm.autotune(specs, HEADLINE, graph_steps=(16, 32, 64), steps=32, tables=tables)
+    best_rows, best_gs = best["rows"], best["graph_steps"]
 
     # ---- timed region: K steps of the headline configuration ----
     K = args.steps
@@ -421,7 +435,10 @@ def run_ours(args, rank, world, local_rank):
             "l2": f"inputs larger than L2 (state {points * state_bytes / 1e6:.0f} MB)",
             "parallelism": f"replicas x{world}",
             "autotune": {"chosen": {"cn_rows_per_thread": best_rows, "graph_steps": best_gs},
-                         "ms_per_step": {f"rows{r}_graph{g}": round(v, 4) for (r, g), v in tune.items()}},
+                         "plan": main["shape"],
+                         "ms_per_step": {k: round(v, 4) for k, v in tune.items()}},
+            "timing": "CUDA-graph replay of the API (graph_steps per replay, remainder launched directly); "
+                      "per-kernel times from a separate phase-by-phase run of min(K, 20) steps",
             "host_setup_s": round(setup_host_s, 2),
         },
         "roofline": roofline,

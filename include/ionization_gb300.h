@@ -230,10 +230,6 @@ enum { ION_SH_REFINE = 1 };
 /* ion_sh_plan.flags: some simulations are in the velocity gauge (their
  * rotation pass runs in its own kernel), or all of them are. */
 enum { ION_SH_VELOCITY = 2, ION_SH_ONLY_VELOCITY = 4 };
-/* ion_sh_plan.flags: run the length gauge's rotation pass with its tile in
- * shared memory (the form used beyond l_bound 256) instead of in registers;
- * the two give the same results bit for bit. */
-enum { ION_SH_ROT_TILE = 8 };
 
 typedef struct ion_sh_plan {
     ion_sh_sim *sims;         /* device array [n_sims] */

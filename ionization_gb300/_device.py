@@ -624,13 +624,10 @@ class ShBatch:
     """Many spherical-harmonic simulations advanced together."""
 
     def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None, cn_rows: int = 0,
-                 rot_rows: int = SH_ROT_ROWS, rot_kernel: str = "registers"):
+                 rot_rows: int = SH_ROT_ROWS):
         self.precision = Precision(precision)
         self.sims: List[ShDeviceSim] = list(sims or [])
         self.cn_rows = int(cn_rows)
-        if rot_kernel not in ("registers", "tile"):
-            raise ValueError("rot_kernel is 'registers' or 'tile'")
-        self.rot_kernel = rot_kernel  # the length gauge's rotation pass: tile in registers or in shared memory
         self.rot_rows = int(rot_rows)
         if self.rot_rows != SH_ROT_ROWS:
             raise ValueError("row tiles of the rotation pass are fixed by the partial-sum layout")
@@ -688,8 +685,6 @@ class ShBatch:
         plan.max_n_l = max([s.n_l for s in sims] + [1])
         plan.max_n_r = max([s.n_r for s in sims] + [2])
         plan.flags = nat.ION_SH_REFINE if any(s.g_lo is not None for s in sims) else 0
-        if self.rot_kernel == "tile":
-            plan.flags |= nat.ION_SH_ROT_TILE
         n_vel = sum(1 for s in sims if s.gauge == nat.ION_GAUGE_VELOCITY)
         if n_vel:
             plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)

@@ -26,7 +26,6 @@ ION_LINE_FFT = 2
 ION_SH_REFINE = 1
 ION_SH_VELOCITY = 2
 ION_SH_ONLY_VELOCITY = 4
-ION_SH_ROT_TILE = 8
 ION_GAUGE_LENGTH = 0
 ION_ADI_STRIDED_FIRST = 0
 ION_ADI_CONTIG_FIRST = 1

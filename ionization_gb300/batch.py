@@ -41,7 +41,7 @@ class BatchedSphericalHarmonicSimulation:
     in complex64 with FP64 fields, coefficient tables and reductions)."""
 
     def __init__(self, specs, precision: Optional[str] = None, graph_steps: int = 64, use_graphs: bool = True,
-                 cn_rows: int = 0, tables=None, rot_kernel: str = "registers"):
+                 cn_rows: int = 0, tables=None):
         self.specs = list(specs)
         self.precision = Precision(precision or self.specs[0].precision)
         if tables is None:
@@ -49,7 +49,7 @@ class BatchedSphericalHarmonicSimulation:
         self.tables = tables
         dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
         self.sims = dsims
-        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows, rot_kernel=rot_kernel)
+        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows)
         self.graph_steps = int(graph_steps)
         self.use_graphs = use_graphs
         self._graphs = {}
@@ -134,33 +134,56 @@ class BatchedSphericalHarmonicSimulation:
         return dev.sh_psi_many(self.sims)
 
 
-def autotune(specs, precision="c64", graph_steps=(32,), steps=32, tables=None):
-    """Choose the launch shape of a batch by timing every candidate on it.
+def _time_steps(specs, precision, tables, rows, gs, steps):
+    """ms per step of ``steps`` steps through the API's own path (CUDA-graph
+    replay of ``gs`` steps), after a warm-up that captures the graph."""
+    b = BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
+    b.step(1 + gs)  # warm-up and capture
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = max(steps, gs) // gs * gs
+    e0.record()
+    b.step(n)
+    e1.record()
+    torch.cuda.synchronize()
+    del b
+    return e0.elapsed_time(e1) / n
 
-    Candidates are (rows per thread of the radial solve -> threads per
-    radial system, graph chunk length).  Each is timed with CUDA events on
-    the launching stream after a warm-up; returns (best, {candidate: ms per
-    step})."""
+
+def autotune(specs, precision="c64", graph_steps=(16, 32, 64), steps=32, tables=None):
+    """Choose the launch shape of a batch by timing candidates on it, in two
+    stages: rows per thread of the radial solve (which sets the threads per
+    radial system and so the CTA size of every bucket), then the CUDA-graph
+    chunk length.  Each candidate runs through the API's graph replay and is
+    timed with CUDA events on the launching stream after a warm-up.  Returns
+    (best, timings): best = dict(rows=, graph_steps=), timings = {candidate
+    label: ms per step}."""
     precision = Precision(precision)
     if tables is None:
         tables = [_host_tables(spec)[0] for spec in specs]
+    gs_mid = sorted(graph_steps)[len(graph_steps) // 2]
     timings = {}
-    for rows in dev.SH_ROWS_CHOICES[precision]:
-        for gs in graph_steps:
-            b = BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows,
-                                                   tables=tables)
-            b.step(1 + gs)  # warm-up and capture
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            n = max(steps, gs)
-            e0.record()
-            b.step(n)
-            e1.record()
-            torch.cuda.synchronize()
-            timings[(rows, gs)] = e0.elapsed_time(e1) / n
-            del b
-    best = min(timings, key=timings.get)
-    return best, timings
+
+    def run(rows, gs):
+        key = f"rows{rows}_graph{gs}"
+        if key not in timings:
+            timings[key] = _time_steps(specs, precision, tables, rows, gs, steps)
+        return timings[key]
+
+    rows = min(dev.SH_ROWS_CHOICES[precision], key=lambda r: run(r, gs_mid))
+    gs = min(graph_steps, key=lambda g: run(rows, g))
+    return dict(rows=rows, graph_steps=gs), timings
+
+
+def plan_shape(batch: "BatchedSphericalHarmonicSimulation") -> dict:
+    """The chosen plan's launch shape: the radial solve's buckets (CTA
+    threads, lines) and the rotation pass's tiles."""
+    p = batch.batch.plan
+    ends = [int(p.cn_bucket_end[b]) for b in range(p.n_cn_buckets)]
+    starts = [0] + ends[:-1]
+    return {"radial_buckets": [{"threads": int(p.cn_bucket_threads[b]), "lines": ends[b] - starts[b]}
+                               for b in range(p.n_cn_buckets)],
+            "rows_per_thread": int(p.cn_rows), "rotation_tiles": int(p.n_rot_items)}
 
 
 def _main(argv=None):

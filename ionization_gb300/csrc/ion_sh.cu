@@ -906,304 +906,6 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
 }
 
 // ---------------------------------------------------------------------------
-// Register rotation pass (length gauge): the same tiles of ROT_ROWS r rows x
-// all l as sh_rot_kernel, with the tile held in registers for the whole pass.
-// Thread (warp w, lane): rows of one parity per warp, jj = 2 (lane mod 16) +
-// (w mod 2), and the l segment s = 2 (w div 2) + lane div 16 of RSEG
-// consecutive l.  The F-order pairing of an operator depends on the row's
-// parity only through r n_l, so every warp applies one pattern: either all
-// its pairs lie inside the segments, or each segment's first and last element
-// pair with the neighbouring segments' last and first (exchanged through
-// shared memory; the partner's own element is updated by its owner with the
-// same arithmetic).  Every operator is followed by the residual's bf16
-// rounding of a store and reload, so the results are those of sh_rot_kernel
-// bit for bit.
-// ---------------------------------------------------------------------------
-template <typename R, int RSEG>
-struct RegSeg {
-    Cx<R> h[RSEG];
-    Cx<R> l[RSEG];  // complex64: the compensation word, as unpacked (unused for complex128)
-};
-
-template <typename R>
-__device__ __forceinline__ typename Tile<R>::Pair rs_make(Cx<R> h0, Cx<R> h1, Cx<R> l0, Cx<R> l1) {
-    if constexpr (Tile<R>::comp)
-        return typename Tile<R>::Pair{h0, h1, l0, l1};
-    else
-        return typename Tile<R>::Pair{h0, h1};
-}
-template <typename R>
-__device__ __forceinline__ Cx<R> rs_lo0(const typename Tile<R>::Pair& p) {
-    if constexpr (Tile<R>::comp) return p.l0;
-    else return Cx<R>{R(0), R(0)};
-}
-template <typename R>
-__device__ __forceinline__ Cx<R> rs_lo1(const typename Tile<R>::Pair& p) {
-    if constexpr (Tile<R>::comp) return p.l1;
-    else return Cx<R>{R(0), R(0)};
-}
-template <typename R, int RSEG>
-__device__ __forceinline__ void rs_quant(RegSeg<R, RSEG>& v) {
-    if constexpr (Tile<R>::comp) {
-#pragma unroll
-        for (int j = 0; j < RSEG; ++j) v.l[j] = lo_round(v.l[j]);
-    }
-}
-
-// the pair (a, b) of the segment turned by (cm1, s), when l + 1 < n_l
-template <typename R, int RSEG>
-__device__ __forceinline__ void rs_rot_in(RegSeg<R, RSEG>& v, int a, R cm1, R s) {
-    typename Tile<R>::Pair p = rs_make<R>(v.h[a], v.h[a + 1], v.l[a], v.l[a + 1]);
-    Tile<R>::rot(p, cm1, s);
-    v.h[a] = p.x0;
-    v.h[a + 1] = p.x1;
-    v.l[a] = rs_lo0<R>(p);
-    v.l[a + 1] = rs_lo1<R>(p);
-}
-
-// One rotation operator of parity ``parity`` on the thread's segment.
-// xch: [2][n_seg][ROT_ROWS] (hi, lo) of every segment's first (0) and last (1)
-// element; halo: whether any warp's pairs cross segments (uniform per CTA).
-template <typename R, int RSEG>
-__device__ __forceinline__ void rs_rotate(RegSeg<R, RSEG>& v, const R* cl, R rq, int nl, int l0, bool active,
-                                          int q, R tau, R ef, bool halo, Cx<R>* xh, Cx<R>* xl, int nseg, int s,
-                                          int jj) {
-    Cx<R> lh = {R(0), R(0)}, ll = lh, rh = lh, rl = lh;
-    if (halo) {
-        __syncthreads();  // the previous exchange is read
-        xh[s * ROT_ROWS + jj] = v.h[0];
-        xl[s * ROT_ROWS + jj] = v.l[0];
-        xh[(nseg + s) * ROT_ROWS + jj] = v.h[RSEG - 1];
-        xl[(nseg + s) * ROT_ROWS + jj] = v.l[RSEG - 1];
-        __syncthreads();
-        if (q == 1) {
-            if (s > 0) {
-                lh = xh[(nseg + s - 1) * ROT_ROWS + jj];
-                ll = xl[(nseg + s - 1) * ROT_ROWS + jj];
-            }
-            if (s + 1 < nseg) {
-                rh = xh[(s + 1) * ROT_ROWS + jj];
-                rl = xl[(s + 1) * ROT_ROWS + jj];
-            }
-        }
-    }
-    if (!active) return;
-    if (q == 0) {
-#pragma unroll
-        for (int j = 0; j < RSEG; j += 2) {
-            const int l = l0 + j;
-            if (l + 1 < nl) {
-                R cm1, sn;
-                rot_coeffs(tau * ((cl[j + 1] * rq) * ef), cm1, sn);
-                rs_rot_in<R, RSEG>(v, j, cm1, sn);
-            }
-        }
-    } else {
-        if (l0 >= 1 && l0 < nl) {  // (l0 - 1, l0): this thread's l0 is the pair's second element
-            R cm1, sn;
-            rot_coeffs(tau * ((cl[0] * rq) * ef), cm1, sn);
-            typename Tile<R>::Pair p = rs_make<R>(lh, v.h[0], ll, v.l[0]);
-            Tile<R>::rot(p, cm1, sn);
-            v.h[0] = p.x1;
-            v.l[0] = rs_lo1<R>(p);
-        }
-#pragma unroll
-        for (int j = 1; j + 1 < RSEG; j += 2) {
-            const int l = l0 + j;
-            if (l + 1 < nl) {
-                R cm1, sn;
-                rot_coeffs(tau * ((cl[j + 1] * rq) * ef), cm1, sn);
-                rs_rot_in<R, RSEG>(v, j, cm1, sn);
-            }
-        }
-        if (l0 + RSEG < nl) {  // (l0 + RSEG - 1, l0 + RSEG): its first element is this thread's
-            R cm1, sn;
-            rot_coeffs(tau * ((cl[RSEG] * rq) * ef), cm1, sn);
-            typename Tile<R>::Pair p = rs_make<R>(v.h[RSEG - 1], rh, v.l[RSEG - 1], rl);
-            Tile<R>::rot(p, cm1, sn);
-            v.h[RSEG - 1] = p.x0;
-            v.l[RSEG - 1] = rs_lo0<R>(p);
-        }
-    }
-    rs_quant<R, RSEG>(v);
-}
-
-template <typename R, int RSEG>
-__global__ void __launch_bounds__(512) sh_rotr_kernel(ion_sh_plan plan, int mode, int pf_dist) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int si = plan.rot_items[2 * blockIdx.x];
-    const int tile_idx = plan.rot_items[2 * blockIdx.x + 1];
-    const ion_sh_sim& S = plan.sims[si];
-    if (S.gauge != ION_GAUGE_LENGTH) return;  // sh_rot_vel_kernel
-    const int64_t t = S.t;
-    const int64_t tf = S.t_final;
-    bool post = false, do_mask = false, reduce = false, pre = false;
-    int64_t n_post = 0, n_pre = 0;
-    if (mode == ROT_PRE_ONLY) {
-        if (t >= tf) return;
-        pre = true;
-        n_pre = t + 1;
-    } else if (mode == ROT_STEP || mode == ROT_STEP_PRE) {
-        if (t >= tf) return;
-        post = true;
-        n_post = t + 1;
-        do_mask = S.mask != nullptr;
-        reduce = is_data_time(t + 1, tf, S.store_every);
-        if (mode == ROT_STEP_PRE && t + 1 < tf) {
-            pre = true;
-            n_pre = t + 2;
-        }
-    } else if (mode == ROT_REDUCE_ONLY) {
-        reduce = is_data_time(t, tf, S.store_every);
-        if (!reduce) return;
-    }
-    const int nr = S.n_r, nl = S.n_l;
-    const int j0 = tile_idx * ROT_ROWS;
-    const int rows = min(ROT_ROWS, nr - j0);
-    if (rows <= 0) return;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int jj = 2 * (lane & 15) + (w & 1);
-    const int s = 2 * (w >> 1) + (lane >> 4);
-    const int nseg = 2 * int(blockDim.x >> 6);
-    const int l0 = s * RSEG;
-    const bool active = jj < rows && l0 < nl;
-    const int j = j0 + jj;
-    // shared memory: the segment-boundary exchange, then the block-sum scratch
-    Cx<R>* xh = reinterpret_cast<Cx<R>*>(smem_raw);
-    Cx<R>* xl = xh + 2 * nseg * ROT_ROWS;
-    double* scratch = reinterpret_cast<double*>(xl + 2 * nseg * ROT_ROWS);
-
-    Cx<R>* g = static_cast<Cx<R>*>(S.g);
-    uint32_t* glo = Tile<R>::comp ? static_cast<uint32_t*>(S.g_lo) : nullptr;
-    RegSeg<R, RSEG> v;
-    const Cx<R> zero = {R(0), R(0)};
-#pragma unroll
-    for (int k = 0; k < RSEG; ++k) {
-        v.h[k] = zero;
-        v.l[k] = zero;
-        if (active && l0 + k < nl) {
-            const int64_t at = int64_t(l0 + k) * nr + j;
-            v.h[k] = ld(g + at);
-            if constexpr (Tile<R>::comp)
-                if (glo) v.l[k] = lo_unpack(glo[at]);
-        }
-    }
-    if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
-    const RotTab<R> tb = RotTab<R>::make(S);
-    R cl[RSEG + 1];  // c_l of the pairs starting at l0 - 1 .. l0 + RSEG - 1
-#pragma unroll
-    for (int k = 0; k <= RSEG; ++k) {
-        const int l = l0 - 1 + k;
-        cl[k] = (l >= 0 && l < nl) ? tb.cl[l] : R(0);
-    }
-    const R rq = active ? tb.rq[j] : R(0);
-    const R tp = post ? R(S.tau[n_post]) : R(0), ep = post ? R(S.efield[n_post]) : R(0);
-    const R tq = pre ? R(S.tau[n_pre]) : R(0), eq = pre ? R(S.efield[n_pre]) : R(0);
-    // the first pair of an operator of parity p starts at l = (j nl + p) mod 2,
-    // the same for every row of the warp (j0 is even); q = 1: the pairs start
-    // at odd l and cross the segments (RSEG is even)
-    const int qbase = int((int64_t(j) * nl) & 1);
-    const bool odd_nl = (nl & 1) != 0;
-    auto op = [&](int parity, R tau, R ef) {
-        const int q = (qbase + parity) & 1;
-        // halos when some warp's pairs cross segments: always for odd n_l, for
-        // the parity-1 operators otherwise
-        const bool halo = odd_nl || parity == 1;
-        rs_rotate<R, RSEG>(v, cl, rq, nl, l0, active, q, tau, ef, halo, xh, xl, nseg, s, jj);
-    };
-    if (post) {
-        op(1, tp, ep);  // odd
-        op(0, tp, ep);  // even
-    }
-    if (do_mask && active) {
-        const R m = tb.mask[j];
-#pragma unroll
-        for (int k = 0; k < RSEG; ++k) {
-            if constexpr (Tile<R>::comp)
-                Tile<R>::scaled(v.h[k], v.l[k], m);
-            else
-                v.h[k] = Tile<R>::scaled(v.h[k], m);
-        }
-        rs_quant<R, RSEG>(v);
-    }
-    if (reduce) {
-        // per-tile partial sums of |g|^2 and conj(s) g for every test state
-        const int nq = 1 + 2 * S.n_states;
-        double acc = 0.0;
-        if (active) {
-#pragma unroll
-            for (int k = 0; k < RSEG; ++k) {
-                if (l0 + k < nl) {
-                    const double re = double(v.h[k].re) + double(v.l[k].re);
-                    const double im = double(v.h[k].im) + double(v.l[k].im);
-                    acc += re * re + im * im;
-                }
-            }
-        }
-        const double tot = block_sum(acc, scratch);
-        if (threadIdx.x == 0) S.partials[int64_t(tile_idx) * nq] = tot;
-        for (int st = 0; st < S.n_states; ++st) {
-            const int ls = S.state_l[st];
-            double re = 0.0, im = 0.0;
-            if (active && ls >= l0 && ls < l0 + RSEG && ls < nl) {
-                Cx<double> x = {0.0, 0.0};
-#pragma unroll
-                for (int k = 0; k < RSEG; ++k)
-                    if (ls == l0 + k)
-                        x = Cx<double>{double(v.h[k].re) + double(v.l[k].re), double(v.h[k].im) + double(v.l[k].im)};
-                const double* sg = S.state_g + (int64_t(st) * S.n_r + j) * 2;
-                const double ar = sg[0], ai = -sg[1];  // conj(state)
-                re = ar * x.re - ai * x.im;
-                im = ar * x.im + ai * x.re;
-            }
-            const double tr = block_sum(re, scratch);
-            const double ti = block_sum(im, scratch);
-            if (threadIdx.x == 0) {
-                S.partials[int64_t(tile_idx) * nq + 1 + 2 * st] = tr;
-                S.partials[int64_t(tile_idx) * nq + 2 + 2 * st] = ti;
-            }
-        }
-    }
-    if (post && pre && Tile<R>::comp && active) {  // as if stored and reloaded between the two
-#pragma unroll
-        for (int k = 0; k < RSEG; ++k)
-            if constexpr (Tile<R>::comp) Tile<R>::renorm(v.h[k], v.l[k], glo != nullptr);
-        rs_quant<R, RSEG>(v);
-    }
-    if (pre) {
-        op(0, tq, eq);  // even
-        op(1, tq, eq);  // odd
-    }
-    if (mode != ROT_REDUCE_ONLY && active) {
-#pragma unroll
-        for (int k = 0; k < RSEG; ++k) {
-            if (l0 + k < nl) {
-                const int64_t at = int64_t(l0 + k) * nr + j;
-                if constexpr (Tile<R>::comp) {
-                    const Cx<float> h = v.h[k], l = v.l[k];
-                    const float sr = h.re + l.re, si2 = h.im + l.im;
-                    st(g + at, Cx<float>{sr, si2});
-                    if (glo) glo[at] = lo_pack(Cx<float>{l.re - (sr - h.re), l.im - (si2 - h.im)});
-                } else {
-                    st(g + at, v.h[k]);
-                }
-            }
-        }
-    }
-}
-
-// threads of the register rotation pass: 64 per pair of segments
-template <int RSEG>
-__host__ __device__ inline int rotr_threads(int max_nl) {
-    const int seg = (max_nl + RSEG - 1) / RSEG;
-    return 64 * ((seg + 1) / 2);
-}
-template <typename R>
-__host__ __device__ inline size_t rotr_smem(int threads) {
-    return size_t(2) * 2 * (threads / 32) * ROT_ROWS * sizeof(Cx<R>) + 32 * sizeof(double);
-}
-
-// ---------------------------------------------------------------------------
 // Velocity gauge (ion_sh_sim.gauge == ION_GAUGE_VELOCITY): the same tiles of
 // ROT_ROWS r rows x all l, loaded with VEL_HALO rows on each side.  h2 couples
 // r and r +- 1, and a tile applies at most 8 such operators per launch (4
@@ -1498,24 +1200,12 @@ template <typename R>
 static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     if (p->n_rot_items == 0) return ION_OK;
     if (!(p->flags & ION_SH_ONLY_VELOCITY)) {
-        const bool tile = (p->flags & ION_SH_ROT_TILE) || rotr_threads<16>(p->max_n_l) > 512;
-        if (tile) {  // the tile through shared memory (any l_bound)
-            const size_t smem = rot_smem<R>(p);
-            if (int e = ensure_smem_limit((const void*)sh_rot_kernel<R>, 200 * 1024, "sh_rot_kernel")) return e;
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
-            sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
-            if (int e = check_launch("sh_rot_kernel")) return e;
-        } else {  // the tile in registers: 8 l a thread up to l_bound 128, 16 up to 256
-            const bool wide = rotr_threads<8>(p->max_n_l) > 512;
-            const int threads = wide ? rotr_threads<16>(p->max_n_l) : rotr_threads<8>(p->max_n_l);
-            const size_t smem = rotr_smem<R>(threads);
-            auto k = wide ? sh_rotr_kernel<R, 16> : sh_rotr_kernel<R, 8>;
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
-            k<<<p->n_rot_items, threads, smem, s>>>(*p, mode, per_sm * num_sms());
-            if (int e = check_launch("sh_rotr_kernel")) return e;
-        }
+        const size_t smem = rot_smem<R>(p);
+        if (int e = ensure_smem_limit((const void*)sh_rot_kernel<R>, 200 * 1024, "sh_rot_kernel")) return e;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh_rot_kernel<R>, ROT_ROWS * ROT_LANES, smem);
+        sh_rot_kernel<R><<<p->n_rot_items, ROT_ROWS * ROT_LANES, smem, s>>>(*p, mode, per_sm * num_sms());
+        if (int e = check_launch("sh_rot_kernel")) return e;
     }
     if (p->flags & (ION_SH_VELOCITY | ION_SH_ONLY_VELOCITY)) {
         const size_t smem = rot_smem_bytes<R>(p->max_n_l, VEL_ROWS);

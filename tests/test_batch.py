@@ -56,9 +56,12 @@ def test_autotune_times_every_candidate(cuda):
     from ionization_gb300 import _device as dev
     from ionization_gb300 import batch as bm
 
-    best, timings = bm.autotune(_specs("c64x"), precision="c64x", graph_steps=(4,), steps=4)
-    assert set(timings) == {(r, 4) for r in dev.SH_ROWS_CHOICES[dev.Precision.C64X]}
-    assert best in timings and all(v > 0 for v in timings.values())
+    best, timings = bm.autotune(_specs("c64x"), precision="c64x", graph_steps=(4, 8), steps=8)
+    rows = dev.SH_ROWS_CHOICES[dev.Precision.C64X]
+    assert {f"rows{r}_graph8" for r in rows} <= set(timings)
+    assert best["rows"] in rows and best["graph_steps"] in (4, 8)
+    assert f"rows{best['rows']}_graph{best['graph_steps']}" in timings
+    assert all(v > 0 for v in timings.values())
 
 
 @pytest.mark.gpu
@@ -120,36 +123,3 @@ def test_strongly_driven_c64x_populations_match_c128(cuda, rows):
     di = np.abs(pb["c64x"] - pb["c128"])
     print(f"rows {rows}: max |dP_ground| {dg.max():.2e}, max |dP_ion| {di.max():.2e}")
     assert dg.max() < 3e-7 and di.max() < 3e-7
-
-
-def _wide_specs(precision):
-    # l_bound beyond 128 (16 l a thread in the register rotation pass), odd and even
-    return [wl.sh_spec(f"wide_{k}", nr, lb, 0.08, 0.1, 2, 0.4 * k, 30, precision=precision, store_data_every=7,
-                       mask_width=0.4 * wl.DR * nr)
-            for k, (nr, lb) in enumerate([(90, 151), (70, 140)])]
-
-
-@pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["c128", "c64x", "c64"])
-@pytest.mark.parametrize("shapes", ["uneven", "wide"])
-def test_register_rotation_pass_equals_tile_pass(cuda, precision, shapes):
-    """The rotation pass with each thread's pairs in registers gives, bit for
-    bit, what the pass through a shared-memory tile gives: psi, norms and
-    inner products, on odd and even l_bound, partial row tiles, data times
-    and l_bound beyond 128."""
-    from ionization_gb300 import batch as bm
-
-    make = _specs if shapes == "uneven" else _wide_specs
-    out = {}
-    for kern in ("registers", "tile"):
-        b = bm.BatchedSphericalHarmonicSimulation(make(precision), graph_steps=8, rot_kernel=kern)
-        b.run()
-        out[kern] = (b.psi_all(), b.results())
-        del b
-    for pr, pt in zip(out["registers"][0], out["tile"][0]):
-        np.testing.assert_array_equal(pr, pt)
-    for rr, rt in zip(out["registers"][1], out["tile"][1]):
-        # the data are summed in another order
-        np.testing.assert_allclose(rr["norm"], rt["norm"], rtol=1e-14, atol=0)
-        for a, c in zip(rr["inner_products"].values(), rt["inner_products"].values()):
-            np.testing.assert_allclose(a, c, rtol=1e-13, atol=1e-16)
