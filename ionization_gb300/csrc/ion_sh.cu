@@ -580,23 +580,37 @@ template <> struct Tile<float> {
         p.l0 = lo_round(p.l0);
         p.l1 = lo_round(p.l1);
     }
+    // x -> x + (cm1 x - i s y) for each element x of the pair and its partner
+    // y, the sum exact through Fast2Sum with its error into lo.  Both
+    // components go through one packed FP32 instruction each (FFMA2 / FADD2 /
+    // FMUL2, per-component IEEE rounding, so the result is that of the scalar
+    // form: x.re + fma(cm1, x.re, s y.im), x.im + fma(cm1, x.im, -(s y.re))).
+    __device__ __forceinline__ static void rot1(Cx<float>& x, Cx<float>& l, Cx<float> y, Cx<float> ly, float2 c2,
+                                                float2 s2) {
+        const float2 X = make_float2(x.re, x.im), L = make_float2(l.re, l.im);
+        const float2 u = __ffma2_rn(c2, X, __fmul2_rn(s2, make_float2(y.im, y.re)));
+        const float2 h = __fadd2_rn(X, u);
+        const float2 d = __fadd2_rn(h, make_float2(-X.x, -X.y));
+        const float2 e = __fadd2_rn(u, make_float2(-d.x, -d.y));  // u - (h - x)
+        const float2 v = __ffma2_rn(c2, L, __fmul2_rn(s2, make_float2(ly.im, ly.re)));
+        const float2 ln = __fadd2_rn(__fadd2_rn(L, v), e);
+        x = Cx<float>{h.x, h.y};
+        l = Cx<float>{ln.x, ln.y};
+    }
     __device__ __forceinline__ static void rot(Pair& p, float cm1, float s) {
         const Cx<float> x0 = p.x0, x1 = p.x1, l0 = p.l0, l1 = p.l1;
-        float e0r, e0i, e1r, e1i;
-        const float h0r = two_sum(x0.re, fmaf(cm1, x0.re, s * x1.im), e0r);
-        const float h0i = two_sum(x0.im, fmaf(cm1, x0.im, -(s * x1.re)), e0i);
-        const float h1r = two_sum(x1.re, fmaf(cm1, x1.re, s * x0.im), e1r);
-        const float h1i = two_sum(x1.im, fmaf(cm1, x1.im, -(s * x0.re)), e1i);
-        p.x0 = Cx<float>{h0r, h0i};
-        p.x1 = Cx<float>{h1r, h1i};
-        p.l0 = Cx<float>{(l0.re + fmaf(cm1, l0.re, s * l1.im)) + e0r, (l0.im + fmaf(cm1, l0.im, -(s * l1.re))) + e0i};
-        p.l1 = Cx<float>{(l1.re + fmaf(cm1, l1.re, s * l0.im)) + e1r, (l1.im + fmaf(cm1, l1.im, -(s * l0.re))) + e1i};
+        const float2 c2 = make_float2(cm1, cm1), s2 = make_float2(s, -s);
+        rot1(p.x0, p.l0, x1, l1, c2, s2);
+        rot1(p.x1, p.l1, x0, l0, c2, s2);
     }
-    // the product's rounding error goes to lo
+    // the product's rounding error goes to lo (packed: the scalar form
+    // pr = h.re m, lo.re = fma(lo.re, m, fma(h.re, m, -pr)) per component)
     __device__ __forceinline__ static void scaled(Cx<float>& h, Cx<float>& l, float m) {
-        const float pr = h.re * m, pi = h.im * m;
-        l = Cx<float>{fmaf(l.re, m, fmaf(h.re, m, -pr)), fmaf(l.im, m, fmaf(h.im, m, -pi))};
-        h = Cx<float>{pr, pi};
+        const float2 M = make_float2(m, m), H = make_float2(h.re, h.im);
+        const float2 P = __fmul2_rn(H, M);
+        const float2 Ln = __ffma2_rn(make_float2(l.re, l.im), M, __ffma2_rn(H, M, make_float2(-P.x, -P.y)));
+        l = Cx<float>{Ln.x, Ln.y};
+        h = Cx<float>{P.x, P.y};
     }
     __device__ __forceinline__ static void scale(Pair& p, float m) {
         scaled(p.x0, p.l0, m);
@@ -629,9 +643,12 @@ template <> struct Tile<float> {
     // rounded, and with a stored residual (keep) its rounding error as lo
     // (Fast2Sum), else lo = 0
     __device__ __forceinline__ static void renorm(Cx<float>& h, Cx<float>& l, bool keep) {
-        const float sr = h.re + l.re, si = h.im + l.im;
-        l = keep ? Cx<float>{l.re - (sr - h.re), l.im - (si - h.im)} : Cx<float>{0.f, 0.f};
-        h = Cx<float>{sr, si};
+        const float2 H = make_float2(h.re, h.im), L = make_float2(l.re, l.im);
+        const float2 S = __fadd2_rn(H, L);
+        const float2 D = __fadd2_rn(S, make_float2(-H.x, -H.y));
+        const float2 E = __fadd2_rn(L, make_float2(-D.x, -D.y));  // l - (s - h)
+        l = keep ? Cx<float>{E.x, E.y} : Cx<float>{0.f, 0.f};
+        h = Cx<float>{S.x, S.y};
     }
     __device__ __forceinline__ static void renorm(Pair& p, bool keep) {
         renorm(p.x0, p.l0, keep);
