@@ -10,7 +10,8 @@ refined radial solves whose residual uses the FP64 Hamiltonian, which keeps
 the final populations of every simulation within 1e-6 of complex128 (see
 ``accuracy``); plain complex64 is timed beside it (``c64_plain``).  A step
 advances all 512 simulations by one time step: three kernel launches (radial
-solve, rotation/mask/reduction pass, time-index advance).
+solve buckets, one per range of line lengths, the rotation/mask/reduction
+pass and the time-index advance).
 
 Prints one JSON line:
   value      mesh-point-steps/s over the timed steps, psi resident in HBM
@@ -228,7 +229,7 @@ class Clocks:
 HEADLINE = "c64x"  # complex64 arithmetic, residual-compensated state: meets the 1e-6 bound
 
 
-def time_batch(specs, tables, precision, K, warmup, rows, gs, local_rank, barrier):
+def time_batch(specs, tables, precision, K, warmup, rows, gs, local_rank, barrier, bucket_rows=()):
     """K steps of the whole batch through the API's own path (CUDA-graph
     replays of ``gs`` steps, the remainder launched directly), timed with CUDA
     events on the launching stream and the clocks sampled meanwhile; then,
@@ -239,7 +240,7 @@ def time_batch(specs, tables, precision, K, warmup, rows, gs, local_rank, barrie
     from ionization_gb300 import batch as bm
 
     b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows,
-                                              tables=tables)
+                                              tables=tables, bucket_rows=bucket_rows)
     b.step(gs + max(warmup, 3))  # captures the graph
     torch.cuda.synchronize()
     plan = b.batch.plan
@@ -295,7 +296,7 @@ def time_phases(plan, precision, K, stream):
     return dict(elapsed_ms=e0.elapsed_time(e1),
                 cn_ms=float(np.mean([a.elapsed_time(c) for a, c in e_cn])),
                 rot_ms=float(np.mean([e_cn[k][1].elapsed_time(e_rot[k]) for k in range(K)])),
-                launches=1 + 3 * K)
+                launches=1 + (max(int(plan.n_cn_buckets), 1) + 2) * K)
 
 
 def run_ours(args, rank, world, local_rank):
@@ -323,14 +324,14 @@ def run_ours(args, rank, world, local_rank):
     points = int(sum(t.n_r * t.n_l for t in tables))
 
     if args.rows:  # a fixed launch shape (e.g. for a profiler run, whose timings would mislead the autotuner)
-        best, tune = dict(rows=args.rows, graph_steps=32), {}
+        best, tune = dict(rows=args.rows, bucket_rows=(), graph_steps=32), {}
     else:
         best, tune = bm.autotune(specs, HEADLINE, graph_steps=(16, 32, 64), steps=32, tables=tables)
-    best_rows, best_gs = best["rows"], best["graph_steps"]
+    best_rows, best_gs, best_br = best["rows"], best["graph_steps"], best["bucket_rows"]
 
     # ---- timed region: K steps of the headline configuration ----
     K = args.steps
-    main = time_batch(specs, tables, HEADLINE, K, args.warmup, best_rows, best_gs, local_rank, barrier)
+    main = time_batch(specs, tables, HEADLINE, K, args.warmup, best_rows, best_gs, local_rank, barrier, best_br)
     elapsed_ms = replicas.max_over_ranks(main["elapsed_ms"])
     cn_ms, rot_ms, clk_summary, gpu_launches = main["cn_ms"], main["rot_ms"], main["clocks"], main["launches"]
     # plain complex64 (no stored residual): faster, above the 1e-6 bound
@@ -384,7 +385,7 @@ def run_ours(args, rank, world, local_rank):
     }
 
     # ---- e2e through the public API from host buffers ----
-    e2e = run_e2e(args, specs, tables, best_rows, best_gs, points, HEADLINE)
+    e2e = run_e2e(args, specs, tables, best_rows, best_gs, points, HEADLINE, best_br)
 
     # ---- plain complex128 drop-in path, single simulation ----
     plain = run_plain_c128(args)
@@ -434,7 +435,8 @@ def run_ours(args, rank, world, local_rank):
             "state_bytes": points * state_bytes,
             "l2": f"inputs larger than L2 (state {points * state_bytes / 1e6:.0f} MB)",
             "parallelism": f"replicas x{world}",
-            "autotune": {"chosen": {"cn_rows_per_thread": best_rows, "graph_steps": best_gs},
+            "autotune": {"chosen": {"cn_rows_per_thread": best_rows, "bucket_rows": list(best_br),
+                                    "graph_steps": best_gs},
                          "plan": main["shape"],
                          "ms_per_step": {k: round(v, 4) for k, v in tune.items()}},
             "timing": "CUDA-graph replay of the API (graph_steps per replay, remainder launched directly); "
@@ -459,7 +461,7 @@ def run_ours(args, rank, world, local_rank):
     return out
 
 
-def run_e2e(args, specs, tables, rows, gs, points, precision):
+def run_e2e(args, specs, tables, rows, gs, points, precision, bucket_rows=()):
     """Public API from host buffers: build the batch (H2D of psi, tables and
     field tables), K steps, then read back every simulation's data and psi."""
     import torch
@@ -469,7 +471,8 @@ def run_e2e(args, specs, tables, rows, gs, points, precision):
     K = args.steps
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
+    b = bm.BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables,
+                                              bucket_rows=bucket_rows)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     b.step(K)

@@ -245,13 +245,16 @@ typedef struct ion_sh_plan {
     int32_t n_rot_items;
     int32_t rot_rows;         /* rows (r points) per tile, <= 64 */
     int32_t cn_rows;          /* rows per thread of the radial solve: 0 = default,
-                                 complex128 4 or 8, complex64 8 or 16 */
+                                 complex128 4 or 8, complex64 4, 8 or 16 */
     int32_t n_cn_buckets;     /* 0: one launch of cn_threads for all items; else the
                                  items are sorted so that bucket b is the range
                                  [cn_bucket_end[b-1], cn_bucket_end[b]) launched with
                                  cn_bucket_threads[b] threads per CTA */
     int32_t cn_bucket_end[8];
     int32_t cn_bucket_threads[8];
+    int32_t cn_bucket_rows[8]; /* rows per thread of bucket b's radial solve (its own
+                                  CTA shape: cn_bucket_threads[b] * rows >= the bucket's
+                                  n_r), or 0 for cn_rows */
 } ion_sh_plan;
 
 /* Advance every simulation of the plan by n_steps (fewer for simulations that

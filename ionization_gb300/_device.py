@@ -171,6 +171,18 @@ def sh_line_threads(n_r: int, precision, rows: int = 0) -> int:
     return (n_r + maxm - 1) // maxm  # the line is padded to whole chunks
 
 
+def sh_bucket_sizes(n_rs, precision, rows: int) -> np.ndarray:
+    """The radial-solve CTA size of each simulation's lines: its threads at
+    ``rows`` rows per thread, rounded up to a granularity (32, doubled while
+    there would be more than 8 distinct sizes).  Lines of equal size form one
+    bucket, one launch."""
+    need = [_round32(sh_line_threads(n, precision, rows)) for n in n_rs]
+    gran = 32
+    while len({(n + gran - 1) // gran * gran for n in need}) > 8:
+        gran *= 2
+    return np.array([(n + gran - 1) // gran * gran for n in need], dtype=np.int64)
+
+
 class _Fill:
     """A host array written straight into its upload buffer (``fill(dest)``,
     dest flat, of ``dtype``) instead of being formed and then copied."""
@@ -624,10 +636,14 @@ class ShBatch:
     """Many spherical-harmonic simulations advanced together."""
 
     def __init__(self, precision, sims: Optional[List[ShDeviceSim]] = None, cn_rows: int = 0,
-                 rot_rows: int = SH_ROT_ROWS):
+                 rot_rows: int = SH_ROT_ROWS, bucket_rows=None):
         self.precision = Precision(precision)
         self.sims: List[ShDeviceSim] = list(sims or [])
         self.cn_rows = int(cn_rows)
+        # rows per thread of each radial bucket (largest lines first; 0 or
+        # missing: cn_rows); a bucket's CTA is sized for its longest line at
+        # its own rows
+        self.bucket_rows = tuple(int(r) for r in (bucket_rows or ()))
         self.rot_rows = int(rot_rows)
         if self.rot_rows != SH_ROT_ROWS:
             raise ValueError("row tiles of the rotation pass are fixed by the partial-sum layout")
@@ -653,11 +669,7 @@ class ShBatch:
         # each bucket is one launch whose blocks have exactly the threads its
         # lines need
         rows = self.cn_rows or sh_default_rows(self.precision, max([s.n_r for s in sims] + [2]))
-        need = [_round32(sh_line_threads(s.n_r, self.precision, rows)) for s in sims]
-        gran = 32
-        while len({(n + gran - 1) // gran * gran for n in need}) > 8:
-            gran *= 2
-        bsize = np.array([(n + gran - 1) // gran * gran for n in need], dtype=np.int64)
+        bsize = sh_bucket_sizes([s.n_r for s in sims], self.precision, rows)
         n_r = np.array([s.n_r for s in sims], dtype=np.int64)
         n_l = np.array([s.n_l for s in sims], dtype=np.int64)
         n_t = np.array([s.n_tiles for s in sims], dtype=np.int64)
@@ -701,9 +713,17 @@ class ShBatch:
         ends = [int(k) for k in starts[1:]] + ([int(cs.size)] if cs.size else [])
         plan.cn_threads = max(threads + [32])
         plan.n_cn_buckets = len(threads)
+        nr_sorted = n_r[cs]
         for b, (e, th) in enumerate(zip(ends, threads)):
             plan.cn_bucket_end[b] = e
             plan.cn_bucket_threads[b] = th
+            br = self.bucket_rows[b] if b < len(self.bucket_rows) else 0
+            if br and br != rows:
+                th_b = _round32(sh_line_threads(int(nr_sorted[starts[b]]), self.precision, br))
+                if br not in SH_ROWS_CHOICES[self.precision] or th_b > sh_max_line_threads(self.precision, br):
+                    raise ValueError(f"bucket {b}: {br} rows per thread cannot hold its lines")
+                plan.cn_bucket_threads[b] = th_b
+                plan.cn_bucket_rows[b] = br
         self._plan = plan
         self._keep = (d_descs, d_cn, d_rot)
 

@@ -104,6 +104,7 @@ class ShPlan(ctypes.Structure):
         ("n_cn_buckets", c_i32),
         ("cn_bucket_end", c_i32 * 8),
         ("cn_bucket_threads", c_i32 * 8),
+        ("cn_bucket_rows", c_i32 * 8),
     ]
 
 

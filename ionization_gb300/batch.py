@@ -41,7 +41,7 @@ class BatchedSphericalHarmonicSimulation:
     in complex64 with FP64 fields, coefficient tables and reductions)."""
 
     def __init__(self, specs, precision: Optional[str] = None, graph_steps: int = 64, use_graphs: bool = True,
-                 cn_rows: int = 0, tables=None):
+                 cn_rows: int = 0, tables=None, bucket_rows=None):
         self.specs = list(specs)
         self.precision = Precision(precision or self.specs[0].precision)
         if tables is None:
@@ -49,7 +49,7 @@ class BatchedSphericalHarmonicSimulation:
         self.tables = tables
         dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
         self.sims = dsims
-        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows)
+        self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows, bucket_rows=bucket_rows)
         self.graph_steps = int(graph_steps)
         self.use_graphs = use_graphs
         self._graphs = {}
@@ -134,10 +134,11 @@ class BatchedSphericalHarmonicSimulation:
         return dev.sh_psi_many(self.sims)
 
 
-def _time_steps(specs, precision, tables, rows, gs, steps):
+def _time_steps(specs, precision, tables, rows, gs, steps, bucket_rows=()):
     """ms per step of ``steps`` steps through the API's own path (CUDA-graph
     replay of ``gs`` steps), after a warm-up that captures the graph."""
-    b = BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables)
+    b = BatchedSphericalHarmonicSimulation(specs, precision=precision, graph_steps=gs, cn_rows=rows, tables=tables,
+                                           bucket_rows=bucket_rows)
     b.step(1 + gs)  # warm-up and capture
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -150,29 +151,58 @@ def _time_steps(specs, precision, tables, rows, gs, steps):
     return e0.elapsed_time(e1) / n
 
 
-def autotune(specs, precision="c64", graph_steps=(16, 32, 64), steps=32, tables=None):
-    """Choose the launch shape of a batch by timing candidates on it, in two
-    stages: rows per thread of the radial solve (which sets the threads per
-    radial system and so the CTA size of every bucket), then the CUDA-graph
-    chunk length.  Each candidate runs through the API's graph replay and is
-    timed with CUDA events on the launching stream after a warm-up.  Returns
-    (best, timings): best = dict(rows=, graph_steps=), timings = {candidate
-    label: ms per step}."""
+def _bucket_lines(precision, tables, rows):
+    """The longest n_r of each radial bucket of the plan at ``rows`` (largest
+    first): the buckets ShBatch forms, without building the batch."""
+    bsize = dev.sh_bucket_sizes([t.n_r for t in tables], precision, rows)
+    return [max(t.n_r for t, b in zip(tables, bsize) if b == th) for th in sorted(set(bsize.tolist()), reverse=True)]
+
+
+def autotune(specs, precision="c64", graph_steps=(16, 32, 64), steps=32, tables=None, per_bucket=True):
+    """Choose the launch shape of a batch by timing candidates on it, in three
+    stages: rows per thread of the radial solve for every bucket (which sets
+    the threads per radial system and so the CTA size of every bucket); then,
+    bucket by bucket (largest lines first), each other row count that holds
+    the bucket's lines, kept when the whole step gets faster by more than 1 %;
+    then the CUDA-graph chunk length.  Each candidate runs through the API's
+    graph replay and is timed with CUDA events on the launching stream after
+    a warm-up.  Returns (best, timings): best = dict(rows=, bucket_rows=,
+    graph_steps=), timings = {candidate label: ms per step}."""
     precision = Precision(precision)
     if tables is None:
         tables = [_host_tables(spec)[0] for spec in specs]
     gs_mid = sorted(graph_steps)[len(graph_steps) // 2]
     timings = {}
 
-    def run(rows, gs):
-        key = f"rows{rows}_graph{gs}"
+    def label(rows, gs, br):
+        extra = "".join(f"_b{b}r{r}" for b, r in enumerate(br) if r)
+        return f"rows{rows}_graph{gs}{extra}"
+
+    def run(rows, gs, br=()):
+        key = label(rows, gs, br)
         if key not in timings:
-            timings[key] = _time_steps(specs, precision, tables, rows, gs, steps)
+            timings[key] = _time_steps(specs, precision, tables, rows, gs, steps, br)
         return timings[key]
 
-    rows = min(dev.SH_ROWS_CHOICES[precision], key=lambda r: run(r, gs_mid))
-    gs = min(graph_steps, key=lambda g: run(rows, g))
-    return dict(rows=rows, graph_steps=gs), timings
+    choices = dev.SH_ROWS_CHOICES[precision]
+    rows = min(choices, key=lambda r: run(r, gs_mid))
+    chosen = []
+    if per_bucket:
+        longest = _bucket_lines(precision, tables, rows)
+        chosen = [0] * len(longest)
+        best_t = run(rows, gs_mid)
+        for b, n_r in enumerate(longest):
+            for r in choices:
+                if r == rows or -(-n_r // r) > dev.sh_max_line_threads(precision, r):
+                    continue
+                cand = list(chosen)
+                cand[b] = r
+                t = run(rows, gs_mid, tuple(cand))
+                if t < 0.99 * best_t:
+                    best_t, chosen = t, cand
+    br = tuple(chosen)
+    gs = min(graph_steps, key=lambda g: run(rows, g, br))
+    return dict(rows=rows, bucket_rows=br, graph_steps=gs), timings
 
 
 def plan_shape(batch: "BatchedSphericalHarmonicSimulation") -> dict:
@@ -181,7 +211,8 @@ def plan_shape(batch: "BatchedSphericalHarmonicSimulation") -> dict:
     p = batch.batch.plan
     ends = [int(p.cn_bucket_end[b]) for b in range(p.n_cn_buckets)]
     starts = [0] + ends[:-1]
-    return {"radial_buckets": [{"threads": int(p.cn_bucket_threads[b]), "lines": ends[b] - starts[b]}
+    return {"radial_buckets": [{"threads": int(p.cn_bucket_threads[b]), "lines": ends[b] - starts[b],
+                                "rows_per_thread": int(p.cn_bucket_rows[b] or p.cn_rows)}
                                for b in range(p.n_cn_buckets)],
             "rows_per_thread": int(p.cn_rows), "rotation_tiles": int(p.n_rot_items)}
 

@@ -6,9 +6,11 @@
 // 815-1080), applied by QuantumMesh.evolve (ionization/mesh/meshes.py:251-257)
 // once per step of MeshSimulation.run (ionization/mesh/sims.py:289-333).
 //
-// Per step three kernels run on the whole batch:
-//   sh_cn_pipelined  the radial solves: persistent CTAs, each walking the
-//                  (simulation, l) lines of one bucket of equal CTA size with
+// Per step three kinds of kernel run on the whole batch:
+//   sh_cn_pipelined  the radial solves, one launch per bucket of lines of
+//                  similar length (each with its own CTA size and rows per
+//                  thread): persistent CTAs, each walking the
+//                  (simulation, l) lines of its bucket with
 //                  the next line's psi streaming into shared memory while the
 //                  current one is solved; y = (1 - i tau H0) psi is formed on
 //                  the fly and (1 + i tau H0) x = y is solved by the block
@@ -311,6 +313,7 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
     if (S.t >= S.t_final) return;
     const int nr = S.n_r;
     const int T = (nr + M - 1) / M;
+    if (T > int(blockDim.x)) return;  // a line longer than the CTA holds: skipped (see below)
     const int npad = T * M;
     const Cx<R>* g = static_cast<const Cx<R>*>(S.g) + int64_t(l) * nr;
     const uint32_t* glo = (lodst && S.g_lo) ? static_cast<const uint32_t*>(S.g_lo) + int64_t(l) * nr : nullptr;
@@ -395,7 +398,9 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
         const int l = plan.cn_items[2 * item + 1];
         const ion_sh_sim& S = plan.sims[si];
         const int64_t t = S.t;
-        if (t < S.t_final) {  // the same for every thread of the CTA
+        // a line the CTA cannot hold (a plan whose bucket does not fit its
+        // lines) is left as it is rather than written out of bounds
+        if (t < S.t_final && (S.n_r + M - 1) / M <= int(blockDim.x)) {  // the same for every thread of the CTA
             const int nr = S.n_r;
             const int T = (nr + M - 1) / M;
             const R tau = R(S.tau[t + 1]);
@@ -794,6 +799,43 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, in
     }
 }
 
+// Neumaier-compensated sum of the per-tile partials into the data slot (at
+// data times), then (ADV_STEP) the time index advance; one CTA per simulation
+__global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
+    ion_sh_sim& S = plan.sims[blockIdx.x];
+    const int64_t t = S.t, tf = S.t_final;
+    int64_t tr;
+    if (mode == ADV_STEP) {
+        if (t >= tf) return;
+        tr = t + 1;
+    } else {
+        tr = t;
+    }
+    if (is_data_time(tr, tf, S.store_every)) {
+        const int nq = 1 + 2 * S.n_states;
+        const int64_t slot = data_slot(tr, tf, S.store_every);
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            double sum = 0.0, comp = 0.0;
+            for (int k = 0; k < S.n_tiles; ++k) {
+                const double v = S.partials[int64_t(k) * nq + q];
+                const double tsum = sum + v;
+                if (fabs(sum) >= fabs(v))
+                    comp += (sum - tsum) + v;
+                else
+                    comp += (v - tsum) + sum;
+                sum = tsum;
+            }
+            sum = (sum + comp) * S.weight;
+            if (q == 0)
+                S.out_norm[slot] = sum;
+            else
+                S.out_ip[(slot * S.n_states) * 2 + (q - 1)] = sum;
+        }
+    }
+    __syncthreads();
+    if (mode == ADV_STEP && threadIdx.x == 0) S.t = t + 1;
+}
+
 // the tile (complex64: hi and the packed lo, 12 bytes an element) and the
 // block-sum scratch
 template <typename R>
@@ -1108,41 +1150,6 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
     }
 }
 
-// Neumaier-compensated sum of the per-tile partials, then advance t
-__global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
-    ion_sh_sim& S = plan.sims[blockIdx.x];
-    const int64_t t = S.t, tf = S.t_final;
-    int64_t tr;
-    if (mode == ADV_STEP) {
-        if (t >= tf) return;
-        tr = t + 1;
-    } else {
-        tr = t;
-    }
-    if (is_data_time(tr, tf, S.store_every)) {
-        const int nq = 1 + 2 * S.n_states;
-        const int64_t slot = data_slot(tr, tf, S.store_every);
-        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-            double sum = 0.0, comp = 0.0;
-            for (int k = 0; k < S.n_tiles; ++k) {
-                const double v = S.partials[int64_t(k) * nq + q];
-                const double tsum = sum + v;
-                if (fabs(sum) >= fabs(v))
-                    comp += (sum - tsum) + v;
-                else
-                    comp += (v - tsum) + sum;
-                sum = tsum;
-            }
-            sum = (sum + comp) * S.weight;
-            if (q == 0)
-                S.out_norm[slot] = sum;
-            else
-                S.out_ip[(slot * S.n_states) * 2 + (q - 1)] = sum;
-        }
-    }
-    __syncthreads();
-    if (mode == ADV_STEP && threadIdx.x == 0) S.t = t + 1;
-}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -1167,6 +1174,11 @@ template <typename R>
 static int sh_rows(const ion_sh_plan* p) {
     return p->cn_rows == 0 ? ShCfg<R>::MAXM : p->cn_rows;
 }
+// rows per thread of bucket b (b < 0: the plan's)
+template <typename R>
+static int sh_bucket_rows(const ion_sh_plan* p, int b) {
+    return (b >= 0 && p->cn_bucket_rows[b] != 0) ? p->cn_bucket_rows[b] : sh_rows<R>(p);
+}
 
 template <typename R>
 static int sh_validate(const ion_sh_plan* p) {
@@ -1183,8 +1195,9 @@ static int sh_validate(const ion_sh_plan* p) {
     }
     for (int b = 0, prev = 0; b < p->n_cn_buckets; ++b) {
         const int th = p->cn_bucket_threads[b];
+        const int br = p->cn_bucket_rows[b];
         if (p->cn_bucket_end[b] < prev || p->cn_bucket_end[b] > p->n_cn_items || th <= 0 ||
-            th > sh_max_threads<R>(sh_rows<R>(p)) || (th & 31) || th > p->cn_threads) {
+            (br != 0 && !ShRows<R>::ok(br)) || th > sh_max_threads<R>(sh_bucket_rows<R>(p, b)) || (th & 31)) {
             set_error("ion_sh: invalid bucket %d", b);
             return ION_ERR_INVALID_ARGUMENT;
         }
@@ -1233,58 +1246,60 @@ static int sh_launch_rot(const ion_sh_plan* p, int mode, cudaStream_t s) {
     return ION_OK;
 }
 
-template <typename R, int MAXM>
-static int sh_launch_cn_pipelined(const ion_sh_plan* p, cudaStream_t s) {
-    if (int e = ensure_smem_limit((const void*)sh_cn_pipelined<R, MAXM, false>, 200 * 1024, "sh_cn_pipelined"))
-        return e;
-    if (int e = ensure_smem_limit((const void*)sh_cn_pipelined<R, MAXM, true>, 200 * 1024, "sh_cn_pipelined"))
-        return e;
+// one bucket of the radial solve: items [begin, end) at M rows per thread
+template <typename R, int M>
+static int sh_launch_cn_bucket(const ion_sh_plan* p, int begin, int end, int threads, cudaStream_t s) {
+    const int refine = (p->flags & ION_SH_REFINE) && sizeof(R) == 4 ? 1 : 0;
+    auto kern = refine ? sh_cn_pipelined<R, M, true> : sh_cn_pipelined<R, M, false>;
+    if (int e = ensure_smem_limit((const void*)kern, 200 * 1024, "sh_cn_pipelined")) return e;
+    int dbuf = 1;
+    size_t smem = sh_cn_pipelined_smem<R>(threads, M, refine, 1);
+    if (smem > 200 * 1024) {
+        dbuf = 0;
+        smem = sh_cn_pipelined_smem<R>(threads, M, refine, 0);
+    }
+    if (smem > 200 * 1024) {
+        set_error("ion_sh: radial line too long for shared memory");
+        return ION_ERR_UNSUPPORTED;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    const int grid = std::min(end - begin, std::max(per_sm, 1) * num_sms());
+    kern<<<grid, threads, smem, s>>>(*p, begin, end, dbuf);
+    return check_launch("sh_cn_pipelined");
+}
+
+template <typename R>
+static int sh_launch_cn_rows(const ion_sh_plan* p, int rows, int begin, int end, int threads, cudaStream_t s);
+template <>
+int sh_launch_cn_rows<double>(const ion_sh_plan* p, int rows, int begin, int end, int threads, cudaStream_t s) {
+    return rows == 4 ? sh_launch_cn_bucket<double, 4>(p, begin, end, threads, s)
+                     : sh_launch_cn_bucket<double, 8>(p, begin, end, threads, s);
+}
+template <>
+int sh_launch_cn_rows<float>(const ion_sh_plan* p, int rows, int begin, int end, int threads, cudaStream_t s) {
+    switch (rows) {
+        case 4: return sh_launch_cn_bucket<float, 4>(p, begin, end, threads, s);
+        case 8: return sh_launch_cn_bucket<float, 8>(p, begin, end, threads, s);
+        default: return sh_launch_cn_bucket<float, 16>(p, begin, end, threads, s);
+    }
+}
+
+// every bucket (or all items at cn_threads) with its own rows per thread
+template <typename R>
+static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s) {
+    if (p->n_cn_items == 0) return ION_OK;
     const int nb = p->n_cn_buckets;
     int begin = 0;
     for (int b = 0; b < (nb > 0 ? nb : 1); ++b) {
         const int end = nb > 0 ? p->cn_bucket_end[b] : p->n_cn_items;
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
-        if (end > begin) {
-            const int refine = (p->flags & ION_SH_REFINE) && sizeof(R) == 4 ? 1 : 0;
-            int dbuf = 1;
-            size_t smem = sh_cn_pipelined_smem<R>(threads, MAXM, refine, 1);
-            if (smem > 200 * 1024) {
-                dbuf = 0;
-                smem = sh_cn_pipelined_smem<R>(threads, MAXM, refine, 0);
-            }
-            if (smem > 200 * 1024) {
-                set_error("ion_sh: radial line too long for shared memory");
-                return ION_ERR_UNSUPPORTED;
-            }
-            auto kern = refine ? sh_cn_pipelined<R, MAXM, true> : sh_cn_pipelined<R, MAXM, false>;
-            int per_sm = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
-            const int grid = std::min(end - begin, std::max(per_sm, 1) * num_sms());
-            kern<<<grid, threads, smem, s>>>(*p, begin, end, dbuf);
-            if (int e = check_launch("sh_cn_pipelined")) return e;
-        }
+        const int rows = sh_bucket_rows<R>(p, nb > 0 ? b : -1);
+        if (end > begin)
+            if (int e = sh_launch_cn_rows<R>(p, rows, begin, end, threads, s)) return e;
         begin = end;
     }
     return ION_OK;
-}
-
-template <typename R>
-static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s);
-
-template <>
-int sh_launch_cn<double>(const ion_sh_plan* p, cudaStream_t s) {
-    if (p->n_cn_items == 0) return ION_OK;
-    return sh_rows<double>(p) == 4 ? sh_launch_cn_pipelined<double, 4>(p, s) : sh_launch_cn_pipelined<double, 8>(p, s);
-}
-
-template <>
-int sh_launch_cn<float>(const ion_sh_plan* p, cudaStream_t s) {
-    if (p->n_cn_items == 0) return ION_OK;
-    switch (sh_rows<float>(p)) {
-        case 4: return sh_launch_cn_pipelined<float, 4>(p, s);
-        case 8: return sh_launch_cn_pipelined<float, 8>(p, s);
-        default: return sh_launch_cn_pipelined<float, 16>(p, s);
-    }
 }
 
 template <typename R>

@@ -60,8 +60,38 @@ def test_autotune_times_every_candidate(cuda):
     rows = dev.SH_ROWS_CHOICES[dev.Precision.C64X]
     assert {f"rows{r}_graph8" for r in rows} <= set(timings)
     assert best["rows"] in rows and best["graph_steps"] in (4, 8)
-    assert f"rows{best['rows']}_graph{best['graph_steps']}" in timings
+    # the per-bucket stage: every other row count for every bucket
+    n_buckets = len(bm._bucket_lines("c64x", [bm._host_tables(s)[0] for s in _specs("c64x")], best["rows"]))
+    assert len(best["bucket_rows"]) == n_buckets
+    assert all(r == 0 or r in rows for r in best["bucket_rows"])
+    per_bucket = [k for k in timings if "_b" in k]
+    assert len(per_bucket) >= n_buckets
+    extra = "".join(f"_b{b}r{r}" for b, r in enumerate(best["bucket_rows"]) if r)
+    assert f"rows{best['rows']}_graph{best['graph_steps']}{extra}" in timings
     assert all(v > 0 for v in timings.values())
+
+
+@pytest.mark.gpu
+def test_bucket_rows_per_bucket(cuda):
+    """Buckets launched at their own rows per thread (16 for the longest
+    lines, 4 for the next): each bucket's CTA is sized for its lines at its
+    rows, and the populations equal the single-shape plan's to 1e-8
+    (measured 1.3e-9: the partition changes where the solve rounds, not what
+    it solves)."""
+    from ionization_gb300 import batch as bm
+
+    base = bm.BatchedSphericalHarmonicSimulation(_specs("c64x"), graph_steps=8)
+    mixed = bm.BatchedSphericalHarmonicSimulation(_specs("c64x"), graph_steps=8, bucket_rows=(16, 4))
+    shape = bm.plan_shape(mixed)["radial_buckets"]
+    assert [b["rows_per_thread"] for b in shape] == [16, 4, 8]
+    nr = sorted((s.r_points for s in _specs("c64x")), reverse=True)
+    assert shape[0]["threads"] == 64 and shape[0]["threads"] * 16 >= nr[0]
+    assert shape[1]["threads"] >= -(-nr[1] // 4)
+    base.run()
+    mixed.run()
+    for a, b in zip(base.results(), mixed.results(), strict=True):
+        assert abs(a["initial_state_overlap"][-1] - b["initial_state_overlap"][-1]) < 1e-8
+        np.testing.assert_allclose(a["norm"], b["norm"], rtol=0, atol=1e-8)
 
 
 @pytest.mark.gpu

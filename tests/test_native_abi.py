@@ -51,7 +51,7 @@ def test_struct_layouts_match_header():
     from ionization_gb300 import _native as nat
 
     # 8-byte pointers, fields in header order
-    assert ctypes.sizeof(nat.ShPlan) == 8 + 4 * 4 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 16 * 4
+    assert ctypes.sizeof(nat.ShPlan) == 8 + 4 * 4 + 8 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 24 * 4
     assert nat.ShSim.g.offset == 0 and nat.ShSim.t.offset == 16
     assert nat.LineSim.t.offset == 16
     assert ctypes.sizeof(nat.CylMesh) == 8 + 9 * 8 + 8 + 2 * 8
