@@ -152,6 +152,9 @@ __device__ __forceinline__ Cx<R> add_exact(Cx<R> h, Cx<R> d, Cx<R>& lo) {
 __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
 }
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
 
 // L2 prefetch of the rows of rotation tile ``item`` (n_l segments of
 // ROT_ROWS points)
@@ -194,8 +197,9 @@ struct ShCnCoef32 {
     // or NULL
     const uint32_t* lob;
     int T, mshift;
-    // the line's row-sum remainders (ion_sh_sim.row_lo, bf16), or NULL: with
-    // them the explicit half applies the FP64 Hamiltonian (the refinement)
+    // the line's row-sum remainders (ion_sh_sim.row_lo, bf16) staged in
+    // shared memory in row order, or NULL: with them the explicit half
+    // applies the FP64 Hamiltonian (the refinement)
     const uint16_t* rlo;
     __device__ __forceinline__ Cx<float> lo_at(int i) const {
         return lo_unpack(lob[(i & ((1 << mshift) - 1)) * T + (i >> mshift)]);
@@ -285,28 +289,70 @@ __device__ __forceinline__ Cx<float> stencil_row(const ShCnCoef32<RES>& c, int i
 template <typename R, bool RES> struct ShCnCoefFor;
 template <bool RES> struct ShCnCoefFor<double, RES> {
     using type = ShCnCoef<double>;
-    __device__ static type make(const ion_sh_sim& S, int l, double tau, const void*, int, int, bool = false) {
+    __device__ static type make(const ion_sh_sim& S, int l, double tau, const void*, int, int,
+                                const uint16_t* = nullptr) {
         return type{ShH<double>::make(S, l), tau, S.n_r};
     }
 };
 template <bool RES> struct ShCnCoefFor<float, RES> {
     using type = ShCnCoef32<RES>;
-    // lob: the line's residual staged in shared memory, or NULL; exact: with
-    // the row-sum remainders (when the simulation carries them)
+    // lob: the line's residual staged in shared memory, or NULL; rlo: its
+    // row-sum remainders staged in shared memory (row i at rlo[i]), or NULL
     __device__ static type make(const ion_sh_sim& S, int l, float tau, const void* lob, int T, int mshift,
-                                bool exact = false) {
+                                const uint16_t* rlo = nullptr) {
         return type{S.kinv32, S.cent32, S.hoff32, float(l) * float(l + 1), (l == 0) ? S.corr0_32 : 0.f, tau, S.n_r,
-                    static_cast<const uint32_t*>(lob), T, mshift,
-                    (exact && S.row_lo) ? S.row_lo + int64_t(l) * S.n_r : nullptr};
+                    static_cast<const uint32_t*>(lob), T, mshift, rlo};
     }
 };
 
-// psi of item ``item`` into ``dst`` (interleaved, zero padding), and its
-// stored residual (packed bf16x2) into ``lodst`` when given (complex64 with
-// g_lo), asynchronously
+// The row-sum remainders of line l (bf16, row_lo + l n_r, any 2-byte
+// alignment) into ``dst`` (16-byte aligned, sh_rlo_words(cap) halfwords) by
+// 16-byte asynchronous copies of the aligned blocks that cover the line: row i
+// lands at dst[rlo_shift(src) + i].  A block that would reach outside the
+// array [row_lo, row_lo + n_l n_r) is copied by element, zero outside.
+__device__ __forceinline__ int rlo_shift(const uint16_t* src) {
+    return int((reinterpret_cast<uintptr_t>(src) & 15u) >> 1);
+}
+__device__ __forceinline__ void stage_row_lo(const ion_sh_sim& S, int l, uint16_t* dst) {
+    const int nr = S.n_r;
+    const uint16_t* src = S.row_lo + int64_t(l) * nr;
+    const uint16_t* base = src - rlo_shift(src);
+    const uint16_t* lo_end = S.row_lo + int64_t(S.n_l) * nr;
+    const int nblk = (rlo_shift(src) + nr + 7) >> 3;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        const uint16_t* p = base + 8 * b;
+        if (p >= S.row_lo && p + 8 <= lo_end) {
+            cp_async16(dst + 8 * b, p);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) dst[8 * b + e] = (p + e >= S.row_lo && p + e < lo_end) ? p[e] : uint16_t(0);
+        }
+    }
+}
+
+// halfwords of one staged row_lo buffer for lines of up to ``cap`` rows
+__host__ __device__ inline int sh_rlo_words(int cap) { return (cap + 8 + 7) / 8 * 8; }
+
+// The coefficient tables of item ``item`` into L1 ahead of its solve (one
+// prefetch per 128-byte line of kinv32, cent32, hoff32): the tables are
+// shared by every l of a simulation and sit in L2, and the solve's chunk
+// loads would otherwise wait for L2 in every thread of the CTA at once.
+__device__ __forceinline__ void sh_cn_prefetch_coef(const ion_sh_plan& plan, int item) {
+    const ion_sh_sim& S = plan.sims[plan.cn_items[2 * item]];
+    const int lines = (S.n_r * 4 + 127) >> 7;
+    for (int f = threadIdx.x; f < 3 * lines; f += blockDim.x) {
+        const int tab = f / lines, c = f - tab * lines;
+        const float* p = tab == 0 ? S.kinv32 : (tab == 1 ? S.cent32 : S.hoff32);
+        if (p) prefetch_l1(reinterpret_cast<const char*>(p) + c * 128);
+    }
+}
+
+// psi of item ``item`` into ``dst`` (interleaved, zero padding), its stored
+// residual (packed bf16x2) into ``lodst`` and its row-sum remainders into
+// ``rlodst`` when given (complex64 with g_lo), asynchronously
 template <typename R, int M>
 __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int item, Cx<R>* dst,
-                                                  uint32_t* lodst = nullptr) {
+                                                  uint32_t* lodst = nullptr, uint16_t* rlodst = nullptr) {
     const int si = plan.cn_items[2 * item];
     const int l = plan.cn_items[2 * item + 1];
     const ion_sh_sim& S = plan.sims[si];
@@ -317,6 +363,7 @@ __device__ __forceinline__ void sh_cn_stage_async(const ion_sh_plan& plan, int i
     const int npad = T * M;
     const Cx<R>* g = static_cast<const Cx<R>*>(S.g) + int64_t(l) * nr;
     const uint32_t* glo = (lodst && S.g_lo) ? static_cast<const uint32_t*>(S.g_lo) + int64_t(l) * nr : nullptr;
+    if (glo && rlodst && S.row_lo) stage_row_lo(S, l, rlodst);
     for (int i = threadIdx.x; i < npad; i += blockDim.x) {
         Cx<R>* d = dst + islot<M>(i, T);
         if (i < nr) {
@@ -365,31 +412,39 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
     constexpr int refine = REFINE ? 1 : 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int cap = blockDim.x * M;
-    // psi (double-buffered), with refinement the increment and the staged
-    // residual (packed, double-buffered like psi), then the PCR scratch
+    // psi (double-buffered), with refinement the increment, the staged
+    // residual (packed) and row-sum remainders (both double-buffered like
+    // psi), then the PCR scratch
+    const int nb = dbuf ? 2 : 1;
     Cx<R>* buf0 = reinterpret_cast<Cx<R>*>(smem_raw);
     Cx<R>* buf1 = buf0 + cap;
-    Cx<R>* ext = buf0 + (dbuf ? 2 : 1) * cap;
+    Cx<R>* ext = buf0 + nb * cap;
     uint32_t* lob0 = reinterpret_cast<uint32_t*>(ext + (refine ? cap : 0));
     uint32_t* lob1 = lob0 + (dbuf ? cap : 0);
-    Cx<R>* red = reinterpret_cast<Cx<R>*>(lob0 + (refine ? (dbuf ? 2 : 1) * cap : 0));
+    uint16_t* rlo0 = reinterpret_cast<uint16_t*>(lob0 + (refine ? nb * cap : 0));
+    uint16_t* rlo1 = rlo0 + (dbuf ? sh_rlo_words(cap) : 0);
+    Cx<R>* red = reinterpret_cast<Cx<R>*>(rlo0 + (refine ? nb * sh_rlo_words(cap) : 0));
     int item = item0 + blockIdx.x;
     if (item >= item_end) return;
     if (dbuf) {
-        sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr);
+        sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr, refine ? rlo0 : nullptr);
         cp_async_commit();
     }
     for (int j = 0; item < item_end; item += gridDim.x, ++j) {
         Cx<R>* cur = (dbuf && (j & 1)) ? buf1 : buf0;
         uint32_t* lob = (dbuf && (j & 1)) ? lob1 : lob0;
+        uint16_t* rlo = (dbuf && (j & 1)) ? rlo1 : rlo0;
         if (dbuf) {
             const int next = item + gridDim.x;
-            if (next < item_end)
-                sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1, refine ? ((j & 1) ? lob0 : lob1) : nullptr);
+            if (next < item_end) {
+                sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1, refine ? ((j & 1) ? lob0 : lob1) : nullptr,
+                                        refine ? ((j & 1) ? rlo0 : rlo1) : nullptr);
+                if (sizeof(R) == 4) sh_cn_prefetch_coef(plan, next);
+            }
             cp_async_commit();
             cp_async_wait<1>();  // this item's psi has landed; the next one stays in flight
         } else {
-            sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr);
+            sh_cn_stage_async<R, M>(plan, item, buf0, refine ? lob0 : nullptr, refine ? rlo0 : nullptr);
             cp_async_commit();
             cp_async_wait<0>();
         }
@@ -424,8 +479,10 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
                 // FP64 system.
                 const bool two = glo != nullptr;
                 if (two) inc = ext;
+                const uint16_t* rl =
+                    (refine && glo && S.row_lo) ? rlo + rlo_shift(S.row_lo + int64_t(l) * nr) : nullptr;
                 const auto coef2 = ShCnCoefFor<R, REFINE>::make(S, l, tau, (refine && glo) ? lob : nullptr, T,
-                                                                mshift, true);
+                                                                mshift, rl);
                 for (int pass = 0; pass < (two ? 2 : 1); ++pass) {
                     // The correction of the second solve is ~1e-7 of delta1,
                     // so its reduced system may stop at couplings below
@@ -471,13 +528,16 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
     cp_async_wait<0>();
 }
 
-// psi (x2 when double-buffered); with refinement the increment and the
-// packed residual (4 bytes a row, x2 when double-buffered); the PCR scratch
+// psi (x2 when double-buffered); with refinement the increment, the packed
+// residual (4 bytes a row) and the row-sum remainders (2 bytes a row, 16-byte
+// blocks), both x2 when double-buffered; the PCR scratch
 template <typename R>
 __host__ __device__ inline size_t sh_cn_pipelined_smem(int threads, int M, int refine, int dbuf) {
     const size_t cap = size_t(threads) * M;
     const size_t nb = dbuf ? 2 : 1;
-    return nb * cap * sizeof(Cx<R>) + (refine ? cap * sizeof(Cx<R>) + nb * cap * 4 : 0) + pcr_cn_smem_bytes<R>(threads);
+    return nb * cap * sizeof(Cx<R>) +
+           (refine ? cap * sizeof(Cx<R>) + nb * cap * 4 + nb * size_t(sh_rlo_words(int(cap))) * 2 : 0) +
+           pcr_cn_smem_bytes<R>(threads);
 }
 
 // ---------------------------------------------------------------------------
