@@ -152,9 +152,6 @@ __device__ __forceinline__ Cx<R> add_exact(Cx<R> h, Cx<R> d, Cx<R>& lo) {
 __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
 }
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-    asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
-}
 
 // L2 prefetch of the rows of rotation tile ``item`` (n_l segments of
 // ROT_ROWS points)
@@ -333,20 +330,6 @@ __device__ __forceinline__ void stage_row_lo(const ion_sh_sim& S, int l, uint16_
 // halfwords of one staged row_lo buffer for lines of up to ``cap`` rows
 __host__ __device__ inline int sh_rlo_words(int cap) { return (cap + 8 + 7) / 8 * 8; }
 
-// The coefficient tables of item ``item`` into L1 ahead of its solve (one
-// prefetch per 128-byte line of kinv32, cent32, hoff32): the tables are
-// shared by every l of a simulation and sit in L2, and the solve's chunk
-// loads would otherwise wait for L2 in every thread of the CTA at once.
-__device__ __forceinline__ void sh_cn_prefetch_coef(const ion_sh_plan& plan, int item) {
-    const ion_sh_sim& S = plan.sims[plan.cn_items[2 * item]];
-    const int lines = (S.n_r * 4 + 127) >> 7;
-    for (int f = threadIdx.x; f < 3 * lines; f += blockDim.x) {
-        const int tab = f / lines, c = f - tab * lines;
-        const float* p = tab == 0 ? S.kinv32 : (tab == 1 ? S.cent32 : S.hoff32);
-        if (p) prefetch_l1(reinterpret_cast<const char*>(p) + c * 128);
-    }
-}
-
 // psi of item ``item`` into ``dst`` (interleaved, zero padding), its stored
 // residual (packed bf16x2) into ``lodst`` and its row-sum remainders into
 // ``rlodst`` when given (complex64 with g_lo), asynchronously
@@ -436,11 +419,9 @@ __global__ void __launch_bounds__(sh_cn_max_threads<R, M>()) sh_cn_pipelined(ion
         uint16_t* rlo = (dbuf && (j & 1)) ? rlo1 : rlo0;
         if (dbuf) {
             const int next = item + gridDim.x;
-            if (next < item_end) {
+            if (next < item_end)
                 sh_cn_stage_async<R, M>(plan, next, (j & 1) ? buf0 : buf1, refine ? ((j & 1) ? lob0 : lob1) : nullptr,
                                         refine ? ((j & 1) ? rlo0 : rlo1) : nullptr);
-                if (sizeof(R) == 4) sh_cn_prefetch_coef(plan, next);
-            }
             cp_async_commit();
             cp_async_wait<1>();  // this item's psi has landed; the next one stays in flight
         } else {
