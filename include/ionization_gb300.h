@@ -523,6 +523,54 @@ int ion_sh_observables_c64(const void *g, const void *g_lo, int32_t n_r, int32_t
                            const double *cl, int32_t n_radii, const double *radii, double weight, double *out,
                            void *scratch, int64_t scratch_bytes, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Energy expectation values (the InternalEnergyExpectationValue and
+ * TotalEnergyExpectationValue datastores, data.py:290-340;
+ * QuantumMesh.expectation_value, meshes.py:206-229).  A Hermitian operator on
+ * an (n_a, n_b) mesh in C order (b contiguous) made of a diagonal and
+ * couplings between nearest neighbours along each axis; every table is FP64
+ * [n_a*n_b] indexed by the point (i, j) it starts from, or NULL (no such
+ * term).  A real coupling c puts c at (k, k') and (k', k); with
+ * ION_HOP_IMAG_B / ION_HOP_IMAG_A it is imaginary: i c at (k, k'), -i c at
+ * (k', k), k' the neighbour at j+1 or i+1 (LineVelocityGaugeOperators'
+ * interaction, mesh_operators.py:358-369).
+ *
+ * ion_expectation_*: out[q] = weight * <g|H_q|g> for 1 <= n_ops <= ION_MAX_HOPS
+ *   operators (ops: a host array), one pass over g; a two-stage FP64 sum with a
+ *   compensated second stage; scratch from ion_expectation_scratch_bytes.
+ * ------------------------------------------------------------------------ */
+enum { ION_HOP_IMAG_B = 1, ION_HOP_IMAG_A = 2, ION_MAX_HOPS = 4 };
+typedef struct ion_hop {
+    const double *diag;  /* [n_a*n_b] or NULL */
+    const double *off_b; /* [n_a*n_b]: coupling of (i, j) and (i, j+1) (j = n_b-1 unused), or NULL */
+    const double *off_a; /* [n_a*n_b]: coupling of (i, j) and (i+1, j) (i = n_a-1 unused), or NULL */
+    int32_t flags;       /* ION_HOP_IMAG_B | ION_HOP_IMAG_A */
+    int32_t pad_;
+} ion_hop;
+int64_t ion_expectation_scratch_bytes(int32_t n_a, int32_t n_b, int32_t n_ops);
+int ion_expectation_c128(const void *g, int32_t n_a, int32_t n_b, int32_t n_ops, const ion_hop *ops, double weight,
+                         double *out, void *scratch, int64_t scratch_bytes, void *stream);
+int ion_expectation_c64(const void *g, const void *g_lo, int32_t n_a, int32_t n_b, int32_t n_ops,
+                        const ion_hop *ops, double weight, double *out, void *scratch, int64_t scratch_bytes,
+                        void *stream);
+
+/* The radial probability current of a spherical-harmonic mesh (the
+ * DirectionalRadialProbabilityCurrent datastore, data.py:467-530, with
+ * SphericalHarmonicMesh.get_radial_probability_current_density_mesh__spatial,
+ * meshes.py:1358-1371, and the r-current operator of
+ * SphericalHarmonicLengthGaugeOperators.r_probability_current__spatial,
+ * mesh_operators.py:1107-1127), on (n_l, n_r) g:
+ *   out[j] (z > 0) and out[n_r + j] (z < 0) =
+ *     r[j]^2 Im(sum_{l,l'} conj(g[l][j]) W[l][l'] (od[j] g[l'][j+1] - od[j-1] g[l'][j-1]))
+ * with W = w_pos or w_neg ([n_l*n_l], symmetric): 2 pi dtheta times the sum
+ * over that hemisphere's theta points of sin(theta) Y_l(theta) Y_l'(theta),
+ * and od [n_r-1] the operator's couplings.  out: device [2*n_r]. */
+int ion_sh_radial_current_c128(const void *g, int32_t n_r, int32_t n_l, const double *od, const double *r,
+                               const double *w_pos, const double *w_neg, double *out, void *stream);
+int ion_sh_radial_current_c64(const void *g, const void *g_lo, int32_t n_r, int32_t n_l, const double *od,
+                              const double *r, const double *w_pos, const double *w_neg, double *out,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif

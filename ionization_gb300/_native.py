@@ -34,6 +34,9 @@ ION_ADI_PASS_CONTIG = 1
 ION_GAUGE_VELOCITY = 1
 ION_LINE_RESIDUAL = 1
 ION_LINE_HAS_FFT = 2
+ION_HOP_IMAG_B = 1
+ION_HOP_IMAG_A = 2
+ION_MAX_HOPS = 4
 
 
 class NativeLibraryError(RuntimeError):
@@ -155,6 +158,16 @@ class LinePlan(ctypes.Structure):
     ]
 
 
+class Hop(ctypes.Structure):
+    _fields_ = [
+        ("diag", c_vp),
+        ("off_b", c_vp),
+        ("off_a", c_vp),
+        ("flags", c_i32),
+        ("pad_", c_i32),
+    ]
+
+
 class CylMesh(ctypes.Structure):
     _fields_ = [
         ("n_z", c_i32),
@@ -220,6 +233,11 @@ _SIGS = {
     "ion_weighted_norms_scratch_bytes": (c_i64, [c_i64, c_i32]),
     "ion_weighted_norms_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
     "ion_weighted_norms_c64": (ctypes.c_int, [c_i64, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
+    "ion_expectation_scratch_bytes": (c_i64, [c_i32, c_i32, c_i32]),
+    "ion_expectation_c128": (ctypes.c_int, [c_vp, c_i32, c_i32, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
+    "ion_expectation_c64": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_i32, c_vp, c_f64, c_vp, c_vp, c_i64, c_vp]),
+    "ion_sh_radial_current_c128": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "ion_sh_radial_current_c64": (ctypes.c_int, [c_vp, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ion_sh_observables_scratch_bytes": (c_i64, [c_i32, c_i32, c_i32]),
     "ion_sh_observables_c128": (ctypes.c_int, [c_vp, c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_f64, c_vp, c_vp,
                                                 c_i64, c_vp]),

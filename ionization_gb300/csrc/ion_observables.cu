@@ -17,6 +17,21 @@
 //                         the norm of each l (SphericalHarmonicMesh.norm_by_l,
 //                         meshes.py:1133-1136);
 //                         the norm within each radius R_k (rows r_j <= R_k).
+//   ion_expectation_*     <g|H|g> for up to four Hermitian operators made of
+//                         a diagonal and nearest-neighbour couplings along
+//                         the two axes of the mesh, in one pass (the
+//                         InternalEnergyExpectationValue and
+//                         TotalEnergyExpectationValue datastores,
+//                         data.py:290-340, QuantumMesh.expectation_value
+//                         with internal_hamiltonian and
+//                         interaction_hamiltonian, meshes.py:206-229,
+//                         mesh_operators.py:244-298);
+//   ion_sh_radial_current_*  the radial probability current through each
+//                         shell r_j, split into z > 0 and z < 0 (the
+//                         DirectionalRadialProbabilityCurrent datastore,
+//                         data.py:467-530, with
+//                         SphericalHarmonicMesh.get_radial_probability_
+//                         current_density_mesh__spatial, meshes.py:1358-1371).
 // The complex64 state may carry its stored residual (g + g_lo).  Stage 1
 // writes FP64 partials per CTA (per row tile for the SH form); stage 2 adds
 // them in CTA order with Neumaier compensation, so results do not depend on
@@ -148,6 +163,103 @@ __global__ void __launch_bounds__(OBS_THREADS) sh_obs_stage1(const Cx<R>* g, con
     }
 }
 
+// <g|H_q|g> partials: grid-stride over the points of the (n_a, n_b) mesh;
+// point (i, j) adds d |g_ij|^2 and its couplings to (i, j+1) and (i+1, j):
+// 2 Re(conj(g) c g') for a real coupling, -2 c Im(conj(g) g') for an
+// imaginary one (H_kl = i c, H_lk = -i c).
+struct ExpOps {
+    ion_hop op[ION_MAX_HOPS];
+    int n;
+};
+
+__device__ __forceinline__ double coupling_term(double c, Cx<double> x, Cx<double> y, bool imag) {
+    const double re = x.re * y.re + x.im * y.im;  // Re(conj(x) y)
+    const double im = x.re * y.im - x.im * y.re;  // Im(conj(x) y)
+    return imag ? -2.0 * c * im : 2.0 * c * re;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(OBS_THREADS) expect_stage1(const Cx<R>* g, const uint32_t* glo, int na, int nb,
+                                                             ExpOps ops, double* part) {
+    __shared__ double sh[32];
+    double acc[ION_MAX_HOPS];
+#pragma unroll
+    for (int q = 0; q < ION_MAX_HOPS; ++q) acc[q] = 0.0;
+    const int64_t n = int64_t(na) * nb;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const int64_t i = k / nb;
+        const int j = int(k - i * nb);
+        const Cx<double> x = value_at(g, glo, k);
+        const double p = x.re * x.re + x.im * x.im;
+        const bool hb = j + 1 < nb, ha = i + 1 < na;
+        const Cx<double> yb = hb ? value_at(g, glo, k + 1) : Cx<double>{0.0, 0.0};
+        const Cx<double> ya = ha ? value_at(g, glo, k + nb) : Cx<double>{0.0, 0.0};
+#pragma unroll
+        for (int q = 0; q < ION_MAX_HOPS; ++q) {
+            if (q >= ops.n) break;
+            const ion_hop& o = ops.op[q];
+            double v = o.diag ? o.diag[k] * p : 0.0;
+            if (hb && o.off_b) v += coupling_term(o.off_b[k], x, yb, (o.flags & ION_HOP_IMAG_B) != 0);
+            if (ha && o.off_a) v += coupling_term(o.off_a[k], x, ya, (o.flags & ION_HOP_IMAG_A) != 0);
+            acc[q] += v;
+        }
+    }
+    for (int q = 0; q < ops.n; ++q) {
+        const double t = obs_block_sum(acc[q], sh);
+        if (threadIdx.x == 0) part[int64_t(blockIdx.x) * ops.n + q] = t;
+    }
+}
+
+// The radial current through shell j of a spherical-harmonic mesh, z > 0 and
+// z < 0: with u_l = g[l][j] and v_l = od[j] g[l][j+1] - od[j-1] g[l][j-1]
+// (the reference's r-current operator, mesh_operators.py:1107-1127: real
+// antisymmetric couplings od[j] = hbar / (2 m dr^3) / ((j+1)^2 - 1/4)),
+//     out[h][j] = r_j^2 Im(sum_{l,l'} conj(u_l) W_h[l][l'] v_l'),
+// W_h[l][l'] = 2 pi dtheta sum over the theta_calc points of hemisphere h of
+// sin(theta) Y_l(theta) Y_l'(theta): the reference's theta sum of
+// Im(conj(psi(r, theta)) (G psi)(r, theta)) sin(theta) dtheta 2 pi with
+// psi(r, theta) = sum_l g_l(r) Y_l(theta) (meshes.py:1497-1517), regrouped
+// over l pairs (W symmetric: w = W u, then sum conj(w_l') v_l').  One thread
+// per shell.
+template <typename R>
+__global__ void __launch_bounds__(128) sh_current_kernel(const Cx<R>* g, const uint32_t* glo, int nr, int nl,
+                                                         const double* od, const double* r, const double* wpos,
+                                                         const double* wneg, double* out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nr) return;
+    const double odp = j + 1 < nr ? od[j] : 0.0, odm = j > 0 ? od[j - 1] : 0.0;
+    double sp = 0.0, sn = 0.0;
+    for (int lp = 0; lp < nl; ++lp) {
+        Cx<double> wp = {0.0, 0.0}, wn = {0.0, 0.0};
+        for (int l = 0; l < nl; ++l) {
+            const Cx<double> u = value_at(g, glo, int64_t(l) * nr + j);
+            const double a = wpos[int64_t(lp) * nl + l], b = wneg[int64_t(lp) * nl + l];
+            wp.re += a * u.re;
+            wp.im += a * u.im;
+            wn.re += b * u.re;
+            wn.im += b * u.im;
+        }
+        const int64_t base = int64_t(lp) * nr + j;
+        Cx<double> v = {0.0, 0.0};
+        if (j + 1 < nr) {
+            const Cx<double> y = value_at(g, glo, base + 1);
+            v.re += odp * y.re;
+            v.im += odp * y.im;
+        }
+        if (j > 0) {
+            const Cx<double> y = value_at(g, glo, base - 1);
+            v.re -= odm * y.re;
+            v.im -= odm * y.im;
+        }
+        sp += wp.re * v.im - wp.im * v.re;  // Im(conj(w) v)
+        sn += wn.re * v.im - wn.im * v.re;
+    }
+    const double r2 = r[j] * r[j];
+    out[j] = r2 * sp;
+    out[nr + j] = r2 * sn;
+}
+
 static int weighted_blocks(int64_t n) {
     const int64_t b = (n + OBS_THREADS - 1) / OBS_THREADS;
     return int(b < OBS_BLOCKS ? b : OBS_BLOCKS);
@@ -199,6 +311,43 @@ static int sh_obs_impl(const void* g, const void* g_lo, int32_t nr, int32_t nl, 
     return check_launch("obs_stage2");
 }
 
+template <typename R>
+static int expect_impl(const void* g, const void* g_lo, int32_t na, int32_t nb, int32_t nops, const ion_hop* ops,
+                       double weight, double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+    if (!g || na < 1 || nb < 1 || nops < 1 || nops > ION_MAX_HOPS || !ops || !out || !scratch) {
+        set_error("ion_expectation: invalid argument (n_a, n_b >= 1, 1 <= n_ops <= %d, pointers set)", ION_MAX_HOPS);
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    const int64_t n = int64_t(na) * nb;
+    const int blocks = weighted_blocks(n);
+    if (scratch_bytes < int64_t(blocks) * nops * int64_t(sizeof(double))) {
+        set_error("ion_expectation: scratch too small");
+        return ION_ERR_SCRATCH_TOO_SMALL;
+    }
+    ExpOps eo{};
+    eo.n = nops;
+    for (int q = 0; q < nops; ++q) eo.op[q] = ops[q];
+    cudaStream_t s = as_stream(stream);
+    double* part = static_cast<double*>(scratch);
+    expect_stage1<R><<<blocks, OBS_THREADS, 0, s>>>(static_cast<const Cx<R>*>(g), static_cast<const uint32_t*>(g_lo),
+                                                    na, nb, eo, part);
+    if (int e = check_launch("expect_stage1")) return e;
+    obs_stage2<<<1, 32, 0, s>>>(blocks, nops, part, weight, out);
+    return check_launch("obs_stage2");
+}
+
+template <typename R>
+static int sh_current_impl(const void* g, const void* g_lo, int32_t nr, int32_t nl, const double* od, const double* r,
+                           const double* wpos, const double* wneg, double* out, void* stream) {
+    if (!g || nr < 1 || nl < 1 || !od || !r || !wpos || !wneg || !out) {
+        set_error("ion_sh_radial_current: invalid argument (n_r, n_l >= 1, pointers set)");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    sh_current_kernel<R><<<(nr + 127) / 128, 128, 0, as_stream(stream)>>>(
+        static_cast<const Cx<R>*>(g), static_cast<const uint32_t*>(g_lo), nr, nl, od, r, wpos, wneg, out);
+    return check_launch("sh_current_kernel");
+}
+
 }  // namespace ion
 
 using namespace ion;
@@ -229,5 +378,25 @@ int ion_sh_observables_c64(const void* g, const void* g_lo, int32_t n_r, int32_t
                            const double* cl, int32_t n_radii, const double* radii, double weight, double* out,
                            void* scratch, int64_t scratch_bytes, void* stream) {
     return sh_obs_impl<float>(g, g_lo, n_r, n_l, r, cl, n_radii, radii, weight, out, scratch, scratch_bytes, stream);
+}
+int64_t ion_expectation_scratch_bytes(int32_t n_a, int32_t n_b, int32_t n_ops) {
+    if (n_a < 1 || n_b < 1 || n_ops < 1) return 0;
+    return int64_t(weighted_blocks(int64_t(n_a) * n_b)) * n_ops * int64_t(sizeof(double));
+}
+int ion_expectation_c128(const void* g, int32_t n_a, int32_t n_b, int32_t n_ops, const ion_hop* ops, double weight,
+                         double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+    return expect_impl<double>(g, nullptr, n_a, n_b, n_ops, ops, weight, out, scratch, scratch_bytes, stream);
+}
+int ion_expectation_c64(const void* g, const void* g_lo, int32_t n_a, int32_t n_b, int32_t n_ops, const ion_hop* ops,
+                        double weight, double* out, void* scratch, int64_t scratch_bytes, void* stream) {
+    return expect_impl<float>(g, g_lo, n_a, n_b, n_ops, ops, weight, out, scratch, scratch_bytes, stream);
+}
+int ion_sh_radial_current_c128(const void* g, int32_t n_r, int32_t n_l, const double* od, const double* r,
+                               const double* w_pos, const double* w_neg, double* out, void* stream) {
+    return sh_current_impl<double>(g, nullptr, n_r, n_l, od, r, w_pos, w_neg, out, stream);
+}
+int ion_sh_radial_current_c64(const void* g, const void* g_lo, int32_t n_r, int32_t n_l, const double* od,
+                              const double* r, const double* w_pos, const double* w_neg, double* out, void* stream) {
+    return sh_current_impl<float>(g, g_lo, n_r, n_l, od, r, w_pos, w_neg, out, stream);
 }
 }

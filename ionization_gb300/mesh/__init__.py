@@ -5,9 +5,16 @@ from .data import (  # noqa: F401
     DEFAULT_DATASTORE_TYPES,
     Data,
     Datastore,
+    DirectionalRadialProbabilityCurrent,
     Fields,
     InnerProducts,
+    InternalEnergyExpectationValue,
     Norm,
+    NormBySphericalHarmonic,
+    NormWithinRadius,
+    RExpectationValue,
+    TotalEnergyExpectationValue,
+    ZExpectationValue,
 )
 from .evolution_methods import (  # noqa: F401
     AlternatingDirectionImplicit,

@@ -1,11 +1,14 @@
-"""Datastores (ionization/mesh/data.py:14-464): Fields, Norm, InnerProducts,
-ZExpectationValue, RExpectationValue, NormWithinRadius, NormBySphericalHarmonic.
+"""Datastores (ionization/mesh/data.py:14-530): Fields, Norm, InnerProducts,
+ZExpectationValue, RExpectationValue, NormWithinRadius, NormBySphericalHarmonic,
+InternalEnergyExpectationValue, TotalEnergyExpectationValue,
+DirectionalRadialProbabilityCurrent.
 
 Norm and InnerProducts are filled from the FP64 device reductions made at the
 data times of the run (fused into the step kernels, or a reduction kernel at
 the data time); ``Fields`` is evaluated on the host from the pulse.  The
-position expectation values and partial norms are device reductions of the
-current wavefunction launched at each data time (``store``).  The attribute
+position and energy expectation values, partial norms and radial currents
+are device reductions of the current wavefunction launched at each data
+time (``store``).  The attribute
 names on ``sim.data`` are the reference's.
 """
 
@@ -259,5 +262,88 @@ class NormBySphericalHarmonic(Datastore):
 
 
 DATA_NAME_TO_DATASTORE_TYPE.update({"norm_by_l": NormBySphericalHarmonic})
+
+class InternalEnergyExpectationValue(Datastore):
+    """<H0> at the data times (data.py:290-313): a device reduction of the
+    internal Hamiltonian's expectation value."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        self.internal_energy_expectation_value = sim.get_blank_data()
+        super().init(sim)
+
+    def store(self):
+        self.internal_energy_expectation_value[self.sim.data_time_index] = (
+            self.sim.mesh.internal_energy_expectation_value())
+
+    def attach(self):
+        self.sim.data.internal_energy_expectation_value = self.internal_energy_expectation_value
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"internal_energy_expectation_value": InternalEnergyExpectationValue})
+
+
+class TotalEnergyExpectationValue(Datastore):
+    """<H0 + V(t)> at the data times (data.py:316-340): the internal
+    Hamiltonian plus the interaction at the data time."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        self.total_energy_expectation_value = sim.get_blank_data()
+        super().init(sim)
+
+    def store(self):
+        self.total_energy_expectation_value[self.sim.data_time_index] = (
+            self.sim.mesh.total_energy_expectation_value())
+
+    def attach(self):
+        self.sim.data.total_energy_expectation_value = self.total_energy_expectation_value
+
+
+DATA_NAME_TO_DATASTORE_TYPE.update({"total_energy_expectation_value": TotalEnergyExpectationValue})
+
+
+class DirectionalRadialProbabilityCurrent(Datastore):
+    """The radial probability current through each shell r_j at the data
+    times, for z > 0 and z < 0 (data.py:467-530), on spherical-harmonic
+    meshes (SphericalHarmonicMesh.radial_probability_current).  Arrays of
+    shape (data times, r_points), NaN until stored.  The reference's own
+    class reads ``self.sim`` in ``init`` before the base class sets it, and
+    its mesh method calls the current operator without the mesh, so it does
+    not run there; this one computes what those lines describe."""
+
+    stores_at_data_times = True
+
+    def init(self, sim):
+        if not hasattr(sim.mesh, "radial_probability_current"):
+            raise exceptions.UnsupportedMesh(
+                f"DirectionalRadialProbabilityCurrent needs a spherical-harmonic mesh, not {type(sim.mesh).__name__}")
+        shape = (sim.data_time_steps, sim.spec.r_points)
+        self.radial_probability_current__pos_z = np.full(shape, np.nan)
+        self.radial_probability_current__neg_z = np.full(shape, np.nan)
+        super().init(sim)
+
+    def store(self):
+        pos, neg = self.sim.mesh.radial_probability_current()
+        self.radial_probability_current__pos_z[self.sim.data_time_index] = pos
+        self.radial_probability_current__neg_z[self.sim.data_time_index] = neg
+
+    def attach(self):
+        self.sim.data.radial_probability_current__pos_z = self.radial_probability_current__pos_z
+        self.sim.data.radial_probability_current__neg_z = self.radial_probability_current__neg_z
+
+    def radial_probability_current__total(self):
+        return self.radial_probability_current__pos_z + self.radial_probability_current__neg_z
+
+
+Data.radial_probability_current__total = link_property_to_data(
+    DirectionalRadialProbabilityCurrent, DirectionalRadialProbabilityCurrent.radial_probability_current__total)
+DATA_NAME_TO_DATASTORE_TYPE.update({
+    "radial_probability_current__pos_z": DirectionalRadialProbabilityCurrent,
+    "radial_probability_current__neg_z": DirectionalRadialProbabilityCurrent,
+    "radial_probability_current__total": DirectionalRadialProbabilityCurrent,
+})
 
 DEFAULT_DATASTORE_TYPES = (Fields, Norm, InnerProducts)

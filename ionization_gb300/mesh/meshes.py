@@ -9,6 +9,7 @@ line (z_points,), spherical harmonic (l_bound, r_points), cylindrical
 (z_points, rho_points).
 """
 
+import ctypes
 from typing import Optional
 
 import numpy as np
@@ -162,6 +163,71 @@ class QuantumMesh:
         """The norm of the mesh points with r <= R, for each R (data.py:420-425)."""
         return self._weighted_norms([(self.r_mesh <= R).astype(np.float64) for R in radii])
 
+    # ---- energy expectation values (device reductions) ----
+    def _energy_operators(self):
+        """((n_a, n_b), internal, interaction, field): the internal
+        Hamiltonian and the interaction per unit field as (diag, off_b, off_a,
+        flags) tables over the (n_a, n_b) C-order layout of g (each array
+        broadcast to the mesh, off-diagonals indexed by the point they start
+        from; ion_hop), and ``field()`` the interaction's field factor at the
+        current time.  interaction None: the total Hamiltonian has no
+        interaction term; the string "unsupported": the device has no form of
+        it."""
+        raise exceptions.UnsupportedMesh(f"no energy expectation values on {type(self).__name__}")
+
+    def _energy_device(self):
+        if getattr(self, "_d_energy", None) is None:
+            (na, nb), internal, inter, field = self._energy_operators()
+            ops = [internal] + ([inter] if isinstance(inter, tuple) else [])
+            hops = (nat.Hop * len(ops))()
+            keep = []
+            for q, (diag, off_b, off_a, flags) in enumerate(ops):
+                for name, arr in (("diag", diag), ("off_b", off_b), ("off_a", off_a)):
+                    if arr is not None:
+                        full = np.broadcast_to(np.asarray(arr, dtype=np.float64), (na, nb)).reshape(-1)
+                        keep.append(dev.to_dev(full))
+                        setattr(hops[q], name, dev.ptr(keep[-1]))
+                hops[q].flags = int(flags)
+            self._d_energy = (na, nb, hops, keep, inter, field)
+        return self._d_energy
+
+    def _energy_terms(self):
+        """weight * <g|H0|g> and, when the mesh has one, weight * <g|V|g> with
+        V the interaction per unit field, in one device pass."""
+        import torch
+
+        na, nb, hops, _, inter, field = self._energy_device()
+        g = self._psi_device()
+        lo = self._psi_residual()
+        nbytes = nat.value("ion_expectation_scratch_bytes", na, nb, len(hops))
+        scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=g.device)
+        res = torch.empty(len(hops), dtype=torch.float64, device=g.device)
+        ops = ctypes.cast(hops, ctypes.c_void_p)
+        w = float(self.inner_product_multiplier)
+        if g.dtype == torch.complex128:
+            nat.call("ion_expectation_c128", dev.ptr(g), na, nb, len(hops), ops, w, dev.ptr(res), dev.ptr(scratch),
+                     int(nbytes), dev.stream_ptr())
+        else:
+            nat.call("ion_expectation_c64", dev.ptr(g), dev.ptr(lo), na, nb, len(hops), ops, w, dev.ptr(res),
+                     dev.ptr(scratch), int(nbytes), dev.stream_ptr())
+        return res.cpu().numpy(), inter, field
+
+    def internal_energy_expectation_value(self):
+        """<H0> of the current wavefunction: the internal Hamiltonian
+        (kinetic energy and internal potential, mesh_operators.py:244-269;
+        QuantumMesh.internal_energy_expectation_value, meshes.py:219-223)."""
+        return float(self._energy_terms()[0][0])
+
+    def total_energy_expectation_value(self):
+        """<H0 + V(t)> of the current wavefunction: the internal Hamiltonian
+        plus the interaction at the current time (total_hamiltonian,
+        mesh_operators.py:271-298; meshes.py:225-229)."""
+        if self._energy_device()[4] == "unsupported":
+            raise exceptions.UnsupportedMesh(
+                f"{type(self.operators).__name__} on {type(self).__name__}: no device form of the interaction energy")
+        v, inter, field = self._energy_terms()
+        return float(v[0]) if inter is None else float(v[0] + field() * v[1])
+
     # ---- stepping ----
     def _method_supported(self):
         raise NotImplementedError
@@ -183,6 +249,41 @@ class QuantumMesh:
         if self._tau_host[t_now] != tau:
             self._tau_host[t_now] = tau
             self._tau_dev()[t_now] = tau
+
+
+def sph_harm_m0(ls, theta) -> np.ndarray:
+    """Y_l^0(theta) = sqrt((2l + 1) / 4 pi) P_l(cos theta) for each l of
+    ``ls`` (rows) at each theta (columns), P_l by the three-term recurrence
+    (n + 1) P_{n+1} = (2n + 1) x P_n - n P_{n-1}: the values scipy's
+    sph_harm(0, l, 0, theta) gives the reference (meshes.py:1487-1490)."""
+    ls = np.asarray(ls, dtype=int)
+    x = np.cos(np.asarray(theta, dtype=np.float64))
+    lmax = int(ls.max()) if ls.size else 0
+    p = np.empty((lmax + 1, x.size))
+    p[0] = 1.0
+    if lmax >= 1:
+        p[1] = x
+    for n in range(1, lmax):
+        p[n + 1] = ((2 * n + 1) * x * p[n] - n * p[n - 1]) / (n + 1)
+    return np.sqrt((2 * ls[:, None] + 1) / (4 * np.pi)) * p[ls]
+
+
+def _two_axis_energy_operators(mesh, n_a, n_b):
+    """Energy operators of a (z, b) mesh whose internal Hamiltonian is
+    H_z + H_b (each kinetic operator with its share of the potential,
+    mesh_operators.py:244-269, device_tables): diagonal hz_d + hr_d,
+    couplings hz_off along z and hr_off along b; the interaction per unit
+    field is -q z on the diagonal times E(t) (interaction_hamiltonian,
+    mesh_operators.py:475-497, 605-627: split over the two directions and
+    summed back by total_hamiltonian, :271-298)."""
+    tb = mesh.operators.device_tables(mesh)
+    diag = (np.asarray(tb["hz_d"], dtype=np.float64) + np.asarray(tb["hr_d"], dtype=np.float64)).reshape(n_a, n_b)
+    off_b = np.append(np.asarray(tb["hr_off"], dtype=np.float64), 0.0)
+    off_a = np.append(np.asarray(tb["hz_off"], dtype=np.float64), 0.0)[:, None]
+    internal = (diag, off_b, off_a, 0)
+    inter = (np.asarray(tb["zq"], dtype=np.float64)[:, None], None, None, 0)
+    spec, sim = mesh.spec, mesh.sim
+    return (n_a, n_b), internal, inter, lambda: float(spec.electric_potential.get_electric_field_amplitude(sim.time))
 
 
 class _AdiDevice:
@@ -335,6 +436,21 @@ class LineMesh(QuantumMesh):
 
     def _psi_residual(self):
         return self._dsim.g_lo
+
+    def _energy_operators(self):
+        """H0 = diag(hd) + hoff couplings along z; the interaction per unit
+        field: -q z on the diagonal times E(t) (length gauge,
+        mesh_operators.py:320-327).  The velocity gauge's interaction
+        (:358-382) has no diagonal, and the line's total_hamiltonian adds only
+        the interaction's diagonal to H0 (mesh_operators.py:271-298), so its
+        total energy is the internal one."""
+        hd, hoff, zq = self.operators.device_tables(self)
+        internal = (hd, np.append(hoff, 0.0), None, 0)
+        if isinstance(self.operators, mo.LineVelocityGaugeOperators):
+            return (1, self.mesh_points), internal, None, None
+        spec, sim = self.spec, self.sim
+        return (1, self.mesh_points), internal, (zq, None, None, 0), lambda: float(
+            spec.electric_potential.get_electric_field_amplitude(sim.time))
 
     def _tau_dev(self):
         return self._dsim.d_tau
@@ -597,6 +713,65 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         """<z>: the F-order dipole operator (mesh_operators.py:1086-1104)."""
         return self._sh_observables()[1]
 
+    def _energy_operators(self):
+        """H0: the radial Hamiltonian of each l (hd, hoff: the Lagrangian
+        kinetic energy, the internal potential and the l = 0 correction,
+        mesh_operators.py:889-928, 244-269) along r; the interaction per unit
+        field: c_l (-q r_j) between l-neighbours at each r times
+        E(t + dt/2) (interaction_hamiltonian, mesh_operators.py:988-1018).
+        The velocity gauge's interaction couples (l, r) with (l+1, r +- 1)
+        as well: the device has no form of it."""
+        tb = self.operators.device_tables(self)
+        L, nr = self.spec.l_bound, self.spec.r_points
+        internal = (np.asarray(tb["hd"], dtype=np.float64).reshape(L, nr), np.append(tb["hoff"], 0.0), None, 0)
+        if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
+            return (L, nr), internal, "unsupported", None
+        cl = np.append(np.asarray(tb["cl"], dtype=np.float64)[: L - 1], 0.0)
+        inter = (None, None, np.outer(cl, np.asarray(tb["rq"], dtype=np.float64)), 0)
+        spec, sim = self.spec, self.sim
+        return (L, nr), internal, inter, lambda: float(
+            spec.electric_potential.get_electric_field_amplitude(sim.time + spec.time_step / 2))
+
+    def radial_probability_current(self):
+        """(z > 0, z < 0): the radial probability current through each shell
+        r_j, as DirectionalRadialProbabilityCurrent.store forms it
+        (data.py:467-505) from get_radial_probability_current_density_mesh__
+        spatial (meshes.py:1358-1371): the r-current operator of
+        r_probability_current__spatial (mesh_operators.py:1107-1127) on psi
+        rebuilt on the theta_calc grid (theta_points from 0 to pi,
+        meshes.py:1456-1458, 1497-1517), Im(conj(psi) G psi) sin(theta)
+        dtheta 2 pi summed over each hemisphere (theta <= pi/2 is z > 0),
+        times r_j^2.  On the device the theta sum is folded into l-pair
+        weights (ion_sh_radial_current_*)."""
+        import torch
+
+        if getattr(self, "_d_current", None) is None:
+            spec = self.spec
+            nr, L = spec.r_points, spec.l_bound
+            theta = np.linspace(0, np.pi, int(spec.theta_points))
+            ylm = sph_harm_m0(np.arange(L), theta)  # (L, n_theta)
+            wt = u.twopi * np.abs(theta[1] - theta[0]) * np.sin(theta)
+            up = theta <= np.pi / 2
+            w_pos = (ylm[:, up] * wt[up]) @ ylm[:, up].T
+            w_neg = (ylm[:, ~up] * wt[~up]) @ ylm[:, ~up].T
+            j = np.arange(1, nr, dtype=np.float64)
+            od = (u.hbar / (2 * spec.test_mass * self.delta_r ** 3)) / (j ** 2 - 0.25)
+            self._d_current = tuple(dev.to_dev(np.ascontiguousarray(a, dtype=np.float64))
+                                    for a in (od, self.r, w_pos, w_neg))
+        d_od, d_r, d_wp, d_wn = self._d_current
+        g = self._psi_device()
+        lo = self._psi_residual()
+        nr, L = self.spec.r_points, self.spec.l_bound
+        out = torch.empty(2 * nr, dtype=torch.float64, device=g.device)
+        if g.dtype == torch.complex128:
+            nat.call("ion_sh_radial_current_c128", dev.ptr(g), nr, L, dev.ptr(d_od), dev.ptr(d_r), dev.ptr(d_wp),
+                     dev.ptr(d_wn), dev.ptr(out), dev.stream_ptr())
+        else:
+            nat.call("ion_sh_radial_current_c64", dev.ptr(g), dev.ptr(lo), nr, L, dev.ptr(d_od), dev.ptr(d_r),
+                     dev.ptr(d_wp), dev.ptr(d_wn), dev.ptr(out), dev.stream_ptr())
+        v = out.cpu().numpy()
+        return v[:nr].copy(), v[nr:].copy()
+
     def r_expectation_value(self):
         return self._sh_observables()[0]
 
@@ -842,6 +1017,9 @@ class RectangleMesh(_AdiDevice, QuantumMesh):
         self._adi_setup(spec.z_points, spec.x_points, arrays, g0, test_g)
         self._cm.order = nat.ION_ADI_CONTIG_FIRST
 
+    def _energy_operators(self):
+        return _two_axis_energy_operators(self, self.spec.z_points, self.spec.x_points)
+
     def _psi_device(self):
         return self._g
 
@@ -936,6 +1114,9 @@ class CylindricalSliceMesh(_AdiDevice, QuantumMesh):
         self._adi_setup(spec.z_points, spec.rho_points, dict(
             hz_d=tb["hz_d"], hz_off=tb["hz_off"], hr_d=tb["hr_d"], hr_off=tb["hr_off"], zq=tb["zq"],
             tau=self._tau_host, efield=efield, mask=mask, hz_off_col=None), g0, test_g)
+
+    def _energy_operators(self):
+        return _two_axis_energy_operators(self, self.spec.z_points, self.spec.rho_points)
 
     def _psi_device(self):
         return self._g

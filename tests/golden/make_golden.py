@@ -32,6 +32,10 @@ Cases (reference call sites in parentheses):
   *_observables_small  line / SH / cylindrical runs with the ZExpectationValue,
                    RExpectationValue, NormWithinRadius and (SH)
                    NormBySphericalHarmonic datastores
+  *_energy_small   line (length and velocity gauge), SH, cylindrical and
+                   rectangle runs with the InternalEnergyExpectationValue and
+                   TotalEnergyExpectationValue datastores; the SH run also
+                   the DirectionalRadialProbabilityCurrent at its final time
 
 Each npz holds the spec parameters (``params`` JSON string), the time grid,
 the initial and final ``g``, and the Norm / InnerProducts datastore arrays.
@@ -390,28 +394,33 @@ def gen_slice(ion):
         save(name, params, out)
 
 
+def rect_spec(ion, name, nz, nx):
+    from ionization import states
+
+    pulse = _pulse_kwargs(0.1, 0.5, 2, 0.3)
+    params = dict(z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0, time_initial=0.0, time_final=20.0,
+                  time_step=0.05, softening_distance=float(np.sqrt(2)), width_z=1.0, width_x=1.5,
+                  center_z=0.5, center_x=-0.25, k_z=0.3, pulse=pulse,
+                  mask=dict(inner_radius=12.0, outer_radius=16.0, smoothness=8), store_data_every=50)
+    init = states.TwoDGaussianWavepacket(center_z=0.5, center_x=-0.25, width_z=1.0, width_x=1.5, k_z=0.3)
+    spec = ion.mesh.RectangleSpecification(
+        name, z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0,
+        internal_potential=ion.potentials.SoftCoulombPotential(softening_distance=np.sqrt(2)),
+        initial_state=init, test_states=[init],
+        electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
+        mask=ion.potentials.RadialCosineMask(inner_radius=12.0, outer_radius=16.0, smoothness=8),
+        time_initial=0.0, time_final=20.0, time_step=0.05, store_data_every=50,
+    )
+    return spec, params
+
+
 def gen_rect(ion):
     """RectangleMesh + RectangleLengthGaugeOperators + ADI (meshes.py:430-506,
     mesh_operators.py:430-505): kinetic energies along z (F order) and x
     (C order) in that order, soft-Coulomb V(r) and -z q E(t) split evenly
     between them; a TwoDGaussianWavepacket initial state."""
-    from ionization import states
-
-    pulse = _pulse_kwargs(0.1, 0.5, 2, 0.3)
     for name, nz, nx in (("rect_adi_small", 96, 80), ("rect_adi_small_odd", 81, 64)):
-        params = dict(z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0, time_initial=0.0, time_final=20.0,
-                      time_step=0.05, softening_distance=float(np.sqrt(2)), width_z=1.0, width_x=1.5,
-                      center_z=0.5, center_x=-0.25, k_z=0.3, pulse=pulse,
-                      mask=dict(inner_radius=12.0, outer_radius=16.0, smoothness=8), store_data_every=50)
-        init = states.TwoDGaussianWavepacket(center_z=0.5, center_x=-0.25, width_z=1.0, width_x=1.5, k_z=0.3)
-        spec = ion.mesh.RectangleSpecification(
-            name, z_points=nz, z_bound=20.0, x_points=nx, x_bound=16.0,
-            internal_potential=ion.potentials.SoftCoulombPotential(softening_distance=np.sqrt(2)),
-            initial_state=init, test_states=[init],
-            electric_potential=ion.potentials.CosSquaredPulse.from_omega_carrier(**pulse),
-            mask=ion.potentials.RadialCosineMask(inner_radius=12.0, outer_radius=16.0, smoothness=8),
-            time_initial=0.0, time_final=20.0, time_step=0.05, store_data_every=50,
-        )
+        spec, params = rect_spec(ion, name, nz, nx)
         _, out = run_and_collect(spec)
         save(name, params, out)
 
@@ -524,11 +533,70 @@ def gen_observables(ion):
     save("cyl_observables_small", params, out)
 
 
+def _energy_datastores(ion):
+    m = ion.mesh
+    return [m.Fields(), m.Norm(), m.InnerProducts(), m.InternalEnergyExpectationValue(),
+            m.TotalEnergyExpectationValue()]
+
+
+def _run_energy(ion, spec, params, name, extra=None):
+    spec.datastores = _energy_datastores(ion)
+    spec.datastore_types = tuple(type(ds) for ds in spec.datastores)
+    sim, out = run_and_collect(spec)
+    out["internal_energy_expectation_value"] = np.asarray(sim.data.internal_energy_expectation_value)
+    out["total_energy_expectation_value"] = np.asarray(sim.data.total_energy_expectation_value)
+    if extra:
+        out.update(extra(sim))
+    save(name, params, out)
+
+
+def _radial_current_final(ion, sim):
+    """DirectionalRadialProbabilityCurrent.store (data.py:467-505) at the final
+    time.  Two lines of the reference keep that datastore from running as
+    written: its init reads self.sim before Datastore.init sets it, and
+    get_radial_probability_current_density_mesh__spatial (meshes.py:1358-1371)
+    calls r_probability_current__spatial() without its mesh argument.  Here
+    the datastore gets sim and spec before init and the operators object a
+    bound call that supplies the mesh; the rest is the reference's code."""
+    ops = sim.mesh.operators
+    meth = type(ops).r_probability_current__spatial
+    ops.r_probability_current__spatial = lambda: meth(ops, sim.mesh)
+    ds = ion.mesh.DirectionalRadialProbabilityCurrent()
+    ds.sim, ds.spec = sim, sim.spec
+    ds.init(sim)
+    sim.data_time_index = len(sim.data_times) - 1
+    ds.store()
+    k = sim.data_time_index
+    return dict(theta_points=np.int64(sim.spec.theta_points),
+                radial_current_pos_z_final=np.asarray(ds.radial_probability_current__pos_z[k]),
+                radial_current_neg_z_final=np.asarray(ds.radial_probability_current__neg_z[k]))
+
+
+def gen_energy(ion):
+    """InternalEnergyExpectationValue and TotalEnergyExpectationValue
+    (data.py:290-340) on line (length and velocity gauge), SH, cylindrical
+    and rectangle runs; the SH run also records the radial probability
+    current of DirectionalRadialProbabilityCurrent at its final time."""
+    line_mask = dict(inner_radius=30.0, outer_radius=40.0, smoothness=8)
+    for gauge, name in (("length", "line_energy_small"), ("velocity", "line_energy_velocity_small")):
+        spec, params = line_spec(ion, name, 512, 40.0, 300, 0.05, _pulse_kwargs(0.1, 0.5, 2, 0.3),
+                                 "SplitInteractionOperator", line_mask, 25, gauge=gauge)
+        _run_energy(ion, spec, params, name)
+    fast_pulse = _pulse_kwargs(0.1, 0.5, 2, 0.0)
+    spec, params = sh_spec(ion, "sh_energy_small", 160, 11, 500, 0.02, fast_pulse, 5.0, 50)
+    _run_energy(ion, spec, params, "sh_energy_small", extra=lambda sim: _radial_current_final(ion, sim))
+    spec, params = cyl_spec(ion, "cyl_energy_small", 120, 15.0, 60, 15.0, 200, 0.05, fast_pulse, 25)
+    _run_energy(ion, spec, params, "cyl_energy_small")
+    spec, params = rect_spec(ion, "rect_energy_small", 96, 80)
+    _run_energy(ion, spec, params, "rect_energy_small")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("IONIZATION_REFERENCE"),
                     help="path of the reference checkout (or set IONIZATION_REFERENCE)")
-    ap.add_argument("--only", default=None, help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice")
+    ap.add_argument("--only", default=None,
+                    help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice,energy")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -540,7 +608,7 @@ def main():
 
     ion = import_reference(args.ref)
     only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect",
-                                                        "num", "slice"}
+                                                        "num", "slice", "energy"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -561,6 +629,8 @@ def main():
         gen_numeric(ion)
     if "slice" in only:
         gen_slice(ion)
+    if "energy" in only:
+        gen_energy(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "ionization_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*\*?\s*\*?\s*(ion_[A-Za-z0-9_]+)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*\*?\s*\*?\s*\b(ion_[A-Za-z0-9_]+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
@@ -69,7 +69,7 @@ def test_struct_offsets_match_the_c_compiler(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     mirrors = {"ion_sh_sim": nat.ShSim, "ion_sh_plan": nat.ShPlan, "ion_line_sim": nat.LineSim,
-               "ion_line_plan": nat.LinePlan, "ion_cyl_mesh": nat.CylMesh}
+               "ion_line_plan": nat.LinePlan, "ion_cyl_mesh": nat.CylMesh, "ion_hop": nat.Hop}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ionization_gb300.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
