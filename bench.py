@@ -761,35 +761,43 @@ def run_per_config(args, peak):
             kernels={"sh_cn_pipelined": t["cn_ms"], "sh_rot_kernel": t["rot_ms"]},
             resident="psi (1.3 MB) is L2-resident: not an HBM-bound run")
         del sim
-    if "cyl_2000x1000" in want:
-        # cfg 3: cylindrical slice 2000 x 1000, ADI, complex128; each pass timed
+    psi_cyl = {}
+    for prec in ("c128", "c64") if "cyl_2000x1000" in want else ():
+        # cfg 3: cylindrical slice 2000 x 1000, ADI, complex128 (and the FP32
+        # sweeps of the complex64 form beside it); each pass timed
         K = 50
-        spec = wl.cyl_hydrogen_2000x1000(steps=K + 10)
+        spec = wl.cyl_hydrogen_2000x1000(steps=K + 10, precision=prec)
         sim = spec.to_sim()
         sim.run(max_steps=5)
         torch.cuda.synchronize()
         m = sim.mesh
         t0 = m._t
         ev = _events(3 * K)
+        fn = "ion_cyl_adi_pass_" + prec
         for k in range(K):
             tn = t0 + k + 1
             ev[3 * k].record(stream)
-            nat.call("ion_cyl_adi_pass_c128", m._cm, m._g.data_ptr(), m._gtmp.data_ptr(), tn, nat.ION_ADI_PASS_STRIDED,
-                     0, stream.cuda_stream)
+            nat.call(fn, m._cm, m._g.data_ptr(), m._gtmp.data_ptr(), tn, nat.ION_ADI_PASS_STRIDED, 0,
+                     stream.cuda_stream)
             ev[3 * k + 1].record(stream)
-            nat.call("ion_cyl_adi_pass_c128", m._cm, m._gtmp.data_ptr(), m._g.data_ptr(), tn, nat.ION_ADI_PASS_CONTIG,
-                     1, stream.cuda_stream)
+            nat.call(fn, m._cm, m._gtmp.data_ptr(), m._g.data_ptr(), tn, nat.ION_ADI_PASS_CONTIG, 1,
+                     stream.cuda_stream)
             ev[3 * k + 2].record(stream)
         torch.cuda.synchronize()
         zp = float(np.mean([ev[3 * k].elapsed_time(ev[3 * k + 1]) for k in range(K)]))
         rp = float(np.mean([ev[3 * k + 1].elapsed_time(ev[3 * k + 2]) for k in range(K)]))
         total = ev[0].elapsed_time(ev[-1])
-        out["cyl_2000x1000_c128"] = dict(
-            name="cyl_2000x1000", workload="cyl_hydrogen_2000x1000: 2000 (z) x 1000 (rho), ADI, complex128",
-            dtype="c128", kind="cyl", points=2_000_000, K=K, total_ms=total,
+        psi_cyl[prec] = m.g
+        out[f"cyl_2000x1000_{prec}"] = dict(
+            name="cyl_2000x1000", workload=f"cyl_hydrogen_2000x1000: 2000 (z) x 1000 (rho), ADI, {prec}",
+            dtype=prec, kind="cyl", points=2_000_000, K=K, total_ms=total,
             kernels={"cyl_zpass_kernel": zp, "cyl_rhopass_kernel": rp},
-            resident="psi 32 MB: within L2 (129 MB) between the passes")
+            resident=f"psi {2_000_000 * (16 if prec == 'c128' else 8) // 10**6} MB: within L2 (129 MB) "
+                     "between the passes")
         del sim, m
+    if len(psi_cyl) == 2:
+        a, b = psi_cyl["c64"], psi_cyl["c128"]
+        out["cyl_2000x1000_c64"]["psi_rel_l2_vs_c128"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
     torch.cuda.synchronize()
     if pool is not None:
         for k, r in cpu_async.items():
@@ -805,6 +813,8 @@ def run_per_config(args, peak):
         res[key] = _per_config_entry(d["name"], d["workload"], d["dtype"], d["kind"], d["points"], d["K"],
                                      d["total_ms"], d["kernels"], peak, cpu.get(d["name"]),
                                      prof.get(key), d.get("resident"))
+        if "psi_rel_l2_vs_c128" in d:
+            res[key]["psi_rel_l2_vs_c128"] = d["psi_rel_l2_vs_c128"]
     return res
 
 

@@ -426,9 +426,12 @@ typedef struct ion_cyl_mesh {
 enum { ION_ADI_STRIDED_FIRST = 0, ION_ADI_CONTIG_FIRST = 1 };
 
 /* Advance psi from time index t0 by n_steps.  g_tmp is a psi-sized buffer.
- * hz_d and zq may be NULL (no such term). */
+ * hz_d and zq may be NULL (no such term).  _c64: psi complex64, the sweeps in
+ * FP32 with coefficients rounded from the FP64 tables (the same tables). */
 int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t t0,
                          int64_t n_steps, void *stream);
+int ion_cyl_adi_run_c64(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t t0,
+                        int64_t n_steps, void *stream);
 
 /* One of the two passes of a step, for callers that interleave their own work
  * between them (and for timing each pass): g_out = (1 + i tau H_a)^-1
@@ -440,7 +443,11 @@ int ion_cyl_adi_run_c128(const ion_cyl_mesh *mesh, void *g, void *g_tmp, int64_t
 enum { ION_ADI_PASS_STRIDED = 0, ION_ADI_PASS_CONTIG = 1 };
 int ion_cyl_adi_pass_c128(const ion_cyl_mesh *mesh, const void *g_in, void *g_out, int64_t t_next,
                           int implicit_axis, int apply_mask, void *stream);
+int ion_cyl_adi_pass_c64(const ion_cyl_mesh *mesh, const void *g_in, void *g_out, int64_t t_next,
+                         int implicit_axis, int apply_mask, void *stream);
+/* Longest line (either axis) of the two passes. */
 int64_t ion_cyl_max_points_c128(void);
+int64_t ion_cyl_max_points_c64(void);
 
 /* ------------------------------------------------------------------------
  * Eigenpairs of batched real symmetric tridiagonal matrices: the numeric

@@ -222,6 +222,9 @@ _SIGS = {
     "ion_psi_split_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp]),
     "ion_cyl_adi_pass_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "ion_cyl_max_points_c128": (c_i64, []),
+    "ion_cyl_adi_run_c64": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
+    "ion_cyl_adi_pass_c64": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
+    "ion_cyl_max_points_c64": (c_i64, []),
     "ion_tridiag_eig_scratch_doubles": (c_i64, [c_i32, c_i32]),
     "ion_tridiag_count_below": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "ion_tridiag_eigvals": (ctypes.c_int, [c_i32, c_i32, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),

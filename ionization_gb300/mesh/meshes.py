@@ -286,9 +286,25 @@ def _two_axis_energy_operators(mesh, n_a, n_b):
     return (n_a, n_b), internal, inter, lambda: float(spec.electric_potential.get_electric_field_amplitude(sim.time))
 
 
+def _adi_precision(mesh, what):
+    """The two-direction ADI kernel pair has complex128 and complex64 forms
+    (FP32 sweeps, FP64 tables and reductions); the stored-residual form
+    (c64x) is the spherical-harmonic split and line kernels' only."""
+    if mesh.precision == core.Precision.C64X:
+        raise exceptions.UnsupportedMesh(
+            f"the {what} device path has complex128 and complex64 forms, no c64x (stored residual) form")
+
+
+def _adi_cap(mesh):
+    """Longest line of the ADI kernel pair at the mesh's precision."""
+    if getattr(mesh.spec, "host_only", False):
+        return 1 << 62
+    return nat.value("ion_cyl_max_points_" + ("c128" if mesh.precision == core.Precision.C128 else "c64"))
+
+
 class _AdiDevice:
     """Device state of a mesh advanced by the two-direction ADI kernel pair
-    (``ion_cyl_adi_run_c128``: a pass implicit along the strided direction,
+    (``ion_cyl_adi_run_c128`` / ``_c64``: a pass implicit along the strided direction,
     then one implicit along the contiguous one), with whole-mesh reductions
     at data times.  Used by the cylindrical slice mesh (z, rho) and by the
     spherical-harmonic mesh under AlternatingDirectionImplicit (l, r)."""
@@ -299,7 +315,8 @@ class _AdiDevice:
         """``arrays``: the ion_cyl_mesh tables by field name (FP64, or None)."""
         f64 = np.float64
         self._d = {k: (dev.to_dev(np.asarray(v).reshape(-1), f64) if v is not None else None) for k, v in arrays.items()}
-        self._g = dev.to_dev(np.asarray(g0, dtype=np.complex128))
+        cdt = np.complex128 if self.precision == core.Precision.C128 else np.complex64
+        self._g = dev.to_dev(np.asarray(g0, dtype=np.complex128).astype(cdt))
         self._gtmp = torch.empty_like(self._g)
         cm = nat.CylMesh()
         cm.n_z, cm.n_rho = int(n_strided), int(n_contig)
@@ -315,8 +332,8 @@ class _AdiDevice:
                                 device=dev.device())
 
     def _adi_evolve_steps(self, n):
-        nat.call("ion_cyl_adi_run_c128", self._cm, dev.ptr(self._g), dev.ptr(self._gtmp), self._t, int(n),
-                 dev.stream_ptr())
+        fn = "ion_cyl_adi_run_c128" if self._g.dtype == torch.complex128 else "ion_cyl_adi_run_c64"
+        nat.call(fn, self._cm, dev.ptr(self._g), dev.ptr(self._gtmp), self._t, int(n), dev.stream_ptr())
         self._t += int(n)
 
     def _adi_reduce_current(self):
@@ -645,12 +662,11 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         spec, sim = self.spec, self.sim
         if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
             raise exceptions.UnsupportedMesh("the velocity gauge's h2 is not tridiagonal: no ADI device path")
-        if self.precision != core.Precision.C128:
-            raise exceptions.UnsupportedMesh("the spherical-harmonic ADI device path is complex128")
+        _adi_precision(self, "spherical-harmonic ADI")
         self._adi = True
         self.fused_data = False
         nr, L = spec.r_points, spec.l_bound
-        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        cap = _adi_cap(self)
         if nr > cap or L > cap:
             raise exceptions.UnsupportedMesh(f"mesh {L} x {nr} exceeds the ADI device limit {cap} per line")
         tb = self.operators.device_tables(self)
@@ -869,8 +885,12 @@ class SphericalSliceMesh(_AdiDevice, QuantumMesh):
             raise exceptions.UnsupportedMesh(
                 f"{type(spec.evolution_method).__name__} has no device path on SphericalSliceMesh")
         if self.precision != core.Precision.C128:
+            # it evolves g / D, D the similarity scaling that makes the theta
+            # operator symmetric and that spans orders of magnitude across
+            # theta; FP32 sweeps of the scaled state lose ~1e-5 in the
+            # populations within a few hundred steps
             raise exceptions.UnsupportedMesh("the spherical-slice device path is complex128")
-        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        cap = _adi_cap(self)
         if spec.r_points > cap or spec.theta_points > cap:
             raise exceptions.UnsupportedMesh(f"mesh {spec.r_points} x {spec.theta_points} exceeds {cap} points per line")
         tb = self.operators.device_tables(self)
@@ -903,7 +923,7 @@ class SphericalSliceMesh(_AdiDevice, QuantumMesh):
     @g.setter
     def g(self, value):
         v = np.asarray(value, dtype=np.complex128).reshape(self.mesh_shape) / self._D
-        self._g.copy_(torch.from_numpy(np.ascontiguousarray(v)).to(self._g.device))
+        self._g.copy_(torch.from_numpy(np.ascontiguousarray(v)).to(self._g.device, self._g.dtype))
 
     def _weighted_norms(self, weights):
         return super()._weighted_norms([np.asarray(w, dtype=np.float64) * self._D ** 2 for w in weights])
@@ -927,9 +947,12 @@ class SphericalSliceMesh(_AdiDevice, QuantumMesh):
         nbytes = nat.value("ion_weighted_norms_scratch_bytes", n, 1)
         if not hasattr(self, "_d_wn_scratch") or self._d_wn_scratch.numel() * 8 < nbytes:
             self._d_wn_scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=dev.device())
-        nat.call("ion_weighted_norms_c128", n, dev.ptr(self._g), 1, dev.ptr(self._d_w2),
-                 float(self.inner_product_multiplier), dev.ptr(self._d_norm[slot:slot + 1]),
-                 dev.ptr(self._d_wn_scratch), int(nbytes), dev.stream_ptr())
+        args = (1, dev.ptr(self._d_w2), float(self.inner_product_multiplier), dev.ptr(self._d_norm[slot:slot + 1]),
+                dev.ptr(self._d_wn_scratch), int(nbytes), dev.stream_ptr())
+        if self._g.dtype == torch.complex128:
+            nat.call("ion_weighted_norms_c128", n, dev.ptr(self._g), *args)
+        else:
+            nat.call("ion_weighted_norms_c64", n, dev.ptr(self._g), None, *args)
 
     def _pull_data(self):
         return self._adi_pull_data()
@@ -994,9 +1017,8 @@ class RectangleMesh(_AdiDevice, QuantumMesh):
             raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on RectangleMesh")
         if not isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
             raise exceptions.UnsupportedMesh(f"{type(spec.evolution_method).__name__} has no device path on RectangleMesh")
-        if self.precision != core.Precision.C128:
-            raise exceptions.UnsupportedMesh("the rectangle device path is complex128")
-        cap = 1 << 62 if getattr(spec, "host_only", False) else nat.value("ion_cyl_max_points_c128")
+        _adi_precision(self, "rectangle")
+        cap = _adi_cap(self)
         if spec.z_points > cap or spec.x_points > cap:
             raise exceptions.UnsupportedMesh(f"mesh {spec.z_points} x {spec.x_points} exceeds {cap} points per line")
         tb = self.operators.device_tables(self)
@@ -1096,8 +1118,7 @@ class CylindricalSliceMesh(_AdiDevice, QuantumMesh):
             raise exceptions.UnsupportedMesh(
                 f"{type(spec.evolution_method).__name__} has no device path on CylindricalSliceMesh"
             )
-        if self.precision != core.Precision.C128:
-            raise exceptions.UnsupportedMesh("the cylindrical device path is complex128")
+        _adi_precision(self, "cylindrical")
         tb = self.operators.device_tables(self)
         times = sim.times
         self._tau_host = np.zeros(len(times))

@@ -127,22 +127,25 @@ def test_mesh_c128_matches_reference(cuda, kind, name):
     _check_against_golden(sim, z)
 
 
-COMPLEX64_CASES = [c for c in CASES if c[0] not in ("cyl", "rect", "slice") and not c[1].startswith("sh_adi")]
+ADI_MESH_CASES = [c for c in CASES if c[0] in ("cyl", "rect", "slice") or c[1].startswith("sh_adi")]
+COMPLEX64_CASES = [c for c in CASES if c not in ADI_MESH_CASES]
 
 
-@pytest.mark.parametrize("kind,name", COMPLEX64_CASES)
+@pytest.mark.parametrize("kind,name", [c for c in CASES if c[0] != "slice"])
 def test_mesh_c64_population_error(cuda, kind, name):
-    """complex64 state with FP64 field, coefficients and reductions: the
-    final population stays within 1e-5 of the reference on these short runs
-    (the measured errors are reported in the design notes)."""
+    """complex64 state with FP64 field, coefficients and reductions (the ADI
+    meshes: FP32 sweeps of the two-direction kernel pair): the final
+    population stays within 1e-5 of the reference on these short runs (the
+    measured errors are reported in the design notes)."""
     params, z = load_golden(name)
     sim = product_spec(kind, params, precision="c64").to_sim()
     sim.run()
     p64 = sim.data.initial_state_overlap[-1]
     p128 = z["initial_state_overlap"][-1]
-    print(f"{name}: |P_c64 - P_ref| = {abs(p64 - p128):.2e}")
+    err = rel_l2(sim.mesh.g, z["g_final"])
+    print(f"{name}: |P_c64 - P_ref| = {abs(p64 - p128):.2e}, psi rel L2 = {err:.2e}")
     assert abs(p64 - p128) < 1e-5
-    assert rel_l2(sim.mesh.g, z["g_final"]) < 1e-4
+    assert err < 1e-4
 
 
 @pytest.mark.parametrize("kind,name", [c for c in COMPLEX64_CASES if not c[1].startswith("line_velocity")])

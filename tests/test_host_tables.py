@@ -113,3 +113,24 @@ def test_residual_packing_rounds_like_bf16():
     assert np.array_equal(u.real.astype(np.float32), want_re)
     assert np.array_equal(u.imag.astype(np.float32), want_im)
     assert u[16] == 1 + 1j * (1 + 2 ** -6)
+
+
+@pytest.mark.parametrize("kind,name", [("cyl", "cyl_adi_small"), ("rect", "rect_adi_small"),
+                                       ("sh", "sh_adi_small_evenL")])
+def test_adi_meshes_have_no_c64x_form(kind, name):
+    """The two-direction ADI kernel pair has complex128 and complex64 forms;
+    asking for the stored-residual form is refused before any device work."""
+    from ionization_gb300 import exceptions
+
+    params, _ = load_golden(name)
+    with pytest.raises(exceptions.UnsupportedMesh, match="c64x"):
+        product_spec(kind, params, precision="c64x", host_only=True).to_sim()
+
+
+@pytest.mark.parametrize("precision", ["c64", "c64x"])
+def test_spherical_slice_is_complex128_only(precision):
+    from ionization_gb300 import exceptions
+
+    params, _ = load_golden("slice_adi_small")
+    with pytest.raises(exceptions.UnsupportedMesh, match="complex128"):
+        product_spec("slice", params, precision=precision, host_only=True).to_sim()
