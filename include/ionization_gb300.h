@@ -215,6 +215,20 @@ typedef struct ion_sh_sim {
     const double *kinv;
     const double *cent;
     double corr0;
+    /* _c128 with ION_SH_COUPLED only, or NULL: the radial Hamiltonian of
+     * kinetic_energy_from_hamiltonian (mesh_operators.py:863-887) is one
+     * tridiagonal over the flattened (l, r) mesh, so it also couples the last
+     * r of each l with the first r of the next (hcross).  Each line is solved
+     * as before; a fix-up then adds that coupling through the line's spikes
+     * spike_s = A_l^-1 e_first and spike_t = A_l^-1 e_last (complex128
+     * [n_l*n_r], A_l = 1 + i tau H_l at the uniform time step), solving the
+     * 2 n_l line-end values together.  edge: complex128 [4*n_l] scratch
+     * (psi's line ends from before the solve, then the coupling
+     * coefficients). */
+    const void *spike_s;
+    const void *spike_t;
+    void *edge;
+    double hcross;
 } ion_sh_sim;
 
 enum { ION_GAUGE_LENGTH = 0, ION_GAUGE_VELOCITY = 1 };
@@ -230,6 +244,10 @@ enum { ION_SH_REFINE = 1 };
 /* ion_sh_plan.flags: some simulations are in the velocity gauge (their
  * rotation pass runs in its own kernel), or all of them are. */
 enum { ION_SH_VELOCITY = 2, ION_SH_ONLY_VELOCITY = 4 };
+/* ion_sh_plan.flags: some simulations carry spikes (ion_sh_sim.spike_s): the
+ * radial phase saves their line ends before the solve and applies the
+ * line-to-line coupling after it (complex128). */
+enum { ION_SH_COUPLED = 8 };
 
 typedef struct ion_sh_plan {
     ion_sh_sim *sims;         /* device array [n_sims] */
@@ -540,18 +558,20 @@ int ion_sh_observables_c64(const void *g, const void *g_lo, int32_t n_r, int32_t
  * term).  A real coupling c puts c at (k, k') and (k', k); with
  * ION_HOP_IMAG_B / ION_HOP_IMAG_A it is imaginary: i c at (k, k'), -i c at
  * (k', k), k' the neighbour at j+1 or i+1 (LineVelocityGaugeOperators'
- * interaction, mesh_operators.py:358-369).
+ * interaction, mesh_operators.py:358-369).  With ION_HOP_WRAP_B the b
+ * coupling of (i, n_b-1) joins it to (i+1, 0): one coupling chain over the
+ * flattened mesh (kinetic_energy_from_hamiltonian, mesh_operators.py:863-887).
  *
  * ion_expectation_*: out[q] = weight * <g|H_q|g> for 1 <= n_ops <= ION_MAX_HOPS
  *   operators (ops: a host array), one pass over g; a two-stage FP64 sum with a
  *   compensated second stage; scratch from ion_expectation_scratch_bytes.
  * ------------------------------------------------------------------------ */
-enum { ION_HOP_IMAG_B = 1, ION_HOP_IMAG_A = 2, ION_MAX_HOPS = 4 };
+enum { ION_HOP_IMAG_B = 1, ION_HOP_IMAG_A = 2, ION_HOP_WRAP_B = 4, ION_MAX_HOPS = 4 };
 typedef struct ion_hop {
     const double *diag;  /* [n_a*n_b] or NULL */
     const double *off_b; /* [n_a*n_b]: coupling of (i, j) and (i, j+1) (j = n_b-1 unused), or NULL */
     const double *off_a; /* [n_a*n_b]: coupling of (i, j) and (i+1, j) (i = n_a-1 unused), or NULL */
-    int32_t flags;       /* ION_HOP_IMAG_B | ION_HOP_IMAG_A */
+    int32_t flags;       /* ION_HOP_IMAG_B | ION_HOP_IMAG_A | ION_HOP_WRAP_B */
     int32_t pad_;
 } ion_hop;
 int64_t ion_expectation_scratch_bytes(int32_t n_a, int32_t n_b, int32_t n_ops);

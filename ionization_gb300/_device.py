@@ -142,6 +142,9 @@ class ShTables:
     # the l rows of g0 that are not zero (None: find them); only those rows
     # are uploaded, the rest are zeroed on the device
     g0_rows: Optional[np.ndarray] = None
+    # kinetic_energy_from_hamiltonian: the coupling between the last r of
+    # each l and the first r of the next (None: the lines are independent)
+    hcross: Optional[float] = None
 
 
 SH_ROT_ROWS = 32
@@ -453,8 +456,34 @@ class ShDeviceSim:
             setattr(self, k, v)
         self.n_states = n_states
         self.g_rows = [int(l) for l in sh_nonzero_rows(tab)]
+        self.d_spike_s = self.d_spike_t = self.d_edge = None
+        if tab.hcross is not None:
+            self._build_spikes()
         if self.g_in is not None and not getattr(self, "_deferred", False):
             _sh_prepare([self])
+
+    def _build_spikes(self):
+        """The coupled-line spikes s_l = A_l^-1 e_first and t_l = A_l^-1 e_last
+        of every line (A_l = 1 + i tau H_l at the run's uniform tau), solved on
+        the device by the batched Thomas solve, and the line-end scratch."""
+        from . import cy
+
+        if self.precision != Precision.C128:
+            raise ValueError("coupled lines have a complex128 form only")
+        L, n = self.n_l, self.n_r
+        tau = float(self.tab.tau[min(self.t + 1, len(self.tab.tau) - 1)])
+        diag = 1 + 1j * tau * np.asarray(self.tab.hd, dtype=np.float64)
+        off = np.zeros(L * n - 1, dtype=np.complex128)
+        for l in range(L):
+            off[l * n: l * n + n - 1] = 1j * tau * np.asarray(self.tab.hoff, dtype=np.float64)
+        d_off, d_diag = to_dev(off), to_dev(diag)
+        e_first = np.zeros(L * n, dtype=np.complex128)
+        e_first[::n] = 1.0
+        e_last = np.zeros(L * n, dtype=np.complex128)
+        e_last[n - 1::n] = 1.0
+        self.d_spike_s = cy.tdma_batched_device(L, n, d_off, d_diag, d_off, to_dev(e_first))
+        self.d_spike_t = cy.tdma_batched_device(L, n, d_off, d_diag, d_off, to_dev(e_last))
+        self.d_edge = torch.zeros(4 * L, dtype=torch.complex128, device=device())
 
     @classmethod
     def bulk(cls, tables: List[ShTables], precision) -> List["ShDeviceSim"]:
@@ -534,6 +563,8 @@ class ShDeviceSim:
         d.h2r, d.h2r32 = ptr(self.d_h2r), ptr(self.d_h2r32)
         d.row_lo = ptr(self.d_row_lo)
         d.kinv, d.cent, d.corr0 = ptr(self.d_kinv64), ptr(self.d_cent64), float(self.tab.corr0)
+        d.spike_s, d.spike_t, d.edge = ptr(self.d_spike_s), ptr(self.d_spike_t), ptr(self.d_edge)
+        d.hcross = float(self.tab.hcross or 0.0)
         return d
 
     def data(self):
@@ -697,6 +728,8 @@ class ShBatch:
         plan.max_n_l = max([s.n_l for s in sims] + [1])
         plan.max_n_r = max([s.n_r for s in sims] + [2])
         plan.flags = nat.ION_SH_REFINE if any(s.g_lo is not None for s in sims) else 0
+        if any(getattr(s, "d_spike_s", None) is not None for s in sims):
+            plan.flags |= nat.ION_SH_COUPLED
         n_vel = sum(1 for s in sims if s.gauge == nat.ION_GAUGE_VELOCITY)
         if n_vel:
             plan.flags |= nat.ION_SH_VELOCITY | (nat.ION_SH_ONLY_VELOCITY if n_vel == len(sims) else 0)

@@ -26,6 +26,7 @@ ION_LINE_FFT = 2
 ION_SH_REFINE = 1
 ION_SH_VELOCITY = 2
 ION_SH_ONLY_VELOCITY = 4
+ION_SH_COUPLED = 8
 ION_GAUGE_LENGTH = 0
 ION_ADI_STRIDED_FIRST = 0
 ION_ADI_CONTIG_FIRST = 1
@@ -36,6 +37,7 @@ ION_LINE_RESIDUAL = 1
 ION_LINE_HAS_FFT = 2
 ION_HOP_IMAG_B = 1
 ION_HOP_IMAG_A = 2
+ION_HOP_WRAP_B = 4
 ION_MAX_HOPS = 4
 
 
@@ -87,6 +89,10 @@ class ShSim(ctypes.Structure):
         ("kinv", c_vp),
         ("cent", c_vp),
         ("corr0", c_f64),
+        ("spike_s", c_vp),
+        ("spike_t", c_vp),
+        ("edge", c_vp),
+        ("hcross", c_f64),
     ]
 
 

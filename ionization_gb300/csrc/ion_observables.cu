@@ -192,15 +192,17 @@ __global__ void __launch_bounds__(OBS_THREADS) expect_stage1(const Cx<R>* g, con
         const int j = int(k - i * nb);
         const Cx<double> x = value_at(g, glo, k);
         const double p = x.re * x.re + x.im * x.im;
-        const bool hb = j + 1 < nb, ha = i + 1 < na;
-        const Cx<double> yb = hb ? value_at(g, glo, k + 1) : Cx<double>{0.0, 0.0};
+        const bool ha = i + 1 < na;
+        const bool hb = j + 1 < nb, wb = !hb && ha;  // wb: the wrap from (i, n_b-1) to (i+1, 0)
+        const Cx<double> yb = (hb || wb) ? value_at(g, glo, k + 1) : Cx<double>{0.0, 0.0};
         const Cx<double> ya = ha ? value_at(g, glo, k + nb) : Cx<double>{0.0, 0.0};
 #pragma unroll
         for (int q = 0; q < ION_MAX_HOPS; ++q) {
             if (q >= ops.n) break;
             const ion_hop& o = ops.op[q];
             double v = o.diag ? o.diag[k] * p : 0.0;
-            if (hb && o.off_b) v += coupling_term(o.off_b[k], x, yb, (o.flags & ION_HOP_IMAG_B) != 0);
+            if ((hb || (wb && (o.flags & ION_HOP_WRAP_B))) && o.off_b)
+                v += coupling_term(o.off_b[k], x, yb, (o.flags & ION_HOP_IMAG_B) != 0);
             if (ha && o.off_a) v += coupling_term(o.off_a[k], x, ya, (o.flags & ION_HOP_IMAG_A) != 0);
             acc[q] += v;
         }

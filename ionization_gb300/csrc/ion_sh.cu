@@ -1193,6 +1193,122 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
 
 
 // ---------------------------------------------------------------------------
+// Coupled lines (kinetic_energy_from_hamiltonian, complex128).  The radial
+// operator joins the last r of line l to the first r of line l+1 with H
+// coupling p (hcross).  With A = A_bd + i C and B = B_bd + C (C those
+// couplings, tau included), the step x = A^-1 (1 - i B) psi is
+//     x = u - i A_bd^-1 C (psi + x),   u = A_bd^-1 (1 - i B_bd) psi,
+// u being what the per-line solve leaves in g.  C (psi + x) lives on the line
+// ends only, so with s_l = A_l^-1 e_first, t_l = A_l^-1 e_last and c = -i tau p
+//     x_l = u_l + c (beta_l s_l + alpha_l t_l),
+//     beta_l = psi_{l-1,last} + x_{l-1,last},  alpha_l = psi_{l+1,first} + x_{l+1,first},
+// and the 2 n_l line-end values (a_l, b_l) = (x_{l,first}, x_{l,last}) solve a
+// block-tridiagonal system of 2x2 blocks (block Thomas, one thread).
+// ---------------------------------------------------------------------------
+__global__ void sh_edge_save_kernel(ion_sh_plan plan) {
+    const ion_sh_sim& S = plan.sims[blockIdx.x];
+    if (!S.spike_s || !S.edge || S.t >= S.t_final) return;
+    const int nr = S.n_r;
+    const Cx<double>* g = static_cast<const Cx<double>*>(S.g);
+    Cx<double>* e = static_cast<Cx<double>*>(S.edge);
+    for (int l = threadIdx.x; l < S.n_l; l += blockDim.x) {
+        e[2 * l] = ld(g + int64_t(l) * nr);
+        e[2 * l + 1] = ld(g + int64_t(l) * nr + nr - 1);
+    }
+}
+
+struct Mat2 {
+    Cx<double> a, b, c, d;  // [[a, b], [c, d]]
+};
+__device__ __forceinline__ Mat2 inv2(const Mat2& m) {
+    const Cx<double> r = crecip(m.a * m.d - m.b * m.c);
+    return Mat2{m.d * r, -(m.b * r), -(m.c * r), m.a * r};
+}
+
+// one CTA per simulation, one thread: the line ends (shared memory: n_l x
+// (G 2x2, h 2) complex), then c beta_l and c alpha_l into edge[2 n_l ..]
+__global__ void sh_coupled_solve_kernel(ion_sh_plan plan) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const ion_sh_sim& S = plan.sims[blockIdx.x];
+    if (!S.spike_s || !S.spike_t || !S.edge || S.t >= S.t_final || S.n_l < 2) return;
+    const int L = S.n_l, nr = S.n_r;
+    Cx<double>* G = reinterpret_cast<Cx<double>*>(smem_raw);  // [L][4]
+    Cx<double>* H = G + 4 * L;                                 // [L][2]
+    Cx<double>* e = static_cast<Cx<double>*>(S.edge);
+    Cx<double>* cf = e + 2 * L;                                 // [L][2]: c beta_l, c alpha_l
+    const Cx<double>* g = static_cast<const Cx<double>*>(S.g);
+    const Cx<double>* sp = static_cast<const Cx<double>*>(S.spike_s);
+    const Cx<double>* tp = static_cast<const Cx<double>*>(S.spike_t);
+    const Cx<double> c = {0.0, -S.tau[S.t + 1] * S.hcross};
+    const Cx<double> zero = {0.0, 0.0}, one = {1.0, 0.0};
+    if (threadIdx.x == 0) {
+        // row l: z_l + P_l z_{l-1} + Q_l z_{l+1} = r_l with z = (a, b),
+        // P_l = -c [[0, s0], [0, sN]], Q_l = -c [[t0, 0], [tN, 0]]
+        Mat2 Gp = {zero, zero, zero, zero};
+        Cx<double> hp0 = zero, hp1 = zero;
+        for (int l = 0; l < L; ++l) {
+            const int64_t f = int64_t(l) * nr, k = f + nr - 1;
+            const Cx<double> s0 = ld(sp + f), sN = ld(sp + k), t0 = ld(tp + f), tN = ld(tp + k);
+            const Cx<double> pb = l > 0 ? e[2 * (l - 1) + 1] : zero;      // psi_{l-1,last}
+            const Cx<double> pa = l + 1 < L ? e[2 * (l + 1)] : zero;      // psi_{l+1,first}
+            Cx<double> r0 = ld(g + f) + c * (s0 * pb + t0 * pa);
+            Cx<double> r1 = ld(g + k) + c * (sN * pb + tN * pa);
+            // D = I - P_l G_{l-1}; r -= P_l h_{l-1}: P_l picks the b row of G and h
+            Mat2 D = {one, zero, zero, one};
+            if (l > 0) {
+                const Cx<double> ps0 = -(c * s0), psN = -(c * sN);
+                D.a = D.a - ps0 * Gp.c;
+                D.b = D.b - ps0 * Gp.d;
+                D.c = D.c - psN * Gp.c;
+                D.d = D.d - psN * Gp.d;
+                r0 = r0 - ps0 * hp1;
+                r1 = r1 - psN * hp1;
+            }
+            const Mat2 Di = inv2(D);
+            // G_l = D^-1 Q_l (Q_l has only a first column), h_l = D^-1 r
+            const Cx<double> q0 = l + 1 < L ? -(c * t0) : zero, q1 = l + 1 < L ? -(c * tN) : zero;
+            Gp = Mat2{Di.a * q0 + Di.b * q1, zero, Di.c * q0 + Di.d * q1, zero};
+            hp0 = Di.a * r0 + Di.b * r1;
+            hp1 = Di.c * r0 + Di.d * r1;
+            G[4 * l] = Gp.a;
+            G[4 * l + 2] = Gp.c;
+            H[2 * l] = hp0;
+            H[2 * l + 1] = hp1;
+        }
+        // back substitution: z_l = h_l - G_l z_{l+1} (G_l has only a first column)
+        Cx<double> an = zero;  // a_{l+1}
+        for (int l = L - 1; l >= 0; --l) {
+            const Cx<double> a = H[2 * l] - G[4 * l] * an, b = H[2 * l + 1] - G[4 * l + 2] * an;
+            H[2 * l] = a;
+            H[2 * l + 1] = b;
+            an = a;
+        }
+        for (int l = 0; l < L; ++l) {
+            const Cx<double> beta = l > 0 ? e[2 * (l - 1) + 1] + H[2 * (l - 1) + 1] : zero;
+            const Cx<double> alpha = l + 1 < L ? e[2 * (l + 1)] + H[2 * (l + 1)] : zero;
+            cf[2 * l] = c * beta;
+            cf[2 * l + 1] = c * alpha;
+        }
+    }
+}
+
+// grid (n_sims, chunks): x = u + c beta_l s_l + c alpha_l t_l on every point
+__global__ void __launch_bounds__(256) sh_coupled_apply_kernel(ion_sh_plan plan) {
+    const ion_sh_sim& S = plan.sims[blockIdx.x];
+    if (!S.spike_s || !S.spike_t || !S.edge || S.t >= S.t_final || S.n_l < 2) return;
+    const int L = S.n_l, nr = S.n_r;
+    Cx<double>* g = static_cast<Cx<double>*>(S.g);
+    const Cx<double>* sp = static_cast<const Cx<double>*>(S.spike_s);
+    const Cx<double>* tp = static_cast<const Cx<double>*>(S.spike_t);
+    const Cx<double>* cf = static_cast<const Cx<double>*>(S.edge) + 2 * L;
+    const int64_t n = int64_t(L) * nr;
+    for (int64_t k = int64_t(blockIdx.y) * blockDim.x + threadIdx.x; k < n; k += int64_t(gridDim.y) * blockDim.x) {
+        const int l = int(k / nr);
+        st(g + k, ld(g + k) + cf[2 * l] * ld(sp + k) + cf[2 * l + 1] * ld(tp + k));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 // rows per thread of the radial solve: the compile-time register capacity
@@ -1343,6 +1459,32 @@ static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s) {
     return ION_OK;
 }
 
+// the radial phase: the line solves, and for plans with coupled lines
+// (complex128) the line ends saved before and the coupling applied after
+template <typename R>
+static int sh_radial_phase(const ion_sh_plan* p, cudaStream_t s) {
+    const bool coupled = (p->flags & ION_SH_COUPLED) && sizeof(R) == 8 && p->n_sims > 0;
+    if (coupled) {
+        sh_edge_save_kernel<<<p->n_sims, 128, 0, s>>>(*p);
+        if (int e = check_launch("sh_edge_save_kernel")) return e;
+    }
+    if (int e = sh_launch_cn<R>(p, s)) return e;
+    if (coupled) {
+        const size_t smem = size_t(p->max_n_l) * 6 * sizeof(Cx<double>);
+        if (smem > 200 * 1024) {
+            set_error("ion_sh: l_bound %d too large for the coupled-line fix-up", p->max_n_l);
+            return ION_ERR_UNSUPPORTED;
+        }
+        if (int e = ensure_smem_limit((const void*)sh_coupled_solve_kernel, 200 * 1024, "sh_coupled_solve_kernel"))
+            return e;
+        sh_coupled_solve_kernel<<<p->n_sims, 32, smem, s>>>(*p);
+        if (int e = check_launch("sh_coupled_solve_kernel")) return e;
+        sh_coupled_apply_kernel<<<dim3(p->n_sims, 32), 256, 0, s>>>(*p);
+        if (int e = check_launch("sh_coupled_apply_kernel")) return e;
+    }
+    return ION_OK;
+}
+
 template <typename R>
 static int sh_run(const ion_sh_plan* p, int64_t n_steps, void* stream) {
     if (int e = sh_validate<R>(p)) return e;
@@ -1354,7 +1496,7 @@ static int sh_run(const ion_sh_plan* p, int64_t n_steps, void* stream) {
     cudaStream_t s = as_stream(stream);
     if (int e = sh_launch_rot<R>(p, ROT_PRE_ONLY, s)) return e;
     for (int64_t k = 0; k < n_steps; ++k) {
-        if (int e = sh_launch_cn<R>(p, s)) return e;
+        if (int e = sh_radial_phase<R>(p, s)) return e;
         if (int e = sh_launch_rot<R>(p, k + 1 < n_steps ? ROT_STEP_PRE : ROT_STEP, s)) return e;
         sh_advance_kernel<<<p->n_sims, 32, 0, s>>>(*p, ADV_STEP);
         if (int e = check_launch("sh_advance_kernel")) return e;
@@ -1370,7 +1512,7 @@ static int sh_phase(const ion_sh_plan* p, int phase, void* stream) {
     cudaStream_t s = as_stream(stream);
     switch (phase) {
         case ION_SH_PHASE_PRE: return sh_launch_rot<R>(p, ROT_PRE_ONLY, s);
-        case ION_SH_PHASE_CN: return sh_launch_cn<R>(p, s);
+        case ION_SH_PHASE_CN: return sh_radial_phase<R>(p, s);
         case ION_SH_PHASE_ROT: return sh_launch_rot<R>(p, ROT_STEP, s);
         case ION_SH_PHASE_ROT_PRE: return sh_launch_rot<R>(p, ROT_STEP_PRE, s);
         case ION_SH_PHASE_ADVANCE:

@@ -221,8 +221,9 @@ class LineVelocityGaugeOperators(LineLengthGaugeOperators):
 
 
 class SphericalHarmonicLengthGaugeOperators(MeshOperators):
-    """mesh_operators.py:815-1080.  Only the Lagrangian kinetic energy has a
-    device path (the reference default)."""
+    """mesh_operators.py:815-1080.  Both kinetic-energy derivations have a
+    device path: the Lagrangian one (the reference default) in every
+    precision, the Hamiltonian one in complex128 with the split operator."""
 
     gauge = core.Gauge.LENGTH
 
@@ -256,11 +257,15 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
 
         Returns a dict with hd [L*Nr] (C order), hoff [Nr-1], rq [Nr], cl [L]
         and the FP64 pieces of the diagonal used by the complex64 path:
-        kinv [Nr] (= beta(j) (-2p) + V(r_j)), cent [Nr] and corr0."""
-        if self.kinetic_energy_derivation != KineticEnergyDerivation.LAGRANGIAN:
-            from ..exceptions import UnsupportedMesh
-
-            raise UnsupportedMesh("only the Lagrangian kinetic energy has a device path")
+        kinv [Nr] (= beta(j) (-2p) + V(r_j)), cent [Nr] and corr0; ``cross``
+        is None (the lines are independent).  With
+        kinetic_energy_derivation "hamiltonian" the radial Hamiltonian is
+        kinetic_energy_from_hamiltonian's (mesh_operators.py:863-887): -2p on
+        the diagonal, p between every pair of consecutive points of the
+        flattened (l, r) mesh, so also between the last r of each l and the
+        first r of the next (``cross`` = p); no l = 0 correction."""
+        if self.kinetic_energy_derivation == KineticEnergyDerivation.HAMILTONIAN:
+            return self._device_tables_hamiltonian(mesh)
         spec = mesh.spec
         nr, L = spec.r_points, spec.l_bound
         M = nr * L
@@ -291,12 +296,32 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
         cent = ((u.hbar ** 2) / (2 * mu)) / (mesh.r ** 2)
         corr0 = (beta_r[0] + corr) * (-2 * p) - beta_r[0] * (-2 * p)
         return dict(hd=hd, hoff=hoff, rq=np.asarray(rq, dtype=np.float64), cl=cl, kinv=kinv, cent=cent,
-                    corr0=float(corr0))
+                    corr0=float(corr0), cross=None)
+
+    def _device_tables_hamiltonian(self, mesh):
+        spec = mesh.spec
+        nr, L = spec.r_points, spec.l_bound
+        mu = u.electron_mass_reduced
+        p = -(u.hbar ** 2) / (2 * mu * (mesh.delta_r ** 2))
+        diag = p * (-2) * np.ones(nr * L, dtype=np.complex128)
+        eff = ((u.hbar ** 2) / (2 * mu)) * mesh.l_mesh * (mesh.l_mesh + 1) / (mesh.r_mesh ** 2)
+        diag += eff.flatten("C")
+        V = spec.internal_potential(r=mesh.r_mesh, test_charge=spec.test_charge)
+        hd = (diag + 1.0 * np.asarray(V).flatten("C")).real.copy()
+        V_r = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge), dtype=np.float64)
+        return dict(hd=hd, hoff=np.full(nr - 1, p), rq=np.asarray(-spec.test_charge * mesh.r, dtype=np.float64),
+                    cl=self.c_l(np.arange(L)), kinv=-2 * p + V_r, cent=((u.hbar ** 2) / (2 * mu)) / (mesh.r ** 2),
+                    corr0=0.0, cross=float(p))
 
     def single_l_hamiltonian(self, mesh, l):
         """(diagonal, off-diagonal) of internal_hamiltonian_for_single_l
         (mesh_operators.py:942-986): the Lagrangian radial kinetic energy of
-        one l, its centrifugal term, and V(r), in the reference's order."""
+        one l, its centrifugal term, and V(r), in the reference's order.  The
+        reference has no single-l form of the Hamiltonian-derived kinetic
+        energy (kinetic_energy_for_single_l_from_hamiltonian raises
+        NotImplementedError, :937-940), and neither does this."""
+        if self.kinetic_energy_derivation == KineticEnergyDerivation.HAMILTONIAN:
+            raise NotImplementedError
         spec = mesh.spec
         nr = spec.r_points
         mu = u.electron_mass_reduced
@@ -318,6 +343,8 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
         off = np.zeros(nr * L - 1)
         for l in range(L):
             off[l * nr: l * nr + nr - 1] = t["hoff"]
+        if t["cross"] is not None:
+            off[nr - 1::nr] = t["cross"]
         m = sparse.diags((off.astype(np.complex128), t["hd"].astype(np.complex128), off.astype(np.complex128)),
                          offsets=(-1, 0, 1))
         return SumOfOperators(DotOperator(m, wrapping_direction="r"))

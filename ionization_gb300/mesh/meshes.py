@@ -601,6 +601,13 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         self._adi = False
         if not isinstance(self.operators, mo.SphericalHarmonicLengthGaugeOperators):
             raise exceptions.UnsupportedMesh(f"{type(self.operators).__name__} has no device path on SphericalHarmonicMesh")
+        derivation = getattr(self.operators, "kinetic_energy_derivation", None)
+        hamiltonian = derivation == mo.KineticEnergyDerivation.HAMILTONIAN
+        if hamiltonian and (self.precision != core.Precision.C128 or
+                            not isinstance(spec.evolution_method, em.SplitInteractionOperator)):
+            raise exceptions.UnsupportedMesh(
+                "kinetic_energy_derivation='hamiltonian' has a device path in complex128 with "
+                "SplitInteractionOperator only")
         if isinstance(spec.evolution_method, em.AlternatingDirectionImplicit):
             return self._init_device_adi()
         if not isinstance(spec.evolution_method, em.SplitInteractionOperator):
@@ -617,6 +624,9 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         times = sim.times
         self._tau_host = np.zeros(len(times))
         self._tau_host[1:] = (times[1:] - times[:-1]) / (2 * u.hbar)
+        if hamiltonian and len(times) > 2 and np.ptp(self._tau_host[1:]) > 1e-12 * abs(self._tau_host[1]):
+            # the coupled-line spikes are built for one tau
+            raise exceptions.UnsupportedMesh("kinetic_energy_derivation='hamiltonian' needs a uniform time step")
         efield = np.zeros(len(times))
         gauge, h2r, rq = nat.ION_GAUGE_LENGTH, None, tb["rq"]
         if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
@@ -644,7 +654,7 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
             state_l=sl, state_g=np.array(sg, dtype=np.complex128).reshape(len(sl), spec.r_points),
             weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
             g0_rows=np.flatnonzero(np.any(np.asarray(g0).reshape(spec.l_bound, spec.r_points) != 0, axis=1)),
-            store_every=spec.store_data_every, gauge=gauge, h2r=h2r,
+            store_every=spec.store_data_every, gauge=gauge, h2r=h2r, hcross=tb.get("cross"),
         )
         if getattr(spec, "host_only", False):
             return
@@ -740,6 +750,8 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         tb = self.operators.device_tables(self)
         L, nr = self.spec.l_bound, self.spec.r_points
         internal = (np.asarray(tb["hd"], dtype=np.float64).reshape(L, nr), np.append(tb["hoff"], 0.0), None, 0)
+        if tb.get("cross") is not None:  # the Hamiltonian-derived kinetic energy joins consecutive lines
+            internal = (internal[0], np.append(tb["hoff"], tb["cross"]), None, nat.ION_HOP_WRAP_B)
         if isinstance(self.operators, mo.SphericalHarmonicVelocityGaugeOperators):
             return (L, nr), internal, "unsupported", None
         cl = np.append(np.asarray(tb["cl"], dtype=np.float64)[: L - 1], 0.0)

@@ -36,6 +36,7 @@ Cases (reference call sites in parentheses):
                    rectangle runs with the InternalEnergyExpectationValue and
                    TotalEnergyExpectationValue datastores; the SH run also
                    the DirectionalRadialProbabilityCurrent at its final time
+  sh_hamiltonian_small  SH split run with kinetic_energy_derivation="hamiltonian"
 
 Each npz holds the spec parameters (``params`` JSON string), the time grid,
 the initial and final ``g``, and the Norm / InnerProducts datastore arrays.
@@ -241,7 +242,7 @@ def gen_line(ion, full=False):
 
 
 def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_every, n_max=3, gauge="length",
-            method="SplitInteractionOperator"):
+            method="SplitInteractionOperator", derivation=None):
     from ionization import states
 
     r_bound = 0.125 * (r_points - 1)
@@ -264,6 +265,15 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
         params["gauge"] = gauge
     if method != "SplitInteractionOperator":
         params["method"] = method
+    if derivation is not None:
+        params["kinetic_energy_derivation"] = derivation
+    if gauge == "velocity":
+        operators = ion.mesh.SphericalHarmonicVelocityGaugeOperators()
+    elif derivation is not None:
+        operators = ion.mesh.SphericalHarmonicLengthGaugeOperators(
+            kinetic_energy_derivation=ion.mesh.KineticEnergyDerivation(derivation))
+    else:
+        operators = ion.mesh.SphericalHarmonicLengthGaugeOperators()
     spec = ion.mesh.SphericalHarmonicSpecification(
         name,
         r_points=r_points,
@@ -277,8 +287,7 @@ def sh_spec(ion, name, r_points, l_bound, steps, dt, pulse, mask_width, store_ev
         time_initial=0.0,
         time_final=steps * dt,
         time_step=dt,
-        operators=(ion.mesh.SphericalHarmonicVelocityGaugeOperators() if gauge == "velocity"
-                   else ion.mesh.SphericalHarmonicLengthGaugeOperators()),
+        operators=operators,
         evolution_method=getattr(ion.mesh, method)(),
         store_data_every=store_every,
     )
@@ -591,12 +600,25 @@ def gen_energy(ion):
     _run_energy(ion, spec, params, "rect_energy_small")
 
 
+def gen_hamiltonian(ion):
+    """SphericalHarmonicLengthGaugeOperators(kinetic_energy_derivation=
+    "hamiltonian") with SplitInteractionOperator (mesh_operators.py:863-887):
+    the radial kinetic energy of the flattened (l, r) mesh, whose couplings
+    also join the last r of each l to the first r of the next.  A short grid
+    (64 points, r up to 8) that the pulse drives out to its edge, so that
+    those couplings act; the energy datastores ride along."""
+    pulse = _pulse_kwargs(0.2, 0.5, 2, 0.0)
+    spec, params = sh_spec(ion, "sh_hamiltonian_small", 64, 7, 400, 0.02, pulse, 1.0, 40,
+                           derivation="hamiltonian")
+    _run_energy(ion, spec, params, "sh_hamiltonian_small")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("IONIZATION_REFERENCE"),
                     help="path of the reference checkout (or set IONIZATION_REFERENCE)")
     ap.add_argument("--only", default=None,
-                    help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice,energy")
+                    help="comma list: tdma,line,sh,cyl,obs,vel,shadi,rect,num,slice,energy,ham")
     ap.add_argument("--full", action="store_true", help="also the full 1D workload")
     ap.add_argument("--full-sh", action="store_true")
     ap.add_argument("--full-cyl", action="store_true")
@@ -608,7 +630,7 @@ def main():
 
     ion = import_reference(args.ref)
     only = set(args.only.split(",")) if args.only else {"tdma", "line", "sh", "cyl", "obs", "vel", "shadi", "rect",
-                                                        "num", "slice", "energy"}
+                                                        "num", "slice", "energy", "ham"}
     if "tdma" in only:
         gen_tdma(ion)
     if "line" in only:
@@ -631,6 +653,8 @@ def main():
         gen_slice(ion)
     if "energy" in only:
         gen_energy(ion)
+    if "ham" in only:
+        gen_hamiltonian(ion)
     if args.full:
         gen_line(ion, full=True)
     if args.full_sh:

@@ -43,6 +43,9 @@ def product_spec(kind, params, **kw):
     if kind == "sh":
         if params.get("gauge", "length") == "velocity":
             common.setdefault("operators", mesh.SphericalHarmonicVelocityGaugeOperators())
+        if "kinetic_energy_derivation" in params:
+            common.setdefault("operators", mesh.SphericalHarmonicLengthGaugeOperators(
+                kinetic_energy_derivation=params["kinetic_energy_derivation"]))
         if "method" in params:
             common.setdefault("evolution_method", getattr(mesh, params["method"])())
         return mesh.SphericalHarmonicSpecification(

@@ -19,7 +19,7 @@ from .specs import product_spec
 
 TOL = 1e-10
 CASES = [("line", "line_energy_small"), ("line", "line_energy_velocity_small"), ("sh", "sh_energy_small"),
-         ("cyl", "cyl_energy_small"), ("rect", "rect_energy_small")]
+         ("cyl", "cyl_energy_small"), ("rect", "rect_energy_small"), ("sh", "sh_hamiltonian_small")]
 
 
 def _apply(ops, g):
@@ -31,6 +31,11 @@ def _apply(ops, g):
     out = 0.0
     if diag is not None:
         out += np.sum(np.broadcast_to(diag, shape) * np.abs(g) ** 2)
+    if off_b is not None and flags & nat.ION_HOP_WRAP_B:  # the chain runs on over the flattened mesh
+        c = np.broadcast_to(off_b, shape).reshape(-1)[:-1]
+        z = np.conj(g.reshape(-1)[:-1]) * g.reshape(-1)[1:]
+        out += np.sum(-2 * c * z.imag) if flags & nat.ION_HOP_IMAG_B else np.sum(2 * c * z.real)
+        off_b = None
     for off, axis, imag in ((off_b, 1, flags & nat.ION_HOP_IMAG_B), (off_a, 0, flags & nat.ION_HOP_IMAG_A)):
         if off is None:
             continue
