@@ -229,6 +229,11 @@ typedef struct ion_sh_sim {
     const void *spike_t;
     void *edge;
     double hcross;
+    /* 1: state_g holds each test state's real radial g, [n_states*n_r]
+     * doubles (hydrogen and numeric eigenstates are real); 0: complex128
+     * pairs as described above */
+    int32_t state_real;
+    int32_t pad3_;
 } ion_sh_sim;
 
 enum { ION_GAUGE_LENGTH = 0, ION_GAUGE_VELOCITY = 1 };

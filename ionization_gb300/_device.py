@@ -299,8 +299,24 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     n_states = len(tab.state_l)
     a["d_state_l"] = np.asarray(tab.state_l, dtype=np.int32).reshape(-1)
     sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(n_states, tab.n_r)
-    a["d_state_g"] = sg.view(np.float64).reshape(-1) if n_states else np.zeros(2)
+    if not n_states:
+        a["d_state_g"] = np.zeros(2)
+    elif sh_states_real(tab):  # half the bytes: the kernels read one double a point
+        a["d_state_g"] = np.ascontiguousarray(sg.real).reshape(-1)
+    else:
+        a["d_state_g"] = sg.view(np.float64).reshape(-1)
     return a
+
+
+def sh_states_real(tab: ShTables) -> bool:
+    """Whether every test state's radial g is real (imaginary parts all
+    exactly zero), cached on the tables."""
+    v = getattr(tab, "_states_real", None)
+    if v is None:
+        sg = np.asarray(tab.state_g, dtype=np.complex128)
+        v = bool(sg.size) and not np.any(sg.imag)
+        tab._states_real = v
+    return v
 
 
 def _sh_device_sizes(tab: ShTables):
@@ -317,12 +333,18 @@ class _Arena:
     def __init__(self, np_dtype):
         self.np_dtype = np.dtype(np_dtype)
         self.items = []  # (key, array, offset)
+        self.placed = {}  # id(array) -> (array, offset): each array object once
         self.size = 0
 
     def add(self, key, arr):
+        """Place ``arr``; the same array object added again shares its place."""
+        if id(arr) in self.placed:
+            self.items.append((key, arr, self.placed[id(arr)][1]))
+            return
         align = max(1, 64 // self.np_dtype.itemsize)
         self.size = (self.size + align - 1) // align * align
         self.items.append((key, arr, self.size))
+        self.placed[id(arr)] = (arr, self.size)
         self.size += arr.size
 
     # staged through page-locked memory, which torch's host allocator keeps
@@ -343,7 +365,8 @@ class _Arena:
         # pack on a few threads: numpy copies and casts of large arrays run
         # outside the GIL
         nthr = max(1, min(16, os.cpu_count() or 1))
-        chunks = [self.items[k::nthr] for k in range(nthr)]
+        unique = [(None, arr, off) for arr, off in self.placed.values()]
+        chunks = [unique[k::nthr] for k in range(nthr)]
 
         def pack(items):
             for _, arr, off in items:
@@ -492,6 +515,20 @@ class ShDeviceSim:
         arenas = {}
         with concurrent.futures.ThreadPoolExecutor(max_workers=8) as pool:  # numpy work outside the GIL
             per = list(pool.map(lambda tab: _sh_host_arrays(tab, precision), tables))
+        # time-step tables that are equal (the same grid of times) are
+        # uploaded once and shared
+        by_key = {}
+        for host in per:
+            tau = host.get("d_tau")
+            if tau is None or tau.size < 2:
+                continue
+            key = (tau.size, float(tau[1]), float(tau[-1]))
+            for other in by_key.get(key, ()):
+                if np.array_equal(other, tau):
+                    host["d_tau"] = other
+                    break
+            else:
+                by_key.setdefault(key, []).append(tau)
         # every simulation's uploaded psi rows first, then the tables
         order = ["g_in"] + [k for k in (per[0] if per else {}) if k != "g_in"]
         for k in order:
@@ -565,6 +602,7 @@ class ShDeviceSim:
         d.kinv, d.cent, d.corr0 = ptr(self.d_kinv64), ptr(self.d_cent64), float(self.tab.corr0)
         d.spike_s, d.spike_t, d.edge = ptr(self.d_spike_s), ptr(self.d_spike_t), ptr(self.d_edge)
         d.hcross = float(self.tab.hcross or 0.0)
+        d.state_real = int(self.n_states > 0 and sh_states_real(self.tab))
         return d
 
     def data(self):

@@ -93,6 +93,8 @@ class ShSim(ctypes.Structure):
         ("spike_t", c_vp),
         ("edge", c_vp),
         ("hcross", c_f64),
+        ("state_real", c_i32),
+        ("pad3_", c_i32),
     ]
 
 

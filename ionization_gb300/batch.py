@@ -33,6 +33,13 @@ def _host_tables(spec):
         spec.host_only = False
 
 
+def host_tables_many(specs):
+    """The host tables of many specifications, one after another (a thread
+    pool was measured slower: most of the per-specification work holds the
+    GIL)."""
+    return [_host_tables(spec)[0] for spec in specs]
+
+
 class BatchedSphericalHarmonicSimulation:
     """Advance ``specs`` (SphericalHarmonicSpecification, split operator,
     length gauge) together on one GPU.
@@ -45,7 +52,7 @@ class BatchedSphericalHarmonicSimulation:
         self.specs = list(specs)
         self.precision = Precision(precision or self.specs[0].precision)
         if tables is None:
-            tables = [_host_tables(spec)[0] for spec in self.specs]
+            tables = host_tables_many(self.specs)
         self.tables = tables
         dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
         self.sims = dsims
@@ -170,7 +177,7 @@ def autotune(specs, precision="c64", graph_steps=(16, 32, 64), steps=32, tables=
     graph_steps=), timings = {candidate label: ms per step}."""
     precision = Precision(precision)
     if tables is None:
-        tables = [_host_tables(spec)[0] for spec in specs]
+        tables = host_tables_many(specs)
     gs_mid = sorted(graph_steps)[len(graph_steps) // 2]
     timings = {}
 

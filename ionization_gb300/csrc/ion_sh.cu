@@ -826,8 +826,11 @@ __device__ void reduce_tile(const ion_sh_sim& S, const Tile<R>& tl, int rows, in
         const int jj = threadIdx.x;
         if (jj < rows && ls < nl) {
             const Cx<double> x = tl.value(ls * ROT_ROWS + jj);
-            const double* sg = S.state_g + (int64_t(s) * S.n_r + j0 + jj) * 2;
-            const double ar = sg[0], ai = -sg[1];  // conj(state)
+            // conj(state); a real state reads one double (ai = -0.0, the
+            // same arithmetic as its complex128 form)
+            const int64_t at = int64_t(s) * S.n_r + j0 + jj;
+            const double ar = S.state_real ? S.state_g[at] : S.state_g[2 * at];
+            const double ai = S.state_real ? -0.0 : -S.state_g[2 * at + 1];
             re = ar * x.re - ai * x.im;
             im = ar * x.im + ai * x.re;
         }
@@ -1160,8 +1163,9 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
             const int jj = threadIdx.x;
             if (jj < rows && ls < nl) {
                 const Cx<double> x = tl.value(ls * VEL_ROWS + VEL_HALO + jj);
-                const double* sg = S.state_g + (int64_t(q) * nr + j0 + jj) * 2;
-                const double ar = sg[0], ai = -sg[1];
+                const int64_t at = int64_t(q) * nr + j0 + jj;
+                const double ar = S.state_real ? S.state_g[at] : S.state_g[2 * at];
+                const double ai = S.state_real ? -0.0 : -S.state_g[2 * at + 1];
                 re = ar * x.re - ai * x.im;
                 im = ar * x.im + ai * x.re;
             }

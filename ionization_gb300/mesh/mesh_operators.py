@@ -268,30 +268,27 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
             return self._device_tables_hamiltonian(mesh)
         spec = mesh.spec
         nr, L = spec.r_points, spec.l_bound
-        M = nr * L
         mu = u.electron_mass_reduced
         p = -(u.hbar ** 2) / (2 * mu * (mesh.delta_r ** 2))
-        j = np.arange(M) % nr
-        diag = self.beta(j).astype(np.complex128)
+        # The reference forms these over the whole flattened mesh, element by
+        # element; beta, alpha and V depend on r alone and the centrifugal
+        # term on (l, r), so each is formed once per r (or per (l, r)) with
+        # the same per-element operations in the same order and broadcast:
+        # diag = ((beta_j (+ corr at the first point)) (-2p) + eff) + V.
+        beta_r = self.beta(np.arange(nr)).astype(np.float64)
         corr = 0.0
         if self.hydrogen_zero_angular_momentum_correction:
             dr = mesh.delta_r / u.bohr_radius
             corr = dr * (1 + dr) / 8
-            diag[0] += corr
-        kk = np.arange(M - 1)
-        off = np.where((kk + 1) % nr != 0, self.alpha(kk % nr), 0).astype(np.complex128)
-        diag *= -2 * p
-        off *= p
-        l_mesh, r_mesh = mesh.l_mesh, mesh.r_mesh
-        eff = ((u.hbar ** 2) / (2 * mu)) * l_mesh * (l_mesh + 1) / (r_mesh ** 2)
-        diag += eff.flatten("C")
-        V = spec.internal_potential(r=r_mesh, test_charge=spec.test_charge)
-        hd = (diag + 1.0 * np.asarray(V).flatten("C")).real.copy()
-        hoff = off.real[: nr - 1].copy()
+        lv = np.arange(L)[:, None]
+        eff = ((u.hbar ** 2) / (2 * mu)) * lv * (lv + 1) / (mesh.r[None, :] ** 2)
+        V_r = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge), dtype=np.float64)
+        hd2 = (beta_r * (-2 * p))[None, :] + eff
+        hd2[0, 0] = (beta_r[0] + corr) * (-2 * p) + eff[0, 0]
+        hd = (hd2 + V_r[None, :]).reshape(-1)
+        hoff = (self.alpha(np.arange(nr - 1)) * p).astype(np.float64)
         rq = -spec.test_charge * mesh.r
         cl = self.c_l(np.arange(L))
-        beta_r = self.beta(np.arange(nr)).astype(np.float64)
-        V_r = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge), dtype=np.float64)
         kinv = beta_r * (-2 * p) + V_r
         cent = ((u.hbar ** 2) / (2 * mu)) / (mesh.r ** 2)
         corr0 = (beta_r[0] + corr) * (-2 * p) - beta_r[0] * (-2 * p)

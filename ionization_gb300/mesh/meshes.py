@@ -500,7 +500,8 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         self.inner_product_multiplier = self.delta_r
         self.l = np.array(range(self.spec.l_bound), dtype=int)
         self.mesh_points = len(self.r) * len(self.l)
-        self.l_mesh, self.r_mesh = np.meshgrid(self.l, self.r, indexing="ij")
+        # read-only broadcast views (the grid is never written through them)
+        self.l_mesh, self.r_mesh = np.meshgrid(self.l, self.r, indexing="ij", copy=False)
         self.mesh_shape = np.shape(self.r_mesh)
         self._radial_cache = {}
         if self.spec.use_numeric_eigenstates:  # meshes.py:1021-1033

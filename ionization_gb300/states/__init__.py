@@ -7,6 +7,7 @@ user QuantumState subclass the 1D Gaussian workload needs.
 """
 
 import abc
+import functools
 from copy import deepcopy
 
 import numpy as np
@@ -172,13 +173,20 @@ class HydrogenBoundState(SphericalHarmonicState):
     def radial_function(self, r):
         """Griffiths-normalised radial function (three_d.py:375-391)."""
         n, l = self.n, self.l
-        normalization = np.sqrt(
-            ((2 / (n * u.bohr_radius)) ** 3)
-            * (special.factorial(n - l - 1) / (2 * n * special.factorial(n + l)))
-        )
+        normalization = _bound_normalization(n, l)
         r_dep = np.exp(-r / (n * u.bohr_radius)) * ((2 * r / (n * u.bohr_radius)) ** l)
         lag_poly = special.eval_genlaguerre(n - l - 1, (2 * l) + 1, 2 * r / (n * u.bohr_radius))
         return self.amplitude * normalization * r_dep * lag_poly
+
+
+@functools.lru_cache(maxsize=None)
+def _bound_normalization(n, l):
+    """The radial function's normalisation constant, formed once per (n, l)
+    (the same expression every call; scipy's factorial is slow to call)."""
+    return np.sqrt(
+        ((2 / (n * u.bohr_radius)) ** 3)
+        * (special.factorial(n - l - 1) / (2 * n * special.factorial(n + l)))
+    )
 
 
 def electron_wavenumber_from_energy(energy):
