@@ -362,8 +362,8 @@ def run_ours(args, rank, world, local_rank):
         "unit": "GB/s",
         "frac": round(achieved / peak, 4),
         "traffic": None if traffic is None else int(traffic * points),
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on a 240-simulation case of the "
-                          "sweep, bytes per point scaled to this workload (profiles/)",
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one steady-state step of this "
+                          "512-simulation sweep (profiles/sh_dram_traffic_c64_uneven.md), per launch",
         "step_traffic": None if step_traffic is None else int(step_traffic * points),
         "step_algorithmic_bytes": 2 * alg_bytes,
         "algorithmic_bytes": alg_bytes,
