@@ -880,11 +880,23 @@ __global__ void sh_advance_kernel(ion_sh_plan plan, int mode) {
     if (mode == ADV_STEP && threadIdx.x == 0) S.t = t + 1;
 }
 
-// the tile (complex64: hi and the packed lo, 12 bytes an element) and the
-// block-sum scratch
+// the tile (complex64: hi and the packed lo, 12 bytes an element), the
+// block-sum scratch and the simulation's c_l (staged once per tile: every
+// pair of every operator reads its c_l, and from shared memory that read is
+// a short one; the global loads cost 9 % of the pass)
 template <typename R>
 __host__ __device__ inline size_t rot_smem_bytes(int max_nl, int rows) {
-    return size_t(max_nl) * rows * (sizeof(Cx<R>) + (std::is_same<R, float>::value ? 4 : 0)) + 32 * sizeof(double);
+    return size_t(max_nl) * rows * (sizeof(Cx<R>) + (std::is_same<R, float>::value ? 4 : 0)) + 32 * sizeof(double) +
+           size_t(max_nl) * sizeof(R);
+}
+
+// c_l of the tile's simulation into shared memory (after the block-sum
+// scratch); the caller's barrier publishes it
+template <typename R>
+__device__ __forceinline__ const R* stage_cl(const RotTab<R>& tb, double* scratch, int nl) {
+    R* cl = reinterpret_cast<R*>(scratch + 32);
+    for (int l = threadIdx.x; l < nl; l += blockDim.x) cl[l] = tb.cl[l];
+    return cl;
 }
 
 template <typename R>
@@ -959,13 +971,14 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
     }
     cp_async_commit();
     if (pf_dist > 0 && blockIdx.x + pf_dist < plan.n_rot_items) prefetch_rot_item<R>(plan, blockIdx.x + pf_dist);
-    // the step's scalars (FP64 tables, converted to R) while the tile lands
+    // the step's scalars (FP64 tables, converted to R) and c_l while the tile lands
     const R tp = post ? R(S.tau[n_post]) : R(0), ep = post ? R(S.efield[n_post]) : R(0);
     const R tq = pre ? R(S.tau[n_pre]) : R(0), eq = pre ? R(S.efield[n_pre]) : R(0);
+    RotTab<R> tb = RotTab<R>::make(S);
+    tb.cl = stage_cl(tb, scratch, nl);
     cp_async_wait<0>();
     __syncthreads();
 
-    const RotTab<R> tb = RotTab<R>::make(S);
     const int jj = threadIdx.x & (ROT_ROWS - 1), lane = threadIdx.x >> 5;
     const int lanes = blockDim.x >> 5;
     if (post && pre && !reduce) {
@@ -1128,9 +1141,10 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
         }
     }
     cp_async_commit();
+    RotTab<R> tb = RotTab<R>::make(S);
+    tb.cl = stage_cl(tb, scratch, nl);
     cp_async_wait<0>();
     __syncthreads();
-    const RotTab<R> tb = RotTab<R>::make(S);
     const R* h2r = VelTab<R>::h2r(S);
     if (post) {  // reversed(S): h2 (odd, odd) ... (even, even), h1 odd, h1 even
         const R tau = R(S.tau[n_post]), af = R(S.efield[n_post]);
