@@ -148,7 +148,8 @@ typedef struct ion_sh_sim {
     int64_t t;           /* current time index; advanced on the device */
     int64_t t_final;     /* last time index (number of steps of the run) */
     int64_t store_every; /* data at t = 0, t = t_final and t % store_every == 0 if >= 1 */
-    /* FP64 tables (complex128 path) */
+    /* FP64 tables (complex128 path; the _c64 entry points read hoff, tau and
+     * efield of these, and the mask flag from mask32) */
     const double *hd;     /* [n_l*n_r] diagonal of the internal Hamiltonian (C order) */
     const double *hoff;   /* [n_r-1]   its off-diagonal (identical for every l) */
     const double *rq;     /* [n_r]     (-test_charge) * r_j */

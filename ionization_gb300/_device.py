@@ -129,7 +129,7 @@ class ShTables:
     cent: np.ndarray  # [n_r]
     corr0: float
     state_l: List[int]
-    state_g: np.ndarray  # [n_states, n_r] complex128
+    state_g: np.ndarray  # [n_states, n_r] complex128, or float64 for real states
     weight: float
     g0: np.ndarray  # [n_l, n_r] complex128
     t0: int
@@ -279,10 +279,11 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     # remainders from (ion_sh_row_lo_c64)
     a["d_kinv64"] = np.asarray(tab.kinv, f64) if x else None
     a["d_cent64"] = np.asarray(tab.cent, f64) if x else None
-    a["d_hoff"] = np.asarray(tab.hoff, f64)
-    a["d_rq"] = np.asarray(tab.rq, f64)
-    a["d_cl"] = np.asarray(tab.cl, f64)
-    a["d_mask"] = np.asarray(tab.mask, f64) if tab.mask is not None else None
+    a["d_hoff"] = np.asarray(tab.hoff, f64)  # the complex64 forms' row-sum remainders read it too
+    # the complex64 rotation pass reads the FP32 copies below
+    a["d_rq"] = np.asarray(tab.rq, f64) if c128 else None
+    a["d_cl"] = np.asarray(tab.cl, f64) if c128 else None
+    a["d_mask"] = np.asarray(tab.mask, f64) if (tab.mask is not None and c128) else None
     a["d_tau"] = np.asarray(tab.tau, f64)
     a["d_ef"] = np.asarray(tab.efield, f64)
     # per-r FP32 tables zero-padded to a multiple of 16 entries: the radial
@@ -298,25 +299,19 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     a["d_h2r32"] = np.asarray(tab.h2r, f32) if vel else None
     n_states = len(tab.state_l)
     a["d_state_l"] = np.asarray(tab.state_l, dtype=np.int32).reshape(-1)
-    sg = np.asarray(tab.state_g, dtype=np.complex128).reshape(n_states, tab.n_r)
     if not n_states:
         a["d_state_g"] = np.zeros(2)
-    elif sh_states_real(tab):  # half the bytes: the kernels read one double a point
-        a["d_state_g"] = np.ascontiguousarray(sg.real).reshape(-1)
+    elif sh_states_real(tab):  # real states: the kernels read one double a point
+        a["d_state_g"] = np.ascontiguousarray(tab.state_g, dtype=np.float64).reshape(-1)
     else:
-        a["d_state_g"] = sg.view(np.float64).reshape(-1)
+        a["d_state_g"] = np.asarray(tab.state_g, dtype=np.complex128).reshape(n_states, tab.n_r).view(
+            np.float64).reshape(-1)
     return a
 
 
 def sh_states_real(tab: ShTables) -> bool:
-    """Whether every test state's radial g is real (imaginary parts all
-    exactly zero), cached on the tables."""
-    v = getattr(tab, "_states_real", None)
-    if v is None:
-        sg = np.asarray(tab.state_g, dtype=np.complex128)
-        v = bool(sg.size) and not np.any(sg.imag)
-        tab._states_real = v
-    return v
+    """Whether the tables hold the test states as real values (float64)."""
+    return np.asarray(tab.state_g).dtype == np.float64
 
 
 def _sh_device_sizes(tab: ShTables):

@@ -919,7 +919,7 @@ __global__ void __maxnreg__(sizeof(R) == 8 ? 64 : 48) sh_rot_kernel(ion_sh_plan 
         if (t >= tf) return;
         post = true;
         n_post = t + 1;
-        do_mask = S.mask != nullptr;
+        do_mask = (sizeof(R) == 8 ? static_cast<const void*>(S.mask) : static_cast<const void*>(S.mask32)) != nullptr;
         reduce = is_data_time(t + 1, tf, S.store_every);
         if (mode == ROT_STEP_PRE && t + 1 < tf) {
             pre = true;
@@ -1096,7 +1096,7 @@ __global__ void __launch_bounds__(ROT_ROWS * ROT_LANES) sh_rot_vel_kernel(ion_sh
         if (t >= tf) return;
         post = true;
         n_post = t + 1;
-        do_mask = S.mask != nullptr;
+        do_mask = (sizeof(R) == 8 ? static_cast<const void*>(S.mask) : static_cast<const void*>(S.mask32)) != nullptr;
         reduce = is_data_time(t + 1, tf, S.store_every);
         if (mode == ROT_STEP_PRE && t + 1 < tf) {
             pre = true;

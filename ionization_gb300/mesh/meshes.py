@@ -286,6 +286,14 @@ def _two_axis_energy_operators(mesh, n_a, n_b):
     return (n_a, n_b), internal, inter, lambda: float(spec.electric_potential.get_electric_field_amplitude(sim.time))
 
 
+def _radial_states_array(gs, n_r) -> np.ndarray:
+    """The test states' radial g as one [n_states, n_r] array: float64 when
+    every value is real (hydrogen and numeric eigenstates), so the device
+    reads (and the upload moves) one double a point, else complex128."""
+    a = np.array(gs, dtype=np.complex128).reshape(len(gs), n_r)
+    return a.real.copy() if a.size and not np.any(a.imag) else a
+
+
 def _adi_precision(mesh, what):
     """The two-direction ADI kernel pair has complex128 and complex64 forms
     (FP32 sweeps, FP64 tables and reductions); the stored-residual form
@@ -652,7 +660,7 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         self.tables = dev.ShTables(
             n_r=spec.r_points, n_l=spec.l_bound, hd=tb["hd"], hoff=tb["hoff"], rq=rq, cl=tb["cl"], mask=mask,
             tau=self._tau_host.copy(), efield=efield, kinv=tb["kinv"], cent=tb["cent"], corr0=tb["corr0"],
-            state_l=sl, state_g=np.array(sg, dtype=np.complex128).reshape(len(sl), spec.r_points),
+            state_l=sl, state_g=_radial_states_array(sg, spec.r_points),
             weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
             g0_rows=np.flatnonzero(np.any(np.asarray(g0).reshape(spec.l_bound, spec.r_points) != 0, axis=1)),
             store_every=spec.store_data_every, gauge=gauge, h2r=h2r, hcross=tb.get("cross"),
