@@ -186,22 +186,6 @@ def sh_bucket_sizes(n_rs, precision, rows: int) -> np.ndarray:
     return np.array([(n + gran - 1) // gran * gran for n in need], dtype=np.int64)
 
 
-class _Fill:
-    """A host array written straight into its upload buffer (``fill(dest)``,
-    dest flat, of ``dtype``) instead of being formed and then copied."""
-
-    def __init__(self, shape, dtype, fill):
-        self.shape = tuple(shape)
-        self.dtype = np.dtype(dtype)
-        self.size = int(np.prod(self.shape))
-        self.fill = fill
-
-    def materialize(self) -> np.ndarray:
-        out = np.empty(self.shape, self.dtype)
-        self.fill(out.reshape(-1))
-        return out
-
-
 def lo_pack(lo) -> np.ndarray:
     """The stored residual of a complex64 state from its complex value: one
     32-bit word a point (int32 holding the bits), the real part's bf16 in the
@@ -322,8 +306,13 @@ def _sh_device_sizes(tab: ShTables):
 
 class _Arena:
     """Arrays of one dtype packed into one pinned host buffer, uploaded with
-    one copy; each array becomes a view of the device buffer, starting on a
-    64-byte boundary (the radial solve's float4 table loads need 16)."""
+    one copy; each array becomes a view of the device buffer.  Arrays added
+    with ``align`` start on a 64-byte boundary (the first of each kind: the
+    radial solve's float4 table loads need 16); the others follow the
+    previous one directly, so a kind's arrays form one run that is packed with
+    one copy.  The arrays of a kind keep the alignment their element needs
+    because every array's byte size is a whole number of those elements (the
+    FP32 tables the solve reads by float4 are padded to 64 bytes)."""
 
     def __init__(self, np_dtype):
         self.np_dtype = np.dtype(np_dtype)
@@ -331,13 +320,14 @@ class _Arena:
         self.placed = {}  # id(array) -> (array, offset): each array object once
         self.size = 0
 
-    def add(self, key, arr):
+    def add(self, key, arr, align=True):
         """Place ``arr``; the same array object added again shares its place."""
         if id(arr) in self.placed:
             self.items.append((key, arr, self.placed[id(arr)][1]))
             return
-        align = max(1, 64 // self.np_dtype.itemsize)
-        self.size = (self.size + align - 1) // align * align
+        if align:
+            a = max(1, 64 // self.np_dtype.itemsize)
+            self.size = (self.size + a - 1) // a * a
         self.items.append((key, arr, self.size))
         self.placed[id(arr)] = (arr, self.size)
         self.size += arr.size
@@ -348,6 +338,17 @@ class _Arena:
     # copy instead: 0.33 s every time)
     pin = True
 
+    def runs(self):
+        """(offset, [arrays]) of the placed arrays that follow one another."""
+        out = []
+        for arr, off in sorted(self.placed.values(), key=lambda x: x[1]):
+            if out and out[-1][0] + out[-1][2] == off:
+                out[-1][1].append(arr)
+                out[-1][2] += arr.size
+            else:
+                out.append([off, [arr], arr.size])
+        return [(off, arrs) for off, arrs, _ in out]
+
     def upload(self, tensors=()) -> dict:
         """Device views by key: torch views for the keys whose name is in
         ``tensors`` (keys are (index, name)), ``_DevSlice`` for the rest."""
@@ -357,21 +358,16 @@ class _Arena:
         n = max(self.size, 1)
         host = torch.empty(n, dtype=tdt, pin_memory=self.pin)
         hv = host.numpy()
-        # pack on a few threads: numpy copies and casts of large arrays run
-        # outside the GIL
-        nthr = max(1, min(16, os.cpu_count() or 1))
-        unique = [(None, arr, off) for arr, off in self.placed.values()]
-        chunks = [unique[k::nthr] for k in range(nthr)]
 
-        def pack(items):
-            for _, arr, off in items:
-                if isinstance(arr, _Fill):
-                    arr.fill(hv[off:off + arr.size])
-                else:
-                    hv[off:off + arr.size] = arr.reshape(-1)
+        def pack(run):  # one copy per run (outside the GIL)
+            off, arrs = run
+            total = sum(a.size for a in arrs)
+            np.concatenate([a.reshape(-1) for a in arrs], out=hv[off:off + total])
 
+        runs = self.runs()
+        nthr = max(1, min(16, os.cpu_count() or 1, len(runs)))
         with concurrent.futures.ThreadPoolExecutor(max_workers=nthr) as pool:
-            list(pool.map(pack, chunks))
+            list(pool.map(pack, runs))
         dev_buf = torch.empty(n, dtype=tdt, device=device())
         dev_buf.copy_(host, non_blocking=self.pin)
         return {key: (dev_buf[off:off + arr.size].view(arr.shape) if key[1] in tensors
@@ -459,8 +455,7 @@ class ShDeviceSim:
         if arrays is None:
             host = _sh_host_arrays(tab, precision)
             self.h2d_bytes = sum(int(v.size) * np.dtype(v.dtype).itemsize for v in host.values() if v is not None)
-            arrays = {k: (to_dev(v.materialize() if isinstance(v, _Fill) else v) if v is not None else None)
-                      for k, v in host.items()}
+            arrays = {k: (to_dev(v) if v is not None else None) for k, v in host.items()}
             arrays.update(_sh_state_buffers(tab.n_l * tab.n_r, self.precision, [tab.n_l * tab.n_r])[0])
             self.n_data, n_states, self.n_tiles = _sh_device_sizes(tab)
             arrays["d_norm"] = torch.full((self.n_data,), float("nan"), dtype=torch.float64, device=device())
@@ -527,10 +522,12 @@ class ShDeviceSim:
         # every simulation's uploaded psi rows first, then the tables
         order = ["g_in"] + [k for k in (per[0] if per else {}) if k != "g_in"]
         for k in order:
+            first = True
             for i, host in enumerate(per):
                 v = host.get(k)
                 if v is not None:
-                    arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v)
+                    arenas.setdefault(v.dtype, _Arena(v.dtype)).add((i, k), v, align=first)
+                    first = False
         views = {}
         for ar in arenas.values():
             views.update(ar.upload(tensors=("g_in",)))
@@ -548,6 +545,7 @@ class ShDeviceSim:
         d_ip = torch.full((max(n_ip, 1),), float("nan"), dtype=torch.float64, device=device())
         d_part = torch.zeros(max(n_part, 1), dtype=torch.float64, device=device())
         sims, o_norm, o_ip, o_part = [], 0, 0, 0
+        counted = set()  # a shared array's bytes count for the first simulation only
         for i, tab in enumerate(tables):
             nd, ns, nt = sizes[i]
             arrays = {k: views.get((i, k)) for k in per[i]}
@@ -558,7 +556,9 @@ class ShDeviceSim:
             sim = cls.__new__(cls)
             sim._deferred = True  # prepared together below
             sim.__init__(tab, precision, arrays=arrays)
-            sim.h2d_bytes = sum(int(v.size) * np.dtype(v.dtype).itemsize for v in per[i].values() if v is not None)
+            sim.h2d_bytes = sum(int(v.size) * np.dtype(v.dtype).itemsize for v in per[i].values()
+                                if v is not None and id(v) not in counted)
+            counted.update(id(v) for v in per[i].values() if v is not None)
             sim._bulk = dict(norm=(d_norm, o_norm, nd), ip=(d_ip, o_ip, nd * max(ns, 1) * 2))
             o_norm += nd
             o_ip += nd * max(ns, 1) * 2
