@@ -120,15 +120,16 @@ class BatchedSphericalHarmonicSimulation:
         torch.cuda.synchronize()
         out = []
         for spec, s, (norm, ips) in zip(self.specs, self.sims, dev.sh_data_many(self.sims)):
-            ip = {st: ips[k] for k, st in enumerate(spec.test_states)}
-            ov = {st: np.abs(v) ** 2 for st, v in ip.items()}
+            states = list(spec.test_states)
+            ov = np.abs(ips) ** 2  # (n_states, n_data), one array operation
+            bound = [k for k, st in enumerate(states) if st.bound]
             out.append(dict(
                 name=spec.name,
                 t=s.t,
                 norm=norm,
-                inner_products=ip,
-                initial_state_overlap=ov[spec.initial_state],
-                bound_state_overlap=sum(v for st, v in ov.items() if st.bound),
+                inner_products=dict(zip(states, ips)),
+                initial_state_overlap=ov[states.index(spec.initial_state)],
+                bound_state_overlap=ov[bound].sum(axis=0) if bound else np.zeros_like(norm),
             ))
         return out
 
