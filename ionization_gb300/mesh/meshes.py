@@ -755,7 +755,9 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
         field: c_l (-q r_j) between l-neighbours at each r times
         E(t + dt/2) (interaction_hamiltonian, mesh_operators.py:988-1018).
         The velocity gauge's interaction couples (l, r) with (l+1, r +- 1)
-        as well: the device has no form of it."""
+        as well: the device has no form of it (the reference's own total
+        energy in that gauge raises: its interaction operators are bare
+        sparse matrices that SumOfOperators.apply cannot apply)."""
         tb = self.operators.device_tables(self)
         L, nr = self.spec.l_bound, self.spec.r_points
         internal = (np.asarray(tb["hd"], dtype=np.float64).reshape(L, nr), np.append(tb["hoff"], 0.0), None, 0)
