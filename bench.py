@@ -593,6 +593,9 @@ def run_accuracy(subset=None):
     pion = lambda r: 1.0 - float(r["bound_state_overlap"][-1])  # noqa: E731
     res = {"n_instances": len(out["c128"]), "steps": SIM_STEPS,
            "subset": "all" if subset is None else list(subset), "wall_s": wall,
+           # the same whole runs (set-up, 10000 steps, data) of the batched
+           # complex128 form against the c64x form
+           "c64x_vs_c128_batch_wall": round(wall["c128"] / max(wall["c64x"], 1e-9), 1),
            "ground_population_c128": {"min": min(pg(c) for c in out["c128"]),
                                       "median": float(np.median([pg(c) for c in out["c128"]]))},
            "ionization_probability_c128": {"max": max(pion(c) for c in out["c128"]),
