@@ -90,6 +90,19 @@ int current_context(int* dev, unsigned long long* ctx_id);
 // context, once per (kernel, device, context); ION_OK or ION_ERR_CUDA
 int ensure_smem_limit(const void* kernel, int bytes, const char* name);
 
+// Streams and events for running independent launches side by side: fork
+// with an event recorded on the caller's stream, join by making it wait for
+// an event recorded on each side stream (also inside stream capture, where
+// these become graph edges).  Made once per device and context, outside
+// capture; NULL when not available (run in stream order instead).
+struct ForkJoin {
+    static constexpr int N = 7;
+    cudaStream_t s[N];
+    cudaEvent_t fork;
+    cudaEvent_t join[N];
+};
+ForkJoin* fork_join(cudaStream_t main);
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // multiprocessors of the current device (queried once per device)

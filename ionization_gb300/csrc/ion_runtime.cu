@@ -106,6 +106,38 @@ int ensure_smem_limit(const void* kernel, int bytes, const char* name) {
     return ION_OK;
 }
 
+// (device) -> (context id, streams and events of that context)
+static std::mutex g_fj_mu;
+static std::map<int, std::pair<unsigned long long, ForkJoin*>> g_fj;
+
+ForkJoin* fork_join(cudaStream_t main) {
+    int dev = 0;
+    unsigned long long ctx = 0;
+    if (current_context(&dev, &ctx)) return nullptr;
+    std::lock_guard<std::mutex> lock(g_fj_mu);
+    auto it = g_fj.find(dev);
+    if (it != g_fj.end() && it->second.first == ctx) return it->second.second;
+    // none for this context yet: make them, but not while the stream is
+    // being captured (the caller then runs its launches in stream order);
+    // handles of an earlier context went with it and are left alone
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(main, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    auto* fj = new ForkJoin{};
+    bool ok = cudaEventCreateWithFlags(&fj->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; ok && k < ForkJoin::N; ++k)
+        ok = cudaStreamCreateWithFlags(&fj->s[k], cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&fj->join[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return nullptr;  // (what was made stays allocated; this is not retried in a loop)
+    }
+    g_fj[dev] = std::make_pair(ctx, fj);
+    return fj;
+}
+
 }  // namespace ion
 
 extern "C" {

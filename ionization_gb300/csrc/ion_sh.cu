@@ -1460,20 +1460,32 @@ int sh_launch_cn_rows<float>(const ion_sh_plan* p, int rows, int begin, int end,
     }
 }
 
-// every bucket (or all items at cn_threads) with its own rows per thread
+// every bucket (or all items at cn_threads) with its own rows per thread.
+// The buckets hold different lines, so they run side by side: bucket 0 on
+// the caller's stream, the others on side streams forked from it and joined
+// back.  CTAs of different buckets then share SMs (a CTA of long lines
+// leaves registers that a CTA of short lines can use) and one bucket's tail
+// overlaps the next one's work.
 template <typename R>
 static int sh_launch_cn(const ion_sh_plan* p, cudaStream_t s) {
     if (p->n_cn_items == 0) return ION_OK;
     const int nb = p->n_cn_buckets;
+    ForkJoin* fj = nb > 1 ? fork_join(s) : nullptr;
+    if (fj && cudaEventRecord(fj->fork, s) != cudaSuccess) return check_launch("sh_launch_cn fork");
     int begin = 0;
     for (int b = 0; b < (nb > 0 ? nb : 1); ++b) {
         const int end = nb > 0 ? p->cn_bucket_end[b] : p->n_cn_items;
         const int threads = nb > 0 ? p->cn_bucket_threads[b] : p->cn_threads;
         const int rows = sh_bucket_rows<R>(p, nb > 0 ? b : -1);
+        cudaStream_t sb = (fj && b > 0) ? fj->s[b - 1] : s;
+        if (sb != s && cudaStreamWaitEvent(sb, fj->fork, 0) != cudaSuccess) return check_launch("sh_launch_cn fork");
         if (end > begin)
-            if (int e = sh_launch_cn_rows<R>(p, rows, begin, end, threads, s)) return e;
+            if (int e = sh_launch_cn_rows<R>(p, rows, begin, end, threads, sb)) return e;
+        if (sb != s && cudaEventRecord(fj->join[b - 1], sb) != cudaSuccess) return check_launch("sh_launch_cn join");
         begin = end;
     }
+    for (int b = 1; fj && b < nb; ++b)
+        if (cudaStreamWaitEvent(s, fj->join[b - 1], 0) != cudaSuccess) return check_launch("sh_launch_cn join");
     return ION_OK;
 }
 
