@@ -60,6 +60,7 @@ class BatchedSphericalHarmonicSimulation:
         self.graph_steps = int(graph_steps)
         self.use_graphs = use_graphs
         self._graphs = {}
+        self._cap_stream = None
         self._started = False
         self.mesh_points = np.array([s.n_r * s.n_l for s in dsims], dtype=np.int64)
 
@@ -81,7 +82,7 @@ class BatchedSphericalHarmonicSimulation:
         if g is None:
             torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()
-            s = torch.cuda.Stream()
+            s = self._capture_stream()
             s.wait_stream(torch.cuda.current_stream())
             with torch.cuda.stream(s):
                 with torch.cuda.graph(g, stream=s):
@@ -90,6 +91,15 @@ class BatchedSphericalHarmonicSimulation:
             torch.cuda.current_stream().wait_stream(s)
             self._graphs[n] = g
         return g
+
+    def _capture_stream(self):
+        """The one stream every graph of this batch is captured on.  The
+        library makes the side streams a radial solve's buckets fork onto
+        once per caller stream and only outside capture, so the first plain
+        step runs on this stream too."""
+        if self._cap_stream is None:
+            self._cap_stream = torch.cuda.Stream()
+        return self._cap_stream
 
     def step(self, n_steps: int = 1):
         """Advance every unfinished simulation by up to ``n_steps``."""
@@ -100,9 +110,14 @@ class BatchedSphericalHarmonicSimulation:
         if not self.use_graphs:
             self.batch.run(n_steps)
             return
-        # first use: run one plain step so every kernel attribute is set
+        # first use: one plain step on the capture stream, so every kernel
+        # attribute is set and that stream's side streams exist
         if not self._graphs and n_steps > 0:
-            self.batch.run(1)
+            cs = self._capture_stream()
+            cs.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(cs):
+                self.batch.run(1)
+            torch.cuda.current_stream().wait_stream(cs)
             n_steps -= 1
         k = self.graph_steps
         while n_steps >= k:

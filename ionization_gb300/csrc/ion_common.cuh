@@ -93,8 +93,10 @@ int ensure_smem_limit(const void* kernel, int bytes, const char* name);
 // Streams and events for running independent launches side by side: fork
 // with an event recorded on the caller's stream, join by making it wait for
 // an event recorded on each side stream (also inside stream capture, where
-// these become graph edges).  Made once per device and context, outside
-// capture; NULL when not available (run in stream order instead).
+// these become graph edges).  Made once per caller stream, device and
+// context, outside capture: a stream whose first call is made under capture
+// gets NULL and runs in stream order, as does any call when they cannot be
+// made.
 struct ForkJoin {
     static constexpr int N = 7;
     cudaStream_t s[N];

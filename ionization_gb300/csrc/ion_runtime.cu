@@ -106,35 +106,53 @@ int ensure_smem_limit(const void* kernel, int bytes, const char* name) {
     return ION_OK;
 }
 
-// (device) -> (context id, streams and events of that context)
+// (device, caller's stream) -> (context id, side streams and events made for
+// that stream).  Each caller stream has its own set, so launches issued on
+// different streams (from one host thread or several) never share a side
+// stream or an event: no false ordering between them, and a fork event is
+// never re-recorded by another stream between its record and its waits.
 static std::mutex g_fj_mu;
-static std::map<int, std::pair<unsigned long long, ForkJoin*>> g_fj;
+static std::map<std::pair<int, cudaStream_t>, std::pair<unsigned long long, ForkJoin*>> g_fj;
+static constexpr int kMaxForkJoinPerDevice = 64;
 
 ForkJoin* fork_join(cudaStream_t main) {
     int dev = 0;
     unsigned long long ctx = 0;
     if (current_context(&dev, &ctx)) return nullptr;
     std::lock_guard<std::mutex> lock(g_fj_mu);
-    auto it = g_fj.find(dev);
+    const auto key = std::make_pair(dev, main);
+    auto it = g_fj.find(key);
     if (it != g_fj.end() && it->second.first == ctx) return it->second.second;
-    // none for this context yet: make them, but not while the stream is
-    // being captured (the caller then runs its launches in stream order);
-    // handles of an earlier context went with it and are left alone
+    // none for this stream in this context yet: make them, but not while the
+    // stream is being captured (the caller then runs its launches in stream
+    // order); handles of an earlier context went with it and are left alone
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(main, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
         cudaGetLastError();
         return nullptr;
     }
+    if (it == g_fj.end()) {
+        int n = 0;
+        for (const auto& e : g_fj) n += e.first.first == dev;
+        if (n >= kMaxForkJoinPerDevice) return nullptr;  // many caller streams: stream order
+    }
+    // side streams at the caller's priority, so a high-priority caller's
+    // work keeps its place in the block scheduler
+    int prio = 0;
+    if (cudaStreamGetPriority(main, &prio) != cudaSuccess) {
+        cudaGetLastError();
+        prio = 0;
+    }
     auto* fj = new ForkJoin{};
     bool ok = cudaEventCreateWithFlags(&fj->fork, cudaEventDisableTiming) == cudaSuccess;
     for (int k = 0; ok && k < ForkJoin::N; ++k)
-        ok = cudaStreamCreateWithFlags(&fj->s[k], cudaStreamNonBlocking) == cudaSuccess &&
+        ok = cudaStreamCreateWithPriority(&fj->s[k], cudaStreamNonBlocking, prio) == cudaSuccess &&
              cudaEventCreateWithFlags(&fj->join[k], cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         return nullptr;  // (what was made stays allocated; this is not retried in a loop)
     }
-    g_fj[dev] = std::make_pair(ctx, fj);
+    g_fj[key] = std::make_pair(ctx, fj);
     return fj;
 }
 
