@@ -526,6 +526,19 @@ int ion_psi_to_c128(int64_t n, const void *hi, const void *lo, void *out, void *
  * (ION_LO_BF16X2) of psi - hi.  n complex elements, device pointers; in may
  * not alias hi or lo. */
 int ion_psi_split_c128(int64_t n, const void *in, void *hi, void *lo, void *stream);
+/* Many uploaded rows in one launch (a batch's initial states, row by row
+ * into each simulation's psi): rows is a DEVICE array of n_rows entries.
+ * With hi_c128 = 0 each row is split as by ion_psi_split_c128 (complex64 hi,
+ * lo as there, may be NULL); with hi_c128 != 0 it is copied into a
+ * complex128 hi and lo is ignored.  Rows may not overlap one another's
+ * outputs nor alias their own input. */
+typedef struct ion_psi_row {
+    const void *in;  /* n complex128 */
+    void *hi;        /* n complex64 (split) or complex128 (copy) */
+    void *lo;        /* n ION_LO_BF16X2 words, or NULL */
+    int64_t n;
+} ion_psi_row;
+int ion_psi_split_rows_c128(int64_t n_rows, const ion_psi_row *rows, int32_t hi_c128, void *stream);
 
 /* ------------------------------------------------------------------------
  * Position expectation values and partial norms (the ZExpectationValue,

@@ -176,6 +176,15 @@ class Hop(ctypes.Structure):
     ]
 
 
+class PsiRow(ctypes.Structure):
+    _fields_ = [
+        ("in", c_vp),  # (a Python keyword: set with setattr or the numpy view)
+        ("hi", c_vp),
+        ("lo", c_vp),
+        ("n", c_i64),
+    ]
+
+
 class CylMesh(ctypes.Structure):
     _fields_ = [
         ("n_z", c_i32),
@@ -228,6 +237,7 @@ _SIGS = {
     "ion_cyl_adi_run_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),
     "ion_sh_row_lo_c64": (ctypes.c_int, [ctypes.POINTER(ShPlan), c_vp]),
     "ion_psi_split_c128": (ctypes.c_int, [c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "ion_psi_split_rows_c128": (ctypes.c_int, [c_i64, c_vp, c_i32, c_vp]),
     "ion_cyl_adi_pass_c128": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i32, c_i32, c_vp]),
     "ion_cyl_max_points_c128": (c_i64, []),
     "ion_cyl_adi_run_c64": (ctypes.c_int, [ctypes.POINTER(CylMesh), c_vp, c_vp, c_i64, c_i64, c_vp]),

@@ -131,6 +131,30 @@ __global__ void __launch_bounds__(256) psi_split_kernel(int64_t n, const Cx<doub
     }
 }
 
+// many rows, one CTA at a time per row (rows of a batch's initial states are
+// a few thousand points each): split into hi and lo as psi_split_kernel, or
+// copied into a complex128 hi
+__global__ void __launch_bounds__(256) psi_split_rows_kernel(int64_t n_rows, const ion_psi_row* rows,
+                                                             int hi_c128) {
+    for (int64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+        const ion_psi_row row = rows[r];
+        const Cx<double>* in = static_cast<const Cx<double>*>(row.in);
+        if (hi_c128) {
+            Cx<double>* out = static_cast<Cx<double>*>(row.hi);
+            for (int64_t i = threadIdx.x; i < row.n; i += blockDim.x) out[i] = in[i];
+            continue;
+        }
+        Cx<float>* hi = static_cast<Cx<float>*>(row.hi);
+        uint32_t* lo = static_cast<uint32_t*>(row.lo);
+        for (int64_t i = threadIdx.x; i < row.n; i += blockDim.x) {
+            const Cx<double> v = in[i];
+            const Cx<float> h = {float(v.re), float(v.im)};
+            hi[i] = h;
+            if (lo) lo[i] = lo_pack(Cx<float>{float(v.re - double(h.re)), float(v.im - double(h.im))});
+        }
+    }
+}
+
 }  // namespace ion
 
 using namespace ion;
@@ -147,6 +171,16 @@ int ion_psi_split_c128(int64_t n, const void* in, void* hi, void* lo, void* stre
     psi_split_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n, static_cast<const Cx<double>*>(in),
                                                              static_cast<Cx<float>*>(hi), static_cast<uint32_t*>(lo));
     return check_launch("psi_split_kernel");
+}
+int ion_psi_split_rows_c128(int64_t n_rows, const ion_psi_row* rows, int32_t hi_c128, void* stream) {
+    if (n_rows < 0 || (n_rows > 0 && !rows)) {
+        set_error("ion_psi_split_rows_c128: invalid argument");
+        return ION_ERR_INVALID_ARGUMENT;
+    }
+    if (n_rows == 0) return ION_OK;
+    const int blocks = int(n_rows < 16 * 152 ? n_rows : 16 * 152);
+    psi_split_rows_kernel<<<blocks, 256, 0, as_stream(stream)>>>(n_rows, rows, hi_c128 ? 1 : 0);
+    return check_launch("psi_split_rows_kernel");
 }
 int64_t ion_reduce_scratch_bytes(int64_t M, int32_t n_states) {
     (void)M;

@@ -69,7 +69,8 @@ def test_struct_offsets_match_the_c_compiler(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     mirrors = {"ion_sh_sim": nat.ShSim, "ion_sh_plan": nat.ShPlan, "ion_line_sim": nat.LineSim,
-               "ion_line_plan": nat.LinePlan, "ion_cyl_mesh": nat.CylMesh, "ion_hop": nat.Hop}
+               "ion_line_plan": nat.LinePlan, "ion_cyl_mesh": nat.CylMesh, "ion_hop": nat.Hop,
+               "ion_psi_row": nat.PsiRow}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ionization_gb300.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')

@@ -35,6 +35,49 @@ def test_device_split_matches_host_packing(cuda):
     assert np.max(err[5:]) < 2.0 ** -31
 
 
+@pytest.mark.parametrize("hi_c128", [0, 1])
+def test_split_rows_matches_one_row_at_a_time(cuda, hi_c128):
+    """ion_psi_split_rows_c128 (all rows of a batch's initial states in one
+    launch) gives what ion_psi_split_c128 gives row by row, or a plain copy
+    into complex128; rows of any length, including 0 and 1, and the words
+    around each destination row untouched."""
+    import torch
+
+    from ionization_gb300 import _device as dev
+    from ionization_gb300 import _native as nat
+
+    rng = np.random.default_rng(11)
+    lengths = [1, 0, 257, 3000, 31, 4096, 2]
+    total = sum(lengths)
+    v = rng.normal(size=total) * np.exp(rng.uniform(-40, 2, total)) + 1j * rng.normal(size=total)
+    d_in = dev.to_dev(v)
+    hdt = torch.complex128 if hi_c128 else torch.complex64
+    gap = 3  # untouched elements between destination rows
+    hi = torch.full((total + gap * len(lengths),), 7.0, dtype=hdt, device="cuda")
+    lo = torch.full((total + gap * len(lengths),), -1, dtype=torch.int32, device="cuda")
+    table, o_in, o_out = [], 0, 0
+    for n in lengths:
+        table.append((d_in.data_ptr() + 16 * o_in, hi.data_ptr() + hi.element_size() * o_out,
+                      0 if hi_c128 else lo.data_ptr() + 4 * o_out, n))
+        o_in += n
+        o_out += n + gap
+    d_table = torch.tensor(table, dtype=torch.int64, device="cuda")
+    assert nat.call("ion_psi_split_rows_c128", len(table), d_table.data_ptr(), hi_c128, dev.stream_ptr()) == 0
+    torch.cuda.synchronize()
+    keep = np.concatenate([np.r_[np.ones(n, bool), np.zeros(gap, bool)] for n in lengths])
+    h, w = hi.cpu().numpy(), lo.cpu().numpy()
+    if hi_c128:
+        np.testing.assert_array_equal(h[keep], v)
+    else:
+        np.testing.assert_array_equal(h[keep], v.astype(np.complex64))
+        np.testing.assert_array_equal(w[keep], dev.lo_pack(v - v.astype(np.complex64).astype(np.complex128)))
+    np.testing.assert_array_equal(h[~keep], 7.0)
+    np.testing.assert_array_equal(w[~keep], -1)
+    assert nat.call("ion_psi_split_rows_c128", 0, None, hi_c128, dev.stream_ptr()) == 0
+    with pytest.raises(nat.IonError):
+        nat.call("ion_psi_split_rows_c128", 3, None, hi_c128, dev.stream_ptr())
+
+
 @pytest.mark.parametrize("index", [146, 300])
 def test_row_remainders_match_host_restatement(cuda, index):
     from ionization_gb300 import _device as dev
