@@ -305,7 +305,7 @@ def _sh_device_sizes(tab: ShTables):
 
 
 class _Arena:
-    """Arrays of one dtype packed into one pinned host buffer, uploaded with
+    """Arrays of one dtype packed into one host buffer, uploaded with
     one copy; each array becomes a view of the device buffer.  Arrays added
     with ``align`` start on a 64-byte boundary (the first of each kind: the
     radial solve's float4 table loads need 16); the others follow the
@@ -516,7 +516,7 @@ class ShDeviceSim:
 
     @classmethod
     def bulk(cls, tables: List[ShTables], precision) -> List["ShDeviceSim"]:
-        """Many simulations with one pinned upload per dtype and one device
+        """Many simulations with one upload per dtype and one device
         buffer per kind of array."""
         arenas = {}
         # one after another: these are many small numpy calls, which a thread
@@ -554,7 +554,7 @@ class ShDeviceSim:
         # sh_psi_many)
         counts = [tab.n_l * tab.n_r for tab in tables]
         state = _sh_state_buffers(sum(counts), Precision(precision), counts)
-        torch.cuda.current_stream().synchronize()  # the pinned sources are released below
+        torch.cuda.current_stream().synchronize()  # the host sources are released below
         sizes = [_sh_device_sizes(tab) for tab in tables]
         n_norm = sum(nd for nd, _, _ in sizes)
         n_ip = sum(nd * max(ns, 1) * 2 for nd, ns, _ in sizes)

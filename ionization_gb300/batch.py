@@ -54,7 +54,7 @@ class BatchedSphericalHarmonicSimulation:
         if tables is None:
             tables = host_tables_many(self.specs)
         self.tables = tables
-        dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one pinned upload per dtype
+        dsims = dev.ShDeviceSim.bulk(tables, self.precision)  # one upload per dtype
         self.sims = dsims
         self.batch = dev.ShBatch(self.precision, dsims, cn_rows=cn_rows, bucket_rows=bucket_rows)
         self.graph_steps = int(graph_steps)
