@@ -283,12 +283,13 @@ typedef struct ion_sh_plan {
 
 /* Advance every simulation of the plan by n_steps (fewer for simulations that
  * reach t_final).  Data reductions happen at data times on the way.  With
- * n_cn_buckets > 1 the buckets' radial solves run side by side on side
- * streams forked from `stream` and joined back to it (graph edges under
- * capture).  The library makes those side streams once per caller stream,
- * outside capture: to keep the overlap in a captured graph, make one
- * uncaptured call on the capture stream first (else the buckets run in
- * stream order, with the same results). */
+ * n_cn_buckets > 1 and `stream` under capture, the buckets' radial solves
+ * run side by side on side streams forked from `stream` and joined back to
+ * it (graph edges); uncaptured calls run them in stream order.  The library
+ * makes those side streams once per caller stream, on an uncaptured call: to
+ * get the overlap in a captured graph, make one uncaptured call on the
+ * capture stream first (else the buckets run in stream order, with the same
+ * results). */
 int ion_sh_split_run_c128(const ion_sh_plan *plan, int64_t n_steps, void *stream);
 int ion_sh_split_run_c64(const ion_sh_plan *plan, int64_t n_steps, void *stream);
 /* One kernel of the step sequence (for per-kernel timing or custom drivers):
