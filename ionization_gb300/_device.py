@@ -9,11 +9,9 @@ simulations of different sizes in one batch.
 """
 
 import concurrent.futures
-import contextlib
 import ctypes
 import dataclasses
 import os
-import threading
 from typing import List, Optional
 
 import numpy as np
@@ -338,9 +336,6 @@ class _Arena:
     # one host-to-device copy.  On GB300 (Grace host, NVLink-C2C) a copy from
     # pageable memory that the host has written runs at ~650 GB/s (229 MB in
     # 1.3 ms), while page-locking a fresh buffer of that size costs ~27 ms.
-    # The buffer is kept for the next upload (``_staging``): packing into
-    # fresh pages runs at the page-fault rate, ~8-10 GB/s whatever the
-    # number of threads.
     chunk_bytes = 8 << 20  # bytes of arrays one packing task copies
 
     def runs(self):
@@ -361,10 +356,7 @@ class _Arena:
                np.dtype(np.int32): torch.int32, np.dtype(np.complex64): torch.complex64,
                np.dtype(np.complex128): torch.complex128}[self.np_dtype]
         n = max(self.size, 1)
-        with _staging(n * self.np_dtype.itemsize) as raw:
-            return self._upload(raw[:n * self.np_dtype.itemsize].view(self.np_dtype), n, tdt, tensors)
-
-    def _upload(self, host, n, tdt, tensors):
+        host = np.empty(n, dtype=self.np_dtype)
         tasks = []  # (offset, arrays) of at most ~chunk_bytes each
         per_task = max(1, self.chunk_bytes // self.np_dtype.itemsize)
         for off, arrs in self.runs():
@@ -636,31 +628,6 @@ class ShDeviceSim:
         if self.g_lo is not None:
             g = g + lo_unpack(self.g_lo.cpu().numpy())
         return g
-
-
-_staging_lock = threading.Lock()
-_staging_buf: Optional[np.ndarray] = None
-
-
-@contextlib.contextmanager
-def _staging(nbytes: int):
-    """The host staging buffer of uploads (bytes, at least ``nbytes``), held
-    by one upload at a time and kept between uploads so that its pages stay
-    faulted in; it grows to the largest upload.  ``release_staging`` frees
-    it."""
-    global _staging_buf
-    with _staging_lock:
-        if _staging_buf is None or _staging_buf.nbytes < nbytes:
-            _staging_buf = None
-            _staging_buf = np.empty(nbytes, dtype=np.uint8)
-        yield _staging_buf
-
-
-def release_staging() -> None:
-    """Free the host staging buffer of uploads (made again when needed)."""
-    global _staging_buf
-    with _staging_lock:
-        _staging_buf = None
 
 
 def _in_threads(fn, items, workers: int = 16):
