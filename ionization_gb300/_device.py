@@ -332,11 +332,12 @@ class _Arena:
         self.placed[id(arr)] = (arr, self.size)
         self.size += arr.size
 
-    # Staged in a pageable host buffer that the packing threads write, then
-    # one host-to-device copy.  On GB300 (Grace host, NVLink-C2C) a copy from
-    # pageable memory that the host has written runs at ~650 GB/s (229 MB in
-    # 1.3 ms), while page-locking a fresh buffer of that size costs ~27 ms.
-    chunk_bytes = 8 << 20  # bytes of arrays one packing task copies
+    # Staged in a pageable host buffer, then one host-to-device copy.  On
+    # GB300 (Grace host, NVLink-C2C) a copy from pageable memory that the host
+    # has written runs at ~650 GB/s (229 MB in 1.3 ms), while page-locking a
+    # fresh buffer of that size costs ~27 ms.  The packing runs in the
+    # calling thread: for the thousands of arrays of a batch, 4 or 16 threads
+    # took longer (23-28 ms against 21 ms for 229 MB).
 
     def runs(self):
         """(offset, [arrays]) of the placed arrays that follow one another."""
@@ -357,25 +358,9 @@ class _Arena:
                np.dtype(np.complex128): torch.complex128}[self.np_dtype]
         n = max(self.size, 1)
         host = np.empty(n, dtype=self.np_dtype)
-        tasks = []  # (offset, arrays) of at most ~chunk_bytes each
-        per_task = max(1, self.chunk_bytes // self.np_dtype.itemsize)
-        for off, arrs in self.runs():
-            group, size = [], 0
-            for arr in arrs:
-                group.append(arr)
-                size += arr.size
-                if size >= per_task:
-                    tasks.append((off, group))
-                    off, group, size = off + size, [], 0
-            if group:
-                tasks.append((off, group))
-
-        def pack(task):  # numpy copies outside the GIL
-            off, arrs = task
+        for off, arrs in self.runs():  # one copy per run
             total = sum(a.size for a in arrs)
             np.concatenate([a.reshape(-1) for a in arrs], out=host[off:off + total])
-
-        _in_threads(pack, tasks)
         dev_buf = torch.empty(n, dtype=tdt, device=device())
         dev_buf.copy_(torch.from_numpy(host))
         return {key: (dev_buf[off:off + arr.size].view(arr.shape) if key[1] in tensors
