@@ -153,3 +153,41 @@ def test_strongly_driven_c64x_populations_match_c128(cuda, rows):
     di = np.abs(pb["c64x"] - pb["c128"])
     print(f"rows {rows}: max |dP_ground| {dg.max():.2e}, max |dP_ion| {di.max():.2e}")
     assert dg.max() < 3e-7 and di.max() < 3e-7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["c64x", "c128"])
+def test_batches_on_two_streams_in_graphs(cuda, precision):
+    """Two batches stepped through CUDA graphs on two streams at once (each
+    graph forks its radial buckets onto side streams of its own capture
+    stream) give, bit for bit, what each gives run alone."""
+    import torch
+
+    from ionization_gb300 import batch as bm
+
+    specs = _specs(precision)
+    sets = (specs[:2] + specs[3:], specs)  # 2 and 3 radial buckets
+    alone = []
+    for ss in sets:
+        b = bm.BatchedSphericalHarmonicSimulation(ss, graph_steps=8)
+        b.run()
+        alone.append((b.psi_all(), b.results()))
+    batches = [bm.BatchedSphericalHarmonicSimulation(ss, graph_steps=8) for ss in sets]
+    assert [len(bm.plan_shape(b)["radial_buckets"]) for b in batches] == [2, 3]
+    streams = [torch.cuda.Stream() for _ in batches]
+    for s in streams:
+        s.wait_stream(torch.cuda.current_stream())
+    while any(b.steps_remaining for b in batches):
+        for b, s in zip(batches, streams):
+            if b.steps_remaining:
+                with torch.cuda.stream(s):
+                    b.step(16)
+    for s in streams:
+        torch.cuda.current_stream().wait_stream(s)
+    for b, (psis, res) in zip(batches, alone, strict=True):
+        for got, want in zip(b.psi_all(), psis, strict=True):
+            np.testing.assert_array_equal(got, want)
+        for got, want in zip(b.results(), res, strict=True):
+            np.testing.assert_array_equal(got["norm"], want["norm"])
+            for k in want["inner_products"]:
+                np.testing.assert_array_equal(got["inner_products"][k], want["inner_products"][k])
