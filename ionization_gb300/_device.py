@@ -118,7 +118,7 @@ class ShTables:
 
     n_r: int
     n_l: int
-    hd: np.ndarray  # [n_l * n_r] internal diagonal, C order
+    hd: np.ndarray  # [n_l * n_r] internal diagonal, C order (may be a LazyArray)
     hoff: np.ndarray  # [n_r - 1]
     rq: np.ndarray  # [n_r]
     cl: np.ndarray  # [n_l]
@@ -131,7 +131,7 @@ class ShTables:
     state_l: List[int]
     state_g: np.ndarray  # [n_states, n_r] complex128, or float64 for real states
     weight: float
-    g0: np.ndarray  # [n_l, n_r] complex128
+    g0: np.ndarray  # [n_l, n_r] complex128 (may be a LazyArray)
     t0: int
     t_final: int
     store_every: int
@@ -142,6 +142,8 @@ class ShTables:
     # the l rows of g0 that are not zero (None: find them); only those rows
     # are uploaded, the rest are zeroed on the device
     g0_rows: Optional[np.ndarray] = None
+    # [len(g0_rows), n_r] complex128: those rows' values (None: read g0)
+    g0_row_data: Optional[np.ndarray] = None
     # kinetic_energy_from_hamiltonian: the coupling between the last r of
     # each l and the first r of the next (None: the lines are independent)
     hcross: Optional[float] = None
@@ -248,7 +250,6 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     absent), by attribute name, in their device dtype."""
     precision = Precision(precision)
     f64, f32 = np.float64, np.float32
-    g0 = np.asarray(tab.g0, dtype=np.complex128)
     c128 = precision == Precision.C128
     x = precision == Precision.C64X
     a = {}
@@ -257,7 +258,12 @@ def _sh_host_arrays(tab: ShTables, precision) -> dict:
     # other rows and, for the complex64 forms, splits these into g and (c64x)
     # its packed residual g_lo (ion_psi_split_c128)
     rows = sh_nonzero_rows(tab)
-    a["g_in"] = np.ascontiguousarray(g0[rows]) if rows.size else np.zeros((1, tab.n_r), np.complex128)
+    if not rows.size:
+        a["g_in"] = np.zeros((1, tab.n_r), np.complex128)
+    elif tab.g0_row_data is not None:
+        a["g_in"] = np.ascontiguousarray(tab.g0_row_data, dtype=np.complex128).reshape(rows.size, tab.n_r)
+    else:
+        a["g_in"] = np.ascontiguousarray(np.asarray(tab.g0, dtype=np.complex128).reshape(tab.n_l, tab.n_r)[rows])
     a["d_hd"] = np.asarray(tab.hd, f64) if c128 else None
     # c64x: the FP64 per-r diagonal tables the device forms the row-sum
     # remainders from (ion_sh_row_lo_c64)
@@ -371,7 +377,11 @@ class _Arena:
 def sh_nonzero_rows(tab: "ShTables") -> np.ndarray:
     """The l rows of a simulation's initial psi that are not all zero."""
     if tab.g0_rows is not None:
-        return np.asarray(tab.g0_rows, dtype=np.int64)
+        rows = np.asarray(tab.g0_rows, dtype=np.int64).reshape(-1)
+        # the device writes these rows of psi: each must be a row of the mesh
+        if rows.size and (rows.min() < 0 or rows.max() >= tab.n_l or np.unique(rows).size != rows.size):
+            raise ValueError(f"initial-state rows {rows.tolist()} are not distinct rows of a mesh of {tab.n_l} l")
+        return rows
     g0 = np.asarray(tab.g0).reshape(tab.n_l, tab.n_r)
     return np.flatnonzero(np.any(g0 != 0, axis=1)).astype(np.int64)
 

@@ -3,6 +3,8 @@
 import dataclasses
 import enum
 
+import numpy as np
+
 
 class StrEnum(str, enum.Enum):
     def __str__(self):
@@ -47,3 +49,40 @@ class SphericalHarmonic:
 
     def __str__(self):
         return f"Y_{self.l}^{self.m}"
+
+
+class LazyArray:
+    """An array formed by ``make()`` when it is first read (``np.asarray``
+    or any numpy call on it), then kept.  Host tables that only some forms
+    upload (the complex128 radial diagonal over the whole (l, r) mesh, the
+    full initial psi of which only the nonzero rows go up) are formed only
+    where they are read."""
+
+    __slots__ = ("_make", "_value")
+
+    def __init__(self, make):
+        self._make, self._value = make, None
+
+    def value(self) -> np.ndarray:
+        if self._value is None:
+            self._value = np.asarray(self._make())
+            self._make = None
+        return self._value
+
+    def __array__(self, dtype=None, copy=None):
+        v = self.value()
+        if dtype is not None and np.dtype(dtype) != v.dtype:
+            return v.astype(dtype)
+        return v.copy() if copy else v
+
+    # indexing and the array's own attributes (shape, dtype, reshape, ...)
+    def __getitem__(self, key):
+        return self.value()[key]
+
+    def __len__(self):
+        return len(self.value())
+
+    def __getattr__(self, name):
+        if name.startswith("_"):
+            raise AttributeError(name)
+        return getattr(self.value(), name)

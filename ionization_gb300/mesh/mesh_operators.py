@@ -280,12 +280,17 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
         if self.hydrogen_zero_angular_momentum_correction:
             dr = mesh.delta_r / u.bohr_radius
             corr = dr * (1 + dr) / 8
-        lv = np.arange(L)[:, None]
-        eff = ((u.hbar ** 2) / (2 * mu)) * lv * (lv + 1) / (mesh.r[None, :] ** 2)
         V_r = np.asarray(spec.internal_potential(r=mesh.r, test_charge=spec.test_charge), dtype=np.float64)
-        hd2 = (beta_r * (-2 * p))[None, :] + eff
-        hd2[0, 0] = (beta_r[0] + corr) * (-2 * p) + eff[0, 0]
-        hd = (hd2 + V_r[None, :]).reshape(-1)
+        r = mesh.r
+
+        def full_hd():  # the (l, r) diagonal: read by the complex128 forms only
+            lv = np.arange(L)[:, None]
+            eff = ((u.hbar ** 2) / (2 * mu)) * lv * (lv + 1) / (r[None, :] ** 2)
+            hd2 = (beta_r * (-2 * p))[None, :] + eff
+            hd2[0, 0] = (beta_r[0] + corr) * (-2 * p) + eff[0, 0]
+            return (hd2 + V_r[None, :]).reshape(-1)
+
+        hd = core.LazyArray(full_hd)
         hoff = (self.alpha(np.arange(nr - 1)) * p).astype(np.float64)
         rq = -spec.test_charge * mesh.r
         cl = self.c_l(np.arange(L))
@@ -342,7 +347,7 @@ class SphericalHarmonicLengthGaugeOperators(MeshOperators):
             off[l * nr: l * nr + nr - 1] = t["hoff"]
         if t["cross"] is not None:
             off[nr - 1::nr] = t["cross"]
-        m = sparse.diags((off.astype(np.complex128), t["hd"].astype(np.complex128), off.astype(np.complex128)),
+        m = sparse.diags((off.astype(np.complex128), np.asarray(t["hd"]).astype(np.complex128), off.astype(np.complex128)),
                          offsets=(-1, 0, 1))
         return SumOfOperators(DotOperator(m, wrapping_direction="r"))
 

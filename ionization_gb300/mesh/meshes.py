@@ -579,16 +579,31 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
 
     def get_g_for_state(self, state):
         """meshes.py:1066-1087."""
+        rows, vals = self._g_rows_for_state(state)
+        g = np.zeros(self.mesh_shape, dtype=np.complex128)
+        for l, v in zip(rows, vals):
+            g[l, :] = v
+        return g
+
+    def _g_rows_for_state(self, state):
+        """The l rows of get_g_for_state(state) that hold its components
+        (sorted) and their values: each component's radial g added into its
+        row in component order, as the full-mesh form adds them."""
         if not all(hasattr(s, "radial_function") for s in state):
             raise NotImplementedError(
                 "States with non-definite angular momentum components are not currently supported by SphericalHarmonicMesh"
             )
         if state.analytic and getattr(self.spec, "use_numeric_eigenstates", False):
             state = getattr(self, "analytic_to_numeric", {}).get(state, state)
-        g = np.zeros(self.mesh_shape, dtype=np.complex128)
+        acc = {}
         for s in state:
-            g[s.l, :] += self.get_radial_g_for_state(s)
-        return g
+            if not 0 <= s.l < self.spec.l_bound:
+                raise IndexError(f"state component with l = {s.l} outside the mesh's l_bound {self.spec.l_bound}")
+            if s.l not in acc:
+                acc[s.l] = np.zeros(self.spec.r_points, dtype=np.complex128)
+            acc[s.l] += self.get_radial_g_for_state(s)
+        rows = sorted(acc)
+        return rows, [acc[l] for l in rows]
 
     def inner_product(self, a=None, b=None):
         """The per-l shortcut of meshes.py:1099-1131 when ``a`` is a state and
@@ -656,13 +671,24 @@ class SphericalHarmonicMesh(_AdiDevice, QuantumMesh):
                 raise exceptions.UnsupportedMesh("device inner products need single-l test states")
             sl.append(comps[0].l)
             sg.append(self.get_radial_g_for_state(comps[0]) * 1)
-        g0 = self.get_g_for_state(spec.initial_state)
+        # the initial psi as its component rows (only they are uploaded); the
+        # full (l, r) array is formed if something reads it
+        g0_rows, g0_vals = self._g_rows_for_state(spec.initial_state)
+        shape = self.mesh_shape
+
+        def full_g0():
+            g = np.zeros(shape, dtype=np.complex128)
+            for l, v in zip(g0_rows, g0_vals):
+                g[l, :] = v
+            return g
+
         self.tables = dev.ShTables(
             n_r=spec.r_points, n_l=spec.l_bound, hd=tb["hd"], hoff=tb["hoff"], rq=rq, cl=tb["cl"], mask=mask,
             tau=self._tau_host.copy(), efield=efield, kinv=tb["kinv"], cent=tb["cent"], corr0=tb["corr0"],
             state_l=sl, state_g=_radial_states_array(sg, spec.r_points),
-            weight=self.inner_product_multiplier, g0=g0, t0=0, t_final=len(times) - 1,
-            g0_rows=np.flatnonzero(np.any(np.asarray(g0).reshape(spec.l_bound, spec.r_points) != 0, axis=1)),
+            weight=self.inner_product_multiplier, g0=core.LazyArray(full_g0), t0=0, t_final=len(times) - 1,
+            g0_rows=np.asarray(g0_rows, dtype=np.int64),
+            g0_row_data=np.array(g0_vals, dtype=np.complex128).reshape(len(g0_rows), spec.r_points),
             store_every=spec.store_data_every, gauge=gauge, h2r=h2r, hcross=tb.get("cross"),
         )
         if getattr(spec, "host_only", False):
