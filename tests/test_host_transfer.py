@@ -66,3 +66,50 @@ def test_host_copy_returns_the_values(n):
     np.testing.assert_array_equal(out, t.numpy())
     c = torch.complex(t, -t)
     np.testing.assert_array_equal(dev._host_copy(c), c.numpy())
+
+
+def test_lazy_array_forms_once_and_reads_like_its_array():
+    from ionization_gb300.core import LazyArray
+
+    calls = []
+
+    def make():
+        calls.append(1)
+        return np.arange(12, dtype=np.float64).reshape(3, 4)
+
+    a = LazyArray(make)
+    assert not calls
+    np.testing.assert_array_equal(np.asarray(a), make())
+    assert np.asarray(a, dtype=np.float32).dtype == np.float32
+    assert a.shape == (3, 4) and a.dtype == np.float64 and len(a) == 3
+    assert a[1, 2] == 6.0 and a.reshape(-1)[5] == 5.0
+    np.testing.assert_array_equal(np.asarray(a, dtype=np.complex128).real, make())
+    assert len(calls) == 3  # one inside LazyArray, two by the test itself
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64x", "c64"])
+def test_lazy_sh_tables_upload_what_eager_ones_do(precision):
+    """The spherical-harmonic host tables form the (l, r) diagonal and the
+    full initial psi only when read: what a simulation uploads equals what
+    the same tables with both formed up front give, and the complex64 forms
+    never form the diagonal."""
+    import dataclasses
+
+    from ionization_gb300 import batch as bm
+    from ionization_gb300 import workloads as wl
+    from ionization_gb300.core import LazyArray
+
+    spec = wl.sh_spec("lazy", 160, 9, 0.05, 0.1, 2, 0.3, 12, precision=precision, mask_width=0.4 * wl.DR * 160)
+    tab = bm._host_tables(spec)[0]
+    assert isinstance(tab.hd, LazyArray) and isinstance(tab.g0, LazyArray)
+    got = dev._sh_host_arrays(tab, precision)
+    assert (tab.hd._value is None) == (precision != "c128")
+    eager = dataclasses.replace(tab, hd=np.array(tab.hd), g0=np.array(tab.g0), g0_rows=None, g0_row_data=None)
+    want = dev._sh_host_arrays(eager, precision)
+    assert got.keys() == want.keys()
+    for k in got:
+        if want[k] is None:
+            assert got[k] is None, k
+        else:
+            np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+    np.testing.assert_array_equal(dev.sh_nonzero_rows(tab), dev.sh_nonzero_rows(eager))
