@@ -532,7 +532,8 @@ int ion_psi_split_c128(int64_t n, const void *in, void *hi, void *lo, void *stre
  * With hi_c128 = 0 each row is split as by ion_psi_split_c128 (complex64 hi,
  * lo as there, may be NULL); with hi_c128 != 0 it is copied into a
  * complex128 hi and lo is ignored.  Rows may not overlap one another's
- * outputs nor alias their own input. */
+ * outputs nor alias their own input; a row with n <= 0 or a NULL in or hi
+ * is skipped. */
 typedef struct ion_psi_row {
     const void *in;  /* n complex128 */
     void *hi;        /* n complex64 (split) or complex128 (copy) */

@@ -138,6 +138,7 @@ __global__ void __launch_bounds__(256) psi_split_rows_kernel(int64_t n_rows, con
                                                              int hi_c128) {
     for (int64_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
         const ion_psi_row row = rows[r];
+        if (row.n <= 0 || !row.in || !row.hi) continue;  // an empty or NULL row writes nothing
         const Cx<double>* in = static_cast<const Cx<double>*>(row.in);
         if (hi_c128) {
             Cx<double>* out = static_cast<Cx<double>*>(row.hi);

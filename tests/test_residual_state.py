@@ -40,7 +40,8 @@ def test_split_rows_matches_one_row_at_a_time(cuda, hi_c128):
     """ion_psi_split_rows_c128 (all rows of a batch's initial states in one
     launch) gives what ion_psi_split_c128 gives row by row, or a plain copy
     into complex128; rows of any length, including 0 and 1, and the words
-    around each destination row untouched."""
+    around each destination row untouched; rows with a NULL input or a
+    negative length write nothing."""
     import torch
 
     from ionization_gb300 import _device as dev
@@ -53,18 +54,22 @@ def test_split_rows_matches_one_row_at_a_time(cuda, hi_c128):
     d_in = dev.to_dev(v)
     hdt = torch.complex128 if hi_c128 else torch.complex64
     gap = 3  # untouched elements between destination rows
-    hi = torch.full((total + gap * len(lengths),), 7.0, dtype=hdt, device="cuda")
-    lo = torch.full((total + gap * len(lengths),), -1, dtype=torch.int32, device="cuda")
+    extra = 8  # the target of rows that must be skipped (NULL input, negative length)
+    hi = torch.full((total + gap * len(lengths) + extra,), 7.0, dtype=hdt, device="cuda")
+    lo = torch.full((total + gap * len(lengths) + extra,), -1, dtype=torch.int32, device="cuda")
     table, o_in, o_out = [], 0, 0
     for n in lengths:
         table.append((d_in.data_ptr() + 16 * o_in, hi.data_ptr() + hi.element_size() * o_out,
                       0 if hi_c128 else lo.data_ptr() + 4 * o_out, n))
         o_in += n
         o_out += n + gap
+    end_hi, end_lo = hi.data_ptr() + hi.element_size() * o_out, lo.data_ptr() + 4 * o_out
+    table.insert(2, (0, end_hi, end_lo, extra))
+    table.append((d_in.data_ptr(), end_hi, end_lo, -3))
     d_table = torch.tensor(table, dtype=torch.int64, device="cuda")
     assert nat.call("ion_psi_split_rows_c128", len(table), d_table.data_ptr(), hi_c128, dev.stream_ptr()) == 0
     torch.cuda.synchronize()
-    keep = np.concatenate([np.r_[np.ones(n, bool), np.zeros(gap, bool)] for n in lengths])
+    keep = np.concatenate([np.r_[np.ones(n, bool), np.zeros(gap, bool)] for n in lengths] + [np.zeros(extra, bool)])
     h, w = hi.cpu().numpy(), lo.cpu().numpy()
     if hi_c128:
         np.testing.assert_array_equal(h[keep], v)
